@@ -1,0 +1,217 @@
+/*
+ * mdg.h -- C ABI of the GB300-native particle hot path (libmddem_gb300.so).
+ *
+ * The reference (SueHeir/MDDEM, Rust) runs this path as plain systems that
+ * share resources inside its App/Scheduler.  This library replaces the systems
+ * below with device-resident CUDA kernels for sm_103a; a host plugin (Rust
+ * shim over FFI, the C++ host in mddem_gb300/host, or Python ctypes) calls
+ * these entry points from the same schedule phases.  Replaced reference
+ * interfaces (paths relative to the reference repository):
+ *
+ *   mdg_create / mdg_batch_create
+ *       NeighborPlugin::build + neighbor_setup   crates/mddem_core/src/neighbor.rs:417-541
+ *       DemAtomPlugin::build (MaterialTable)      crates/dem_atom/src/lib.rs:592-664, 389-515
+ *       HertzMindlinContactPlugin::build          crates/dem_granular/src/contact.rs:52-91
+ *       LJForcePlugin + build_lj_pair_table       crates/md_lj/src/lib.rs:290-384
+ *       NoseHooverPlugin + setup_nose_hoover      crates/md_thermostat/src/lib.rs:166-243
+ *   mdg_upload_state / mdg_download_state
+ *       Atom SoA + DemAtom + ContactHistoryStore  crates/mddem_core/src/atom.rs:310-335,
+ *                                                 crates/dem_atom/src/lib.rs:530-557,
+ *                                                 crates/dem_granular/src/tangential.rs:54-133
+ *   mdg_step (one call = nsteps full timesteps, schedule order of schedule.dot:45-153)
+ *       initial_integration / final_integration   crates/mddem_verlet/src/lib.rs:97-154
+ *       initial_rotation / final_rotation         crates/dem_granular/src/rotational.rs:59-100
+ *       nh_pre_initial / nh_post_final            crates/md_thermostat/src/lib.rs:254-353
+ *       decide_rebuild                            crates/mddem_core/src/neighbor.rs:639-674
+ *       zero_all_forces / remove_ghost_atoms      crates/mddem_core/src/atom.rs:523-533
+ *       pbc                                       crates/mddem_core/src/domain.rs:413-459
+ *       forward_comm / borders / reverse_send_force
+ *                                                 crates/mddem_core/src/comm.rs:367-656
+ *                                                 (replaced by on-device periodic images)
+ *       sort_atoms_by_bin / bin_neighbor_list     crates/mddem_core/src/neighbor.rs:686-1080
+ *       hertz_mindlin_contact_force / hooke_contact_force
+ *                                                 crates/dem_granular/src/contact.rs:103-990
+ *       lj_force                                  crates/md_lj/src/lib.rs:488-633
+ *       zero_virial_stress / VirialStress         crates/mddem_core/src/virial.rs:48-121
+ *   mdg_force_only  (neighbor rebuild + force phase, no integration)
+ *   mdg_get_pairs   Neighbor::pairs               crates/mddem_core/src/neighbor.rs:172-227
+ *   mdg_get_history ContactHistoryStore.contacts  crates/dem_granular/src/tangential.rs:54-75
+ *   mdg_thermo      compute_ke + print_granular_temperature + NoseHooverState
+ *                                                 crates/mddem_core/src/atom.rs:489-502,
+ *                                                 crates/dem_granular/src/granular_temp.rs:44-134
+ *
+ * Conventions: every call returns an int status (MDG_OK = 0); nothing in the
+ * library aborts the process.  Host arrays are borrowed for the duration of a
+ * call and copied; the context owns all device memory.  A context is used by
+ * one host thread at a time (one CUDA stream per context); distinct contexts
+ * may be used from different threads.  Vectors are interleaved per particle
+ * (x0,y0,z0,x1,...).  Units are the caller's (SI for DEM, reduced for LJ).
+ */
+#ifndef MDG_H
+#define MDG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MDG_ABI_VERSION 1
+
+/* status codes */
+enum {
+    MDG_OK = 0,
+    MDG_ERR_CONFIG = 1,        /* invalid configuration (reference: process::exit(1)) */
+    MDG_ERR_CUDA = 2,          /* CUDA runtime error */
+    MDG_ERR_OOM = 3,           /* device allocation failed */
+    MDG_ERR_BUDGET = 4,        /* request exceeds the HBM budget */
+    MDG_ERR_OVERLAP_LIMIT = 5, /* > 500 large overlaps in one step (reference panics) */
+    MDG_ERR_NAN = 6,           /* non-finite value in the state */
+    MDG_ERR_LIST_OVERFLOW = 7, /* neighbor or contact-history capacity exceeded */
+    MDG_ERR_TIMEOUT = 8,       /* a bounded device wait gave up */
+    MDG_ERR_ARG = 9,           /* bad argument (null pointer, index, size) */
+    MDG_ERR_STATE = 10,        /* call out of order (e.g. step before upload) */
+    MDG_ERR_NODEVICE = 11      /* no CUDA device */
+};
+
+enum { MDG_KIND_DEM = 0, MDG_KIND_LJ = 1 };
+enum { MDG_FP64 = 0, MDG_MIXED = 1 };
+enum { MDG_CONTACT_HERTZ = 0, MDG_CONTACT_HOOKE = 1 };
+enum { MDG_ADHESION_JKR = 0, MDG_ADHESION_DMT = 1 };
+enum { MDG_MODEL_CONSTANT = 0, MDG_MODEL_SDS = 1 };
+/* Rebuild policy.  REFERENCE: rebuild when any atom moved more than the skin
+ * share or left the box (decide_rebuild, neighbor.rs:639-674); positions are
+ * wrapped only on rebuild steps.  DISPLACEMENT: rebuild on displacement only;
+ * positions stay unwrapped between rebuilds (periodic images are carried by
+ * the list), which removes the per-crossing rebuilds of large boxes. */
+enum { MDG_REBUILD_REFERENCE = 0, MDG_REBUILD_DISPLACEMENT = 1 };
+
+/* One [[dem.materials]] entry (crates/dem_atom/src/lib.rs:78-121). */
+typedef struct mdg_material {
+    double youngs_mod, poisson_ratio, restitution, friction;
+    double rolling_friction, twisting_friction, cohesion_energy, surface_energy;
+    double kn, kt, rolling_stiffness, rolling_damping, twisting_stiffness, twisting_damping;
+} mdg_material;
+
+/* One simulation (a "system"): the TOML sections the plugins read. */
+typedef struct mdg_config {
+    int kind;                    /* MDG_KIND_* */
+    int precision;               /* MDG_FP64 or MDG_MIXED ([gpu] precision) */
+    double box_lo[3], box_hi[3]; /* [domain]; all three axes periodic */
+    double dt;                   /* [run] dt (> 0) */
+    /* [neighbor] (crates/mddem_core/src/neighbor.rs:44-80) */
+    double skin_fraction, bin_size;
+    int every, check, sort_every, newton;
+    /* [dem] */
+    int n_materials;
+    const mdg_material* materials;
+    int contact_model, adhesion_model, rolling_model, twisting_model;
+    /* [lj] single type (crates/md_lj/src/lib.rs:115-140) */
+    double lj_epsilon, lj_sigma, lj_cutoff;
+    /* [thermostat] Nose-Hoover (crates/md_thermostat/src/lib.rs:85-97) */
+    int nose_hoover;
+    double nh_temperature, nh_coupling;
+    int virial;                  /* accumulate the 6-component virial each step */
+    /* [gpu] */
+    int rebuild_policy;          /* MDG_REBUILD_* */
+    int threads_per_particle;    /* 0 = auto; 1,2,4,8,16,32 for the force kernels */
+    int neighbor_capacity;       /* 0 = auto: max full-list entries per particle */
+    int history_capacity;        /* 0 = auto: max stored contacts per particle */
+} mdg_config;
+
+/* SoA view of one system's particles (caller-owned, n particles). */
+typedef struct mdg_state_view {
+    size_t n;
+    uint32_t* tag;
+    uint32_t* type;          /* material index (DEM) or LJ type */
+    double* pos;             /* n*3 */
+    double* vel;             /* n*3 */
+    double* force;           /* n*3 (download only; may be NULL) */
+    double* mass;            /* n */
+    double* cutoff_radius;   /* n: neighbor cutoff radius (DEM: radius; LJ: lattice skin) */
+    int32_t* image;          /* n*3 periodic image counters (may be NULL) */
+    /* DEM only (NULL for LJ) */
+    double* radius;          /* n */
+    double* inv_inertia;     /* n */
+    double* omega;           /* n*3 */
+    double* torque;          /* n*3 (download only; may be NULL) */
+    double* quat;            /* n*4 [w,x,y,z] */
+} mdg_state_view;
+
+/* Thermo record (print_thermo / GranularTemp columns plus extended state). */
+typedef struct mdg_thermo_t {
+    double ke;               /* 0.5 sum m |v|^2 */
+    double pe;               /* LJ 12-6 energy sum over pairs (unshifted) */
+    double temp;             /* 2 KE / (3N - 3) */
+    double p_xi;             /* Nose-Hoover thermostat momentum */
+    double granular_temp;    /* sum m |v - vbar|^2 / (3 M) */
+    double momentum;         /* |sum m v| */
+    double virial[6];        /* xx yy zz xy xz yz of the last force evaluation */
+    int64_t step;
+    int64_t nbuilds;         /* neighbor-list builds so far */
+    int64_t n;
+    int32_t status;          /* sticky device status word for this system */
+    int32_t max_neighbors;   /* largest full-list row seen at the last build */
+} mdg_thermo_t;
+
+typedef struct mdg_ctx mdg_ctx;
+
+/* Library / device */
+int  mdg_abi_version(void);
+const char* mdg_status_string(int status);
+int  mdg_device_count(int* count);
+
+/* Context lifecycle.  mdg_create makes a context holding one system;
+ * mdg_batch_create makes one context advancing nsys systems (replicas of
+ * uneven sizes) with one launch per kernel per step.  capacity[k] is the
+ * largest particle count system k will hold. */
+int  mdg_create(const mdg_config* cfg, size_t capacity, mdg_ctx** out);
+int  mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, mdg_ctx** out);
+void mdg_destroy(mdg_ctx* ctx);
+int  mdg_num_systems(const mdg_ctx* ctx);
+
+/* State transfer for system `sys` (0 for single-system contexts).
+ * Upload resets neighbor/rebuild state (next step performs a full rebuild,
+ * like the reference's first step) and clears contact history. */
+int  mdg_upload_state(mdg_ctx* ctx, int sys, const mdg_state_view* st);
+int  mdg_download_state(mdg_ctx* ctx, int sys, mdg_state_view* st);
+
+/* Contact history transfer: keys = (owner tag, partner tag) pairs, vals = 7
+ * doubles per entry, in the reference's canonical (lower-tag) frame. */
+int  mdg_set_history(mdg_ctx* ctx, int sys, size_t n, const uint32_t* keys, const double* vals);
+int  mdg_get_history(mdg_ctx* ctx, int sys, uint32_t* keys, double* vals, size_t cap, size_t* n);
+
+/* Advance every system of the context by nsteps timesteps.  Returns the
+ * first non-zero system status, if any. */
+int  mdg_step(mdg_ctx* ctx, int64_t nsteps);
+/* Neighbor rebuild + force evaluation at the current state (no integration). */
+int  mdg_force_only(mdg_ctx* ctx);
+/* Half-list pairs at the last build as (owner tag, partner tag). */
+int  mdg_get_pairs(mdg_ctx* ctx, int sys, uint32_t* pairs, size_t cap, size_t* n);
+int  mdg_thermo(mdg_ctx* ctx, int sys, mdg_thermo_t* out);
+/* Block until all device work of the context is complete. */
+int  mdg_synchronize(mdg_ctx* ctx);
+/* Device kernels launched by this context so far (for launch accounting). */
+int64_t mdg_kernel_launches(const mdg_ctx* ctx);
+/* Capture the per-step kernel sequence into a CUDA graph (1) or launch
+ * kernels individually (0).  Default 1. */
+int  mdg_set_graph_mode(mdg_ctx* ctx, int enabled);
+
+/* Device timing of individual steps (tracing).  Each step runs as one
+ * captured graph bracketed by CUDA events on the context's stream, with event
+ * records between its phases; before each step, outside the events, the L2
+ * cache is flushed by writing l2_flush_bytes of scratch memory (0 = no
+ * flush).  per_step receives nsteps records. */
+typedef struct mdg_step_timing {
+    double step_ms;          /* whole step, first to last event */
+    double phase_ms[4];      /* initial integration, rebuild pipeline, force, final */
+    int32_t kernels;         /* kernels launched by the step */
+    int32_t rebuilt;         /* 1 if any system rebuilt its list this step */
+} mdg_step_timing;
+int  mdg_timed_steps(mdg_ctx* ctx, int64_t nsteps, size_t l2_flush_bytes, mdg_step_timing* per_step);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MDG_H */

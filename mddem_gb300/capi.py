@@ -1,0 +1,308 @@
+"""ctypes binding of the C ABI in include/mdg.h.
+
+This is the Python face of the drop-in boundary: each method maps to one
+``extern "C"`` entry point of libmddem_gb300.so.  The library must be built
+(``mddem_gb300.build.build()``); there is no CPU fallback, and every call
+raises ``MdgError`` on a non-zero status.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .config import SimConfig
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libmddem_gb300.so")
+
+MDG_OK = 0
+STATUS_NAMES = {
+    0: "MDG_OK", 1: "MDG_ERR_CONFIG", 2: "MDG_ERR_CUDA", 3: "MDG_ERR_OOM", 4: "MDG_ERR_BUDGET",
+    5: "MDG_ERR_OVERLAP_LIMIT", 6: "MDG_ERR_NAN", 7: "MDG_ERR_LIST_OVERFLOW", 8: "MDG_ERR_TIMEOUT",
+    9: "MDG_ERR_ARG", 10: "MDG_ERR_STATE", 11: "MDG_ERR_NODEVICE",
+}
+
+# every symbol include/mdg.h declares
+EXPORTS = [
+    "mdg_abi_version", "mdg_status_string", "mdg_device_count", "mdg_create", "mdg_batch_create", "mdg_destroy",
+    "mdg_num_systems", "mdg_upload_state", "mdg_download_state", "mdg_set_history", "mdg_get_history",
+    "mdg_step", "mdg_force_only", "mdg_get_pairs", "mdg_thermo", "mdg_synchronize", "mdg_kernel_launches",
+    "mdg_set_graph_mode", "mdg_timed_steps",
+]
+
+
+class MdgError(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        super().__init__(f"{what}: {STATUS_NAMES.get(status, status)}")
+
+
+class Material(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "youngs_mod", "poisson_ratio", "restitution", "friction", "rolling_friction", "twisting_friction",
+        "cohesion_energy", "surface_energy", "kn", "kt", "rolling_stiffness", "rolling_damping",
+        "twisting_stiffness", "twisting_damping")]
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int), ("precision", C.c_int),
+        ("box_lo", C.c_double * 3), ("box_hi", C.c_double * 3), ("dt", C.c_double),
+        ("skin_fraction", C.c_double), ("bin_size", C.c_double),
+        ("every", C.c_int), ("check", C.c_int), ("sort_every", C.c_int), ("newton", C.c_int),
+        ("n_materials", C.c_int), ("materials", C.POINTER(Material)),
+        ("contact_model", C.c_int), ("adhesion_model", C.c_int), ("rolling_model", C.c_int),
+        ("twisting_model", C.c_int),
+        ("lj_epsilon", C.c_double), ("lj_sigma", C.c_double), ("lj_cutoff", C.c_double),
+        ("nose_hoover", C.c_int), ("nh_temperature", C.c_double), ("nh_coupling", C.c_double),
+        ("virial", C.c_int),
+        ("rebuild_policy", C.c_int), ("threads_per_particle", C.c_int), ("neighbor_capacity", C.c_int),
+        ("history_capacity", C.c_int),
+    ]
+
+
+class StateView(C.Structure):
+    _fields_ = [
+        ("n", C.c_size_t),
+        ("tag", C.POINTER(C.c_uint32)), ("type", C.POINTER(C.c_uint32)),
+        ("pos", C.POINTER(C.c_double)), ("vel", C.POINTER(C.c_double)), ("force", C.POINTER(C.c_double)),
+        ("mass", C.POINTER(C.c_double)), ("cutoff_radius", C.POINTER(C.c_double)),
+        ("image", C.POINTER(C.c_int32)),
+        ("radius", C.POINTER(C.c_double)), ("inv_inertia", C.POINTER(C.c_double)),
+        ("omega", C.POINTER(C.c_double)), ("torque", C.POINTER(C.c_double)), ("quat", C.POINTER(C.c_double)),
+    ]
+
+
+class Thermo(C.Structure):
+    _fields_ = [
+        ("ke", C.c_double), ("pe", C.c_double), ("temp", C.c_double), ("p_xi", C.c_double),
+        ("granular_temp", C.c_double), ("momentum", C.c_double), ("virial", C.c_double * 6),
+        ("step", C.c_int64), ("nbuilds", C.c_int64), ("n", C.c_int64), ("status", C.c_int32),
+        ("max_neighbors", C.c_int32),
+    ]
+
+
+class StepTiming(C.Structure):
+    _fields_ = [("step_ms", C.c_double), ("phase_ms", C.c_double * 4), ("kernels", C.c_int32),
+                ("rebuilt", C.c_int32)]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libmddem_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build the CUDA extension with mddem_gb300.build.build()")
+    lib = C.CDLL(path)
+    P = C.POINTER
+    lib.mdg_abi_version.restype = C.c_int
+    lib.mdg_status_string.restype = C.c_char_p
+    lib.mdg_status_string.argtypes = [C.c_int]
+    lib.mdg_device_count.argtypes = [P(C.c_int)]
+    lib.mdg_create.argtypes = [P(Config), C.c_size_t, P(C.c_void_p)]
+    lib.mdg_batch_create.argtypes = [P(Config), P(C.c_size_t), C.c_int, P(C.c_void_p)]
+    lib.mdg_destroy.argtypes = [C.c_void_p]
+    lib.mdg_destroy.restype = None
+    lib.mdg_num_systems.argtypes = [C.c_void_p]
+    lib.mdg_upload_state.argtypes = [C.c_void_p, C.c_int, P(StateView)]
+    lib.mdg_download_state.argtypes = [C.c_void_p, C.c_int, P(StateView)]
+    lib.mdg_set_history.argtypes = [C.c_void_p, C.c_int, C.c_size_t, P(C.c_uint32), P(C.c_double)]
+    lib.mdg_get_history.argtypes = [C.c_void_p, C.c_int, P(C.c_uint32), P(C.c_double), C.c_size_t,
+                                    P(C.c_size_t)]
+    lib.mdg_step.argtypes = [C.c_void_p, C.c_int64]
+    lib.mdg_force_only.argtypes = [C.c_void_p]
+    lib.mdg_get_pairs.argtypes = [C.c_void_p, C.c_int, P(C.c_uint32), C.c_size_t, P(C.c_size_t)]
+    lib.mdg_thermo.argtypes = [C.c_void_p, C.c_int, P(Thermo)]
+    lib.mdg_synchronize.argtypes = [C.c_void_p]
+    lib.mdg_kernel_launches.argtypes = [C.c_void_p]
+    lib.mdg_kernel_launches.restype = C.c_int64
+    lib.mdg_set_graph_mode.argtypes = [C.c_void_p, C.c_int]
+    lib.mdg_timed_steps.argtypes = [C.c_void_p, C.c_int64, C.c_size_t, C.POINTER(StepTiming)]
+    _lib = lib
+    return lib
+
+
+def _check(status, what):
+    if status != MDG_OK:
+        raise MdgError(status, what)
+
+
+def _ptr(a, ct):
+    return None if a is None else a.ctypes.data_as(C.POINTER(ct))
+
+
+_KIND = {"dem": 0, "lj": 1}
+_PREC = {"fp64": 0, "mixed": 1}
+_POLICY = {"reference": 0, "displacement": 1}
+
+
+def to_c_config(c: SimConfig):
+    """Fill the C struct; returns (Config, keepalive) - keep both alive."""
+    mats = (Material * max(1, len(c.materials)))()
+    for k, m in enumerate(c.materials):
+        for f, _ in Material._fields_:
+            setattr(mats[k], f, float(getattr(m, f)))
+    cc = Config()
+    cc.kind = _KIND[c.kind]
+    cc.precision = _PREC[c.precision]
+    cc.box_lo[:] = [float(x) for x in c.box_lo]
+    cc.box_hi[:] = [float(x) for x in c.box_hi]
+    cc.dt = float(c.dt)
+    cc.skin_fraction = float(c.skin_fraction)
+    cc.bin_size = float(c.bin_size)
+    cc.every, cc.check, cc.sort_every, cc.newton = int(c.every), int(c.check), int(c.sort_every), int(c.newton)
+    cc.n_materials = len(c.materials) if c.kind == "dem" else 0
+    cc.materials = C.cast(mats, C.POINTER(Material))
+    cc.contact_model = {"hertz": 0, "hooke": 1}[c.contact_model]
+    cc.adhesion_model = {"jkr": 0, "dmt": 1}[c.adhesion_model]
+    cc.rolling_model = {"constant": 0, "sds": 1}[c.rolling_model]
+    cc.twisting_model = {"constant": 0, "sds": 1}[c.twisting_model]
+    cc.lj_epsilon, cc.lj_sigma, cc.lj_cutoff = float(c.lj_epsilon), float(c.lj_sigma), float(c.lj_cutoff)
+    cc.nose_hoover = int(c.nose_hoover)
+    cc.nh_temperature, cc.nh_coupling = float(c.nh_temperature), float(c.nh_coupling)
+    cc.virial = int(c.virial)
+    cc.rebuild_policy = _POLICY[c.rebuild_policy]
+    cc.threads_per_particle = int(c.threads_per_particle)
+    cc.neighbor_capacity = int(c.neighbor_capacity)
+    cc.history_capacity = int(c.history_capacity)
+    return cc, mats
+
+
+class Context:
+    """One device context advancing one or more independent systems."""
+
+    def __init__(self, configs, capacities):
+        if isinstance(configs, SimConfig):
+            configs, capacities = [configs], [capacities]
+        self.lib = load()
+        self.configs = list(configs)
+        n = len(self.configs)
+        arr = (Config * n)()
+        self._keep = []
+        for k, c in enumerate(self.configs):
+            cc, mats = to_c_config(c)
+            arr[k] = cc
+            self._keep.append(mats)
+        caps = (C.c_size_t * n)(*[int(x) for x in capacities])
+        h = C.c_void_p()
+        _check(self.lib.mdg_batch_create(arr, caps, n, C.byref(h)), "mdg_batch_create")
+        self.h = h
+        self.n = [0] * n
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mdg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- state -------------------------------------------------------------------
+    def upload(self, state, sys=0):
+        n = len(state["tag"])
+        keep = {k: np.ascontiguousarray(v) for k, v in state.items() if isinstance(v, np.ndarray)}
+        v = StateView()
+        v.n = n
+        v.tag = _ptr(keep["tag"].astype(np.uint32, copy=False), C.c_uint32)
+        t = keep.get("type")
+        v.type = _ptr(t.astype(np.uint32, copy=False), C.c_uint32) if t is not None else None
+        v.pos = _ptr(keep["pos"], C.c_double)
+        v.vel = _ptr(keep["vel"], C.c_double)
+        v.mass = _ptr(keep["mass"], C.c_double)
+        v.cutoff_radius = _ptr(keep["cutoff_radius"], C.c_double)
+        if "image" in keep:
+            keep["image"] = keep["image"].astype(np.int32)
+            v.image = _ptr(keep["image"], C.c_int32)
+        for f in ("radius", "inv_inertia", "omega", "quat"):
+            if f in keep:
+                setattr(v, f, _ptr(keep[f], C.c_double))
+        _check(self.lib.mdg_upload_state(self.h, sys, C.byref(v)), "mdg_upload_state")
+        self.n[sys] = n
+
+    def download(self, sys=0):
+        n = self.n[sys]
+        dem = self.configs[sys].kind == "dem"
+        out = {
+            "tag": np.zeros(n, np.uint32), "type": np.zeros(n, np.uint32), "pos": np.zeros((n, 3)),
+            "vel": np.zeros((n, 3)), "force": np.zeros((n, 3)), "mass": np.zeros(n),
+            "cutoff_radius": np.zeros(n), "image": np.zeros((n, 3), np.int32),
+        }
+        if dem:
+            out.update(radius=np.zeros(n), inv_inertia=np.zeros(n), omega=np.zeros((n, 3)),
+                       torque=np.zeros((n, 3)), quat=np.zeros((n, 4)))
+        v = StateView()
+        v.n = n
+        v.tag = _ptr(out["tag"], C.c_uint32)
+        v.type = _ptr(out["type"], C.c_uint32)
+        v.image = _ptr(out["image"], C.c_int32)
+        for f in ("pos", "vel", "force", "mass", "cutoff_radius", "radius", "inv_inertia", "omega", "torque", "quat"):
+            if f in out:
+                setattr(v, f, _ptr(out[f], C.c_double))
+        _check(self.lib.mdg_download_state(self.h, sys, C.byref(v)), "mdg_download_state")
+        return out
+
+    def step(self, nsteps=1):
+        _check(self.lib.mdg_step(self.h, int(nsteps)), "mdg_step")
+
+    def force_only(self):
+        _check(self.lib.mdg_force_only(self.h), "mdg_force_only")
+
+    def pairs(self, sys=0):
+        cnt = C.c_size_t()
+        _check(self.lib.mdg_get_pairs(self.h, sys, None, 0, C.byref(cnt)), "mdg_get_pairs")
+        buf = np.zeros((max(1, cnt.value), 2), np.uint32)
+        _check(self.lib.mdg_get_pairs(self.h, sys, _ptr(buf, C.c_uint32), cnt.value, C.byref(cnt)),
+               "mdg_get_pairs")
+        return buf[: cnt.value]
+
+    def history(self, sys=0):
+        cnt = C.c_size_t()
+        _check(self.lib.mdg_get_history(self.h, sys, None, None, 0, C.byref(cnt)), "mdg_get_history")
+        keys = np.zeros((max(1, cnt.value), 2), np.uint32)
+        vals = np.zeros((max(1, cnt.value), 7))
+        _check(self.lib.mdg_get_history(self.h, sys, _ptr(keys, C.c_uint32), _ptr(vals, C.c_double), cnt.value,
+                                        C.byref(cnt)), "mdg_get_history")
+        return keys[: cnt.value], vals[: cnt.value]
+
+    def set_history(self, keys, vals, sys=0):
+        keys = np.ascontiguousarray(keys, np.uint32)
+        vals = np.ascontiguousarray(vals, np.float64)
+        _check(self.lib.mdg_set_history(self.h, sys, len(keys), _ptr(keys, C.c_uint32), _ptr(vals, C.c_double)),
+               "mdg_set_history")
+
+    def thermo(self, sys=0):
+        t = Thermo()
+        _check(self.lib.mdg_thermo(self.h, sys, C.byref(t)), "mdg_thermo")
+        return {f: (list(getattr(t, f)) if f == "virial" else getattr(t, f)) for f, _ in Thermo._fields_}
+
+    def synchronize(self):
+        _check(self.lib.mdg_synchronize(self.h), "mdg_synchronize")
+
+    def launches(self):
+        return int(self.lib.mdg_kernel_launches(self.h))
+
+    def timed_steps(self, nsteps, l2_flush_bytes=0):
+        """Per-step device timings (ms): array (nsteps, 5) = step, initial,
+        rebuild, force, final; plus kernels per step and rebuild flags."""
+        buf = (StepTiming * max(1, nsteps))()
+        _check(self.lib.mdg_timed_steps(self.h, int(nsteps), int(l2_flush_bytes), buf), "mdg_timed_steps")
+        t = np.array([[b.step_ms, *b.phase_ms] for b in buf[:nsteps]])
+        return t, np.array([b.kernels for b in buf[:nsteps]]), np.array([b.rebuilt for b in buf[:nsteps]])
+
+    def set_graph_mode(self, on):
+        _check(self.lib.mdg_set_graph_mode(self.h, int(on)), "mdg_set_graph_mode")

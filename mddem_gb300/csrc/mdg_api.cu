@@ -1,0 +1,997 @@
+// mdg_api.cu -- host implementation of the C ABI declared in include/mdg.h.
+//
+// Owns the device state of one context (one or more systems), restates the
+// reference's setup computations on the host (neighbor_setup/compute_bin_grid,
+// MaterialTable::build_pair_tables, LJPairCoeffs::from_params,
+// setup_nose_hoover) and drives the per-step kernel sequence, eagerly or as
+// captured CUDA graphs.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <map>
+#include <new>
+#include <vector>
+
+#include "../../include/mdg.h"
+#include "mdg_internal.cuh"
+
+using namespace mdg;
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+
+template <class T>
+T* dalloc(size_t n, int& err) {
+    if (err) return nullptr;
+    if (n == 0) n = 1;
+    void* p = nullptr;
+    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) {
+        cudaGetLastError();
+        err = MDG_ERR_OOM;
+        return nullptr;
+    }
+    cudaMemset(p, 0, n * sizeof(T));
+    return static_cast<T*>(p);
+}
+
+inline long long round_up(long long a, long long b) { return (a + b - 1) / b * b; }
+
+// MaterialTable::build_pair_tables (crates/dem_atom/src/lib.rs:389-515):
+// packed [table][i][j] for one system.
+void material_tables(const mdg_material* m, int n, std::vector<double>& out) {
+    const size_t nn = (size_t)n * n;
+    out.assign(nn * NTAB, 0.0);
+    auto at = [&](int t, int i, int j) -> double& { return out[(size_t)t * nn + (size_t)i * n + j]; };
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) {
+            const double e_ij = std::sqrt(m[i].restitution * m[j].restitution);
+            const double log_e = std::log(e_ij);
+            at(T_BETA, i, j) = -log_e / std::sqrt(kPi * kPi + log_e * log_e);
+            at(T_FRICTION, i, j) = std::sqrt(m[i].friction * m[j].friction);
+            at(T_ROLL_FRICTION, i, j) = std::sqrt(m[i].rolling_friction * m[j].rolling_friction);
+            at(T_COHESION, i, j) = std::sqrt(m[i].cohesion_energy * m[j].cohesion_energy);
+            at(T_SURFACE, i, j) = std::sqrt(m[i].surface_energy * m[j].surface_energy);
+            at(T_TWIST_FRICTION, i, j) =
+                std::sqrt(std::fmax(m[i].twisting_friction, 0.0) * std::fmax(m[j].twisting_friction, 0.0));
+            const double nu_i = m[i].poisson_ratio, nu_j = m[j].poisson_ratio;
+            at(T_EEFF, i, j) = 1.0 / ((1.0 - nu_i * nu_i) / m[i].youngs_mod + (1.0 - nu_j * nu_j) / m[j].youngs_mod);
+            at(T_GEFF, i, j) = 1.0 / (2.0 * (2.0 - nu_i) * (1.0 + nu_i) / m[i].youngs_mod +
+                                      2.0 * (2.0 - nu_j) * (1.0 + nu_j) / m[j].youngs_mod);
+            const double ki = m[i].kn, kj = m[j].kn;
+            at(T_KN, i, j) = (ki > 0.0 && kj > 0.0) ? 2.0 * ki * kj / (ki + kj) : 0.0;
+            const double kti = m[i].kt, ktj = m[j].kt;
+            at(T_KT, i, j) = (kti > 0.0 && ktj > 0.0) ? 2.0 * kti * ktj / (kti + ktj) : 0.0;
+            const double kri = m[i].rolling_stiffness, krj = m[j].rolling_stiffness;
+            at(T_KROLL, i, j) = (kri > 0.0 && krj > 0.0) ? 2.0 * kri * krj / (kri + krj) : (kri > 0.0 ? kri : krj);
+            at(T_GROLL, i, j) = std::sqrt(std::fmax(m[i].rolling_damping, 0.0) * std::fmax(m[j].rolling_damping, 0.0));
+            const double kwi = m[i].twisting_stiffness, kwj = m[j].twisting_stiffness;
+            at(T_KTWIST, i, j) = (kwi > 0.0 && kwj > 0.0) ? 2.0 * kwi * kwj / (kwi + kwj) : (kwi > 0.0 ? kwi : kwj);
+            at(T_GTWIST, i, j) =
+                std::sqrt(std::fmax(m[i].twisting_damping, 0.0) * std::fmax(m[j].twisting_damping, 0.0));
+        }
+}
+
+int validate_config(const mdg_config& c) {
+    if (c.kind != MDG_KIND_DEM && c.kind != MDG_KIND_LJ) return MDG_ERR_CONFIG;
+    if (c.precision != MDG_FP64 && c.precision != MDG_MIXED) return MDG_ERR_CONFIG;
+    if (!(c.dt > 0.0) || !std::isfinite(c.dt)) return MDG_ERR_CONFIG;
+    for (int d = 0; d < 3; d++)
+        if (!(c.box_hi[d] > c.box_lo[d])) return MDG_ERR_CONFIG;
+    if (!(c.skin_fraction >= 1.0) || !(c.bin_size > 0.0)) return MDG_ERR_CONFIG;
+    if (c.every < 0 || c.sort_every < 0) return MDG_ERR_CONFIG;
+    if (c.kind == MDG_KIND_DEM) {
+        if (c.n_materials < 1 || !c.materials) return MDG_ERR_CONFIG;
+        for (int k = 0; k < c.n_materials; k++) {
+            const mdg_material& m = c.materials[k];
+            if (!(m.youngs_mod > 0.0) || !(m.restitution > 0.0) || m.restitution > 1.0) return MDG_ERR_CONFIG;
+            if (m.poisson_ratio < 0.0 || m.poisson_ratio >= 0.5) return MDG_ERR_CONFIG;
+        }
+        if (c.contact_model == MDG_CONTACT_HOOKE) {
+            for (int k = 0; k < c.n_materials; k++)
+                if (!(c.materials[k].kn > 0.0)) return MDG_ERR_CONFIG;
+        }
+    } else {
+        if (!(c.lj_epsilon > 0.0) || !(c.lj_sigma > 0.0) || !(c.lj_cutoff > 0.0)) return MDG_ERR_CONFIG;
+    }
+    if (c.nose_hoover && (!(c.nh_temperature > 0.0) || !(c.nh_coupling > 0.0))) return MDG_ERR_CONFIG;
+    if (c.precision == MDG_MIXED && (c.kind == MDG_KIND_DEM || c.virial)) return MDG_ERR_CONFIG;
+    const int t = c.threads_per_particle;
+    if (!(t == 0 || t == 1 || t == 2 || t == 4 || t == 8)) return MDG_ERR_CONFIG;
+    if (c.neighbor_capacity < 0 || c.history_capacity < 0) return MDG_ERR_CONFIG;
+    return MDG_OK;
+}
+
+}  // namespace
+
+struct mdg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int nsys = 0;
+    std::vector<mdg_config> cfg;
+    std::vector<std::vector<mdg_material>> mats;
+    std::vector<SysParams> sp;
+    std::vector<size_t> capacity;
+    std::vector<int> uploaded;
+    std::vector<int> ncap_sys;  // current list capacity per system
+    Dev d{};
+    int hcur = 0;
+    bool has_lj = false, has_dem = false, has_mixed = false, any_virial = false;
+    int tpp_lj = 1;
+    long long cells_alloc = 0, lst_alloc = 0;
+    int* d_blk_sys = nullptr;
+    int* d_cblk_sys = nullptr;
+    int* d_cblk0 = nullptr;
+    SysParams* d_sp = nullptr;
+    double* d_mat = nullptr;
+    double* d_thermo = nullptr;
+    std::vector<long long> mat_off;
+    int graph_mode = 1;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t tgraph[2] = {nullptr, nullptr};  // timed single-step graphs
+    cudaEvent_t tev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    int tkernels = 0;
+    void* flush_buf = nullptr;
+    size_t flush_bytes = 0;
+    int graph_steps = 0;
+    long long launches = 0;
+    std::vector<void*> allocs;
+
+    ~mdg_ctx() {
+        for (int k = 0; k < 2; k++) {
+            if (graph[k]) cudaGraphExecDestroy(graph[k]);
+            if (tgraph[k]) cudaGraphExecDestroy(tgraph[k]);
+        }
+        for (auto& e : tev)
+            if (e) cudaEventDestroy(e);
+        if (flush_buf) cudaFree(flush_buf);
+        for (void* p : allocs) cudaFree(p);
+        if (stream) cudaStreamDestroy(stream);
+    }
+    template <class T>
+    T* alloc(size_t n, int& err) {
+        T* p = dalloc<T>(n, err);
+        if (p) allocs.push_back(p);
+        return p;
+    }
+    void free_ptr(void* p) {
+        if (!p) return;
+        auto it = std::find(allocs.begin(), allocs.end(), p);
+        if (it != allocs.end()) allocs.erase(it);
+        cudaFree(p);
+    }
+    void drop_graphs() {
+        for (int k = 0; k < 2; k++) {
+            if (graph[k]) {
+                cudaGraphExecDestroy(graph[k]);
+                graph[k] = nullptr;
+            }
+            if (tgraph[k]) {
+                cudaGraphExecDestroy(tgraph[k]);
+                tgraph[k] = nullptr;
+            }
+        }
+    }
+};
+
+namespace {
+
+int cuda_err(cudaError_t e) {
+    if (e == cudaSuccess) return MDG_OK;
+    if (e == cudaErrorMemoryAllocation) return MDG_ERR_OOM;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return MDG_ERR_NODEVICE;
+    return MDG_ERR_CUDA;
+}
+
+// neighbor_setup + compute_bin_grid (crates/mddem_core/src/neighbor.rs:480-541,
+// 290-371) for one rank, from the uploaded cutoff radii.
+int setup_grid(const mdg_config& c, const double* cutr, size_t n, SysParams& p) {
+    double max_skin = 0.0, min_skin = std::numeric_limits<double>::max();
+    for (size_t i = 0; i < n; i++) {
+        max_skin = std::fmax(max_skin, cutr[i]);
+        min_skin = std::fmin(min_skin, cutr[i]);
+    }
+    const double sf = c.skin_fraction;
+    double bin_min = c.bin_size;
+    const double max_cutoff = max_skin > 0.0 ? 2.0 * max_skin * sf : bin_min;
+    const double disp_buf = (min_skin < std::numeric_limits<double>::max() * 0.5) ? (sf - 1.0) * min_skin : 0.0;
+    const double ghost_cutoff = std::fmax(max_cutoff + 2.0 * disp_buf, 0.0);
+    if (bin_min < max_cutoff) bin_min = max_cutoff;
+    const double min_bin = std::fmax(bin_min, max_cutoff);
+    const double ghost_cut = ghost_cutoff > max_cutoff ? ghost_cutoff : max_cutoff;
+    long long ncell = 1;
+    for (int d = 0; d < 3; d++) {
+        p.lo[d] = c.box_lo[d];
+        p.hi[d] = c.box_hi[d];
+        p.L[d] = c.box_hi[d] - c.box_lo[d];
+        const int xi = (int)std::fmax(std::floor(p.L[d] / min_bin), 1.0);
+        p.nc[d] = xi;
+        p.bin[d] = p.L[d] / (double)xi;
+        p.inv_bin[d] = 1.0 / p.bin[d];
+        const int sr = (int)std::ceil(max_cutoff / p.bin[d]);
+        p.sl[d] = (int)std::ceil(ghost_cut / p.bin[d]) + sr;
+        p.ext[d] = xi + 2 * p.sl[d];
+        p.origin[d] = p.lo[d] - p.bin[d] * (double)p.sl[d];
+        p.win[d] = sr;
+        ncell *= p.ext[d];
+        // one periodic image per neighbour: the box must exceed twice the list cutoff
+        if (!(p.L[d] > 2.0 * max_cutoff)) return MDG_ERR_CONFIG;
+        if (p.win[d] > xi) return MDG_ERR_CONFIG;
+    }
+    if (ncell > (1LL << 30)) return MDG_ERR_CONFIG;
+    p.ncell = (int)ncell;
+    p.max_cutoff = max_cutoff;
+    p.stencil_cut_sq = max_cutoff * max_cutoff;
+    p.skin_fraction = sf;
+    p.sf2 = sf * sf;
+    p.min_skin = min_skin;
+    p.uniform = std::fabs(max_skin - min_skin) < 1e-15;
+    const double uc = 2.0 * min_skin * sf;
+    p.uniform_cutoff_sq = uc * uc;
+    const double per_atom_skin = (sf - 1.0) * min_skin;
+    p.disp_thr_sq = per_atom_skin * per_atom_skin;
+    // fp32 prefilter: bound the error of (x_j_hi + s L_f) - x_i_hi per axis
+    double xmax = 0.0;
+    for (int d = 0; d < 3; d++) xmax = std::fmax(xmax, std::fmax(std::fabs(p.lo[d]), std::fabs(p.hi[d])) + 2.0 * p.L[d]);
+    const double E = 8.0 * std::ldexp(1.0, -24) * xmax;
+    const double rpre = max_cutoff + 2.0 * std::sqrt(3.0) * E;
+    p.pre_cut2 = std::nextafter((float)(rpre * rpre * (1.0 + 1e-5)), std::numeric_limits<float>::infinity());
+    return MDG_OK;
+}
+
+int auto_ncap(const mdg_config& c, const SysParams& p, size_t n) {
+    if (c.neighbor_capacity > 0) return c.neighbor_capacity;
+    const double vol = p.L[0] * p.L[1] * p.L[2];
+    const double rho = (double)n / vol;
+    const double rc = p.max_cutoff;
+    const double expect = rho * 4.0 / 3.0 * kPi * rc * rc * rc;
+    int cap;
+    if (c.kind == MDG_KIND_LJ) cap = (int)std::ceil(expect * 1.4) + 24;
+    else cap = std::max(32, (int)std::ceil(expect * 3.0) + 24);
+    return std::min(cap, 1024);
+}
+
+int sys_status_to_err(int st) {
+    if (st & ST_OVERLAP) return MDG_ERR_OVERLAP_LIMIT;
+    if (st & ST_NAN) return MDG_ERR_NAN;
+    if (st & (ST_NBR_OVF | ST_HIST_OVF)) return MDG_ERR_LIST_OVERFLOW;
+    if (st & ST_TIMEOUT) return MDG_ERR_TIMEOUT;
+    return MDG_OK;
+}
+
+// (Re)compute cell and list segment offsets; (re)allocate when they grow.
+// Cell arrays only live within one rebuild, so they are simply reallocated.
+// Neighbour-list blocks of systems other than `fresh` (whose list is rebuilt
+// on its next step anyway) are copied to their new offsets, so a system
+// uploaded into a running batch does not disturb the others.
+int ensure_layout(mdg_ctx* c, int fresh = -1) {
+    int err = 0;
+    long long cells = 0;
+    std::vector<int> cblk_sys, cblk0(c->nsys);
+    std::vector<long long> old_lst0(c->nsys);
+    long long lst = 0;
+    for (int s = 0; s < c->nsys; s++) {
+        SysParams& p = c->sp[s];
+        p.c0 = (int)cells;
+        const long long seg = round_up((long long)p.ncell + 1, BLK);
+        cblk0[s] = (int)(cells / BLK);
+        for (long long b = 0; b < seg / BLK; b++) cblk_sys.push_back(s);
+        cells += seg;
+        old_lst0[s] = p.lst0;
+        p.lst0 = lst;
+        lst += (long long)p.ncap * p.npad;
+    }
+    bool realloc_cells = cells > c->cells_alloc;
+    bool moved = false;
+    for (int s = 0; s < c->nsys; s++)
+        if (s != fresh && c->uploaded[s] && old_lst0[s] != c->sp[s].lst0) moved = true;
+    bool realloc_lst = lst > c->lst_alloc || moved;
+    if (realloc_cells) {
+        c->free_ptr(c->d.cnt);
+        c->free_ptr(c->d.cstart);
+        c->free_ptr(c->d_cblk_sys);
+        c->d.cnt = c->alloc<int>(cells, err);
+        c->d.cstart = c->alloc<int>(cells, err);
+        c->d_cblk_sys = c->alloc<int>(cells / BLK, err);
+        if (err) return err;
+        c->cells_alloc = cells;
+        c->drop_graphs();
+    }
+    if (realloc_lst) {
+        const long long cap = std::max(lst, c->lst_alloc);
+        uint32_t* nl = c->alloc<uint32_t>(cap, err);
+        if (err) return err;
+        if (c->d.nlist) {
+            for (int s = 0; s < c->nsys; s++) {
+                if (s == fresh || !c->uploaded[s]) continue;
+                const SysParams& p = c->sp[s];
+                cudaMemcpy(nl + p.lst0, c->d.nlist + old_lst0[s], (size_t)p.ncap * p.npad * sizeof(uint32_t),
+                           cudaMemcpyDeviceToDevice);
+            }
+        }
+        c->free_ptr(c->d.nlist);
+        c->d.nlist = nl;
+        c->lst_alloc = cap;
+        c->drop_graphs();
+    }
+    cudaMemcpy(c->d_cblk_sys, cblk_sys.data(), cblk_sys.size() * sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpy(c->d_cblk0, cblk0.data(), cblk0.size() * sizeof(int), cudaMemcpyHostToDevice);
+    c->d.cblk_sys = c->d_cblk_sys;
+    c->d.cblk0 = c->d_cblk0;
+    c->d.ncblocks = (int)(cells / BLK);
+    cudaMemcpy(c->d_sp, c->sp.data(), c->nsys * sizeof(SysParams), cudaMemcpyHostToDevice);
+    return cuda_err(cudaGetLastError());
+}
+
+int enqueue_step(mdg_ctx* c, int hcur, cudaStream_t st) {
+    int n = 0;
+    n += launch_initial(c->d, st);
+    n += launch_rebuild(c->d, hcur, st);
+    if (c->has_mixed) n += launch_force_mixed(c->d, hcur, c->has_lj, c->has_dem, c->tpp_lj, st);
+    else n += launch_force_fp64(c->d, hcur, c->has_lj, c->has_dem, c->tpp_lj, st);
+    n += launch_final(c->d, st, 1);
+    return n;
+}
+
+int build_graph(mdg_ctx* c, int hstart) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_err(e);
+    int h = hstart;
+    for (int k = 0; k < c->graph_steps; k++) {
+        enqueue_step(c, h, c->stream);
+        h ^= 1;
+    }
+    e = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) return cuda_err(e);
+    e = cudaGraphInstantiate(&c->graph[hstart], g, 0);
+    cudaGraphDestroy(g);
+    return cuda_err(e);
+}
+
+// One step captured with event records between its phases.
+int build_timed_graph(mdg_ctx* c, int h) {
+    for (auto& e : c->tev)
+        if (!e && cudaEventCreate(&e) != cudaSuccess) return MDG_ERR_CUDA;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_err(e);
+    int n = 0;
+    cudaEventRecordWithFlags(c->tev[0], c->stream, cudaEventRecordExternal);
+    n += launch_initial(c->d, c->stream);
+    cudaEventRecordWithFlags(c->tev[1], c->stream, cudaEventRecordExternal);
+    n += launch_rebuild(c->d, h, c->stream);
+    cudaEventRecordWithFlags(c->tev[2], c->stream, cudaEventRecordExternal);
+    if (c->has_mixed) n += launch_force_mixed(c->d, h, c->has_lj, c->has_dem, c->tpp_lj, c->stream);
+    else n += launch_force_fp64(c->d, h, c->has_lj, c->has_dem, c->tpp_lj, c->stream);
+    cudaEventRecordWithFlags(c->tev[3], c->stream, cudaEventRecordExternal);
+    n += launch_final(c->d, c->stream, 1);
+    cudaEventRecordWithFlags(c->tev[4], c->stream, cudaEventRecordExternal);
+    e = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) return cuda_err(e);
+    e = cudaGraphInstantiate(&c->tgraph[h], g, 0);
+    cudaGraphDestroy(g);
+    c->tkernels = n;
+    return cuda_err(e);
+}
+
+int check_status(mdg_ctx* c) {
+    std::vector<SysState> ss(c->nsys);
+    cudaError_t e = cudaMemcpy(ss.data(), c->d.ss, c->nsys * sizeof(SysState), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(e);
+    for (int s = 0; s < c->nsys; s++) {
+        int r = sys_status_to_err(ss[s].status);
+        if (r) return r;
+    }
+    return MDG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mdg_abi_version(void) { return MDG_ABI_VERSION; }
+
+const char* mdg_status_string(int s) {
+    switch (s) {
+        case MDG_OK: return "ok";
+        case MDG_ERR_CONFIG: return "invalid configuration";
+        case MDG_ERR_CUDA: return "CUDA runtime error";
+        case MDG_ERR_OOM: return "device allocation failed";
+        case MDG_ERR_BUDGET: return "request exceeds the HBM budget";
+        case MDG_ERR_OVERLAP_LIMIT: return "more than 500 large overlaps in one step";
+        case MDG_ERR_NAN: return "non-finite value in the particle state";
+        case MDG_ERR_LIST_OVERFLOW: return "neighbor or contact-history capacity exceeded";
+        case MDG_ERR_TIMEOUT: return "bounded device wait gave up";
+        case MDG_ERR_ARG: return "bad argument";
+        case MDG_ERR_STATE: return "call out of order";
+        case MDG_ERR_NODEVICE: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+int mdg_device_count(int* count) {
+    if (!count) return MDG_ERR_ARG;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *count = 0;
+        return MDG_ERR_NODEVICE;
+    }
+    *count = n;
+    return MDG_OK;
+}
+
+int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, mdg_ctx** out) {
+    if (!cfgs || !capacity || nsys < 1 || !out) return MDG_ERR_ARG;
+    *out = nullptr;
+    for (int s = 0; s < nsys; s++) {
+        int r = validate_config(cfgs[s]);
+        if (r) return r;
+        if (capacity[s] < 1 || capacity[s] > (size_t)IDX_MASK) return MDG_ERR_ARG;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return MDG_ERR_NODEVICE;
+    }
+    mdg_ctx* c = new (std::nothrow) mdg_ctx();
+    if (!c) return MDG_ERR_OOM;
+    cudaGetDevice(&c->device);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return MDG_ERR_CUDA;
+    }
+    c->nsys = nsys;
+    c->cfg.assign(cfgs, cfgs + nsys);
+    c->mats.resize(nsys);
+    c->sp.assign(nsys, SysParams{});
+    c->capacity.assign(capacity, capacity + nsys);
+    c->uploaded.assign(nsys, 0);
+    long long P = 0;
+    int nblocks = 0;
+    long long hist_entries = 0;
+    std::vector<int> blk_sys;
+    std::vector<double> mat_all;
+    int has_mixed = -1;
+    for (int s = 0; s < nsys; s++) {
+        const mdg_config& k = cfgs[s];
+        SysParams& p = c->sp[s];
+        p.kind = k.kind;
+        p.precision = k.precision;
+        if (has_mixed < 0) has_mixed = k.precision;
+        else if (has_mixed != k.precision) {
+            delete c;
+            return MDG_ERR_CONFIG;  // one precision per context
+        }
+        p.contact_model = k.contact_model;
+        p.adhesion_model = k.adhesion_model;
+        p.rolling_model = k.rolling_model;
+        p.twisting_model = k.twisting_model;
+        p.npad = (int)round_up((long long)capacity[s], BLK);
+        p.p0 = (int)P;
+        p.n = 0;
+        p.b0 = nblocks;
+        p.nb = p.npad / BLK;
+        for (int b = 0; b < p.nb; b++) blk_sys.push_back(s);
+        nblocks += p.nb;
+        P += p.npad;
+        p.dt = k.dt;
+        p.policy = k.rebuild_policy;
+        p.every = k.every;
+        p.check = k.check;
+        p.sort_every = k.sort_every;
+        p.newton = k.newton;
+        p.virial = k.virial;
+        p.tpp = k.threads_per_particle ? k.threads_per_particle : 1;
+        p.ncap = 0;
+        if (k.kind == MDG_KIND_DEM) {
+            c->has_dem = true;
+            c->mats[s].assign(k.materials, k.materials + k.n_materials);
+            c->cfg[s].materials = c->mats[s].data();
+            std::vector<double> tabs;
+            material_tables(k.materials, k.n_materials, tabs);
+            p.nmat = k.n_materials;
+            p.mat0 = (long long)mat_all.size();
+            mat_all.insert(mat_all.end(), tabs.begin(), tabs.end());
+            p.hcap = k.history_capacity ? k.history_capacity : 24;
+            p.h0 = hist_entries;
+            hist_entries += (long long)p.hcap * p.npad;
+        } else {
+            c->has_lj = true;
+            // LJPairCoeffs::from_params (crates/md_lj/src/lib.rs:230-239)
+            const double s2 = k.lj_sigma * k.lj_sigma;
+            const double sigma6 = s2 * s2 * s2;
+            p.lj1 = 48.0 * k.lj_epsilon * sigma6 * sigma6;
+            p.lj2 = 24.0 * k.lj_epsilon * sigma6;
+            p.lj3 = 4.0 * k.lj_epsilon * sigma6 * sigma6;
+            p.lj4 = 4.0 * k.lj_epsilon * sigma6;
+            const double rc = k.lj_cutoff * k.lj_sigma;
+            p.lj_cut2 = rc * rc;
+            p.nmat = 1;
+            p.mat0 = 0;
+            p.hcap = 0;
+        }
+        if (k.virial) c->any_virial = true;
+        if (k.threads_per_particle > 1) c->tpp_lj = k.threads_per_particle;
+    }
+    if (P > (long long)IDX_MASK * 8) {
+        delete c;
+        return MDG_ERR_ARG;
+    }
+    c->has_mixed = has_mixed == MDG_MIXED;
+    int err = 0;
+    Dev& d = c->d;
+    d.P = P;
+    d.nsys = nsys;
+    d.nblocks = nblocks;
+    d.pos = c->alloc<double4>(P, err);
+    d.vel = c->alloc<double4>(P, err);
+    d.frc = c->alloc<double4>(P, err);
+    d.lbp = c->alloc<double4>(P, err);
+    d.mass = c->alloc<double>(P, err);
+    d.cutr = c->alloc<double>(P, err);
+    d.tag = c->alloc<uint32_t>(P, err);
+    d.type = c->alloc<uint32_t>(P, err);
+    d.img = c->alloc<int4>(P, err);
+    d.nnum = c->alloc<int>(P, err);
+    d.cell = c->alloc<int>(P, err);
+    d.perm = c->alloc<int>(P, err);
+    d.s_pos = c->alloc<double4>(P, err);
+    d.s_vel = c->alloc<double4>(P, err);
+    d.s_mass = c->alloc<double>(P, err);
+    d.s_cutr = c->alloc<double>(P, err);
+    d.s_tag = c->alloc<uint32_t>(P, err);
+    d.s_type = c->alloc<uint32_t>(P, err);
+    d.s_img = c->alloc<int4>(P, err);
+    d.pos_hi = c->alloc<float4>(P, err);
+    d.pos_lo = c->alloc<float4>(P, err);
+    if (c->has_dem) {
+        d.omg = c->alloc<double4>(P, err);
+        d.trq = c->alloc<double4>(P, err);
+        d.quat = c->alloc<double4>(P, err);
+        d.s_omg = c->alloc<double4>(P, err);
+        d.s_quat = c->alloc<double4>(P, err);
+        d.hist_any = 1;
+        for (int b = 0; b < 2; b++) {
+            d.hcnt[b] = c->alloc<int>(P, err);
+            d.htag[b] = c->alloc<uint32_t>(hist_entries, err);
+            d.hval[b] = c->alloc<double>(hist_entries * 7, err);
+        }
+        d.s_hcnt = c->alloc<int>(P, err);
+        d.s_htag = c->alloc<uint32_t>(hist_entries, err);
+        d.s_hval = c->alloc<double>(hist_entries * 7, err);
+    }
+    if (c->any_virial) d.vir = c->alloc<double>(6 * P, err);
+    d.blkpart = c->alloc<double>((size_t)nblocks * 8, err);
+    c->d_blk_sys = c->alloc<int>(nblocks, err);
+    c->d_cblk0 = c->alloc<int>(nsys, err);
+    c->d_sp = c->alloc<SysParams>(nsys, err);
+    d.ss = c->alloc<SysState>(nsys, err);
+    c->d_mat = c->alloc<double>(std::max<size_t>(mat_all.size(), 1), err);
+    c->d_thermo = c->alloc<double>((size_t)nsys * 16, err);
+    if (err) {
+        delete c;
+        return err;
+    }
+    cudaMemcpy(c->d_blk_sys, blk_sys.data(), blk_sys.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (!mat_all.empty())
+        cudaMemcpy(c->d_mat, mat_all.data(), mat_all.size() * sizeof(double), cudaMemcpyHostToDevice);
+    d.blk_sys = c->d_blk_sys;
+    d.sp = c->d_sp;
+    d.mat = c->d_mat;
+    for (int s = 0; s < nsys; s++) {
+        // a placeholder grid until the first upload
+        SysParams& p = c->sp[s];
+        p.ncell = 1;
+        p.ncap = 1;
+    }
+    int r = ensure_layout(c);
+    if (r) {
+        delete c;
+        return r;
+    }
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        delete c;
+        return cuda_err(e);
+    }
+    c->graph_steps = 2;
+    *out = c;
+    return MDG_OK;
+}
+
+int mdg_create(const mdg_config* cfg, size_t capacity, mdg_ctx** out) {
+    return mdg_batch_create(cfg, &capacity, 1, out);
+}
+
+void mdg_destroy(mdg_ctx* c) { delete c; }
+
+int mdg_num_systems(const mdg_ctx* c) { return c ? c->nsys : 0; }
+
+int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
+    if (!c || !st || sys < 0 || sys >= c->nsys) return MDG_ERR_ARG;
+    const mdg_config& k = c->cfg[sys];
+    const size_t n = st->n;
+    if (n < 2 || n > c->capacity[sys]) return MDG_ERR_ARG;
+    if (!st->tag || !st->pos || !st->vel || !st->mass || !st->cutoff_radius) return MDG_ERR_ARG;
+    if (k.kind == MDG_KIND_DEM && (!st->radius || !st->inv_inertia)) return MDG_ERR_ARG;
+    SysParams& p = c->sp[sys];
+    for (size_t i = 0; i < n; i++) {
+        for (int q = 0; q < 3; q++)
+            if (!std::isfinite(st->pos[3 * i + q]) || !std::isfinite(st->vel[3 * i + q])) return MDG_ERR_NAN;
+        if (!(st->mass[i] > 0.0) || !(st->cutoff_radius[i] > 0.0)) return MDG_ERR_ARG;
+        if (st->type && k.kind == MDG_KIND_DEM && (int)st->type[i] >= k.n_materials) return MDG_ERR_ARG;
+    }
+    int r = setup_grid(k, st->cutoff_radius, n, p);
+    if (r) return r;
+    p.n = (int)n;
+    const int ncap = auto_ncap(k, p, n);
+    p.ncap = ncap;
+    if (k.nose_hoover) {
+        // setup_nose_hoover (crates/md_thermostat/src/lib.rs:195-243)
+        p.nh = 1;
+        p.nh_ndof = 3.0 * (double)n - 3.0;
+        p.nh_T = k.nh_temperature;
+        p.nh_Q = p.nh_ndof * p.nh_T * k.nh_coupling * k.nh_coupling;
+    } else {
+        p.nh = 0;
+    }
+    r = ensure_layout(c, sys);
+    if (r) return r;
+    const size_t np = (size_t)p.npad;
+    std::vector<double4> pos(np), vel(np), zero4(np), omg, quat;
+    std::vector<double> mass(np, 1.0), cutr(np, 0.0);
+    std::vector<uint32_t> tag(np, 0xffffffffu), type(np, 0);
+    std::vector<int4> img(np);
+    std::vector<int> zi(np, 0);
+    for (size_t i = 0; i < np; i++) {
+        zero4[i] = make_double4(0, 0, 0, 0);
+        img[i] = make_int4(0, 0, 0, 0);
+        pos[i] = zero4[i];
+        vel[i] = zero4[i];
+    }
+    const bool dem = k.kind == MDG_KIND_DEM;
+    if (dem) {
+        omg.assign(np, zero4[0]);
+        quat.assign(np, make_double4(1, 0, 0, 0));
+    }
+    for (size_t i = 0; i < n; i++) {
+        pos[i] = make_double4(st->pos[3 * i], st->pos[3 * i + 1], st->pos[3 * i + 2], dem ? st->radius[i] : 0.0);
+        vel[i] = make_double4(st->vel[3 * i], st->vel[3 * i + 1], st->vel[3 * i + 2], 1.0 / st->mass[i]);
+        mass[i] = st->mass[i];
+        cutr[i] = st->cutoff_radius[i];
+        tag[i] = st->tag[i];
+        type[i] = st->type ? st->type[i] : 0;
+        if (st->image) img[i] = make_int4(st->image[3 * i], st->image[3 * i + 1], st->image[3 * i + 2], 0);
+        if (dem) {
+            const double* w = st->omega;
+            omg[i] = make_double4(w ? w[3 * i] : 0.0, w ? w[3 * i + 1] : 0.0, w ? w[3 * i + 2] : 0.0, st->inv_inertia[i]);
+            if (st->quat)
+                quat[i] = make_double4(st->quat[4 * i], st->quat[4 * i + 1], st->quat[4 * i + 2], st->quat[4 * i + 3]);
+        }
+    }
+    const size_t o = (size_t)p.p0;
+    Dev& d = c->d;
+    cudaStream_t s0 = c->stream;
+    cudaMemcpyAsync(d.pos + o, pos.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
+    cudaMemcpyAsync(d.lbp + o, pos.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
+    cudaMemcpyAsync(d.vel + o, vel.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
+    cudaMemcpyAsync(d.frc + o, zero4.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
+    cudaMemcpyAsync(d.mass + o, mass.data(), np * sizeof(double), cudaMemcpyHostToDevice, s0);
+    cudaMemcpyAsync(d.cutr + o, cutr.data(), np * sizeof(double), cudaMemcpyHostToDevice, s0);
+    cudaMemcpyAsync(d.tag + o, tag.data(), np * sizeof(uint32_t), cudaMemcpyHostToDevice, s0);
+    cudaMemcpyAsync(d.type + o, type.data(), np * sizeof(uint32_t), cudaMemcpyHostToDevice, s0);
+    cudaMemcpyAsync(d.img + o, img.data(), np * sizeof(int4), cudaMemcpyHostToDevice, s0);
+    cudaMemcpyAsync(d.nnum + o, zi.data(), np * sizeof(int), cudaMemcpyHostToDevice, s0);
+    if (dem) {
+        cudaMemcpyAsync(d.omg + o, omg.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
+        cudaMemcpyAsync(d.trq + o, zero4.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
+        cudaMemcpyAsync(d.quat + o, quat.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
+        for (int b = 0; b < 2; b++) cudaMemcpyAsync(d.hcnt[b] + o, zi.data(), np * sizeof(int), cudaMemcpyHostToDevice, s0);
+    }
+    SysState ss{};
+    ss.rebuild = 1;  // the first step performs a full rebuild (CommState::FullRebuild)
+    cudaMemcpyAsync(d.ss + sys, &ss, sizeof(SysState), cudaMemcpyHostToDevice, s0);
+    cudaError_t e = cudaStreamSynchronize(s0);
+    if (e != cudaSuccess) return cuda_err(e);
+    c->launches += launch_ke_init(d, s0);
+    e = cudaStreamSynchronize(s0);
+    if (e != cudaSuccess) return cuda_err(e);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(e);
+    c->uploaded[sys] = 1;
+    return MDG_OK;
+}
+
+int mdg_download_state(mdg_ctx* c, int sys, mdg_state_view* st) {
+    if (!c || !st || sys < 0 || sys >= c->nsys) return MDG_ERR_ARG;
+    if (!c->uploaded[sys]) return MDG_ERR_STATE;
+    const SysParams& p = c->sp[sys];
+    const size_t n = (size_t)p.n;
+    if (st->n < n) return MDG_ERR_ARG;
+    st->n = n;
+    const size_t o = (size_t)p.p0;
+    Dev& d = c->d;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(e);
+    std::vector<double4> pos(n), vel(n), frc(n);
+    std::vector<double> mass(n), cutr(n);
+    std::vector<uint32_t> tag(n), type(n);
+    std::vector<int4> img(n);
+    cudaMemcpy(pos.data(), d.pos + o, n * sizeof(double4), cudaMemcpyDeviceToHost);
+    cudaMemcpy(vel.data(), d.vel + o, n * sizeof(double4), cudaMemcpyDeviceToHost);
+    cudaMemcpy(frc.data(), d.frc + o, n * sizeof(double4), cudaMemcpyDeviceToHost);
+    cudaMemcpy(mass.data(), d.mass + o, n * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(cutr.data(), d.cutr + o, n * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaMemcpy(tag.data(), d.tag + o, n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaMemcpy(type.data(), d.type + o, n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaMemcpy(img.data(), d.img + o, n * sizeof(int4), cudaMemcpyDeviceToHost);
+    const bool dem = p.kind == MDG_KIND_DEM;
+    std::vector<double4> omg, trq, quat;
+    if (dem) {
+        omg.resize(n);
+        trq.resize(n);
+        quat.resize(n);
+        cudaMemcpy(omg.data(), d.omg + o, n * sizeof(double4), cudaMemcpyDeviceToHost);
+        cudaMemcpy(trq.data(), d.trq + o, n * sizeof(double4), cudaMemcpyDeviceToHost);
+        cudaMemcpy(quat.data(), d.quat + o, n * sizeof(double4), cudaMemcpyDeviceToHost);
+    }
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(e);
+    for (size_t i = 0; i < n; i++) {
+        if (st->tag) st->tag[i] = tag[i];
+        if (st->type) st->type[i] = type[i];
+        if (st->pos) { st->pos[3 * i] = pos[i].x; st->pos[3 * i + 1] = pos[i].y; st->pos[3 * i + 2] = pos[i].z; }
+        if (st->vel) { st->vel[3 * i] = vel[i].x; st->vel[3 * i + 1] = vel[i].y; st->vel[3 * i + 2] = vel[i].z; }
+        if (st->force) { st->force[3 * i] = frc[i].x; st->force[3 * i + 1] = frc[i].y; st->force[3 * i + 2] = frc[i].z; }
+        if (st->mass) st->mass[i] = mass[i];
+        if (st->cutoff_radius) st->cutoff_radius[i] = cutr[i];
+        if (st->image) { st->image[3 * i] = img[i].x; st->image[3 * i + 1] = img[i].y; st->image[3 * i + 2] = img[i].z; }
+        if (dem) {
+            if (st->radius) st->radius[i] = pos[i].w;
+            if (st->inv_inertia) st->inv_inertia[i] = omg[i].w;
+            if (st->omega) { st->omega[3 * i] = omg[i].x; st->omega[3 * i + 1] = omg[i].y; st->omega[3 * i + 2] = omg[i].z; }
+            if (st->torque) { st->torque[3 * i] = trq[i].x; st->torque[3 * i + 1] = trq[i].y; st->torque[3 * i + 2] = trq[i].z; }
+            if (st->quat) {
+                st->quat[4 * i] = quat[i].x; st->quat[4 * i + 1] = quat[i].y;
+                st->quat[4 * i + 2] = quat[i].z; st->quat[4 * i + 3] = quat[i].w;
+            }
+        }
+    }
+    return MDG_OK;
+}
+
+int mdg_set_history(mdg_ctx* c, int sys, size_t nent, const uint32_t* keys, const double* vals) {
+    if (!c || sys < 0 || sys >= c->nsys || (nent && (!keys || !vals))) return MDG_ERR_ARG;
+    const SysParams& p = c->sp[sys];
+    if (p.kind != MDG_KIND_DEM) return MDG_ERR_ARG;
+    if (!c->uploaded[sys]) return MDG_ERR_STATE;
+    const size_t n = (size_t)p.n, np = (size_t)p.npad, o = (size_t)p.p0;
+    Dev& d = c->d;
+    cudaStreamSynchronize(c->stream);
+    std::vector<uint32_t> tag(n);
+    cudaMemcpy(tag.data(), d.tag + o, n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    std::map<uint32_t, size_t> idx;
+    for (size_t i = 0; i < n; i++) idx[tag[i]] = i;
+    std::vector<int> cnt(np, 0);
+    std::vector<uint32_t> ht((size_t)p.hcap * np, 0);
+    std::vector<double> hv((size_t)p.hcap * 7 * np, 0.0);
+    for (size_t k = 0; k < nent; k++) {
+        auto it = idx.find(keys[2 * k]);
+        if (it == idx.end()) return MDG_ERR_ARG;
+        const size_t i = it->second;
+        const int cc = cnt[i];
+        if (cc >= p.hcap) return MDG_ERR_LIST_OVERFLOW;
+        ht[(size_t)cc * np + i] = keys[2 * k + 1];
+        for (int q = 0; q < 7; q++) hv[(size_t)(cc * 7 + q) * np + i] = vals[7 * k + q];
+        cnt[i] = cc + 1;
+    }
+    const int h = c->hcur;
+    cudaMemcpy(d.hcnt[h] + o, cnt.data(), np * sizeof(int), cudaMemcpyHostToDevice);
+    cudaMemcpy(d.htag[h] + p.h0, ht.data(), ht.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    cudaMemcpy(d.hval[h] + p.h0 * 7, hv.data(), hv.size() * sizeof(double), cudaMemcpyHostToDevice);
+    return cuda_err(cudaGetLastError());
+}
+
+int mdg_get_history(mdg_ctx* c, int sys, uint32_t* keys, double* vals, size_t cap, size_t* nout) {
+    if (!c || sys < 0 || sys >= c->nsys || !nout) return MDG_ERR_ARG;
+    const SysParams& p = c->sp[sys];
+    *nout = 0;
+    if (p.kind != MDG_KIND_DEM) return MDG_OK;
+    if (!c->uploaded[sys]) return MDG_ERR_STATE;
+    const size_t n = (size_t)p.n, np = (size_t)p.npad, o = (size_t)p.p0;
+    Dev& d = c->d;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(e);
+    std::vector<uint32_t> tag(n);
+    std::vector<int> cnt(n);
+    std::vector<uint32_t> ht((size_t)p.hcap * np);
+    std::vector<double> hv((size_t)p.hcap * 7 * np);
+    const int h = c->hcur;
+    cudaMemcpy(tag.data(), d.tag + o, n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaMemcpy(cnt.data(), d.hcnt[h] + o, n * sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemcpy(ht.data(), d.htag[h] + p.h0, ht.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaMemcpy(hv.data(), d.hval[h] + p.h0 * 7, hv.size() * sizeof(double), cudaMemcpyDeviceToHost);
+    size_t m = 0;
+    for (size_t i = 0; i < n; i++)
+        for (int cc = 0; cc < cnt[i]; cc++) {
+            if (m < cap && keys && vals) {
+                keys[2 * m] = tag[i];
+                keys[2 * m + 1] = ht[(size_t)cc * np + i];
+                for (int q = 0; q < 7; q++) vals[7 * m + q] = hv[(size_t)(cc * 7 + q) * np + i];
+            }
+            m++;
+        }
+    *nout = m;
+    return cuda_err(cudaGetLastError());
+}
+
+int mdg_step(mdg_ctx* c, int64_t nsteps) {
+    if (!c || nsteps < 0) return MDG_ERR_ARG;
+    for (int s = 0; s < c->nsys; s++)
+        if (!c->uploaded[s]) return MDG_ERR_STATE;
+    int64_t left = nsteps;
+    if (c->graph_mode && c->graph_steps > 0) {
+        while (left >= c->graph_steps) {
+            const int h = c->hcur;
+            if (!c->graph[h]) {
+                int r = build_graph(c, h);
+                if (r) return r;
+            }
+            cudaError_t e = cudaGraphLaunch(c->graph[h], c->stream);
+            if (e != cudaSuccess) return cuda_err(e);
+            c->launches += (long long)c->graph_steps * (10 + (c->has_lj && c->has_dem ? 1 : 0));
+            if (c->graph_steps % 2) c->hcur ^= 1;
+            left -= c->graph_steps;
+        }
+    }
+    for (int64_t k = 0; k < left; k++) {
+        c->launches += enqueue_step(c, c->hcur, c->stream);
+        c->hcur ^= 1;
+    }
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(e);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(e);
+    return check_status(c);
+}
+
+int mdg_force_only(mdg_ctx* c) {
+    if (!c) return MDG_ERR_ARG;
+    for (int s = 0; s < c->nsys; s++)
+        if (!c->uploaded[s]) return MDG_ERR_STATE;
+    std::vector<SysState> ss(c->nsys);
+    cudaMemcpy(ss.data(), c->d.ss, c->nsys * sizeof(SysState), cudaMemcpyDeviceToHost);
+    for (auto& x : ss) x.rebuild = 1;
+    cudaMemcpy(c->d.ss, ss.data(), c->nsys * sizeof(SysState), cudaMemcpyHostToDevice);
+    cudaStream_t st = c->stream;
+    c->launches += launch_rebuild(c->d, c->hcur, st);
+    if (c->has_mixed) c->launches += launch_force_mixed(c->d, c->hcur, c->has_lj, c->has_dem, c->tpp_lj, st);
+    else c->launches += launch_force_fp64(c->d, c->hcur, c->has_lj, c->has_dem, c->tpp_lj, st);
+    c->launches += launch_final(c->d, st, 0);  // reductions + bookkeeping, no integration
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_err(e);
+    c->hcur ^= 1;
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(e);
+    return check_status(c);
+}
+
+int mdg_get_pairs(mdg_ctx* c, int sys, uint32_t* pairs, size_t cap, size_t* nout) {
+    if (!c || sys < 0 || sys >= c->nsys || !nout) return MDG_ERR_ARG;
+    if (!c->uploaded[sys]) return MDG_ERR_STATE;
+    const SysParams& p = c->sp[sys];
+    const size_t n = (size_t)p.n, np = (size_t)p.npad, o = (size_t)p.p0;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(e);
+    std::vector<int> nn(n);
+    std::vector<uint32_t> tag(n), lst((size_t)p.ncap * np);
+    cudaMemcpy(nn.data(), c->d.nnum + o, n * sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemcpy(tag.data(), c->d.tag + o, n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaMemcpy(lst.data(), c->d.nlist + p.lst0, lst.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    size_t m = 0;
+    for (size_t i = 0; i < n; i++)
+        for (int k = 0; k < nn[i]; k++) {
+            const uint32_t e2 = lst[(size_t)k * np + i];
+            if ((e2 >> IDX_BITS) < 27u) continue;
+            if (pairs && m < cap) {
+                pairs[2 * m] = tag[i];
+                pairs[2 * m + 1] = tag[e2 & IDX_MASK];
+            }
+            m++;
+        }
+    *nout = m;
+    return cuda_err(cudaGetLastError());
+}
+
+int mdg_thermo(mdg_ctx* c, int sys, mdg_thermo_t* out) {
+    if (!c || !out || sys < 0 || sys >= c->nsys) return MDG_ERR_ARG;
+    if (!c->uploaded[sys]) return MDG_ERR_STATE;
+    c->launches += launch_thermo(c->d, c->d_thermo, c->stream);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(e);
+    double t[16];
+    SysState ss;
+    cudaMemcpy(t, c->d_thermo + (size_t)sys * 16, sizeof(t), cudaMemcpyDeviceToHost);
+    cudaMemcpy(&ss, c->d.ss + sys, sizeof(SysState), cudaMemcpyDeviceToHost);
+    const SysParams& p = c->sp[sys];
+    const double ndof = 3.0 * (double)p.n - 3.0;
+    out->ke = t[0];
+    out->pe = ss.pe;
+    out->temp = ndof > 0 ? 2.0 * t[0] / ndof : 0.0;
+    out->p_xi = ss.p_xi_post;
+    out->granular_temp = t[4];
+    out->momentum = t[5];
+    for (int k = 0; k < 6; k++) out->virial[k] = ss.vir[k];
+    out->step = ss.step;
+    out->nbuilds = ss.nbuilds;
+    out->n = p.n;
+    out->status = ss.status;
+    out->max_neighbors = ss.max_nbr;
+    return cuda_err(cudaGetLastError());
+}
+
+int mdg_synchronize(mdg_ctx* c) {
+    if (!c) return MDG_ERR_ARG;
+    return cuda_err(cudaStreamSynchronize(c->stream));
+}
+
+int64_t mdg_kernel_launches(const mdg_ctx* c) { return c ? c->launches : 0; }
+
+int mdg_timed_steps(mdg_ctx* c, int64_t nsteps, size_t l2_flush_bytes, mdg_step_timing* out) {
+    if (!c || nsteps < 0 || (nsteps && !out)) return MDG_ERR_ARG;
+    for (int s = 0; s < c->nsys; s++)
+        if (!c->uploaded[s]) return MDG_ERR_STATE;
+    if (l2_flush_bytes > c->flush_bytes) {
+        if (c->flush_buf) cudaFree(c->flush_buf);
+        c->flush_buf = nullptr;
+        c->flush_bytes = 0;
+        if (cudaMalloc(&c->flush_buf, l2_flush_bytes) != cudaSuccess) {
+            cudaGetLastError();
+            return MDG_ERR_OOM;
+        }
+        c->flush_bytes = l2_flush_bytes;
+    }
+    std::vector<SysState> ss(c->nsys);
+    for (int64_t k = 0; k < nsteps; k++) {
+        const int h = c->hcur;
+        if (!c->tgraph[h]) {
+            int r = build_timed_graph(c, h);
+            if (r) return r;
+        }
+        if (l2_flush_bytes) cudaMemsetAsync(c->flush_buf, (int)(k & 0xff), l2_flush_bytes, c->stream);
+        cudaError_t e = cudaGraphLaunch(c->tgraph[h], c->stream);
+        if (e != cudaSuccess) return cuda_err(e);
+        e = cudaEventSynchronize(c->tev[4]);
+        if (e != cudaSuccess) return cuda_err(e);
+        float ms[5];
+        cudaEventElapsedTime(&ms[0], c->tev[0], c->tev[4]);
+        for (int q = 0; q < 4; q++) cudaEventElapsedTime(&ms[1 + q], c->tev[q], c->tev[q + 1]);
+        out[k].step_ms = ms[0];
+        for (int q = 0; q < 4; q++) out[k].phase_ms[q] = ms[1 + q];
+        out[k].kernels = c->tkernels;
+        cudaMemcpy(ss.data(), c->d.ss, c->nsys * sizeof(SysState), cudaMemcpyDeviceToHost);
+        int rb = 0;
+        for (int s = 0; s < c->nsys; s++) rb |= (ss[s].steps_since_build == 0);
+        out[k].rebuilt = rb;
+        c->launches += c->tkernels;
+        c->hcur ^= 1;
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(e);
+    return check_status(c);
+}
+
+int mdg_set_graph_mode(mdg_ctx* c, int enabled) {
+    if (!c) return MDG_ERR_ARG;
+    c->graph_mode = enabled ? 1 : 0;
+    return MDG_OK;
+}
+
+}  // extern "C"

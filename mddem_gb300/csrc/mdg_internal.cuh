@@ -1,0 +1,162 @@
+// mdg_internal.cuh -- device data layout shared by the kernels and the C ABI.
+//
+// Layout in HBM (one context = one or more independent systems):
+//   * Particles of all systems live in one SoA address space.  System s owns
+//     [p0, p0 + n) padded to npad (a multiple of BLK) so that every block of a
+//     per-particle kernel belongs to exactly one system (blk_sys[b]).
+//   * 32-byte rows for everything a pair kernel gathers: pos = (x,y,z,radius),
+//     vel = (vx,vy,vz,1/m), omg = (wx,wy,wz,1/I).  One sector per neighbour.
+//   * Neighbour list: per-system ELL block [ncap][npad] of u32 entries
+//     (j | code << 26), code = owner*27 + periodic-image shift (base 3).
+//   * Contact history: per particle up to hcap (partner tag, 7 doubles),
+//     layout [c][npad] / [c*7+k][npad] per system, double-buffered per step.
+//   * Bin grid: per system the reference's extended grid (interior + ghost
+//     layers), counts/starts over ext cells, particles sorted by ext cell.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace mdg {
+
+constexpr int BLK = 128;               // particles per block (segment padding unit)
+constexpr int IDX_BITS = 26;
+constexpr uint32_t IDX_MASK = (1u << IDX_BITS) - 1u;
+constexpr int NTAB = 14;               // material pair tables
+
+// device status bits (sticky per system)
+enum : int {
+    ST_OVERLAP = 1,
+    ST_NAN = 2,
+    ST_NBR_OVF = 4,
+    ST_HIST_OVF = 8,
+    ST_TIMEOUT = 16,
+};
+
+// material pair table ids (MaterialTable::build_pair_tables order)
+enum : int {
+    T_BETA = 0, T_FRICTION, T_ROLL_FRICTION, T_COHESION, T_SURFACE, T_EEFF, T_GEFF,
+    T_TWIST_FRICTION, T_KN, T_KT, T_KROLL, T_GROLL, T_KTWIST, T_GTWIST
+};
+
+struct SysParams {
+    int kind;            // 0 DEM, 1 LJ
+    int precision;       // 0 fp64, 1 mixed
+    int contact_model, adhesion_model, rolling_model, twisting_model;
+    int p0, n, npad;     // particle segment
+    int b0, nb;          // block segment
+    int c0, ncell;       // ext-cell segment
+    int nc[3];           // interior cells per axis
+    int ext[3];          // extended grid (interior + 2*layers)
+    int sl[3];           // ghost layers per side
+    int win[3];          // enumeration half-width in interior cells
+    double lo[3], hi[3], L[3];
+    double bin[3], inv_bin[3], origin[3];
+    double max_cutoff, stencil_cut_sq;
+    float pre_cut2;      // fp32 prefilter radius^2 for the list build (conservative)
+    float pad_f;
+    double skin_fraction, sf2;
+    int uniform;         // all cutoff radii equal
+    double uniform_cutoff_sq;
+    double min_skin;
+    double disp_thr_sq;
+    double dt;
+    int policy, every, check, sort_every, newton;
+    int nmat;
+    long long mat0;      // offset into the packed material tables
+    double lj1, lj2, lj3, lj4, lj_cut2;
+    int nh;
+    double nh_T, nh_Q, nh_ndof;
+    int virial;
+    int ncap;            // neighbour-list capacity per particle
+    long long lst0;      // offset of this system's ELL block
+    int hcap;            // contact-history capacity per particle
+    long long h0;        // offset of this system's history block (entries)
+    int tpp;             // threads per particle in force kernels
+};
+
+struct SysState {
+    int rebuild;         // 1: rebuild this step (FullRebuild)
+    int periodic_sort;   // 1: periodic spatial sort this step
+    int nonid;           // periodic sort produced a non-identity permutation
+    int status;          // sticky error bits
+    int steps_since_build;
+    int sort_counter;
+    int nbuilds;
+    int max_nbr;
+    int overlap;         // large-overlap count this step
+    unsigned int red_count;
+    double ke;           // KE after the last post-final (NH)
+    double p_xi_pre;     // p_xi after the pre-initial half step
+    double p_xi_post;    // p_xi after the post-final half step
+    double vir[6];
+    double pe;
+    long long step;
+};
+
+struct Dev {
+    // per particle
+    double4* pos;   // x y z radius
+    double4* vel;   // vx vy vz inv_mass
+    double4* frc;   // fx fy fz pe_i
+    double4* omg;   // wx wy wz inv_inertia
+    double4* trq;   // tx ty tz 0
+    double4* quat;  // w x y z
+    double4* lbp;   // last build position
+    double* mass;
+    double* cutr;
+    uint32_t* tag;
+    uint32_t* type;
+    int4* img;
+    // contact history, buffer [cur] read and [cur^1] written each step
+    int* hcnt[2];
+    uint32_t* htag[2];
+    double* hval[2];
+    // neighbour list
+    int* nnum;
+    uint32_t* nlist;
+    // rebuild scratch
+    int* cell;       // ext flat cell of each particle (system-relative)
+    int* cnt;        // per ext cell count / cursor
+    int* cstart;     // per ext cell start (absolute particle index), +1 sentinel per system
+    int* perm;       // new -> old (absolute)
+    // gather scratch (same shapes as the primaries)
+    double4 *s_pos, *s_vel, *s_omg, *s_quat;
+    double *s_mass, *s_cutr;
+    uint32_t *s_tag, *s_type;
+    int4* s_img;
+    int* s_hcnt;
+    uint32_t* s_htag;
+    double* s_hval;
+    // fp32 geometry copy (x_hi, x_lo) for the list prefilter and the mixed path
+    float4* pos_hi;
+    float4* pos_lo;
+    // per-particle virial (6 x P) when any system accumulates it
+    double* vir;
+    // reductions
+    double* blkpart;   // [nblocks][8]
+    const int* blk_sys;   // particle block -> system
+    const int* cblk_sys;  // cell block -> system
+    const int* cblk0;     // first cell block of each system
+    int ncblocks;
+    const SysParams* sp;
+    SysState* ss;
+    const double* mat;
+    int nsys;
+    int nblocks;
+    long long P;       // total padded particles
+    int hist_any;      // history arrays allocated
+};
+
+// ---- kernel launchers (mdg_kernels_fp64.cu / mdg_kernels_mixed.cu) ----------
+// Each returns the number of kernels it launched on `st`.
+int launch_initial(const Dev& d, cudaStream_t st);
+int launch_rebuild(const Dev& d, int hcur, cudaStream_t st);
+int launch_force_fp64(const Dev& d, int hcur, int has_lj, int has_dem, int tpp, cudaStream_t st);
+int launch_force_mixed(const Dev& d, int hcur, int has_lj, int has_dem, int tpp, cudaStream_t st);
+int launch_final(const Dev& d, cudaStream_t st, int integrate);
+int launch_ke_init(const Dev& d, cudaStream_t st);
+// thermo reduction for all systems into out[nsys][16] (device pointer)
+int launch_thermo(const Dev& d, double* out, cudaStream_t st);
+// history injection/extraction helpers run on the host side of the API
+
+}  // namespace mdg

@@ -1,0 +1,1153 @@
+// mdg_kernels_fp64.cu -- FP64 kernels of the hot path (the plain path).
+//
+// Compiled with -fmad=false: every multiply and add rounds separately, and
+// fma() appears exactly where the reference uses f64::mul_add, so per-pair
+// arithmetic is bit-identical to the reference's CPU path.  Per-particle sums
+// run in a fixed per-row order (deterministic run to run) that differs from
+// the reference's scatter-then-reverse-comm order, hence a 1e-12 relative
+// bound on forces rather than bit equality.
+//
+// One timestep = k_initial -> [rebuild: k_cells, k_scan, k_scatter,
+// k_cellsort, k_gather, k_copyback, k_build] -> force -> k_final.  Rebuild
+// kernels return at once for systems that do not rebuild this step.
+#include "mdg_internal.cuh"
+
+namespace mdg {
+
+// ----------------------------------------------------------------------------
+// helpers
+// ----------------------------------------------------------------------------
+// Ghost position = pos + periodic_offset * size (comm.rs:281, 404-406); the
+// offset is +-1.0, so the image coordinate is x + L or x + (-L) exactly.
+__device__ __forceinline__ double img_coord(double x, int s, double L) {
+    return s > 0 ? x + L : (s < 0 ? x + (-L) : x);
+}
+
+// ((p - bin_origin) * inv_bs).floor() as i32, clamped (neighbor.rs:848-853)
+__device__ __forceinline__ int ext_cell_1d(double x, double origin, double inv_bin, int ext) {
+    int c = (int)floor((x - origin) * inv_bin);
+    return c < 0 ? 0 : (c > ext - 1 ? ext - 1 : c);
+}
+
+__device__ __forceinline__ void decode_shift(int sc, int& sx, int& sy, int& sz) {
+    sx = sc / 9 - 1;
+    sy = (sc / 3) % 3 - 1;
+    sz = sc % 3 - 1;
+}
+
+// Per-system reduction of NV doubles.  Every block of the system contributes a
+// partial; the last block to arrive sums the partials with a fixed order
+// (strided lanes, then a fixed tree) so the result is deterministic.  Returns
+// true on the last block (all threads), totals valid in out[] on thread 0.
+// The grid must be exactly the particle-block grid.
+template <int NV>
+__device__ bool system_reduce(const Dev& d, int s, const double (&v)[NV], double (&out)[NV]) {
+    static_assert(NV <= 8, "blkpart holds 8 doubles per block");
+    __shared__ double sh[NV][BLK];
+    __shared__ int last;
+    const SysParams& sp = d.sp[s];
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < NV; k++) sh[k][t] = v[k];
+    __syncthreads();
+    for (int w = BLK / 2; w > 0; w >>= 1) {
+        if (t < w) {
+#pragma unroll
+            for (int k = 0; k < NV; k++) sh[k][t] = sh[k][t] + sh[k][t + w];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) d.blkpart[(size_t)blockIdx.x * 8 + k] = sh[k][0];
+        __threadfence();
+        unsigned int prev = atomicAdd(&d.ss[s].red_count, 1u);
+        last = (prev == (unsigned)(sp.nb - 1)) ? 1 : 0;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) acc[k] = 0.0;
+    for (int b = t; b < sp.nb; b += BLK) {
+        const volatile double* p = d.blkpart + (size_t)(sp.b0 + b) * 8;
+#pragma unroll
+        for (int k = 0; k < NV; k++) acc[k] = acc[k] + p[k];
+    }
+#pragma unroll
+    for (int k = 0; k < NV; k++) sh[k][t] = acc[k];
+    __syncthreads();
+    for (int w = BLK / 2; w > 0; w >>= 1) {
+        if (t < w) {
+#pragma unroll
+            for (int k = 0; k < NV; k++) sh[k][t] = sh[k][t] + sh[k][t + w];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) out[k] = sh[k][0];
+        d.ss[s].red_count = 0;
+    }
+    return true;
+}
+
+__device__ __forceinline__ int vload(const int* p) { return *((const volatile int*)p); }
+
+// ----------------------------------------------------------------------------
+// initial integration + rebuild decision
+// ----------------------------------------------------------------------------
+// nh_pre_initial (md_thermostat/src/lib.rs:254-301) or initial_integration
+// (mddem_verlet/src/lib.rs:97-123) + initial_rotation (rotational.rs:59-84),
+// fused with decide_rebuild's per-atom tests (neighbor.rs:564-674).
+__global__ void __launch_bounds__(BLK) k_initial(Dev d) {
+    const int s = d.blk_sys[blockIdx.x];
+    const SysParams& sp = d.sp[s];
+    SysState* st = d.ss + s;
+    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    const bool act = li < sp.n;
+    const long long i = (long long)sp.p0 + li;
+    const double dt = sp.dt;
+    double scale = 1.0;
+    if (sp.nh) {
+        double ke = st->ke;
+        double pxi = st->p_xi_post + (dt / 2.0) * (2.0 * ke - sp.nh_ndof * sp.nh_T);
+        scale = exp(-dt / 2.0 * pxi / sp.nh_Q);
+        if (li == 0) st->p_xi_pre = pxi;
+    }
+    if (li == 0)
+        st->periodic_sort =
+            (sp.policy == 0 && sp.sort_every > 0 && st->sort_counter + 1 >= sp.sort_every) ? 1 : 0;
+    const int already = vload(&st->rebuild);
+    int need = 0;
+    if (act) {
+        double4 v = d.vel[i];
+        const double4 f = d.frc[i];
+        double4 x = d.pos[i];
+        if (sp.nh) {
+            v.x *= scale;
+            v.y *= scale;
+            v.z *= scale;
+        }
+        const double h = 0.5 * dt * v.w;
+        v.x += h * f.x;
+        v.y += h * f.y;
+        v.z += h * f.z;
+        x.x += v.x * dt;
+        x.y += v.y * dt;
+        x.z += v.z * dt;
+        d.vel[i] = v;
+        d.pos[i] = x;
+        if (sp.precision == 1) {
+            // two-float geometry copy relative to the box corner for the mixed kernels
+            const double rx = x.x - sp.lo[0], ry = x.y - sp.lo[1], rz = x.z - sp.lo[2];
+            const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
+            d.pos_hi[i] = make_float4(hx, hy, hz, (float)x.w);
+            d.pos_lo[i] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy), (float)(rz - (double)hz), 0.f);
+        }
+        if (sp.kind == 0) {
+            double4 w = d.omg[i];
+            if (w.w != 0.0) {
+                const double4 tq = d.trq[i];
+                w.x += 0.5 * dt * tq.x * w.w;
+                w.y += 0.5 * dt * tq.y * w.w;
+                w.z += 0.5 * dt * tq.z * w.w;
+                const double om = sqrt(w.x * w.x + w.y * w.y + w.z * w.z);
+                const double angle = om * dt;
+                if (angle > 1e-14) {
+                    const double inv = 1.0 / om;
+                    const double half = angle * 0.5;
+                    const double sn = sin(half), cs = cos(half);
+                    const double a0 = cs, a1 = w.x * inv * sn, a2 = w.y * inv * sn, a3 = w.z * inv * sn;
+                    const double4 q = d.quat[i];
+                    double4 r;  // Hamilton product dq * q (rotational.rs:34-41)
+                    r.x = a0 * q.x - a1 * q.y - a2 * q.z - a3 * q.w;
+                    r.y = a0 * q.y + a1 * q.x + a2 * q.w - a3 * q.z;
+                    r.z = a0 * q.z - a1 * q.w + a2 * q.x + a3 * q.y;
+                    r.w = a0 * q.w + a1 * q.z - a2 * q.y + a3 * q.x;
+                    d.quat[i] = r;
+                }
+                d.omg[i] = w;
+            }
+        }
+        if (!already) {
+            bool disp = false;
+            if (sp.every == 0 || sp.check) {
+                const double4 b = d.lbp[i];
+                double dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
+                const double hbx = sp.L[0] * 0.5, hby = sp.L[1] * 0.5, hbz = sp.L[2] * 0.5;
+                if (dx > hbx) dx -= sp.L[0]; else if (dx < -hbx) dx += sp.L[0];
+                if (dy > hby) dy -= sp.L[1]; else if (dy < -hby) dy += sp.L[1];
+                if (dz > hbz) dz -= sp.L[2]; else if (dz < -hbz) dz += sp.L[2];
+                disp = dx * dx + dy * dy + dz * dz > sp.disp_thr_sq;
+            }
+            if (sp.every == 0) need = disp;
+            else if (sp.check) need = (st->steps_since_build >= sp.every) || disp;
+            else need = st->steps_since_build >= sp.every;
+            if (!need && sp.policy == 0)
+                need = (x.x < sp.lo[0] || x.x >= sp.hi[0] || x.y < sp.lo[1] || x.y >= sp.hi[1] ||
+                        x.z < sp.lo[2] || x.z >= sp.hi[2]);
+        }
+    }
+    if (__any_sync(0xffffffffu, need) && (threadIdx.x & 31) == 0) atomicOr(&st->rebuild, 1);
+}
+
+// ----------------------------------------------------------------------------
+// rebuild pipeline
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ bool do_sort(const SysState* st) {
+    return vload(&st->rebuild) || vload(&st->periodic_sort);
+}
+__device__ __forceinline__ bool do_rebuild(const SysState* st) {
+    return vload(&st->rebuild) || (vload(&st->periodic_sort) && vload(&st->nonid));
+}
+
+// pbc (domain.rs:413-459, rebuild steps only) + bin key (neighbor.rs:721-738)
+__global__ void __launch_bounds__(BLK) k_cells(Dev d) {
+    const int s = d.blk_sys[blockIdx.x];
+    const SysParams& sp = d.sp[s];
+    const SysState* st = d.ss + s;
+    if (!do_sort(st)) return;
+    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    if (li >= sp.n) return;
+    const long long i = (long long)sp.p0 + li;
+    double4 x = d.pos[i];
+    if (vload(&st->rebuild)) {
+        int4 im = d.img[i];
+        const double hx = sp.lo[0] + sp.L[0], hy = sp.lo[1] + sp.L[1], hz = sp.lo[2] + sp.L[2];
+        if (x.x < sp.lo[0]) { x.x += sp.L[0]; im.x -= 1; } else if (x.x >= hx) { x.x -= sp.L[0]; im.x += 1; }
+        if (x.y < sp.lo[1]) { x.y += sp.L[1]; im.y -= 1; } else if (x.y >= hy) { x.y -= sp.L[1]; im.y += 1; }
+        if (x.z < sp.lo[2]) { x.z += sp.L[2]; im.z -= 1; } else if (x.z >= hz) { x.z -= sp.L[2]; im.z += 1; }
+        d.pos[i] = x;
+        d.img[i] = im;
+    }
+    const int cx = ext_cell_1d(x.x, sp.origin[0], sp.inv_bin[0], sp.ext[0]);
+    const int cy = ext_cell_1d(x.y, sp.origin[1], sp.inv_bin[1], sp.ext[1]);
+    const int cz = ext_cell_1d(x.z, sp.origin[2], sp.inv_bin[2], sp.ext[2]);
+    const int flat = (cx * sp.ext[1] + cy) * sp.ext[2] + cz;
+    d.cell[i] = flat;
+    atomicAdd(&d.cnt[sp.c0 + flat], 1);
+}
+
+// exclusive scan of one system's cell counts -> absolute starts (+ sentinel);
+// counts are reset for use as scatter cursors.  One block per system.
+__global__ void __launch_bounds__(1024) k_scan(Dev d) {
+    const int s = blockIdx.x;
+    const SysParams& sp = d.sp[s];
+    if (!do_sort(d.ss + s)) return;
+    __shared__ int wsum[32];
+    __shared__ int carry;
+    const int t = threadIdx.x;
+    if (t == 0) carry = sp.p0;
+    __syncthreads();
+    for (int base = 0; base < sp.ncell; base += 1024) {
+        const int c = base + t;
+        const int v = c < sp.ncell ? d.cnt[sp.c0 + c] : 0;
+        int x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, x, o);
+            if ((t & 31) >= o) x += y;
+        }
+        if ((t & 31) == 31) wsum[t >> 5] = x;
+        __syncthreads();
+        if (t < 32) {
+            int w = wsum[t];
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, w, o);
+                if (t >= o) w += y;
+            }
+            wsum[t] = w;
+        }
+        __syncthreads();
+        const int incl = x + ((t >> 5) ? wsum[(t >> 5) - 1] : 0);
+        const int c0v = carry;
+        if (c < sp.ncell) {
+            d.cstart[sp.c0 + c] = c0v + incl - v;
+            d.cnt[sp.c0 + c] = 0;
+        }
+        __syncthreads();
+        if (t == 1023) carry = c0v + incl;
+        __syncthreads();
+    }
+    if (t == 0) d.cstart[sp.c0 + sp.ncell] = carry;
+}
+
+__global__ void __launch_bounds__(BLK) k_scatter(Dev d) {
+    const int s = d.blk_sys[blockIdx.x];
+    const SysParams& sp = d.sp[s];
+    if (!do_sort(d.ss + s)) return;
+    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    if (li >= sp.n) return;
+    const long long i = (long long)sp.p0 + li;
+    const int c = d.cell[i];
+    const int slot = d.cstart[sp.c0 + c] + atomicAdd(&d.cnt[sp.c0 + c], 1);
+    d.perm[slot] = (int)i;
+}
+
+// Stable order inside each cell (by old index): the sort of sort_atoms_by_bin
+// made stable (documented deviation from sort_unstable_by_key,
+// neighbor.rs:740).  Also detects a non-identity permutation, which turns a
+// periodic sort into a rebuild (neighbor.rs:784-793).
+__global__ void __launch_bounds__(BLK) k_cellsort(Dev d) {
+    const int s = d.cblk_sys[blockIdx.x];
+    const SysParams& sp = d.sp[s];
+    SysState* st = d.ss + s;
+    if (!do_sort(st)) return;
+    const int c = (blockIdx.x - d.cblk0[s]) * BLK + threadIdx.x;
+    if (c >= sp.ncell) return;
+    const int start = d.cstart[sp.c0 + c];
+    const int m = d.cnt[sp.c0 + c];
+    int* p = d.perm + start;
+    for (int a = 1; a < m; a++) {
+        const int key = p[a];
+        int b = a - 1;
+        while (b >= 0 && p[b] > key) {
+            p[b + 1] = p[b];
+            b--;
+        }
+        p[b + 1] = key;
+    }
+    bool ident = true;
+    for (int a = 0; a < m; a++)
+        if (p[a] != start + a) ident = false;
+    d.cnt[sp.c0 + c] = 0;
+    if (!ident) atomicOr(&st->nonid, 1);
+}
+
+// Atom::apply_permutation + AtomDataRegistry::apply_permutation_all +
+// ContactHistoryStore::apply_permutation (atom.rs:383-394, 197-202,
+// tangential.rs:92-96): gather every per-atom array into scratch.
+__global__ void __launch_bounds__(BLK) k_gather(Dev d, int hcur) {
+    const int s = d.blk_sys[blockIdx.x];
+    const SysParams& sp = d.sp[s];
+    if (!do_rebuild(d.ss + s)) return;
+    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    if (li >= sp.n) return;
+    const long long k = (long long)sp.p0 + li;
+    const long long o = d.perm[k];
+    d.s_pos[k] = d.pos[o];
+    d.s_vel[k] = d.vel[o];
+    d.s_mass[k] = d.mass[o];
+    d.s_cutr[k] = d.cutr[o];
+    d.s_tag[k] = d.tag[o];
+    d.s_type[k] = d.type[o];
+    d.s_img[k] = d.img[o];
+    if (sp.kind == 0) {
+        d.s_omg[k] = d.omg[o];
+        d.s_quat[k] = d.quat[o];
+        if (d.hist_any) {
+            const long long lo_ = o - sp.p0;
+            const int hc = d.hcnt[hcur][o];
+            d.s_hcnt[k] = hc;
+            for (int c = 0; c < hc; c++) {
+                d.s_htag[sp.h0 + (long long)c * sp.npad + li] = d.htag[hcur][sp.h0 + (long long)c * sp.npad + lo_];
+                for (int q = 0; q < 7; q++)
+                    d.s_hval[sp.h0 * 7 + (long long)(c * 7 + q) * sp.npad + li] =
+                        d.hval[hcur][sp.h0 * 7 + (long long)(c * 7 + q) * sp.npad + lo_];
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(BLK) k_copyback(Dev d, int hcur) {
+    const int s = d.blk_sys[blockIdx.x];
+    const SysParams& sp = d.sp[s];
+    if (!do_rebuild(d.ss + s)) return;
+    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    if (li >= sp.n) return;
+    const long long k = (long long)sp.p0 + li;
+    const double4 x = d.s_pos[k];
+    d.pos[k] = x;
+    d.vel[k] = d.s_vel[k];
+    d.mass[k] = d.s_mass[k];
+    d.cutr[k] = d.s_cutr[k];
+    d.tag[k] = d.s_tag[k];
+    d.type[k] = d.s_type[k];
+    d.img[k] = d.s_img[k];
+    if (sp.kind == 0) {
+        d.omg[k] = d.s_omg[k];
+        d.quat[k] = d.s_quat[k];
+        if (d.hist_any) {
+            const int hc = d.s_hcnt[k];
+            d.hcnt[hcur][k] = hc;
+            for (int c = 0; c < hc; c++) {
+                d.htag[hcur][sp.h0 + (long long)c * sp.npad + li] = d.s_htag[sp.h0 + (long long)c * sp.npad + li];
+                for (int q = 0; q < 7; q++)
+                    d.hval[hcur][sp.h0 * 7 + (long long)(c * 7 + q) * sp.npad + li] =
+                        d.s_hval[sp.h0 * 7 + (long long)(c * 7 + q) * sp.npad + li];
+            }
+        }
+    }
+    // two-float geometry copy relative to the box corner: list-build prefilter
+    // and the mixed-precision pair kernels
+    const double rx = x.x - sp.lo[0], ry = x.y - sp.lo[1], rz = x.z - sp.lo[2];
+    const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
+    d.pos_hi[k] = make_float4(hx, hy, hz, (float)x.w);
+    d.pos_lo[k] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy), (float)(rz - (double)hz), 0.f);
+}
+
+// Owner rule of the reference's half list (bin_neighbor_list,
+// neighbor.rs:938-1065): local `o`, in ext cell eo, scanning its self cell
+// (entries after it in bin order) and its forward stencil cells finds the
+// image of `p` that lies in ext cell g.  `ghost`: the image is a periodic copy
+// (ghosts follow all locals in bin order).  newton=false: full stencil, all
+// entries but self.
+__device__ __forceinline__ bool owner_test(const SysParams& sp, int eox, int eoy, int eoz, int gx, int gy,
+                                           int gz, bool ghost, long long o, long long p) {
+    const int dx = gx - eox, dy = gy - eoy, dz = gz - eoz;
+    if (abs(dx) > sp.sl[0] || abs(dy) > sp.sl[1] || abs(dz) > sp.sl[2]) return false;
+    const double mdx = (double)(abs(dx) > 0 ? abs(dx) - 1 : 0) * sp.bin[0];
+    const double mdy = (double)(abs(dy) > 0 ? abs(dy) - 1 : 0) * sp.bin[1];
+    const double mdz = (double)(abs(dz) > 0 ? abs(dz) - 1 : 0) * sp.bin[2];
+    if (!(mdx * mdx + mdy * mdy + mdz * mdz < sp.stencil_cut_sq)) return false;
+    const long long flat = ((long long)dx * sp.ext[1] + dy) * sp.ext[2] + dz;
+    if (sp.newton) {
+        if (flat > 0) return true;
+        if (flat < 0) return false;
+        return ghost || p > o;
+    }
+    return !(flat == 0 && !ghost && p == o);
+}
+
+// uniform: r2 < (2 r sf)^2; polydisperse: r2 < (s_i + s_j)^2 sf^2 (neighbor.rs:959-1060)
+__device__ __forceinline__ bool cut_ok(const SysParams& sp, double r2, double so, double sq) {
+    if (sp.uniform) return r2 < sp.uniform_cutoff_sq;
+    const double ss = so + sq;
+    return r2 < ss * ss * sp.sf2;
+}
+
+// Neighbour list build.  Enumerates, for particle i, every periodic image of
+// every particle in the 3x3x3 (or wider) interior-cell window around it,
+// prefilters in fp32, and applies the reference's exact fp64 cutoff test and
+// owner rule twice: `own` (i holds the pair in the reference's half list) and
+// `oth` (the partner holds it).  Both go into i's full row, so forces can be
+// summed per particle without atomics while pair arithmetic stays in the
+// owner's frame.  Also saves last_build_pos (neighbor.rs:545-561).
+__global__ void __launch_bounds__(BLK) k_build(Dev d) {
+    const int s = d.blk_sys[blockIdx.x];
+    const SysParams& sp = d.sp[s];
+    SysState* st = d.ss + s;
+    if (!do_rebuild(st)) return;
+    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    if (li >= sp.n) return;
+    const long long i = (long long)sp.p0 + li;
+    const double4 xi = d.pos[i];
+    const float4 xif = d.pos_hi[i];
+    const double si = d.cutr[i];
+    d.lbp[i] = xi;
+    const int ex = ext_cell_1d(xi.x, sp.origin[0], sp.inv_bin[0], sp.ext[0]);
+    const int ey = ext_cell_1d(xi.y, sp.origin[1], sp.inv_bin[1], sp.ext[1]);
+    const int ez = ext_cell_1d(xi.z, sp.origin[2], sp.inv_bin[2], sp.ext[2]);
+    const int qx0 = min(max(ex - sp.sl[0], 0), sp.nc[0] - 1);
+    const int qy0 = min(max(ey - sp.sl[1], 0), sp.nc[1] - 1);
+    const int qz0 = min(max(ez - sp.sl[2], 0), sp.nc[2] - 1);
+    const float pre2 = sp.pre_cut2;
+    const float Lf0 = (float)sp.L[0], Lf1 = (float)sp.L[1], Lf2 = (float)sp.L[2];
+    int count = 0;
+    const long long base = sp.lst0 + li;
+    for (int ox = -sp.win[0]; ox <= sp.win[0]; ox++) {
+        int qx = qx0 + ox, sx = 0;
+        if (qx < 0) { qx += sp.nc[0]; sx = -1; } else if (qx >= sp.nc[0]) { qx -= sp.nc[0]; sx = 1; }
+        if (qx < 0 || qx >= sp.nc[0]) continue;
+        for (int oy = -sp.win[1]; oy <= sp.win[1]; oy++) {
+            int qy = qy0 + oy, sy = 0;
+            if (qy < 0) { qy += sp.nc[1]; sy = -1; } else if (qy >= sp.nc[1]) { qy -= sp.nc[1]; sy = 1; }
+            if (qy < 0 || qy >= sp.nc[1]) continue;
+            for (int oz = -sp.win[2]; oz <= sp.win[2]; oz++) {
+                int qz = qz0 + oz, sz = 0;
+                if (qz < 0) { qz += sp.nc[2]; sz = -1; } else if (qz >= sp.nc[2]) { qz -= sp.nc[2]; sz = 1; }
+                if (qz < 0 || qz >= sp.nc[2]) continue;
+                const bool shifted = (sx | sy | sz) != 0;
+                const float fsx = (float)sx * Lf0, fsy = (float)sy * Lf1, fsz = (float)sz * Lf2;
+                // source ext cells: the interior cell and the ghost-layer cells that
+                // clamp into it (particles whose bin coordinate rounded just outside)
+                const int axa = (qx == 0) ? -1 : 0, axb = (qx == sp.nc[0] - 1) ? 1 : 0;
+                const int aya = (qy == 0) ? -1 : 0, ayb = (qy == sp.nc[1] - 1) ? 1 : 0;
+                const int aza = (qz == 0) ? -1 : 0, azb = (qz == sp.nc[2] - 1) ? 1 : 0;
+                for (int ax = axa; ax <= axb; ax++)
+                    for (int ay = aya; ay <= ayb; ay++)
+                        for (int az = aza; az <= azb; az++) {
+                            const int Ex = qx + sp.sl[0] + ax, Ey = qy + sp.sl[1] + ay, Ez = qz + sp.sl[2] + az;
+                            const int flatE = (Ex * sp.ext[1] + Ey) * sp.ext[2] + Ez;
+                            const int m0 = d.cstart[sp.c0 + flatE], m1 = d.cstart[sp.c0 + flatE + 1];
+                            for (int m = m0; m < m1; m++) {
+                                const long long j = m;
+                                if (!shifted && j == i) continue;
+                                const float4 xjf = d.pos_hi[j];
+                                const float fx = (xjf.x + fsx) - xif.x;
+                                const float fy = (xjf.y + fsy) - xif.y;
+                                const float fz = (xjf.z + fsz) - xif.z;
+                                if (fx * fx + fy * fy + fz * fz > pre2) continue;
+                                const double4 xj = d.pos[j];
+                                const double sj = d.cutr[j];
+                                const double ix = img_coord(xj.x, sx, sp.L[0]);
+                                const double iy = img_coord(xj.y, sy, sp.L[1]);
+                                const double iz = img_coord(xj.z, sz, sp.L[2]);
+                                const double dx = ix - xi.x, dy = iy - xi.y, dz = iz - xi.z;
+                                const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+                                bool own, oth = false;
+                                if (!shifted) {
+                                    // dx from j's side is exactly -dx: same r2
+                                    if (!cut_ok(sp, r2, si, sj)) continue;
+                                    own = owner_test(sp, ex, ey, ez, Ex, Ey, Ez, false, i, j);
+                                    if (sp.newton) oth = owner_test(sp, Ex, Ey, Ez, ex, ey, ez, false, j, i);
+                                } else {
+                                    own = false;
+                                    if (cut_ok(sp, r2, si, sj)) {
+                                        const int gx = ext_cell_1d(ix, sp.origin[0], sp.inv_bin[0], sp.ext[0]);
+                                        const int gy = ext_cell_1d(iy, sp.origin[1], sp.inv_bin[1], sp.ext[1]);
+                                        const int gz = ext_cell_1d(iz, sp.origin[2], sp.inv_bin[2], sp.ext[2]);
+                                        own = owner_test(sp, ex, ey, ez, gx, gy, gz, true, i, j);
+                                    }
+                                    if (sp.newton) {
+                                        const double jx = img_coord(xi.x, -sx, sp.L[0]);
+                                        const double jy = img_coord(xi.y, -sy, sp.L[1]);
+                                        const double jz = img_coord(xi.z, -sz, sp.L[2]);
+                                        const double ux = jx - xj.x, uy = jy - xj.y, uz = jz - xj.z;
+                                        const double r2o = fma(ux, ux, fma(uy, uy, uz * uz));
+                                        if (cut_ok(sp, r2o, sj, si)) {
+                                            const int hx = ext_cell_1d(jx, sp.origin[0], sp.inv_bin[0], sp.ext[0]);
+                                            const int hy = ext_cell_1d(jy, sp.origin[1], sp.inv_bin[1], sp.ext[1]);
+                                            const int hz = ext_cell_1d(jz, sp.origin[2], sp.inv_bin[2], sp.ext[2]);
+                                            oth = owner_test(sp, Ex, Ey, Ez, hx, hy, hz, true, j, i);
+                                        }
+                                    }
+                                }
+                                const uint32_t sc = (uint32_t)((sx + 1) * 9 + (sy + 1) * 3 + (sz + 1));
+                                const uint32_t jl = (uint32_t)(j - sp.p0);
+                                if (own) {
+                                    if (count < sp.ncap)
+                                        d.nlist[base + (long long)count * sp.npad] = jl | ((sc + 27u) << IDX_BITS);
+                                    count++;
+                                }
+                                if (oth) {
+                                    if (count < sp.ncap)
+                                        d.nlist[base + (long long)count * sp.npad] = jl | (sc << IDX_BITS);
+                                    count++;
+                                }
+                            }
+                        }
+            }
+        }
+    }
+    if (count > sp.ncap) {
+        atomicOr(&st->status, ST_NBR_OVF);
+        atomicMax(&st->max_nbr, count);
+        count = sp.ncap;
+    } else {
+        atomicMax(&st->max_nbr, count);
+    }
+    d.nnum[i] = count;
+}
+
+// ----------------------------------------------------------------------------
+// LJ 12-6 force (lj_force, md_lj/src/lib.rs:488-633) over the full list.
+// TPP lanes share one particle's row and combine with warp shuffles.
+// ----------------------------------------------------------------------------
+template <int TPP>
+__global__ void __launch_bounds__(BLK) k_lj_fp64(Dev d) {
+    const int pb = blockIdx.x / TPP;
+    const int sub = blockIdx.x % TPP;
+    const int s = d.blk_sys[pb];
+    const SysParams& sp = d.sp[s];
+    if (sp.kind != 1) return;
+    const int lane = threadIdx.x % TPP;
+    const int li = (pb - sp.b0) * BLK + sub * (BLK / TPP) + threadIdx.x / TPP;
+    const bool act = li < sp.n;
+    const long long i = (long long)sp.p0 + li;
+    double fx = 0, fy = 0, fz = 0, pe = 0;
+    double v0 = 0, v1 = 0, v2 = 0, v3 = 0, v4 = 0, v5 = 0;
+    if (act) {
+        const double4 xi = d.pos[i];
+        const int nn = d.nnum[i];
+        const long long base = sp.lst0 + li;
+        const double lj1 = sp.lj1, lj2 = sp.lj2, lj3 = sp.lj3, lj4 = sp.lj4, cut2 = sp.lj_cut2;
+        const double half = sp.newton ? 1.0 : 0.5;
+        for (int k = lane; k < nn; k += TPP) {
+            const uint32_t e = d.nlist[base + (long long)k * sp.npad];
+            const long long j = sp.p0 + (e & IDX_MASK);
+            const uint32_t code = e >> IDX_BITS;
+            const bool own = code >= 27u;
+            int sx, sy, sz;
+            decode_shift((int)(own ? code - 27u : code), sx, sy, sz);
+            const double4 xj = d.pos[j];
+            double dx, dy, dz;
+            if (own) {
+                dx = img_coord(xj.x, sx, sp.L[0]) - xi.x;
+                dy = img_coord(xj.y, sy, sp.L[1]) - xi.y;
+                dz = img_coord(xj.z, sz, sp.L[2]) - xi.z;
+            } else {  // owner frame: partner i's image seen from j
+                dx = img_coord(xi.x, -sx, sp.L[0]) - xj.x;
+                dy = img_coord(xi.y, -sy, sp.L[1]) - xj.y;
+                dz = img_coord(xi.z, -sz, sp.L[2]) - xj.z;
+            }
+            const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+            if (r2 >= cut2) continue;
+            const double r2inv = 1.0 / r2;
+            const double r6inv = r2inv * r2inv * r2inv;
+            const double fpair = r2inv * r6inv * fma(lj1, r6inv, -lj2);
+            if (!sp.virial) {
+                if (own) {
+                    fx = fma(-fpair, dx, fx);
+                    fy = fma(-fpair, dy, fy);
+                    fz = fma(-fpair, dz, fz);
+                } else {
+                    fx = fma(fpair, dx, fx);
+                    fy = fma(fpair, dy, fy);
+                    fz = fma(fpair, dz, fz);
+                }
+            } else {
+                const double px = -fpair * dx, py = -fpair * dy, pz = -fpair * dz;
+                if (own) {
+                    fx += px; fy += py; fz += pz;
+                    v0 += dx * px * half; v1 += dy * py * half; v2 += dz * pz * half;
+                    v3 += dx * py * half; v4 += dx * pz * half; v5 += dy * pz * half;
+                } else {
+                    fx -= px; fy -= py; fz -= pz;
+                }
+            }
+            if (own) pe += r6inv * (lj3 * r6inv - lj4) * half;
+        }
+    }
+    if (TPP > 1) {
+#pragma unroll
+        for (int o = TPP / 2; o > 0; o >>= 1) {
+            fx += __shfl_down_sync(0xffffffffu, fx, o, TPP);
+            fy += __shfl_down_sync(0xffffffffu, fy, o, TPP);
+            fz += __shfl_down_sync(0xffffffffu, fz, o, TPP);
+            pe += __shfl_down_sync(0xffffffffu, pe, o, TPP);
+            if (sp.virial) {
+                v0 += __shfl_down_sync(0xffffffffu, v0, o, TPP);
+                v1 += __shfl_down_sync(0xffffffffu, v1, o, TPP);
+                v2 += __shfl_down_sync(0xffffffffu, v2, o, TPP);
+                v3 += __shfl_down_sync(0xffffffffu, v3, o, TPP);
+                v4 += __shfl_down_sync(0xffffffffu, v4, o, TPP);
+                v5 += __shfl_down_sync(0xffffffffu, v5, o, TPP);
+            }
+        }
+    }
+    if (act && lane == 0) {
+        d.frc[i] = make_double4(fx, fy, fz, pe);
+        if (sp.virial) {
+            d.vir[0 * d.P + i] = v0; d.vir[1 * d.P + i] = v1; d.vir[2 * d.P + i] = v2;
+            d.vir[3 * d.P + i] = v3; d.vir[4 * d.P + i] = v4; d.vir[5 * d.P + i] = v5;
+        }
+    }
+}
+
+// ----------------------------------------------------------------------------
+// Hertz-Mindlin / Hooke contact with tangential history
+// (hertz_mindlin_contact_force, contact.rs:103-615; hooke_contact_force,
+// contact.rs:622-990).  The pair is always evaluated in the owner's frame
+// (i = owner, j = partner), exactly as the reference's half list does.
+// ----------------------------------------------------------------------------
+struct PairOut {
+    double fn[3];      // normal force (owner -= fn, partner += fn)
+    double ft[3];      // tangential force (owner += ft, partner -= ft)
+    double ti[3];      // tangential torque on the owner
+    double tj[3];      // tangential torque on the partner (same sign rule)
+    double tr[3];      // rolling torque (owner +=, partner -=)
+    double tw[3];      // twisting torque (owner +=, partner -=)
+    double spring[7];  // updated history, canonical frame
+    double vir[6];     // owner-side virial contribution
+    bool hit;          // a force was applied
+    bool tang;         // tangential/rolling/twisting stage reached
+    bool overlap;      // large-overlap warning (d / (r1 + r2) < 0.90)
+};
+
+__device__ __forceinline__ double mtab(const Dev& d, const SysParams& sp, int tab, int a, int b) {
+    return d.mat[sp.mat0 + ((long long)tab * sp.nmat + a) * sp.nmat + b];
+}
+
+__device__ void hm_pair(const Dev& d, const SysParams& sp, double dx, double dy, double dz, double r1, double r2,
+                        const double4& v_i, const double4& v_j, const double4& w_i, const double4& w_j,
+                        double mass_i, double mass_j, int mi, int mj, uint32_t tag_i, uint32_t tag_j,
+                        const double* stored, PairOut& o) {
+    const double kPi = 3.14159265358979323846;
+    const double SQRT_5_3 = 0.9128709291752768;  // dem_atom/src/lib.rs:63
+    const double EPS = 1e-30;                    // TANGENTIAL_EPSILON
+    const bool hooke = sp.contact_model == 1;
+    const bool use_dmt = sp.adhesion_model == 1;
+    const double dt = sp.dt;
+    o.hit = false;
+    o.tang = false;
+    o.overlap = false;
+    const double dist_sq = dx * dx + dy * dy + dz * dz;
+    const double sum_r = r1 + r2;
+    const double surface_energy = hooke ? 0.0 : mtab(d, sp, T_SURFACE, mi, mj);
+    const double r_eff = (r1 * r2) / sum_r;
+    const double e_eff = mtab(d, sp, T_EEFF, mi, mj);
+    double delta_pulloff = 0.0;
+    if (!hooke && surface_energy > 0.0 && !use_dmt) {
+        const double g = surface_energy;
+        delta_pulloff = cbrt(kPi * kPi * g * g * r_eff / (4.0 * e_eff * e_eff));
+    }
+    const double interaction_r = sum_r + delta_pulloff;
+    if (dist_sq >= interaction_r * interaction_r) return;
+    const double distance = sqrt(dist_sq);
+    if (distance == 0.0) return;
+    const double r_min = fmin(r1, r2);
+    const double delta = fmin(sum_r - distance, 0.5 * r_min);
+    if (hooke && delta <= 0.0) return;
+    if (delta > 0.0 && distance / sum_r < 0.90) o.overlap = true;
+    if (!hooke && delta <= 0.0 && surface_energy <= 0.0) return;
+    o.hit = true;
+    const double inv_dist = 1.0 / distance;
+    const double nx = dx * inv_dist, ny = dy * inv_dist, nz = dz * inv_dist;
+    const double g_eff = mtab(d, sp, T_GEFF, mi, mj);
+    const double inv_m_i = v_i.w > 0.0 ? v_i.w : 1.0 / mass_i;
+    const double inv_m_j = v_j.w > 0.0 ? v_j.w : 1.0 / mass_j;
+    const double m_r = 1.0 / (inv_m_i + inv_m_j);
+    const double beta = mtab(d, sp, T_BETA, mi, mj);
+    const double mu = mtab(d, sp, T_FRICTION, mi, mj);
+    const double mu_r = mtab(d, sp, T_ROLL_FRICTION, mi, mj);
+    const double mu_tw = mtab(d, sp, T_TWIST_FRICTION, mi, mj);
+    const double cohesion_energy = mtab(d, sp, T_COHESION, mi, mj);
+    const bool jkr_adhesion_only = !hooke && surface_energy > 0.0 && !use_dmt && delta <= 0.0;
+    double s_n = 0, k_n = 0, k_t = 0, kn = 0, kt = 0, gamma_n = 0;
+    if (hooke) {
+        kn = mtab(d, sp, T_KN, mi, mj);
+        kt = mtab(d, sp, T_KT, mi, mj);
+        gamma_n = 2.0 * beta * sqrt(kn * m_r);
+    } else if (delta > 0.0) {
+        const double sdr = sqrt(delta * r_eff);
+        s_n = 2.0 * e_eff * sdr;
+        k_n = 4.0 / 3.0 * e_eff * sdr;
+        k_t = 8.0 * g_eff * sdr;
+    }
+    const double oix = w_i.x, oiy = w_i.y, oiz = w_i.z;
+    const double ojx = w_j.x, ojy = w_j.y, ojz = w_j.z;
+    const double r1nx = r1 * nx, r1ny = r1 * ny, r1nz = r1 * nz;
+    const double vcix = v_i.x + (oiy * r1nz - oiz * r1ny);
+    const double vciy = v_i.y + (oiz * r1nx - oix * r1nz);
+    const double vciz = v_i.z + (oix * r1ny - oiy * r1nx);
+    const double r2nx = r2 * nx, r2ny = r2 * ny, r2nz = r2 * nz;
+    const double vcjx = v_j.x + (-ojy * r2nz + ojz * r2ny);
+    const double vcjy = v_j.y + (-ojz * r2nx + ojx * r2nz);
+    const double vcjz = v_j.z + (-ojx * r2ny + ojy * r2nx);
+    const double vrx = vcjx - vcix, vry = vcjy - vciy, vrz = vcjz - vciz;
+    const double v_n = vrx * nx + vry * ny + vrz * nz;
+    double f_n_mag;
+    if (hooke) {
+        if (cohesion_energy > 0.0) {
+            const double f_coh = cohesion_energy * kPi * delta * r_eff;
+            f_n_mag = kn * delta - gamma_n * v_n - f_coh;
+        } else {
+            f_n_mag = fmax(kn * delta - gamma_n * v_n, 0.0);
+        }
+    } else if (surface_energy > 0.0 && use_dmt) {
+        const double f_dmt = 2.0 * kPi * surface_energy * r_eff;
+        const double f_diss = 2.0 * beta * SQRT_5_3 * sqrt(s_n * m_r) * v_n;
+        f_n_mag = k_n * delta - f_diss - f_dmt;
+    } else if (surface_energy > 0.0) {
+        const double f_adh = 1.5 * kPi * surface_energy * r_eff;
+        if (jkr_adhesion_only) {
+            f_n_mag = -f_adh;
+        } else {
+            const double f_diss = 2.0 * beta * SQRT_5_3 * sqrt(s_n * m_r) * v_n;
+            f_n_mag = k_n * delta - f_diss - f_adh;
+        }
+    } else if (cohesion_energy > 0.0) {
+        const double f_diss = 2.0 * beta * SQRT_5_3 * sqrt(s_n * m_r) * v_n;
+        const double f_coh = cohesion_energy * kPi * delta * r_eff;
+        f_n_mag = k_n * delta - f_diss - f_coh;
+    } else {
+        const double f_diss = 2.0 * beta * SQRT_5_3 * sqrt(s_n * m_r) * v_n;
+        f_n_mag = fmax(k_n * delta - f_diss, 0.0);
+    }
+    o.fn[0] = f_n_mag * nx;
+    o.fn[1] = f_n_mag * ny;
+    o.fn[2] = f_n_mag * nz;
+    const double vs = sp.newton ? 1.0 : 0.5;
+    if (jkr_adhesion_only) {
+        const double fx = -o.fn[0] * vs, fy = -o.fn[1] * vs, fz = -o.fn[2] * vs;
+        o.vir[0] = dx * fx; o.vir[1] = dy * fy; o.vir[2] = dz * fz;
+        o.vir[3] = dx * fy; o.vir[4] = dx * fz; o.vir[5] = dy * fz;
+        return;
+    }
+    o.tang = true;
+    const double vtx = vrx - v_n * nx, vty = vry - v_n * ny, vtz = vrz - v_n * nz;
+    const double sign = tag_i < tag_j ? 1.0 : -1.0;
+    double sx = sign * stored[0], sy = sign * stored[1], sz = sign * stored[2];
+    const double sdn = sx * nx + sy * ny + sz * nz;
+    sx -= sdn * nx;
+    sy -= sdn * ny;
+    sz -= sdn * nz;
+    sx += vtx * dt;
+    sy += vty * dt;
+    sz += vtz * dt;
+    const double ktt = hooke ? kt : k_t;
+    const double s_mag = sqrt(sx * sx + sy * sy + sz * sz);
+    const double fts = ktt * s_mag;
+    const double ft_max = mu * fabs(f_n_mag);
+    if (fts > ft_max && fts > EPS) {
+        const double sc = ft_max / fts;
+        sx *= sc; sy *= sc; sz *= sc;
+    }
+    const double gamma_t = 2.0 * SQRT_5_3 * beta * sqrt(ktt * m_r);
+    double ftx = ktt * sx - gamma_t * vtx;
+    double fty = ktt * sy - gamma_t * vty;
+    double ftz = ktt * sz - gamma_t * vtz;
+    const double ftm = sqrt(ftx * ftx + fty * fty + ftz * ftz);
+    if (ftm > ft_max && ftm > EPS) {
+        const double sc = ft_max / ftm;
+        ftx *= sc; fty *= sc; ftz *= sc;
+    }
+    o.ft[0] = ftx; o.ft[1] = fty; o.ft[2] = ftz;
+    o.ti[0] = r1ny * ftz - r1nz * fty; o.ti[1] = r1nz * ftx - r1nx * ftz; o.ti[2] = r1nx * fty - r1ny * ftx;
+    o.tj[0] = r2ny * ftz - r2nz * fty; o.tj[1] = r2nz * ftx - r2nx * ftz; o.tj[2] = r2nx * fty - r2ny * ftx;
+    const double orx = oix - ojx, ory = oiy - ojy, orz = oiz - ojz;
+    const double odn = orx * nx + ory * ny + orz * nz;
+    const double rollx = orx - odn * nx, rolly = ory - odn * ny, rollz = orz - odn * nz;
+    double rdx = sign * stored[3], rdy = sign * stored[4], rdz = sign * stored[5];
+    double twd = sign * stored[6];
+    o.tr[0] = o.tr[1] = o.tr[2] = 0.0;
+    o.tw[0] = o.tw[1] = o.tw[2] = 0.0;
+    if (mu_r > 0.0) {
+        const double roll_mag = sqrt(rollx * rollx + rolly * rolly + rollz * rollz);
+        if (sp.rolling_model == 1) {
+            const double k_roll = mtab(d, sp, T_KROLL, mi, mj);
+            const double g_roll = mtab(d, sp, T_GROLL, mi, mj);
+            const double rdn = rdx * nx + rdy * ny + rdz * nz;
+            rdx -= rdn * nx; rdy -= rdn * ny; rdz -= rdn * nz;
+            rdx += rollx * dt; rdy += rolly * dt; rdz += rollz * dt;
+            double tx = -k_roll * rdx - g_roll * rollx;
+            double ty = -k_roll * rdy - g_roll * rolly;
+            double tz = -k_roll * rdz - g_roll * rollz;
+            const double trm = sqrt(tx * tx + ty * ty + tz * tz);
+            const double tau_max = mu_r * fabs(f_n_mag) * r_eff;
+            if (trm > tau_max && trm > EPS) {
+                const double sc = tau_max / trm;
+                tx *= sc; ty *= sc; tz *= sc;
+                if (k_roll > EPS) {
+                    rdx = (tx + g_roll * rollx) / (-k_roll);
+                    rdy = (ty + g_roll * rolly) / (-k_roll);
+                    rdz = (tz + g_roll * rollz) / (-k_roll);
+                }
+            }
+            o.tr[0] = tx; o.tr[1] = ty; o.tr[2] = tz;
+        } else if (roll_mag > 1e-30) {
+            const double tau_mag = mu_r * fabs(f_n_mag) * r_eff;
+            const double inv_roll = tau_mag / roll_mag;
+            o.tr[0] = -inv_roll * rollx; o.tr[1] = -inv_roll * rolly; o.tr[2] = -inv_roll * rollz;
+        }
+    }
+    if (mu_tw > 0.0) {
+        const double twist_vel = odn;
+        if (sp.twisting_model == 1) {
+            const double k_tw = mtab(d, sp, T_KTWIST, mi, mj);
+            const double g_tw = mtab(d, sp, T_GTWIST, mi, mj);
+            twd += twist_vel * dt;
+            double tau_tw = -k_tw * twd - g_tw * twist_vel;
+            const double tau_max = mu_tw * fabs(f_n_mag) * r_eff;
+            if (fabs(tau_tw) > tau_max) {
+                tau_tw = copysign(1.0, tau_tw) * tau_max;
+                if (k_tw > EPS) twd = (tau_tw + g_tw * twist_vel) / (-k_tw);
+            }
+            o.tw[0] = tau_tw * nx; o.tw[1] = tau_tw * ny; o.tw[2] = tau_tw * nz;
+        } else if (fabs(twist_vel) > 1e-30) {
+            const double tau = mu_tw * fabs(f_n_mag) * r_eff;
+            const double sg = twist_vel > 0.0 ? -1.0 : 1.0;
+            o.tw[0] = sg * tau * nx; o.tw[1] = sg * tau * ny; o.tw[2] = sg * tau * nz;
+        }
+    }
+    {
+        const double vfx = (-o.fn[0] + ftx) * vs, vfy = (-o.fn[1] + fty) * vs, vfz = (-o.fn[2] + ftz) * vs;
+        o.vir[0] = dx * vfx; o.vir[1] = dy * vfy; o.vir[2] = dz * vfz;
+        o.vir[3] = dx * vfy; o.vir[4] = dx * vfz; o.vir[5] = dy * vfz;
+    }
+    o.spring[0] = sign * sx; o.spring[1] = sign * sy; o.spring[2] = sign * sz;
+    o.spring[3] = sign * rdx; o.spring[4] = sign * rdy; o.spring[5] = sign * rdz;
+    o.spring[6] = sign * twd;
+}
+
+// Look up the spring stored by particle `p` (local index lp in its system)
+// for partner tag `t` in history buffer `hc`.
+__device__ __forceinline__ bool hist_find(const Dev& d, const SysParams& sp, int hc, long long p, int lp,
+                                          uint32_t t, double* out) {
+    const int n = d.hcnt[hc][p];
+    for (int c = 0; c < n; c++) {
+        if (d.htag[hc][sp.h0 + (long long)c * sp.npad + lp] == t) {
+            for (int q = 0; q < 7; q++) out[q] = d.hval[hc][sp.h0 * 7 + (long long)(c * 7 + q) * sp.npad + lp];
+            return true;
+        }
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(BLK) k_dem_fp64(Dev d, int hcur) {
+    const int s = d.blk_sys[blockIdx.x];
+    const SysParams& sp = d.sp[s];
+    if (sp.kind != 0) return;
+    SysState* st = d.ss + s;
+    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    if (li >= sp.n) return;
+    const long long i = (long long)sp.p0 + li;
+    const int hn = hcur ^ 1;
+    const double4 xi = d.pos[i];
+    const double4 vi = d.vel[i];
+    const double4 wi = d.omg[i];
+    const double mass_i = d.mass[i];
+    const int ti_ = (int)d.type[i];
+    const uint32_t tag_i = d.tag[i];
+    const int nn = d.nnum[i];
+    const long long base = sp.lst0 + li;
+    double F[3] = {0, 0, 0}, T[3] = {0, 0, 0}, V[6] = {0, 0, 0, 0, 0, 0};
+    int nh = 0, nover = 0;
+    PairOut o;
+    for (int k = 0; k < nn; k++) {
+        const uint32_t e = d.nlist[base + (long long)k * sp.npad];
+        const int lj = (int)(e & IDX_MASK);
+        const long long j = sp.p0 + lj;
+        const uint32_t code = e >> IDX_BITS;
+        const bool own = code >= 27u;
+        int sx, sy, sz;
+        decode_shift((int)(own ? code - 27u : code), sx, sy, sz);
+        const double4 xj = d.pos[j];
+        const double4 vj = d.vel[j];
+        const double4 wj = d.omg[j];
+        const double mass_j = d.mass[j];
+        const int tj_ = (int)d.type[j];
+        const uint32_t tag_j = d.tag[j];
+        double stored[7] = {0, 0, 0, 0, 0, 0, 0};
+        if (own) {
+            hist_find(d, sp, hcur, i, li, tag_j, stored);
+            const double dx = img_coord(xj.x, sx, sp.L[0]) - xi.x;
+            const double dy = img_coord(xj.y, sy, sp.L[1]) - xi.y;
+            const double dz = img_coord(xj.z, sz, sp.L[2]) - xi.z;
+            hm_pair(d, sp, dx, dy, dz, xi.w, xj.w, vi, vj, wi, wj, mass_i, mass_j, ti_, tj_, tag_i, tag_j, stored, o);
+            if (!o.hit) continue;
+            F[0] -= o.fn[0]; F[1] -= o.fn[1]; F[2] -= o.fn[2];
+            if (o.overlap) nover++;
+            for (int q = 0; q < 6; q++) V[q] += o.vir[q];
+            if (!o.tang) continue;
+            F[0] += o.ft[0]; F[1] += o.ft[1]; F[2] += o.ft[2];
+            T[0] += o.ti[0]; T[1] += o.ti[1]; T[2] += o.ti[2];
+            T[0] += o.tr[0]; T[1] += o.tr[1]; T[2] += o.tr[2];
+            T[0] += o.tw[0]; T[1] += o.tw[1]; T[2] += o.tw[2];
+            if (nh < sp.hcap) {
+                d.htag[hn][sp.h0 + (long long)nh * sp.npad + li] = tag_j;
+                for (int q = 0; q < 7; q++)
+                    d.hval[hn][sp.h0 * 7 + (long long)(nh * 7 + q) * sp.npad + li] = o.spring[q];
+            }
+            nh++;
+        } else {
+            hist_find(d, sp, hcur, j, lj, tag_i, stored);
+            const double dx = img_coord(xi.x, -sx, sp.L[0]) - xj.x;
+            const double dy = img_coord(xi.y, -sy, sp.L[1]) - xj.y;
+            const double dz = img_coord(xi.z, -sz, sp.L[2]) - xj.z;
+            hm_pair(d, sp, dx, dy, dz, xj.w, xi.w, vj, vi, wj, wi, mass_j, mass_i, tj_, ti_, tag_j, tag_i, stored, o);
+            if (!o.hit) continue;
+            F[0] += o.fn[0]; F[1] += o.fn[1]; F[2] += o.fn[2];
+            if (!o.tang) continue;
+            F[0] -= o.ft[0]; F[1] -= o.ft[1]; F[2] -= o.ft[2];
+            T[0] += o.tj[0]; T[1] += o.tj[1]; T[2] += o.tj[2];
+            T[0] -= o.tr[0]; T[1] -= o.tr[1]; T[2] -= o.tr[2];
+            T[0] -= o.tw[0]; T[1] -= o.tw[1]; T[2] -= o.tw[2];
+        }
+    }
+    if (nh > sp.hcap) {
+        atomicOr(&st->status, ST_HIST_OVF);
+        nh = sp.hcap;
+    }
+    if (d.hist_any) d.hcnt[hn][i] = nh;
+    if (nover) atomicAdd(&st->overlap, nover);
+    d.frc[i] = make_double4(F[0], F[1], F[2], 0.0);
+    d.trq[i] = make_double4(T[0], T[1], T[2], 0.0);
+    if (sp.virial)
+        for (int q = 0; q < 6; q++) d.vir[q * d.P + i] = V[q];
+}
+
+// ----------------------------------------------------------------------------
+// final integration + thermostat half step + per-step bookkeeping
+// ----------------------------------------------------------------------------
+// final_integration (mddem_verlet/src/lib.rs:136-154), final_rotation
+// (rotational.rs:87-100), nh_post_final (md_thermostat/src/lib.rs:313-353).
+// integrate = 0: reductions and rebuild bookkeeping only (force-only evaluation).
+__global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
+    const int s = d.blk_sys[blockIdx.x];
+    const SysParams& sp = d.sp[s];
+    SysState* st = d.ss + s;
+    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    const bool act = li < sp.n;
+    const long long i = (long long)sp.p0 + li;
+    const double dt = sp.dt;
+    double vals[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    int bad = 0;
+    if (act) {
+        const double4 f = d.frc[i];
+        double4 v = d.vel[i];
+        if (integrate) {
+            const double h = 0.5 * dt * v.w;
+            v.x += h * f.x;
+            v.y += h * f.y;
+            v.z += h * f.z;
+            if (sp.nh) {
+                const double scale = exp(-dt / 2.0 * st->p_xi_pre / sp.nh_Q);
+                v.x *= scale;
+                v.y *= scale;
+                v.z *= scale;
+            }
+            d.vel[i] = v;
+        }
+        vals[0] = d.mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z);
+        vals[7] = f.w;
+        if (sp.kind == 0 && integrate) {
+            double4 w = d.omg[i];
+            if (w.w != 0.0) {
+                const double4 tq = d.trq[i];
+                w.x += 0.5 * dt * tq.x * w.w;
+                w.y += 0.5 * dt * tq.y * w.w;
+                w.z += 0.5 * dt * tq.z * w.w;
+                d.omg[i] = w;
+            }
+        }
+        if (sp.virial)
+            for (int q = 0; q < 6; q++) vals[1 + q] = d.vir[q * d.P + i];
+        const double4 x = d.pos[i];
+        if (!isfinite(v.x + v.y + v.z + x.x + x.y + x.z)) bad = 1;
+    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&st->status, ST_NAN);
+    double out[8];
+    if (system_reduce<8>(d, s, vals, out) && threadIdx.x == 0) {
+        const double ke = 0.5 * out[0];
+        st->ke = ke;
+        if (sp.nh && integrate) st->p_xi_post = st->p_xi_pre + (dt / 2.0) * (2.0 * ke - sp.nh_ndof * sp.nh_T);
+        if (sp.virial)
+            for (int q = 0; q < 6; q++) st->vir[q] = out[1 + q];
+        st->pe = out[7];
+        const bool rb = do_rebuild(st);
+        if (integrate) {
+            st->steps_since_build = rb ? 0 : st->steps_since_build + 1;
+            st->sort_counter = st->periodic_sort ? 0 : st->sort_counter + 1;
+            st->step += 1;
+        } else if (rb) {
+            st->steps_since_build = 0;
+        }
+        if (rb) st->nbuilds += 1;
+        if (st->overlap > 500) st->status |= ST_OVERLAP;
+        st->overlap = 0;
+        st->rebuild = 0;
+        st->periodic_sort = 0;
+        st->nonid = 0;
+    }
+}
+
+// KE of the uploaded velocities (the first nh_pre_initial's compute_ke).
+__global__ void __launch_bounds__(BLK) k_ke_init(Dev d) {
+    const int s = d.blk_sys[blockIdx.x];
+    const SysParams& sp = d.sp[s];
+    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    double vals[1] = {0.0};
+    if (li < sp.n) {
+        const long long i = (long long)sp.p0 + li;
+        const double4 v = d.vel[i];
+        vals[0] = d.mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z);
+    }
+    double out[1];
+    if (system_reduce<1>(d, s, vals, out) && threadIdx.x == 0) d.ss[s].ke = 0.5 * out[0];
+}
+
+// thermo pass 1: sum m, sum m v, compute_ke sum, pe  (granular_temp.rs:62-101, atom.rs:489-502)
+__global__ void __launch_bounds__(BLK) k_thermo1(Dev d, double* out16) {
+    const int s = d.blk_sys[blockIdx.x];
+    const SysParams& sp = d.sp[s];
+    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    double vals[6] = {0, 0, 0, 0, 0, 0};
+    if (li < sp.n) {
+        const long long i = (long long)sp.p0 + li;
+        const double4 v = d.vel[i];
+        const double m = d.mass[i];
+        vals[0] = m;
+        vals[1] = m * v.x;
+        vals[2] = m * v.y;
+        vals[3] = m * v.z;
+        vals[4] = m * (v.x * v.x + v.y * v.y + v.z * v.z);
+        vals[5] = d.frc[i].w;
+    }
+    double out[6];
+    if (system_reduce<6>(d, s, vals, out) && threadIdx.x == 0) {
+        double* o = out16 + (size_t)s * 16;
+        o[0] = 0.5 * out[4];
+        o[1] = out[5];
+        o[5] = sqrt(out[1] * out[1] + out[2] * out[2] + out[3] * out[3]);
+        o[8 + 0] = out[0];
+        o[8 + 1] = out[1] / out[0];
+        o[8 + 2] = out[2] / out[0];
+        o[8 + 3] = out[3] / out[0];
+    }
+}
+
+// thermo pass 2: sum m |v - vbar|^2 -> granular temperature
+__global__ void __launch_bounds__(BLK) k_thermo2(Dev d, double* out16) {
+    const int s = d.blk_sys[blockIdx.x];
+    const SysParams& sp = d.sp[s];
+    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    const double* o = out16 + (size_t)s * 16;
+    double vals[1] = {0.0};
+    if (li < sp.n) {
+        const long long i = (long long)sp.p0 + li;
+        const double4 v = d.vel[i];
+        const double m = d.mass[i];
+        const double dx = v.x - o[9], dy = v.y - o[10], dz = v.z - o[11];
+        vals[0] = m * (dx * dx) + m * (dy * dy) + m * (dz * dz);
+    }
+    double out[1];
+    if (system_reduce<1>(d, s, vals, out) && threadIdx.x == 0) out16[(size_t)s * 16 + 4] = out[0] / (3.0 * o[8]);
+}
+
+// ----------------------------------------------------------------------------
+// launchers
+// ----------------------------------------------------------------------------
+int launch_initial(const Dev& d, cudaStream_t st) {
+    k_initial<<<d.nblocks, BLK, 0, st>>>(d);
+    return 1;
+}
+
+int launch_rebuild(const Dev& d, int hcur, cudaStream_t st) {
+    k_cells<<<d.nblocks, BLK, 0, st>>>(d);
+    k_scan<<<d.nsys, 1024, 0, st>>>(d);
+    k_scatter<<<d.nblocks, BLK, 0, st>>>(d);
+    k_cellsort<<<d.ncblocks, BLK, 0, st>>>(d);
+    k_gather<<<d.nblocks, BLK, 0, st>>>(d, hcur);
+    k_copyback<<<d.nblocks, BLK, 0, st>>>(d, hcur);
+    k_build<<<d.nblocks, BLK, 0, st>>>(d);
+    return 7;
+}
+
+int launch_force_fp64(const Dev& d, int hcur, int has_lj, int has_dem, int tpp, cudaStream_t st) {
+    int n = 0;
+    if (has_lj) {
+        switch (tpp) {
+            case 2: k_lj_fp64<2><<<d.nblocks * 2, BLK, 0, st>>>(d); break;
+            case 4: k_lj_fp64<4><<<d.nblocks * 4, BLK, 0, st>>>(d); break;
+            case 8: k_lj_fp64<8><<<d.nblocks * 8, BLK, 0, st>>>(d); break;
+            default: k_lj_fp64<1><<<d.nblocks, BLK, 0, st>>>(d); break;
+        }
+        n++;
+    }
+    if (has_dem) {
+        k_dem_fp64<<<d.nblocks, BLK, 0, st>>>(d, hcur);
+        n++;
+    }
+    return n;
+}
+
+int launch_final(const Dev& d, cudaStream_t st, int integrate) {
+    k_final<<<d.nblocks, BLK, 0, st>>>(d, integrate);
+    return 1;
+}
+
+int launch_ke_init(const Dev& d, cudaStream_t st) {
+    k_ke_init<<<d.nblocks, BLK, 0, st>>>(d);
+    return 1;
+}
+
+int launch_thermo(const Dev& d, double* out, cudaStream_t st) {
+    k_thermo1<<<d.nblocks, BLK, 0, st>>>(d, out);
+    k_thermo2<<<d.nblocks, BLK, 0, st>>>(d, out);
+    return 2;
+}
+
+}  // namespace mdg

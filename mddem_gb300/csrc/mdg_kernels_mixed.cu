@@ -1,0 +1,120 @@
+// mdg_kernels_mixed.cu -- mixed-precision force kernels.
+//
+// Positions stay FP64 in the integrator; the pair kernels read a two-float
+// copy relative to the box corner, x - lo = hi + lo_part (pos_hi, pos_lo),
+// written by the integrator each step.  Pair separations are formed as
+// (x_j,hi - x_i,hi) + (x_j,lo - x_i,lo), with a periodic shift applied to the
+// coordinate that sits next to the crossed face so that the hi-part
+// difference stays exact (Sterbenz); the separation then carries ~1e-7
+// relative error.  Force arithmetic is FP32; per-particle sums use Kahan
+// compensation (Kahan 1965) and are handed to the FP64 integrator as doubles.
+#include "mdg_internal.cuh"
+
+namespace mdg {
+
+struct Kahan {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ float sep(float xj_hi, float xj_lo, float xi_hi, float xi_lo, int s, float Lh, float Ll) {
+    float dh, dl;
+    if (s > 0) {
+        dh = xj_hi - (xi_hi - Lh);
+        dl = xj_lo - (xi_lo - Ll);
+    } else if (s < 0) {
+        dh = (xj_hi - Lh) - xi_hi;
+        dl = (xj_lo - Ll) - xi_lo;
+    } else {
+        dh = xj_hi - xi_hi;
+        dl = xj_lo - xi_lo;
+    }
+    return dh + dl;
+}
+
+// LJ 12-6 in FP32 with compensated per-particle sums (same list, same owner
+// frames as the FP64 kernel).
+template <int TPP>
+__global__ void __launch_bounds__(BLK) k_lj_mixed(Dev d) {
+    const int pb = blockIdx.x / TPP;
+    const int sub = blockIdx.x % TPP;
+    const int s = d.blk_sys[pb];
+    const SysParams& sp = d.sp[s];
+    if (sp.kind != 1) return;
+    const int lane = threadIdx.x % TPP;
+    const int li = (pb - sp.b0) * BLK + sub * (BLK / TPP) + threadIdx.x / TPP;
+    const bool act = li < sp.n;
+    const long long i = (long long)sp.p0 + li;
+    Kahan kx, ky, kz, kp;
+    if (act) {
+        const float4 hi = d.pos_hi[i];
+        const float4 lo = d.pos_lo[i];
+        const int nn = d.nnum[i];
+        const long long base = sp.lst0 + li;
+        const float lj1 = (float)sp.lj1, lj2 = (float)sp.lj2, lj3 = (float)sp.lj3, lj4 = (float)sp.lj4;
+        const float cut2 = (float)sp.lj_cut2;
+        const float half = sp.newton ? 1.f : 0.5f;
+        const float Lh0 = (float)sp.L[0], Lh1 = (float)sp.L[1], Lh2 = (float)sp.L[2];
+        const float Ll0 = (float)(sp.L[0] - (double)Lh0), Ll1 = (float)(sp.L[1] - (double)Lh1),
+                    Ll2 = (float)(sp.L[2] - (double)Lh2);
+        for (int k = lane; k < nn; k += TPP) {
+            const uint32_t e = __ldg(d.nlist + base + (long long)k * sp.npad);
+            const long long j = sp.p0 + (e & IDX_MASK);
+            const uint32_t code = e >> IDX_BITS;
+            const bool own = code >= 27u;
+            const int sc = (int)(own ? code - 27u : code);
+            const int sx = sc / 9 - 1, sy = (sc / 3) % 3 - 1, sz = sc % 3 - 1;
+            const float4 hj = __ldg(d.pos_hi + j);
+            const float4 lj = __ldg(d.pos_lo + j);
+            // owner frame: d = x_partner(+shift) - x_owner; as seen from i the
+            // partner-side sign flips, so use d_i = x_j(+s) - x_i in both cases
+            const float dx = sep(hj.x, lj.x, hi.x, lo.x, sx, Lh0, Ll0);
+            const float dy = sep(hj.y, lj.y, hi.y, lo.y, sy, Lh1, Ll1);
+            const float dz = sep(hj.z, lj.z, hi.z, lo.z, sz, Lh2, Ll2);
+            const float r2 = dx * dx + dy * dy + dz * dz;
+            if (r2 >= cut2) continue;
+            const float r2inv = __frcp_rn(r2);
+            const float r6inv = r2inv * r2inv * r2inv;
+            const float fpair = r2inv * r6inv * (lj1 * r6inv - lj2);
+            kx.add(-fpair * dx);
+            ky.add(-fpair * dy);
+            kz.add(-fpair * dz);
+            if (own) kp.add(r6inv * (lj3 * r6inv - lj4) * half);
+        }
+    }
+    double fx = kx.value(), fy = ky.value(), fz = kz.value(), pe = kp.value();
+    if (TPP > 1) {
+#pragma unroll
+        for (int o = TPP / 2; o > 0; o >>= 1) {
+            fx += __shfl_down_sync(0xffffffffu, fx, o, TPP);
+            fy += __shfl_down_sync(0xffffffffu, fy, o, TPP);
+            fz += __shfl_down_sync(0xffffffffu, fz, o, TPP);
+            pe += __shfl_down_sync(0xffffffffu, pe, o, TPP);
+        }
+    }
+    if (act && lane == 0) d.frc[i] = make_double4(fx, fy, fz, pe);
+}
+
+int launch_force_mixed(const Dev& d, int hcur, int has_lj, int has_dem, int tpp, cudaStream_t st) {
+    (void)hcur;
+    (void)has_dem;
+    int n = 0;
+    if (has_lj) {
+        switch (tpp) {
+            case 2: k_lj_mixed<2><<<d.nblocks * 2, BLK, 0, st>>>(d); break;
+            case 4: k_lj_mixed<4><<<d.nblocks * 4, BLK, 0, st>>>(d); break;
+            case 8: k_lj_mixed<8><<<d.nblocks * 8, BLK, 0, st>>>(d); break;
+            default: k_lj_mixed<1><<<d.nblocks, BLK, 0, st>>>(d); break;
+        }
+        n++;
+    }
+    return n;
+}
+
+}  // namespace mdg

@@ -1,0 +1,90 @@
+/*
+ * mdg_oracle.h -- C interface of the CPU FP64 oracle.
+ *
+ * TEST INFRASTRUCTURE ONLY. The oracle is a plain C++17 restatement of
+ * MDDEM's single-rank CPU path for the particle hot path (periodic ghosts,
+ * bin sort, half neighbor list, Hertz-Mindlin / Hooke contact with history,
+ * LJ 12-6, velocity Verlet, rotational Verlet, Nose-Hoover).  It is used by
+ * tests/, by __graft_entry__.smoke() and by bench.py's CPU baseline leg as the
+ * checker, never as the product path.
+ *
+ * Parity pin: the reference (Rust, un-vendored git dependency grass @ ea21ea36)
+ * cannot be built here, so the oracle is pinned against the known-answer tests
+ * held in the reference's own unit tests (analytic Hertz force, Verlet exact
+ * values, rotational kick, beta(e) formula, bin list vs brute force), restated
+ * in tests/test_oracle_kat.py and tests/golden/.
+ */
+#ifndef MDG_ORACLE_H
+#define MDG_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_material {
+    double youngs_mod, poisson_ratio, restitution, friction;
+    double rolling_friction, twisting_friction, cohesion_energy, surface_energy;
+    double kn, kt, rolling_stiffness, rolling_damping, twisting_stiffness, twisting_damping;
+} orc_material;
+
+typedef struct orc_config {
+    int kind;                 /* 0 = DEM granular, 1 = LJ */
+    double lo[3], hi[3];      /* [domain], fully periodic */
+    double dt;                /* [run] dt */
+    double skin_fraction;     /* [neighbor] */
+    double bin_size;
+    int every, check, sort_every, newton;
+    int n_materials;          /* [[dem.materials]] */
+    const orc_material* materials;
+    int contact_model;        /* 0 hertz, 1 hooke */
+    int adhesion_model;       /* 0 jkr, 1 dmt */
+    int rolling_model;        /* 0 constant, 1 sds */
+    int twisting_model;       /* 0 constant, 1 sds */
+    double lj_epsilon, lj_sigma, lj_cutoff;   /* [lj] single type */
+    int nose_hoover;          /* 1 = NoseHooverPlugin present */
+    double nh_temperature, nh_coupling;
+    int virial;               /* VirialStress active each step */
+} orc_config;
+
+enum {
+    ORC_F_POS = 0, ORC_F_VEL = 1, ORC_F_FORCE = 2, ORC_F_OMEGA = 3, ORC_F_TORQUE = 4,
+    ORC_F_QUAT = 5, ORC_F_MASS = 6, ORC_F_RADIUS = 7, ORC_F_LAST_BUILD_POS = 8
+};
+
+void*  orc_create(const orc_config* cfg);
+void   orc_destroy(void* h);
+/* Load nlocal particles (SoA, xyz interleaved per particle).  DEM arrays may be
+ * NULL for LJ.  image may be NULL (zeros). */
+int    orc_load(void* h, size_t n, const uint32_t* tag, const uint32_t* type,
+                const double* pos, const double* vel, const double* mass,
+                const double* cutoff_radius, const double* radius,
+                const double* density, const double* inv_inertia,
+                const double* omega, const double* quat);
+/* Advance nsteps full timesteps (reference schedule order). */
+int    orc_step(void* h, long nsteps);
+/* Ghost rebuild + bin list + force evaluation at the current state, no
+ * integration (single-step force parity). */
+int    orc_force_only(void* h);
+size_t orc_nlocal(void* h);
+/* Copy a per-local-atom field out (3 or 4 doubles per atom). */
+int    orc_get_field(void* h, int field, double* out);
+int    orc_get_tags(void* h, uint32_t* out);
+int    orc_get_image(void* h, int32_t* out);
+/* Half-list pairs as (owner tag, partner tag); returns count, fills up to cap. */
+size_t orc_get_pairs(void* h, uint32_t* out, size_t cap);
+/* Contact history: (owner tag, partner tag) + 7 doubles per entry. */
+size_t orc_get_history(void* h, uint32_t* keys, double* vals, size_t cap);
+/* Inject history entries (owner tag, partner tag, 7 doubles). */
+int    orc_set_history(void* h, size_t n, const uint32_t* keys, const double* vals);
+/* thermo: [ke, pe, temp(3N-3), p_xi, granular_temp, |momentum|,
+ *          vxx, vyy, vzz, vxy, vxz, vyz, nbuilds, step, ndof, q_mass] */
+int    orc_thermo(void* h, double* out16);
+long   orc_overlap_count(void* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,218 @@
+"""GPU parity: CUDA path (through the C ABI) vs the CPU FP64 oracle.
+
+Tolerances (stated here, as the bar of the FP64 path):
+  * neighbour pair sets and contact-history keys: identical;
+  * single-step forces and torques: per particle
+    |F_gpu - F_ref|_inf / max(|F_ref|_inf, sum_pairs |f_pair|, tiny) <= 1e-12;
+  * contact-history values: <= 1e-12 relative to the largest spring;
+  * 100-step trajectories: positions within 1e-10 of the box length for the
+    chaotic LJ melt and 1e-12 for the granular gas.
+"""
+import numpy as np
+import pytest
+
+from helpers import by_tag, lj_pair_force_scale, overlapping_spheres, pair_set, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx(cfg, st):
+    from mddem_gb300 import capi
+
+    ctx = capi.Context(cfg, len(st["tag"]))
+    ctx.upload(st)
+    return ctx
+
+
+def _oracle(cfg, st):
+    from oracle.oracle import Oracle
+
+    o = Oracle(cfg)
+    o.load(st)
+    return o
+
+
+def test_lj_force_only_parity(gpu_lib):
+    from mddem_gb300 import config, inputs
+
+    cfg = config.lj_fluid_config()
+    st = inputs.lj_fcc(6, 10.06, 0.85, 0.85, seed=5)
+    rng = np.random.default_rng(0)
+    st["pos"] = st["pos"] + rng.normal(scale=0.05, size=st["pos"].shape)  # off-lattice
+    ctx = _ctx(cfg, st)
+    ctx.force_only()
+    g = ctx.download()
+    gp = ctx.pairs()
+    o = _oracle(cfg, st)
+    o.force_only()
+    r = o.state()
+    rp = o.pairs()
+    assert pair_set(gp) == pair_set(rp)
+    assert len(gp) == len(rp)
+    (gf,) = by_tag(g, "force")
+    rf, rpos = by_tag(r, "force", "pos")
+    scale = lj_pair_force_scale(rpos, cfg.box, rp)
+    assert rel_err(gf, rf, scale) <= 1e-12
+    assert abs(ctx.thermo()["pe"] - o.thermo()["pe"]) <= 1e-12 * abs(o.thermo()["pe"])
+
+
+def test_lj_100_steps_nose_hoover(gpu_lib):
+    from mddem_gb300 import config, inputs
+
+    cfg = config.lj_fluid_config()
+    st = inputs.lj_fcc(6, 10.06, 0.85, 0.85, seed=7)
+    ctx = _ctx(cfg, st)
+    o = _oracle(cfg, st)
+    ctx.step(100)
+    o.step(100)
+    g = ctx.download()
+    r = o.state()
+    gpos, gvel = by_tag(g, "pos", "vel")
+    rpos, rvel = by_tag(r, "pos", "vel")
+    assert np.max(np.abs(gpos - rpos)) <= 1e-10 * 10.06
+    assert np.max(np.abs(gvel - rvel)) <= 1e-9
+    tg, tr = ctx.thermo(), o.thermo()
+    for k in ("ke", "pe"):
+        assert abs(tg[k] - tr[k]) <= 1e-10 * abs(tr[k]), k
+    assert abs(tg["p_xi"] - tr["p_xi"]) <= 1e-8 * max(1.0, abs(tr["p_xi"]))
+    assert tg["nbuilds"] == tr["nbuilds"]
+
+
+def _dem_cfg(**kw):
+    from mddem_gb300 import config
+
+    return config.granular_gas_config(box=0.012, dt=1e-7, **kw)
+
+
+def _dem_state(seed=1, n=900):
+    return overlapping_spheres(n, 0.012, 5e-4, seed=seed)
+
+
+def _check_dem_force_parity(cfg, st, hist=True):
+    ctx = _ctx(cfg, st)
+    o = _oracle(cfg, st)
+    if hist:
+        # seed the spring history of every owner pair with random springs
+        o.force_only()
+        keys, vals = o.history()
+        rng = np.random.default_rng(3)
+        vals = rng.normal(scale=1e-6, size=vals.shape)
+        o2 = _oracle(cfg, st)
+        o2.set_history(keys, vals)
+        ctx.set_history(keys, vals)
+        o = o2
+    ctx.force_only()
+    o.force_only()
+    g = ctx.download()
+    r = o.state()
+    assert pair_set(ctx.pairs()) == pair_set(o.pairs())
+    gf, gt = by_tag(g, "force", "torque")
+    rf, rt = by_tag(r, "force", "torque")
+    fs = np.max(np.abs(rf)) * 1e-3
+    ts = np.max(np.abs(rt)) * 1e-3 if np.max(np.abs(rt)) > 0 else 1e-300
+    assert rel_err(gf, rf, fs) <= 1e-12
+    assert rel_err(gt, rt, ts) <= 1e-12
+    gk, gv = ctx.history()
+    rk, rv = o.history()
+    assert pair_set(gk) == pair_set(rk)
+    gd = {tuple(k): v for k, v in zip(gk.tolist(), gv)}
+    vmax = max(1e-300, float(np.max(np.abs(rv)))) if len(rv) else 1.0
+    for k, v in zip(rk.tolist(), rv):
+        assert np.max(np.abs(gd[tuple(k)] - v)) <= 1e-12 * vmax
+    return len(rk)
+
+
+def test_dem_hertz_force_history_parity(gpu_lib):
+    n = _check_dem_force_parity(_dem_cfg(), _dem_state())
+    assert n > 100
+
+
+@pytest.mark.parametrize("variant", [
+    dict(contact_model="hooke"),
+    dict(rolling=0.05, twisting=0.03),
+    dict(rolling=0.05, twisting=0.03, rolling_model="sds", twisting_model="sds"),
+    dict(surface_energy=0.05),
+    dict(surface_energy=0.05, adhesion_model="dmt"),
+    dict(cohesion_energy=500.0),
+])
+def test_dem_contact_variants(gpu_lib, variant):
+    from mddem_gb300.config import Material
+
+    m = Material()
+    v = dict(variant)
+    if v.pop("contact_model", None) == "hooke":
+        m.kn, m.kt = 2e5, 5e4
+        cfg = _dem_cfg(contact_model="hooke")
+    else:
+        cfg = _dem_cfg()
+    m.rolling_friction = v.pop("rolling", 0.0)
+    m.twisting_friction = v.pop("twisting", 0.0)
+    m.surface_energy = v.pop("surface_energy", 0.0)
+    m.cohesion_energy = v.pop("cohesion_energy", 0.0)
+    if v.get("rolling_model") == "sds":
+        m.rolling_stiffness, m.rolling_damping = 1e-4, 1e-7
+        m.twisting_stiffness, m.twisting_damping = 1e-4, 1e-7
+    cfg = cfg.replace(materials=[m], **v)
+    _check_dem_force_parity(cfg, _dem_state(seed=2))
+
+
+def test_dem_100_steps_trajectory(gpu_lib):
+    cfg = _dem_cfg()
+    st = _dem_state(seed=4)
+    ctx = _ctx(cfg, st)
+    o = _oracle(cfg, st)
+    ctx.step(100)
+    o.step(100)
+    g = ctx.download()
+    r = o.state()
+    gpos, gw, gq = by_tag(g, "pos", "omega", "quat")
+    rpos, rw, rq = by_tag(r, "pos", "omega", "quat")
+    assert np.max(np.abs(gpos - rpos)) <= 1e-12 * 0.012
+    assert np.max(np.abs(gw - rw)) <= 1e-9 * np.max(np.abs(rw))
+    assert np.max(np.abs(gq - rq)) <= 1e-12
+    assert pair_set(ctx.history()[0]) == pair_set(o.history()[0])
+    assert ctx.thermo()["nbuilds"] == o.thermo()["nbuilds"]
+
+
+def test_mixed_lj_force_error(gpu_lib):
+    from mddem_gb300 import config, inputs
+
+    cfg64 = config.lj_fluid_config()
+    cfgmx = config.lj_fluid_config(precision="mixed")
+    st = inputs.lj_fcc(6, 10.06, 0.85, 0.85, seed=5)
+    rng = np.random.default_rng(0)
+    st["pos"] = st["pos"] + rng.normal(scale=0.05, size=st["pos"].shape)
+    a = _ctx(cfg64, st)
+    b = _ctx(cfgmx, st)
+    a.force_only()
+    b.force_only()
+    ga, gb = a.download(), b.download()
+    fa, pa = by_tag(ga, "force", "pos")
+    (fb,) = by_tag(gb, "force")
+    scale = lj_pair_force_scale(pa, cfg64.box, a.pairs())
+    err = rel_err(fb, fa, scale)
+    assert err <= 1e-5, err
+
+
+def test_batch_equals_single(gpu_lib):
+    from mddem_gb300 import capi, config, inputs
+
+    c1 = config.lj_fluid_config()
+    s1 = inputs.lj_fcc(6, 10.06, 0.85, 0.85, seed=11)
+    c2 = _dem_cfg()
+    s2 = _dem_state(seed=6, n=600)
+    alone = []
+    for c, s in ((c1, s1), (c2, s2)):
+        ctx = _ctx(c, s)
+        ctx.step(20)
+        alone.append(ctx.download())
+    b = capi.Context([c1, c2], [len(s1["tag"]), len(s2["tag"])])
+    b.upload(s1, 0)
+    b.upload(s2, 1)
+    b.step(20)
+    for k in range(2):
+        g = b.download(k)
+        for f in ("pos", "vel"):
+            (x,) = by_tag(g, f)
+            (y,) = by_tag(alone[k], f)
+            assert np.array_equal(x, y), (k, f)
