@@ -212,6 +212,8 @@ def main():
     ap.add_argument("--workload", default="lj256k")
     ap.add_argument("--precision", default="mixed")
     ap.add_argument("--policy", default="displacement")
+    ap.add_argument("--tpp", type=int, default=0, help="threads per particle in the force kernel (0 = auto)")
+    ap.add_argument("--eager", action="store_true", help="launch kernels one by one (for profilers)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     a = ap.parse_args()
@@ -233,11 +235,13 @@ def main():
 
     build.build()
     desc, cfg, make = workload(a.workload)
-    cfg = cfg.replace(precision=a.precision, rebuild_policy=a.policy)
+    cfg = cfg.replace(precision=a.precision, rebuild_policy=a.policy, threads_per_particle=a.tpp)
     st = make()
     n = len(st["tag"])
     ctx = capi.Context(cfg, n)
     ctx.upload(st)
+    if a.eager:
+        ctx.set_graph_mode(0)
     ctx.timed_steps(a.warmup, L2_FLUSH)
     if dist:
         dist.barrier()

@@ -127,7 +127,7 @@ typedef struct mdg_state_view {
     uint32_t* type;          /* material index (DEM) or LJ type */
     double* pos;             /* n*3 */
     double* vel;             /* n*3 */
-    double* force;           /* n*3 (download only; may be NULL) */
+    double* force;           /* n*3: initial force on upload (restart), NULL = zero */
     double* mass;            /* n */
     double* cutoff_radius;   /* n: neighbor cutoff radius (DEM: radius; LJ: lattice skin) */
     int32_t* image;          /* n*3 periodic image counters (may be NULL) */
@@ -135,7 +135,7 @@ typedef struct mdg_state_view {
     double* radius;          /* n */
     double* inv_inertia;     /* n */
     double* omega;           /* n*3 */
-    double* torque;          /* n*3 (download only; may be NULL) */
+    double* torque;          /* n*3: initial torque on upload (restart), NULL = zero */
     double* quat;            /* n*4 [w,x,y,z] */
 } mdg_state_view;
 

@@ -228,7 +228,7 @@ class Context:
         if "image" in keep:
             keep["image"] = keep["image"].astype(np.int32)
             v.image = _ptr(keep["image"], C.c_int32)
-        for f in ("radius", "inv_inertia", "omega", "quat"):
+        for f in ("radius", "inv_inertia", "omega", "quat", "force", "torque"):
             if f in keep:
                 setattr(v, f, _ptr(keep[f], C.c_double))
         _check(self.lib.mdg_upload_state(self.h, sys, C.byref(v)), "mdg_upload_state")

@@ -111,6 +111,7 @@ int validate_config(const mdg_config& c) {
 struct mdg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;  // captures the conditional rebuild branch
     int nsys = 0;
     std::vector<mdg_config> cfg;
     std::vector<std::vector<mdg_material>> mats;
@@ -151,6 +152,7 @@ struct mdg_ctx {
         if (flush_buf) cudaFree(flush_buf);
         for (void* p : allocs) cudaFree(p);
         if (stream) cudaStreamDestroy(stream);
+        if (stream2) cudaStreamDestroy(stream2);
     }
     template <class T>
     T* alloc(size_t n, int& err) {
@@ -226,12 +228,34 @@ int setup_grid(const mdg_config& c, const double* cutr, size_t n, SysParams& p) 
     p.ncell = (int)ncell;
     p.max_cutoff = max_cutoff;
     p.stencil_cut_sq = max_cutoff * max_cutoff;
+    // stencil membership of every offset (compute_bin_grid's distance test,
+    // neighbor.rs:341-361), as a bit table indexed by the offset
+    const int wx = 2 * p.sl[0] + 1, wy = 2 * p.sl[1] + 1, wz = 2 * p.sl[2] + 1;
+    if ((long long)wx * wy * wz > 32 * 32) return MDG_ERR_CONFIG;
+    std::memset(p.stencil_bits, 0, sizeof(p.stencil_bits));
+    for (int dx = -p.sl[0]; dx <= p.sl[0]; dx++)
+        for (int dy = -p.sl[1]; dy <= p.sl[1]; dy++)
+            for (int dz = -p.sl[2]; dz <= p.sl[2]; dz++) {
+                const double mdx = (double)std::max(std::abs(dx) - 1, 0) * p.bin[0];
+                const double mdy = (double)std::max(std::abs(dy) - 1, 0) * p.bin[1];
+                const double mdz = (double)std::max(std::abs(dz) - 1, 0) * p.bin[2];
+                if (mdx * mdx + mdy * mdy + mdz * mdz < p.stencil_cut_sq) {
+                    const int b = ((dx + p.sl[0]) * wy + (dy + p.sl[1])) * wz + (dz + p.sl[2]);
+                    p.stencil_bits[b >> 5] |= 1u << (b & 31);
+                }
+            }
     p.skin_fraction = sf;
     p.sf2 = sf * sf;
     p.min_skin = min_skin;
     p.uniform = std::fabs(max_skin - min_skin) < 1e-15;
     const double uc = 2.0 * min_skin * sf;
     p.uniform_cutoff_sq = uc * uc;
+    p.ucut2f = (float)p.uniform_cutoff_sq;
+    p.sf2f = (float)p.sf2;
+    for (int d = 0; d < 3; d++) {
+        p.Lh[d] = (float)p.L[d];
+        p.Ll[d] = (float)(p.L[d] - (double)p.Lh[d]);
+    }
     const double per_atom_skin = (sf - 1.0) * min_skin;
     p.disp_thr_sq = per_atom_skin * per_atom_skin;
     // fp32 prefilter: bound the error of (x_j_hi + s L_f) - x_i_hi per axis
@@ -337,16 +361,71 @@ int enqueue_step(mdg_ctx* c, int hcur, cudaStream_t st) {
     return n;
 }
 
+// Capture one step into the graph being captured on c->stream: the rebuild
+// pipeline sits in the body of an IF conditional node whose condition
+// k_initial sets on the device.  ev (optional) = 5 events bracketing the
+// phases.  Returns kernels in the step (rebuild kernels counted when run).
+int capture_step(mdg_ctx* c, int h, cudaEvent_t* ev, int* nk) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, nullptr, nullptr, nullptr);
+    if (e != cudaSuccess) return cuda_err(e);
+    cudaGraphConditionalHandle hd;
+    e = cudaGraphConditionalHandleCreate(&hd, g, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return cuda_err(e);
+    Dev d = c->d;
+    d.cond = (unsigned long long)hd;
+    d.use_cond = 1;
+    int n = 0;
+    if (ev) cudaEventRecordWithFlags(ev[0], c->stream, cudaEventRecordExternal);
+    n += launch_initial(d, c->stream);
+    if (ev) cudaEventRecordWithFlags(ev[1], c->stream, cudaEventRecordExternal);
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    e = cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return cuda_err(e);
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = hd;
+    np.conditional.type = cudaGraphCondTypeIf;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &np);
+    if (e != cudaSuccess) return cuda_err(e);
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    e = cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return cuda_err(e);
+    e = cudaStreamBeginCaptureToGraph(c->stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_err(e);
+    n += launch_rebuild(d, h, c->stream2);
+    cudaGraph_t body_out = nullptr;
+    e = cudaStreamEndCapture(c->stream2, &body_out);
+    if (e != cudaSuccess) return cuda_err(e);
+    if (ev) cudaEventRecordWithFlags(ev[2], c->stream, cudaEventRecordExternal);
+    if (c->has_mixed) n += launch_force_mixed(d, h, c->has_lj, c->has_dem, c->tpp_lj, c->stream);
+    else n += launch_force_fp64(d, h, c->has_lj, c->has_dem, c->tpp_lj, c->stream);
+    if (ev) cudaEventRecordWithFlags(ev[3], c->stream, cudaEventRecordExternal);
+    n += launch_final(d, c->stream, 1);
+    if (ev) cudaEventRecordWithFlags(ev[4], c->stream, cudaEventRecordExternal);
+    if (nk) *nk = n;
+    return MDG_OK;
+}
+
 int build_graph(mdg_ctx* c, int hstart) {
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_err(e);
     int h = hstart;
-    for (int k = 0; k < c->graph_steps; k++) {
-        enqueue_step(c, h, c->stream);
+    int r = MDG_OK;
+    for (int k = 0; k < c->graph_steps && !r; k++) {
+        r = capture_step(c, h, nullptr, nullptr);
         h ^= 1;
     }
     e = cudaStreamEndCapture(c->stream, &g);
+    if (r) {
+        if (g) cudaGraphDestroy(g);
+        return r;
+    }
     if (e != cudaSuccess) return cuda_err(e);
     e = cudaGraphInstantiate(&c->graph[hstart], g, 0);
     cudaGraphDestroy(g);
@@ -361,17 +440,12 @@ int build_timed_graph(mdg_ctx* c, int h) {
     cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_err(e);
     int n = 0;
-    cudaEventRecordWithFlags(c->tev[0], c->stream, cudaEventRecordExternal);
-    n += launch_initial(c->d, c->stream);
-    cudaEventRecordWithFlags(c->tev[1], c->stream, cudaEventRecordExternal);
-    n += launch_rebuild(c->d, h, c->stream);
-    cudaEventRecordWithFlags(c->tev[2], c->stream, cudaEventRecordExternal);
-    if (c->has_mixed) n += launch_force_mixed(c->d, h, c->has_lj, c->has_dem, c->tpp_lj, c->stream);
-    else n += launch_force_fp64(c->d, h, c->has_lj, c->has_dem, c->tpp_lj, c->stream);
-    cudaEventRecordWithFlags(c->tev[3], c->stream, cudaEventRecordExternal);
-    n += launch_final(c->d, c->stream, 1);
-    cudaEventRecordWithFlags(c->tev[4], c->stream, cudaEventRecordExternal);
+    int r = capture_step(c, h, c->tev, &n);
     e = cudaStreamEndCapture(c->stream, &g);
+    if (r) {
+        if (g) cudaGraphDestroy(g);
+        return r;
+    }
     if (e != cudaSuccess) return cuda_err(e);
     e = cudaGraphInstantiate(&c->tgraph[h], g, 0);
     cudaGraphDestroy(g);
@@ -443,7 +517,8 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     mdg_ctx* c = new (std::nothrow) mdg_ctx();
     if (!c) return MDG_ERR_OOM;
     cudaGetDevice(&c->device);
-    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {
         delete c;
         return MDG_ERR_CUDA;
     }
@@ -575,6 +650,7 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     d.ss = c->alloc<SysState>(nsys, err);
     c->d_mat = c->alloc<double>(std::max<size_t>(mat_all.size(), 1), err);
     c->d_thermo = c->alloc<double>((size_t)nsys * 16, err);
+    d.grid_ctr = c->alloc<unsigned int>(1, err);
     if (err) {
         delete c;
         return err;
@@ -618,7 +694,7 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
     if (!c || !st || sys < 0 || sys >= c->nsys) return MDG_ERR_ARG;
     const mdg_config& k = c->cfg[sys];
     const size_t n = st->n;
-    if (n < 2 || n > c->capacity[sys]) return MDG_ERR_ARG;
+    if (n < 1 || n > c->capacity[sys]) return MDG_ERR_ARG;
     if (!st->tag || !st->pos || !st->vel || !st->mass || !st->cutoff_radius) return MDG_ERR_ARG;
     if (k.kind == MDG_KIND_DEM && (!st->radius || !st->inv_inertia)) return MDG_ERR_ARG;
     SysParams& p = c->sp[sys];
@@ -645,7 +721,7 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
     r = ensure_layout(c, sys);
     if (r) return r;
     const size_t np = (size_t)p.npad;
-    std::vector<double4> pos(np), vel(np), zero4(np), omg, quat;
+    std::vector<double4> pos(np), vel(np), zero4(np), frc(np), trq, omg, quat;
     std::vector<double> mass(np, 1.0), cutr(np, 0.0);
     std::vector<uint32_t> tag(np, 0xffffffffu), type(np, 0);
     std::vector<int4> img(np);
@@ -655,10 +731,12 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
         img[i] = make_int4(0, 0, 0, 0);
         pos[i] = zero4[i];
         vel[i] = zero4[i];
+        frc[i] = zero4[i];
     }
     const bool dem = k.kind == MDG_KIND_DEM;
     if (dem) {
         omg.assign(np, zero4[0]);
+        trq.assign(np, zero4[0]);
         quat.assign(np, make_double4(1, 0, 0, 0));
     }
     for (size_t i = 0; i < n; i++) {
@@ -669,6 +747,8 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
         tag[i] = st->tag[i];
         type[i] = st->type ? st->type[i] : 0;
         if (st->image) img[i] = make_int4(st->image[3 * i], st->image[3 * i + 1], st->image[3 * i + 2], 0);
+        if (st->force) frc[i] = make_double4(st->force[3 * i], st->force[3 * i + 1], st->force[3 * i + 2], 0.0);
+        if (dem && st->torque) trq[i] = make_double4(st->torque[3 * i], st->torque[3 * i + 1], st->torque[3 * i + 2], 0.0);
         if (dem) {
             const double* w = st->omega;
             omg[i] = make_double4(w ? w[3 * i] : 0.0, w ? w[3 * i + 1] : 0.0, w ? w[3 * i + 2] : 0.0, st->inv_inertia[i]);
@@ -682,7 +762,7 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
     cudaMemcpyAsync(d.pos + o, pos.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
     cudaMemcpyAsync(d.lbp + o, pos.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
     cudaMemcpyAsync(d.vel + o, vel.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
-    cudaMemcpyAsync(d.frc + o, zero4.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
+    cudaMemcpyAsync(d.frc + o, frc.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
     cudaMemcpyAsync(d.mass + o, mass.data(), np * sizeof(double), cudaMemcpyHostToDevice, s0);
     cudaMemcpyAsync(d.cutr + o, cutr.data(), np * sizeof(double), cudaMemcpyHostToDevice, s0);
     cudaMemcpyAsync(d.tag + o, tag.data(), np * sizeof(uint32_t), cudaMemcpyHostToDevice, s0);
@@ -691,7 +771,7 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
     cudaMemcpyAsync(d.nnum + o, zi.data(), np * sizeof(int), cudaMemcpyHostToDevice, s0);
     if (dem) {
         cudaMemcpyAsync(d.omg + o, omg.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
-        cudaMemcpyAsync(d.trq + o, zero4.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
+        cudaMemcpyAsync(d.trq + o, trq.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
         cudaMemcpyAsync(d.quat + o, quat.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
         for (int b = 0; b < 2; b++) cudaMemcpyAsync(d.hcnt[b] + o, zi.data(), np * sizeof(int), cudaMemcpyHostToDevice, s0);
     }
@@ -846,7 +926,7 @@ int mdg_step(mdg_ctx* c, int64_t nsteps) {
             }
             cudaError_t e = cudaGraphLaunch(c->graph[h], c->stream);
             if (e != cudaSuccess) return cuda_err(e);
-            c->launches += (long long)c->graph_steps * (10 + (c->has_lj && c->has_dem ? 1 : 0));
+            c->launches += (long long)c->graph_steps * (3 + (c->has_lj && c->has_dem ? 1 : 0));
             if (c->graph_steps % 2) c->hcur ^= 1;
             left -= c->graph_steps;
         }
@@ -959,14 +1039,34 @@ int mdg_timed_steps(mdg_ctx* c, int64_t nsteps, size_t l2_flush_bytes, mdg_step_
         c->flush_bytes = l2_flush_bytes;
     }
     std::vector<SysState> ss(c->nsys);
+    for (auto& ev : c->tev)
+        if (!ev && cudaEventCreate(&ev) != cudaSuccess) return MDG_ERR_CUDA;
     for (int64_t k = 0; k < nsteps; k++) {
         const int h = c->hcur;
-        if (!c->tgraph[h]) {
+        if (c->graph_mode && !c->tgraph[h]) {
             int r = build_timed_graph(c, h);
             if (r) return r;
         }
         if (l2_flush_bytes) cudaMemsetAsync(c->flush_buf, (int)(k & 0xff), l2_flush_bytes, c->stream);
-        cudaError_t e = cudaGraphLaunch(c->tgraph[h], c->stream);
+        cudaError_t e = cudaSuccess;
+        if (c->graph_mode) {
+            e = cudaGraphLaunch(c->tgraph[h], c->stream);
+        } else {
+            // eager launches (profilers see every kernel); rebuild kernels always run
+            cudaStream_t st = c->stream;
+            int n = 0;
+            cudaEventRecord(c->tev[0], st);
+            n += launch_initial(c->d, st);
+            cudaEventRecord(c->tev[1], st);
+            n += launch_rebuild(c->d, h, st);
+            cudaEventRecord(c->tev[2], st);
+            if (c->has_mixed) n += launch_force_mixed(c->d, h, c->has_lj, c->has_dem, c->tpp_lj, st);
+            else n += launch_force_fp64(c->d, h, c->has_lj, c->has_dem, c->tpp_lj, st);
+            cudaEventRecord(c->tev[3], st);
+            n += launch_final(c->d, st, 1);
+            cudaEventRecord(c->tev[4], st);
+            c->tkernels = n;
+        }
         if (e != cudaSuccess) return cuda_err(e);
         e = cudaEventSynchronize(c->tev[4]);
         if (e != cudaSuccess) return cuda_err(e);
@@ -975,12 +1075,13 @@ int mdg_timed_steps(mdg_ctx* c, int64_t nsteps, size_t l2_flush_bytes, mdg_step_
         for (int q = 0; q < 4; q++) cudaEventElapsedTime(&ms[1 + q], c->tev[q], c->tev[q + 1]);
         out[k].step_ms = ms[0];
         for (int q = 0; q < 4; q++) out[k].phase_ms[q] = ms[1 + q];
-        out[k].kernels = c->tkernels;
         cudaMemcpy(ss.data(), c->d.ss, c->nsys * sizeof(SysState), cudaMemcpyDeviceToHost);
         int rb = 0;
         for (int s = 0; s < c->nsys; s++) rb |= (ss[s].steps_since_build == 0);
         out[k].rebuilt = rb;
-        c->launches += c->tkernels;
+        // the 7 rebuild-pipeline kernels run only when the conditional opened
+        out[k].kernels = c->tkernels - ((rb || !c->graph_mode) ? 0 : 7);
+        c->launches += out[k].kernels;
         c->hcur ^= 1;
     }
     cudaError_t e = cudaGetLastError();

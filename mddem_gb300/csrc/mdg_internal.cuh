@@ -52,8 +52,11 @@ struct SysParams {
     double lo[3], hi[3], L[3];
     double bin[3], inv_bin[3], origin[3];
     double max_cutoff, stencil_cut_sq;
+    unsigned int stencil_bits[32];  // offsets in [-sl, sl]^3 that pass the stencil distance test
     float pre_cut2;      // fp32 prefilter radius^2 for the list build (conservative)
-    float pad_f;
+    float ucut2f;        // fp32 copy of uniform_cutoff_sq
+    float sf2f;          // fp32 copy of sf2
+    float Lh[3], Ll[3];  // two-float split of the box lengths
     double skin_fraction, sf2;
     int uniform;         // all cutoff radii equal
     double uniform_cutoff_sq;
@@ -88,6 +91,7 @@ struct SysState {
     double ke;           // KE after the last post-final (NH)
     double p_xi_pre;     // p_xi after the pre-initial half step
     double p_xi_post;    // p_xi after the post-final half step
+    double nh_scale;     // exp(-dt/2 p_xi_pre / Q) for the current step (pre and post)
     double vir[6];
     double pe;
     long long step;
@@ -115,7 +119,8 @@ struct Dev {
     int* nnum;
     uint32_t* nlist;
     // rebuild scratch
-    int* cell;       // ext flat cell of each particle (system-relative)
+    int* cell;       // ext flat cell of each particle (system-relative); after the
+                     // permutation bit 31 flags a bin coordinate within 1e-9 of a bin edge
     int* cnt;        // per ext cell count / cursor
     int* cstart;     // per ext cell start (absolute particle index), +1 sentinel per system
     int* perm;       // new -> old (absolute)
@@ -145,7 +150,32 @@ struct Dev {
     int nblocks;
     long long P;       // total padded particles
     int hist_any;      // history arrays allocated
+    // graph mode: k_initial's last block sets this IF-node condition to
+    // "some system rebuilds (or sorts) this step"; 0 = no conditional
+    unsigned long long cond;
+    int use_cond;
+    unsigned int* grid_ctr;
 };
+
+// Two-float separation (x_j + s L) - x_i from positions stored relative to
+// the box corner as hi + lo floats.  The shift is applied to the coordinate
+// that sits next to the crossed face, which keeps the hi-part difference exact
+// (Sterbenz); the result carries ~1e-7 relative error.
+__device__ __forceinline__ float two_float_sep(float xj_hi, float xj_lo, float xi_hi, float xi_lo, int s, float Lh,
+                                               float Ll) {
+    float dh, dl;
+    if (s > 0) {
+        dh = xj_hi - (xi_hi - Lh);
+        dl = xj_lo - (xi_lo - Ll);
+    } else if (s < 0) {
+        dh = (xj_hi - Lh) - xi_hi;
+        dl = (xj_lo - Ll) - xi_lo;
+    } else {
+        dh = xj_hi - xi_hi;
+        dl = xj_lo - xi_lo;
+    }
+    return dh + dl;
+}
 
 // ---- kernel launchers (mdg_kernels_fp64.cu / mdg_kernels_mixed.cu) ----------
 // Each returns the number of kernels it launched on `st`.

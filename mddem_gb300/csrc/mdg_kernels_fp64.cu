@@ -109,13 +109,9 @@ __global__ void __launch_bounds__(BLK) k_initial(Dev d) {
     const bool act = li < sp.n;
     const long long i = (long long)sp.p0 + li;
     const double dt = sp.dt;
-    double scale = 1.0;
-    if (sp.nh) {
-        double ke = st->ke;
-        double pxi = st->p_xi_post + (dt / 2.0) * (2.0 * ke - sp.nh_ndof * sp.nh_T);
-        scale = exp(-dt / 2.0 * pxi / sp.nh_Q);
-        if (li == 0) st->p_xi_pre = pxi;
-    }
+    // exp(-dt/2 p_xi / Q) after the pre-initial half step of p_xi, computed
+    // once per system by the previous step's reduction (k_final / k_ke_init)
+    const double scale = sp.nh ? st->nh_scale : 1.0;
     if (li == 0)
         st->periodic_sort =
             (sp.policy == 0 && sp.sort_every > 0 && st->sort_counter + 1 >= sp.sort_every) ? 1 : 0;
@@ -191,6 +187,24 @@ __global__ void __launch_bounds__(BLK) k_initial(Dev d) {
         }
     }
     if (__any_sync(0xffffffffu, need) && (threadIdx.x & 31) == 0) atomicOr(&st->rebuild, 1);
+    if (d.use_cond) {
+        // grid-wide last block: open the rebuild branch of the step graph only
+        // when some system rebuilds or sorts
+        __shared__ int last;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            last = atomicAdd(d.grid_ctr, 1u) == (unsigned)(gridDim.x - 1);
+        }
+        __syncthreads();
+        if (last && threadIdx.x == 0) {
+            __threadfence();
+            unsigned int any = 0;
+            for (int q = 0; q < d.nsys; q++) any |= (unsigned)(vload(&d.ss[q].rebuild) | vload(&d.ss[q].periodic_sort));
+            *d.grid_ctr = 0;
+            cudaGraphSetConditional((cudaGraphConditionalHandle)d.cond, any ? 1u : 0u);
+        }
+    }
 }
 
 // ----------------------------------------------------------------------------
@@ -379,12 +393,32 @@ __global__ void __launch_bounds__(BLK) k_copyback(Dev d, int hcur) {
             }
         }
     }
-    // two-float geometry copy relative to the box corner: list-build prefilter
-    // and the mixed-precision pair kernels
+    // two-float geometry copy relative to the box corner (list build and the
+    // mixed-precision pair kernels); w = cutoff radius
     const double rx = x.x - sp.lo[0], ry = x.y - sp.lo[1], rz = x.z - sp.lo[2];
     const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
-    d.pos_hi[k] = make_float4(hx, hy, hz, (float)x.w);
+    d.pos_hi[k] = make_float4(hx, hy, hz, (float)d.s_cutr[k]);
     d.pos_lo[k] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy), (float)(rz - (double)hz), 0.f);
+    // ext cell in the new order, with a flag when a bin coordinate lies within
+    // 1e-9 of a bin edge (the list build then recomputes image cells in fp64)
+    const double ux = (x.x - sp.origin[0]) * sp.inv_bin[0];
+    const double uy = (x.y - sp.origin[1]) * sp.inv_bin[1];
+    const double uz = (x.z - sp.origin[2]) * sp.inv_bin[2];
+    const int cx = min(max((int)floor(ux), 0), sp.ext[0] - 1);
+    const int cy = min(max((int)floor(uy), 0), sp.ext[1] - 1);
+    const int cz = min(max((int)floor(uz), 0), sp.ext[2] - 1);
+    const double fx = ux - floor(ux), fy = uy - floor(uy), fz = uz - floor(uz);
+    const bool edge = fx < 1e-9 || fx > 1.0 - 1e-9 || fy < 1e-9 || fy > 1.0 - 1e-9 || fz < 1e-9 || fz > 1.0 - 1e-9;
+    d.cell[k] = ((cx * sp.ext[1] + cy) * sp.ext[2] + cz) | (edge ? (int)0x80000000u : 0);
+}
+
+// Stencil membership of a cell offset (compute_bin_grid's distance test,
+// neighbor.rs:341-361, tabulated on the host).
+__device__ __forceinline__ bool stencil_ok(const SysParams& sp, int dx, int dy, int dz) {
+    if (abs(dx) > sp.sl[0] || abs(dy) > sp.sl[1] || abs(dz) > sp.sl[2]) return false;
+    const int wy = 2 * sp.sl[1] + 1, wz = 2 * sp.sl[2] + 1;
+    const int b = ((dx + sp.sl[0]) * wy + (dy + sp.sl[1])) * wz + (dz + sp.sl[2]);
+    return (sp.stencil_bits[b >> 5] >> (b & 31)) & 1u;
 }
 
 // Owner rule of the reference's half list (bin_neighbor_list,
@@ -396,11 +430,7 @@ __global__ void __launch_bounds__(BLK) k_copyback(Dev d, int hcur) {
 __device__ __forceinline__ bool owner_test(const SysParams& sp, int eox, int eoy, int eoz, int gx, int gy,
                                            int gz, bool ghost, long long o, long long p) {
     const int dx = gx - eox, dy = gy - eoy, dz = gz - eoz;
-    if (abs(dx) > sp.sl[0] || abs(dy) > sp.sl[1] || abs(dz) > sp.sl[2]) return false;
-    const double mdx = (double)(abs(dx) > 0 ? abs(dx) - 1 : 0) * sp.bin[0];
-    const double mdy = (double)(abs(dy) > 0 ? abs(dy) - 1 : 0) * sp.bin[1];
-    const double mdz = (double)(abs(dz) > 0 ? abs(dz) - 1 : 0) * sp.bin[2];
-    if (!(mdx * mdx + mdy * mdy + mdz * mdz < sp.stencil_cut_sq)) return false;
+    if (!stencil_ok(sp, dx, dy, dz)) return false;
     const long long flat = ((long long)dx * sp.ext[1] + dy) * sp.ext[2] + dz;
     if (sp.newton) {
         if (flat > 0) return true;
@@ -417,13 +447,24 @@ __device__ __forceinline__ bool cut_ok(const SysParams& sp, double r2, double so
     return r2 < ss * ss * sp.sf2;
 }
 
-// Neighbour list build.  Enumerates, for particle i, every periodic image of
-// every particle in the 3x3x3 (or wider) interior-cell window around it,
-// prefilters in fp32, and applies the reference's exact fp64 cutoff test and
-// owner rule twice: `own` (i holds the pair in the reference's half list) and
-// `oth` (the partner holds it).  Both go into i's full row, so forces can be
-// summed per particle without atomics while pair arithmetic stays in the
-// owner's frame.  Also saves last_build_pos (neighbor.rs:545-561).
+// ext cell of an image coordinate (fp64, exactly as the reference bins ghosts)
+__device__ __forceinline__ void ext_cell3(const SysParams& sp, double x, double y, double z, int& cx, int& cy,
+                                          int& cz) {
+    cx = ext_cell_1d(x, sp.origin[0], sp.inv_bin[0], sp.ext[0]);
+    cy = ext_cell_1d(y, sp.origin[1], sp.inv_bin[1], sp.ext[1]);
+    cz = ext_cell_1d(z, sp.origin[2], sp.inv_bin[2], sp.ext[2]);
+}
+
+// Neighbour list build.  For particle i, every periodic image of every
+// particle in the interior-cell window around it is screened with a two-float
+// fp32 separation; the reference's cutoff test (fp64, fma form) is evaluated
+// exactly only for the rare pairs within 1e-5 of the cutoff.  The reference's
+// owner rule is applied twice: `own` (i holds the pair in the reference's half
+// list) and `oth` (the partner holds it).  Both go into i's full row, so forces
+// are summed per particle without atomics while pair arithmetic stays in the
+// owner's frame.  Image cells are integer shifts of the bin index except for
+// particles flagged as sitting within 1e-9 of a bin edge, which are rebinned in
+// fp64.  Also saves last_build_pos (neighbor.rs:545-561).
 __global__ void __launch_bounds__(BLK) k_build(Dev d) {
     const int s = d.blk_sys[blockIdx.x];
     const SysParams& sp = d.sp[s];
@@ -433,17 +474,19 @@ __global__ void __launch_bounds__(BLK) k_build(Dev d) {
     if (li >= sp.n) return;
     const long long i = (long long)sp.p0 + li;
     const double4 xi = d.pos[i];
-    const float4 xif = d.pos_hi[i];
-    const double si = d.cutr[i];
     d.lbp[i] = xi;
-    const int ex = ext_cell_1d(xi.x, sp.origin[0], sp.inv_bin[0], sp.ext[0]);
-    const int ey = ext_cell_1d(xi.y, sp.origin[1], sp.inv_bin[1], sp.ext[1]);
-    const int ez = ext_cell_1d(xi.z, sp.origin[2], sp.inv_bin[2], sp.ext[2]);
+    const float4 hi = d.pos_hi[i];
+    const float4 lo = d.pos_lo[i];
+    const int ci = d.cell[i];
+    const bool edge_i = ci < 0;
+    const int flat_i = ci & 0x7fffffff;
+    const int ez = flat_i % sp.ext[2];
+    const int ey = (flat_i / sp.ext[2]) % sp.ext[1];
+    const int ex = flat_i / (sp.ext[2] * sp.ext[1]);
     const int qx0 = min(max(ex - sp.sl[0], 0), sp.nc[0] - 1);
     const int qy0 = min(max(ey - sp.sl[1], 0), sp.nc[1] - 1);
     const int qz0 = min(max(ez - sp.sl[2], 0), sp.nc[2] - 1);
-    const float pre2 = sp.pre_cut2;
-    const float Lf0 = (float)sp.L[0], Lf1 = (float)sp.L[1], Lf2 = (float)sp.L[2];
+    const float band_hi = 1.00001f, band_lo = 0.99999f;
     int count = 0;
     const long long base = sp.lst0 + li;
     for (int ox = -sp.win[0]; ox <= sp.win[0]; ox++) {
@@ -459,7 +502,7 @@ __global__ void __launch_bounds__(BLK) k_build(Dev d) {
                 if (qz < 0) { qz += sp.nc[2]; sz = -1; } else if (qz >= sp.nc[2]) { qz -= sp.nc[2]; sz = 1; }
                 if (qz < 0 || qz >= sp.nc[2]) continue;
                 const bool shifted = (sx | sy | sz) != 0;
-                const float fsx = (float)sx * Lf0, fsy = (float)sy * Lf1, fsz = (float)sz * Lf2;
+                const uint32_t sc = (uint32_t)((sx + 1) * 9 + (sy + 1) * 3 + (sz + 1));
                 // source ext cells: the interior cell and the ghost-layer cells that
                 // clamp into it (particles whose bin coordinate rounded just outside)
                 const int axa = (qx == 0) ? -1 : 0, axb = (qx == sp.nc[0] - 1) ? 1 : 0;
@@ -474,47 +517,63 @@ __global__ void __launch_bounds__(BLK) k_build(Dev d) {
                             for (int m = m0; m < m1; m++) {
                                 const long long j = m;
                                 if (!shifted && j == i) continue;
-                                const float4 xjf = d.pos_hi[j];
-                                const float fx = (xjf.x + fsx) - xif.x;
-                                const float fy = (xjf.y + fsy) - xif.y;
-                                const float fz = (xjf.z + fsz) - xif.z;
-                                if (fx * fx + fy * fy + fz * fz > pre2) continue;
-                                const double4 xj = d.pos[j];
-                                const double sj = d.cutr[j];
-                                const double ix = img_coord(xj.x, sx, sp.L[0]);
-                                const double iy = img_coord(xj.y, sy, sp.L[1]);
-                                const double iz = img_coord(xj.z, sz, sp.L[2]);
-                                const double dx = ix - xi.x, dy = iy - xi.y, dz = iz - xi.z;
-                                const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+                                const float4 hj = d.pos_hi[j];
+                                const float4 lj = d.pos_lo[j];
+                                const float fx = two_float_sep(hj.x, lj.x, hi.x, lo.x, sx, sp.Lh[0], sp.Ll[0]);
+                                const float fy = two_float_sep(hj.y, lj.y, hi.y, lo.y, sy, sp.Lh[1], sp.Ll[1]);
+                                const float fz = two_float_sep(hj.z, lj.z, hi.z, lo.z, sz, sp.Lh[2], sp.Ll[2]);
+                                const float r2f = fx * fx + fy * fy + fz * fz;
+                                float c2f;
+                                if (sp.uniform) {
+                                    c2f = sp.ucut2f;
+                                } else {
+                                    const float ss = hi.w + hj.w;
+                                    c2f = ss * ss * sp.sf2f;
+                                }
+                                if (r2f > c2f * band_hi) continue;
+                                bool ok_i = true, ok_j = true;
+                                const bool band = r2f >= c2f * band_lo;
+                                double4 xj;
+                                if (band || (shifted && (edge_i || d.cell[j] < 0))) xj = d.pos[j];
+                                if (band) {
+                                    // the reference's own test, in its own arithmetic
+                                    const double si = d.cutr[i], sj = d.cutr[j];
+                                    const double dx = img_coord(xj.x, sx, sp.L[0]) - xi.x;
+                                    const double dy = img_coord(xj.y, sy, sp.L[1]) - xi.y;
+                                    const double dz = img_coord(xj.z, sz, sp.L[2]) - xi.z;
+                                    ok_i = cut_ok(sp, fma(dx, dx, fma(dy, dy, dz * dz)), si, sj);
+                                    if (shifted) {
+                                        const double ux = img_coord(xi.x, -sx, sp.L[0]) - xj.x;
+                                        const double uy = img_coord(xi.y, -sy, sp.L[1]) - xj.y;
+                                        const double uz = img_coord(xi.z, -sz, sp.L[2]) - xj.z;
+                                        ok_j = cut_ok(sp, fma(ux, ux, fma(uy, uy, uz * uz)), sj, si);
+                                    } else {
+                                        ok_j = ok_i;
+                                    }
+                                    if (!ok_i && !ok_j) continue;
+                                }
                                 bool own, oth = false;
                                 if (!shifted) {
-                                    // dx from j's side is exactly -dx: same r2
-                                    if (!cut_ok(sp, r2, si, sj)) continue;
-                                    own = owner_test(sp, ex, ey, ez, Ex, Ey, Ez, false, i, j);
-                                    if (sp.newton) oth = owner_test(sp, Ex, Ey, Ez, ex, ey, ez, false, j, i);
+                                    own = ok_i && owner_test(sp, ex, ey, ez, Ex, Ey, Ez, false, i, j);
+                                    if (sp.newton) oth = ok_j && owner_test(sp, Ex, Ey, Ez, ex, ey, ez, false, j, i);
                                 } else {
-                                    own = false;
-                                    if (cut_ok(sp, r2, si, sj)) {
-                                        const int gx = ext_cell_1d(ix, sp.origin[0], sp.inv_bin[0], sp.ext[0]);
-                                        const int gy = ext_cell_1d(iy, sp.origin[1], sp.inv_bin[1], sp.ext[1]);
-                                        const int gz = ext_cell_1d(iz, sp.origin[2], sp.inv_bin[2], sp.ext[2]);
-                                        own = owner_test(sp, ex, ey, ez, gx, gy, gz, true, i, j);
+                                    int gx, gy, gz, hx, hy, hz;
+                                    if (!edge_i && d.cell[j] >= 0) {
+                                        gx = min(max(Ex + sx * sp.nc[0], 0), sp.ext[0] - 1);
+                                        gy = min(max(Ey + sy * sp.nc[1], 0), sp.ext[1] - 1);
+                                        gz = min(max(Ez + sz * sp.nc[2], 0), sp.ext[2] - 1);
+                                        hx = min(max(ex - sx * sp.nc[0], 0), sp.ext[0] - 1);
+                                        hy = min(max(ey - sy * sp.nc[1], 0), sp.ext[1] - 1);
+                                        hz = min(max(ez - sz * sp.nc[2], 0), sp.ext[2] - 1);
+                                    } else {
+                                        ext_cell3(sp, img_coord(xj.x, sx, sp.L[0]), img_coord(xj.y, sy, sp.L[1]),
+                                                  img_coord(xj.z, sz, sp.L[2]), gx, gy, gz);
+                                        ext_cell3(sp, img_coord(xi.x, -sx, sp.L[0]), img_coord(xi.y, -sy, sp.L[1]),
+                                                  img_coord(xi.z, -sz, sp.L[2]), hx, hy, hz);
                                     }
-                                    if (sp.newton) {
-                                        const double jx = img_coord(xi.x, -sx, sp.L[0]);
-                                        const double jy = img_coord(xi.y, -sy, sp.L[1]);
-                                        const double jz = img_coord(xi.z, -sz, sp.L[2]);
-                                        const double ux = jx - xj.x, uy = jy - xj.y, uz = jz - xj.z;
-                                        const double r2o = fma(ux, ux, fma(uy, uy, uz * uz));
-                                        if (cut_ok(sp, r2o, sj, si)) {
-                                            const int hx = ext_cell_1d(jx, sp.origin[0], sp.inv_bin[0], sp.ext[0]);
-                                            const int hy = ext_cell_1d(jy, sp.origin[1], sp.inv_bin[1], sp.ext[1]);
-                                            const int hz = ext_cell_1d(jz, sp.origin[2], sp.inv_bin[2], sp.ext[2]);
-                                            oth = owner_test(sp, Ex, Ey, Ez, hx, hy, hz, true, j, i);
-                                        }
-                                    }
+                                    own = ok_i && owner_test(sp, ex, ey, ez, gx, gy, gz, true, i, j);
+                                    if (sp.newton) oth = ok_j && owner_test(sp, Ex, Ey, Ez, hx, hy, hz, true, j, i);
                                 }
-                                const uint32_t sc = (uint32_t)((sx + 1) * 9 + (sy + 1) * 3 + (sz + 1));
                                 const uint32_t jl = (uint32_t)(j - sp.p0);
                                 if (own) {
                                     if (count < sp.ncap)
@@ -984,7 +1043,7 @@ __global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
             v.y += h * f.y;
             v.z += h * f.z;
             if (sp.nh) {
-                const double scale = exp(-dt / 2.0 * st->p_xi_pre / sp.nh_Q);
+                const double scale = st->nh_scale;
                 v.x *= scale;
                 v.y *= scale;
                 v.z *= scale;
@@ -1005,15 +1064,38 @@ __global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
         }
         if (sp.virial)
             for (int q = 0; q < 6; q++) vals[1 + q] = d.vir[q * d.P + i];
+        // non-finite test on the exponent bits (integer ops only)
         const double4 x = d.pos[i];
-        if (!isfinite(v.x + v.y + v.z + x.x + x.y + x.z)) bad = 1;
+        const int ex = 0x7ff00000;
+        bad = ((__double2hiint(v.x) & ex) == ex) | ((__double2hiint(v.y) & ex) == ex) |
+              ((__double2hiint(v.z) & ex) == ex) | ((__double2hiint(x.x) & ex) == ex) |
+              ((__double2hiint(x.y) & ex) == ex) | ((__double2hiint(x.z) & ex) == ex);
     }
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&st->status, ST_NAN);
     double out[8];
-    if (system_reduce<8>(d, s, vals, out) && threadIdx.x == 0) {
+    bool last;
+    if (sp.virial) {
+        last = system_reduce<8>(d, s, vals, out);
+    } else {
+        // KE and PE only
+        const double v2[2] = {vals[0], vals[7]};
+        double o2[2];
+        last = system_reduce<2>(d, s, v2, o2);
+        out[0] = o2[0];
+        out[7] = o2[1];
+    }
+    if (last && threadIdx.x == 0) {
         const double ke = 0.5 * out[0];
         st->ke = ke;
-        if (sp.nh && integrate) st->p_xi_post = st->p_xi_pre + (dt / 2.0) * (2.0 * ke - sp.nh_ndof * sp.nh_T);
+        if (sp.nh && integrate) {
+            // nh_post_final's half step, then the next nh_pre_initial's half step
+            // (its compute_ke sees the same velocities) and its exp scale
+            const double post = st->p_xi_pre + (dt / 2.0) * (2.0 * ke - sp.nh_ndof * sp.nh_T);
+            st->p_xi_post = post;
+            const double pre = post + (dt / 2.0) * (2.0 * ke - sp.nh_ndof * sp.nh_T);
+            st->p_xi_pre = pre;
+            st->nh_scale = exp(-dt / 2.0 * pre / sp.nh_Q);
+        }
         if (sp.virial)
             for (int q = 0; q < 6; q++) st->vir[q] = out[1 + q];
         st->pe = out[7];
@@ -1046,7 +1128,17 @@ __global__ void __launch_bounds__(BLK) k_ke_init(Dev d) {
         vals[0] = d.mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z);
     }
     double out[1];
-    if (system_reduce<1>(d, s, vals, out) && threadIdx.x == 0) d.ss[s].ke = 0.5 * out[0];
+    if (system_reduce<1>(d, s, vals, out) && threadIdx.x == 0) {
+        SysState* st = d.ss + s;
+        const double ke = 0.5 * out[0];
+        st->ke = ke;
+        if (sp.nh) {
+            const double dt = sp.dt;
+            const double pre = st->p_xi_post + (dt / 2.0) * (2.0 * ke - sp.nh_ndof * sp.nh_T);
+            st->p_xi_pre = pre;
+            st->nh_scale = exp(-dt / 2.0 * pre / sp.nh_Q);
+        }
+    }
 }
 
 // thermo pass 1: sum m, sum m v, compute_ke sum, pe  (granular_temp.rs:62-101, atom.rs:489-502)

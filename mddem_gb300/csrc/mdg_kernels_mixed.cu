@@ -23,21 +23,6 @@ struct Kahan {
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
-__device__ __forceinline__ float sep(float xj_hi, float xj_lo, float xi_hi, float xi_lo, int s, float Lh, float Ll) {
-    float dh, dl;
-    if (s > 0) {
-        dh = xj_hi - (xi_hi - Lh);
-        dl = xj_lo - (xi_lo - Ll);
-    } else if (s < 0) {
-        dh = (xj_hi - Lh) - xi_hi;
-        dl = (xj_lo - Ll) - xi_lo;
-    } else {
-        dh = xj_hi - xi_hi;
-        dl = xj_lo - xi_lo;
-    }
-    return dh + dl;
-}
-
 // LJ 12-6 in FP32 with compensated per-particle sums (same list, same owner
 // frames as the FP64 kernel).
 template <int TPP>
@@ -60,32 +45,47 @@ __global__ void __launch_bounds__(BLK) k_lj_mixed(Dev d) {
         const float lj1 = (float)sp.lj1, lj2 = (float)sp.lj2, lj3 = (float)sp.lj3, lj4 = (float)sp.lj4;
         const float cut2 = (float)sp.lj_cut2;
         const float half = sp.newton ? 1.f : 0.5f;
-        const float Lh0 = (float)sp.L[0], Lh1 = (float)sp.L[1], Lh2 = (float)sp.L[2];
-        const float Ll0 = (float)(sp.L[0] - (double)Lh0), Ll1 = (float)(sp.L[1] - (double)Lh1),
-                    Ll2 = (float)(sp.L[2] - (double)Lh2);
-        for (int k = lane; k < nn; k += TPP) {
-            const uint32_t e = __ldg(d.nlist + base + (long long)k * sp.npad);
-            const long long j = sp.p0 + (e & IDX_MASK);
-            const uint32_t code = e >> IDX_BITS;
-            const bool own = code >= 27u;
-            const int sc = (int)(own ? code - 27u : code);
-            const int sx = sc / 9 - 1, sy = (sc / 3) % 3 - 1, sz = sc % 3 - 1;
-            const float4 hj = __ldg(d.pos_hi + j);
-            const float4 lj = __ldg(d.pos_lo + j);
-            // owner frame: d = x_partner(+shift) - x_owner; as seen from i the
-            // partner-side sign flips, so use d_i = x_j(+s) - x_i in both cases
-            const float dx = sep(hj.x, lj.x, hi.x, lo.x, sx, Lh0, Ll0);
-            const float dy = sep(hj.y, lj.y, hi.y, lo.y, sy, Lh1, Ll1);
-            const float dz = sep(hj.z, lj.z, hi.z, lo.z, sz, Lh2, Ll2);
-            const float r2 = dx * dx + dy * dy + dz * dz;
-            if (r2 >= cut2) continue;
-            const float r2inv = __frcp_rn(r2);
-            const float r6inv = r2inv * r2inv * r2inv;
-            const float fpair = r2inv * r6inv * (lj1 * r6inv - lj2);
-            kx.add(-fpair * dx);
-            ky.add(-fpair * dy);
-            kz.add(-fpair * dz);
-            if (own) kp.add(r6inv * (lj3 * r6inv - lj4) * half);
+        const float Lh0 = sp.Lh[0], Lh1 = sp.Lh[1], Lh2 = sp.Lh[2];
+        const float Ll0 = sp.Ll[0], Ll1 = sp.Ll[1], Ll2 = sp.Ll[2];
+        // U entries in flight per lane: list loads first, then the gathers, then
+        // the arithmetic, so each lane keeps U independent load chains open
+        constexpr int U = 4;
+        for (int k0 = lane; k0 < nn; k0 += U * TPP) {
+            uint32_t e[U];
+            float4 hj[U], lj[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int k = k0 + u * TPP;
+                e[u] = k < nn ? __ldg(d.nlist + base + (long long)k * sp.npad) : 0xffffffffu;
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const long long j = sp.p0 + (e[u] != 0xffffffffu ? (e[u] & IDX_MASK) : 0u);
+                hj[u] = __ldg(d.pos_hi + j);
+                lj[u] = __ldg(d.pos_lo + j);
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                if (e[u] == 0xffffffffu) continue;
+                const uint32_t code = e[u] >> IDX_BITS;
+                const bool own = code >= 27u;
+                const int sc = (int)(own ? code - 27u : code);
+                const int sx = sc / 9 - 1, sy = (sc / 3) % 3 - 1, sz = sc % 3 - 1;
+                // d_i = x_j(+s) - x_i for owner and partner entries alike: the
+                // force on i is -fpair d_i either way
+                const float dx = two_float_sep(hj[u].x, lj[u].x, hi.x, lo.x, sx, Lh0, Ll0);
+                const float dy = two_float_sep(hj[u].y, lj[u].y, hi.y, lo.y, sy, Lh1, Ll1);
+                const float dz = two_float_sep(hj[u].z, lj[u].z, hi.z, lo.z, sz, Lh2, Ll2);
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                if (r2 >= cut2) continue;
+                const float r2inv = __frcp_rn(r2);
+                const float r6inv = r2inv * r2inv * r2inv;
+                const float fpair = r2inv * r6inv * (lj1 * r6inv - lj2);
+                kx.add(-fpair * dx);
+                ky.add(-fpair * dy);
+                kz.add(-fpair * dz);
+                if (own) kp.add(r6inv * (lj3 * r6inv - lj4) * half);
+            }
         }
     }
     double fx = kx.value(), fy = ky.value(), fz = kz.value(), pe = kp.value();

@@ -206,7 +206,8 @@ def write_csv(path, state):
     with open(path, "w") as f:
         f.write("x,y,z,radius,vx,vy,vz,type\n")
         for p, r, v, t in zip(state["pos"], state["radius"], state["vel"], state["type"]):
-            f.write(f"{p[0]!r},{p[1]!r},{p[2]!r},{r!r},{v[0]!r},{v[1]!r},{v[2]!r},{int(t)}\n")
+            vals = [float(p[0]), float(p[1]), float(p[2]), float(r), float(v[0]), float(v[1]), float(v[2])]
+            f.write(",".join(repr(x) for x in vals) + f",{int(t)}\n")
 
 
 def read_csv(path, density=2500.0):

@@ -1116,6 +1116,16 @@ int orc_load(void* h, size_t n, const uint32_t* tag, const uint32_t* type, const
     return 0;
 }
 
+int orc_set_force(void* h, size_t i, const double* f3, const double* t3) {
+    Sim* s = static_cast<Sim*>(h);
+    if (i >= (size_t)s->nlocal) return 9;
+    for (int d = 0; d < 3; d++) {
+        if (f3) s->force[i][d] = f3[d];
+        if (t3 && s->dem) s->torque[i][d] = t3[d];
+    }
+    return 0;
+}
+
 int orc_step(void* h, long nsteps) {
     Sim* s = static_cast<Sim*>(h);
     for (long k = 0; k < nsteps && !s->error; k++) s->step();

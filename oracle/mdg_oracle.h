@@ -63,6 +63,8 @@ int    orc_load(void* h, size_t n, const uint32_t* tag, const uint32_t* type,
                 const double* cutoff_radius, const double* radius,
                 const double* density, const double* inv_inertia,
                 const double* omega, const double* quat);
+/* Set the current force (and torque, DEM) of local atom i (restart state). */
+int    orc_set_force(void* h, size_t i, const double* f3, const double* t3);
 /* Advance nsteps full timesteps (reference schedule order). */
 int    orc_step(void* h, long nsteps);
 /* Ghost rebuild + bin list + force evaluation at the current state, no

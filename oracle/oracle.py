@@ -66,6 +66,7 @@ def _load():
         lib.orc_destroy.argtypes = [C.c_void_p]
         lib.orc_load.argtypes = [C.c_void_p, C.c_size_t, P(C.c_uint32), P(C.c_uint32)] + [P(C.c_double)] * 9
         lib.orc_step.argtypes = [C.c_void_p, C.c_long]
+        lib.orc_set_force.argtypes = [C.c_void_p, C.c_size_t, P(C.c_double), P(C.c_double)]
         lib.orc_force_only.argtypes = [C.c_void_p]
         lib.orc_nlocal.argtypes = [C.c_void_p]
         lib.orc_nlocal.restype = C.c_size_t
@@ -142,6 +143,12 @@ class Oracle:
             _p(keep.get("quat")) if dem else None)
         if r:
             raise RuntimeError(f"orc_load failed: {r}")
+        for f in ("force", "torque"):
+            if f in keep:
+                for i in range(n):
+                    row = np.ascontiguousarray(keep[f][i], np.float64)
+                    args = (row, None) if f == "force" else (None, row)
+                    self.lib.orc_set_force(self.h, i, _p(args[0]), _p(args[1]))
 
     def step(self, n=1):
         r = self.lib.orc_step(self.h, int(n))

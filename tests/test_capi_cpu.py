@@ -1,0 +1,184 @@
+"""CPU checks of the drop-in boundary: the library builds and exports every
+entry point include/mdg.h declares; configuration parsing follows the
+reference's TOML sections (unknown keys rejected like deny_unknown_fields)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from mddem_gb300 import build, capi
+
+    build.build()
+    return capi.load()
+
+
+def header_symbols():
+    with open(os.path.join(ROOT, "include", "mdg.h")) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mdg_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_header_declares_expected_entry_points():
+    from mddem_gb300 import capi
+
+    syms = header_symbols()
+    assert syms == sorted(capi.EXPORTS)
+
+
+def test_library_exports_every_header_symbol(lib):
+    for s in header_symbols():
+        assert hasattr(lib, s), s
+
+
+def test_status_strings(lib):
+    assert lib.mdg_status_string(0) == b"ok"
+    assert b"overlap" in lib.mdg_status_string(5)
+    assert lib.mdg_abi_version() == 1
+
+
+def test_create_without_device_reports_nodevice(lib):
+    from mddem_gb300 import capi, config
+
+    n = ctypes.c_int(-1)
+    if lib.mdg_device_count(ctypes.byref(n)) == 0 and n.value > 0:
+        pytest.skip("a CUDA device is present")
+    with pytest.raises(capi.MdgError) as e:
+        capi.Context(config.lj_fluid_config(), 10)
+    assert e.value.status == 11
+
+
+def test_invalid_config_rejected_before_device(lib):
+    from mddem_gb300 import capi, config
+
+    bad = config.lj_fluid_config().replace(dt=-1.0)
+    with pytest.raises(capi.MdgError) as e:
+        capi.Context(bad, 10)
+    assert e.value.status == 1
+
+
+REF_DEM_TOML = """
+[domain]
+x_low = 0.0
+x_high = 0.025
+y_low = 0.0
+y_high = 0.025
+z_low = 0.0
+z_high = 0.025
+boundary_x = "periodic"
+boundary_y = "periodic"
+boundary_z = "periodic"
+
+[neighbor]
+skin_fraction = 1.1
+bin_size = 0.005
+
+[run]
+dt = 2.934e-7
+
+[[dem.materials]]
+name = "glass"
+youngs_mod = 8.7e9
+poisson_ratio = 0.3
+restitution = 0.95
+friction = 0.4
+"""
+
+REF_LJ_TOML = """
+[domain]
+x_high = 10.06
+y_high = 10.06
+z_high = 10.06
+
+[neighbor]
+skin_fraction = 1.12
+bin_size = 1.0
+
+[lj]
+epsilon = 1.0
+sigma = 1.0
+cutoff = 2.5
+
+[lattice]
+density = 0.85
+
+[thermostat]
+temperature = 0.85
+coupling = 1.0
+
+[gpu]
+precision = "mixed"
+"""
+
+
+def test_toml_dem_sections():
+    from mddem_gb300 import from_toml
+
+    c = from_toml(REF_DEM_TOML)
+    assert c.kind == "dem" and c.box == pytest.approx((0.025, 0.025, 0.025))
+    assert c.skin_fraction == 1.1 and c.bin_size == 0.005 and c.dt == 2.934e-7
+    assert c.every == 0 and c.check and c.sort_every == 1000 and c.newton  # reference defaults
+    m = c.materials[0]
+    assert (m.youngs_mod, m.poisson_ratio, m.restitution, m.friction) == (8.7e9, 0.3, 0.95, 0.4)
+    assert m.rolling_friction == 0.0 and c.contact_model == "hertz"
+
+
+def test_toml_lj_sections():
+    from mddem_gb300 import from_toml
+
+    c = from_toml(REF_LJ_TOML)
+    assert c.kind == "lj" and c.dt == 0.005  # lattice_set_dt
+    assert c.nose_hoover and c.nh_temperature == 0.85 and c.precision == "mixed"
+
+
+def test_toml_unknown_field_rejected():
+    from mddem_gb300 import ConfigError, from_toml
+
+    with pytest.raises(ConfigError):
+        from_toml(REF_DEM_TOML.replace("bin_size = 0.005", "bin_size = 0.005\nbogus = 1"))
+    with pytest.raises(ConfigError):
+        from_toml(REF_DEM_TOML.replace('boundary_x = "periodic"', 'boundary_x = "fixed"'))
+
+
+def test_rayleigh_dt_matches_reference_formula():
+    from mddem_gb300 import config
+
+    dt = config.rayleigh_dt(1e-3, 2500.0, 8.7e9, 0.3, fraction=0.1)
+    assert dt == pytest.approx(2.934e-7, rel=1e-3)
+
+
+def test_generators_are_seeded_and_non_overlapping():
+    from mddem_gb300 import inputs
+
+    a = inputs.dem_granular_gas(200, seed=3)
+    b = inputs.dem_granular_gas(200, seed=3)
+    assert np.array_equal(a["pos"], b["pos"]) and np.array_equal(a["vel"], b["vel"])
+    p = a["pos"]
+    d = p[:, None, :] - p[None, :, :]
+    d -= 0.025 * np.round(d / 0.025)
+    r = np.sqrt((d ** 2).sum(-1)) + np.eye(len(p))
+    assert r.min() > 1.1 * 2e-3
+    assert np.allclose(np.linalg.norm(a["vel"], axis=1), 0.5)
+    lj = inputs.lj_fcc(6, 10.06, 0.85, 0.85, seed=1)
+    assert len(lj["tag"]) == 864
+    v = lj["vel"]
+    assert np.allclose(v.sum(axis=0), 0.0, atol=1e-12)
+    assert 0.5 * (v ** 2).sum() * 2 / (3 * 864 - 3) == pytest.approx(0.85, rel=1e-12)
+
+
+def test_csv_roundtrip(tmp_path):
+    from mddem_gb300 import inputs
+
+    a = inputs.dem_granular_gas(50, seed=1)
+    p = tmp_path / "p.csv"
+    inputs.write_csv(p, a)
+    b = inputs.read_csv(p)
+    for k in ("pos", "vel", "radius", "mass", "inv_inertia"):
+        assert np.array_equal(a[k], b[k]), k
