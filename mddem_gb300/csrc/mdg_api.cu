@@ -258,12 +258,18 @@ int setup_grid(const mdg_config& c, const double* cutr, size_t n, SysParams& p) 
     }
     const double per_atom_skin = (sf - 1.0) * min_skin;
     p.disp_thr_sq = per_atom_skin * per_atom_skin;
+    p.disp_thr2f = (float)(p.disp_thr_sq * (1.0 - 1e-5));
     // fp32 prefilter: bound the error of (x_j_hi + s L_f) - x_i_hi per axis
     double xmax = 0.0;
     for (int d = 0; d < 3; d++) xmax = std::fmax(xmax, std::fmax(std::fabs(p.lo[d]), std::fabs(p.hi[d])) + 2.0 * p.L[d]);
     const double E = 8.0 * std::ldexp(1.0, -24) * xmax;
     const double rpre = max_cutoff + 2.0 * std::sqrt(3.0) * E;
     p.pre_cut2 = std::nextafter((float)(rpre * rpre * (1.0 + 1e-5)), std::numeric_limits<float>::infinity());
+    // |r2_hi - r2| <= (2 r + 2 sqrt(3) E) 2 sqrt(3) E + fp32 rounding; relative to the
+    // smallest pair cutoff of the system
+    const double rmin_cut = std::fmax(2.0 * min_skin * sf, 1e-300);
+    const double eabs = (2.0 * rpre + 2.0 * std::sqrt(3.0) * E) * 2.0 * std::sqrt(3.0) * E;
+    p.band_rel = (float)(2.0 * eabs / (rmin_cut * rmin_cut) + 1e-5);
     return MDG_OK;
 }
 
@@ -588,6 +594,11 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
             p.lj4 = 4.0 * k.lj_epsilon * sigma6;
             const double rc = k.lj_cutoff * k.lj_sigma;
             p.lj_cut2 = rc * rc;
+            p.lj1f = (float)p.lj1;
+            p.lj2f = (float)p.lj2;
+            p.lj3f = (float)p.lj3;
+            p.lj4f = (float)p.lj4;
+            p.lj_cut2f = (float)p.lj_cut2;
             p.nmat = 1;
             p.mat0 = 0;
             p.hcap = 0;
@@ -624,8 +635,8 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     d.s_tag = c->alloc<uint32_t>(P, err);
     d.s_type = c->alloc<uint32_t>(P, err);
     d.s_img = c->alloc<int4>(P, err);
-    d.pos_hi = c->alloc<float4>(P, err);
-    d.pos_lo = c->alloc<float4>(P, err);
+    d.pos2 = c->alloc<float4>(2 * P, err);
+    if (c->has_mixed) d.lbp2 = c->alloc<float4>(2 * P, err);
     if (c->has_dem) {
         d.omg = c->alloc<double4>(P, err);
         d.trq = c->alloc<double4>(P, err);
@@ -1003,7 +1014,7 @@ int mdg_thermo(mdg_ctx* c, int sys, mdg_thermo_t* out) {
     const SysParams& p = c->sp[sys];
     const double ndof = 3.0 * (double)p.n - 3.0;
     out->ke = t[0];
-    out->pe = ss.pe;
+    out->pe = t[1];
     out->temp = ndof > 0 ? 2.0 * t[0] / ndof : 0.0;
     out->p_xi = ss.p_xi_post;
     out->granular_temp = t[4];

@@ -54,6 +54,7 @@ struct SysParams {
     double max_cutoff, stencil_cut_sq;
     unsigned int stencil_bits[32];  // offsets in [-sl, sl]^3 that pass the stencil distance test
     float pre_cut2;      // fp32 prefilter radius^2 for the list build (conservative)
+    float band_rel;      // relative error bound of the hi-only fp32 r^2 in the list build
     float ucut2f;        // fp32 copy of uniform_cutoff_sq
     float sf2f;          // fp32 copy of sf2
     float Lh[3], Ll[3];  // two-float split of the box lengths
@@ -67,6 +68,8 @@ struct SysParams {
     int nmat;
     long long mat0;      // offset into the packed material tables
     double lj1, lj2, lj3, lj4, lj_cut2;
+    float lj1f, lj2f, lj3f, lj4f, lj_cut2f;
+    float disp_thr2f;    // fp32 rebuild threshold of the mixed path, 1e-5 on the safe side
     int nh;
     double nh_T, nh_Q, nh_ndof;
     int virial;
@@ -132,9 +135,11 @@ struct Dev {
     int* s_hcnt;
     uint32_t* s_htag;
     double* s_hval;
-    // fp32 geometry copy (x_hi, x_lo) for the list prefilter and the mixed path
-    float4* pos_hi;
-    float4* pos_lo;
+    // two-float geometry copy relative to the box corner, interleaved so one
+    // particle is one 32-byte sector: pos2[2i] = (x_hi, y_hi, z_hi, cutoff
+    // radius), pos2[2i+1] = (x_lo, y_lo, z_lo, 0).  lbp2: same at the last build.
+    float4* pos2;
+    float4* lbp2;
     // per-particle virial (6 x P) when any system accumulates it
     double* vir;
     // reductions
@@ -175,6 +180,17 @@ __device__ __forceinline__ float two_float_sep(float xj_hi, float xj_lo, float x
         dl = xj_lo - xi_lo;
     }
     return dh + dl;
+}
+
+// (hi, lo) += t for a two-float value (Knuth two-sum, then renormalised).
+__device__ __forceinline__ void two_float_add(float& hi, float& lo, float t) {
+    const float s = hi + t;
+    const float bb = s - hi;
+    const float err = (hi - (s - bb)) + (t - bb);
+    const float l = lo + err;
+    const float h2 = s + l;
+    lo = l - (h2 - s);
+    hi = h2;
 }
 
 // ---- kernel launchers (mdg_kernels_fp64.cu / mdg_kernels_mixed.cu) ----------

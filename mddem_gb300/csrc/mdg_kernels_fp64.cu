@@ -130,17 +130,35 @@ __global__ void __launch_bounds__(BLK) k_initial(Dev d) {
         v.x += h * f.x;
         v.y += h * f.y;
         v.z += h * f.z;
-        x.x += v.x * dt;
-        x.y += v.y * dt;
-        x.z += v.z * dt;
+        const double tx = v.x * dt, ty = v.y * dt, tz = v.z * dt;
+        x.x += tx;
+        x.y += ty;
+        x.z += tz;
         d.vel[i] = v;
         d.pos[i] = x;
         if (sp.precision == 1) {
-            // two-float geometry copy relative to the box corner for the mixed kernels
-            const double rx = x.x - sp.lo[0], ry = x.y - sp.lo[1], rz = x.z - sp.lo[2];
-            const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
-            d.pos_hi[i] = make_float4(hx, hy, hz, (float)x.w);
-            d.pos_lo[i] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy), (float)(rz - (double)hz), 0.f);
+            // advance the two-float copy by the same drift in fp32 (exact two-sum,
+            // renormalised); it is re-derived from the fp64 position at every build
+            float4 ph = d.pos2[2 * i], pl = d.pos2[2 * i + 1];
+            two_float_add(ph.x, pl.x, (float)tx);
+            two_float_add(ph.y, pl.y, (float)ty);
+            two_float_add(ph.z, pl.z, (float)tz);
+            d.pos2[2 * i] = ph;
+            d.pos2[2 * i + 1] = pl;
+            if (!already) {
+                // rebuild decision in fp32 on the two-float copy, erring early
+                const float4 bh = d.lbp2[2 * i], bl = d.lbp2[2 * i + 1];
+                const float dx = (ph.x - bh.x) + (pl.x - bl.x);
+                const float dy = (ph.y - bh.y) + (pl.y - bl.y);
+                const float dz = (ph.z - bh.z) + (pl.z - bl.z);
+                bool nd = dx * dx + dy * dy + dz * dz > sp.disp_thr2f;
+                if (sp.every > 0) nd = (sp.check && nd) || st->steps_since_build >= sp.every;
+                if (!nd && sp.policy == 0) {
+                    const float rx = ph.x + pl.x, ry = ph.y + pl.y, rz = ph.z + pl.z;
+                    nd = rx < 0.f || rx >= sp.Lh[0] || ry < 0.f || ry >= sp.Lh[1] || rz < 0.f || rz >= sp.Lh[2];
+                }
+                need = nd;
+            }
         }
         if (sp.kind == 0) {
             double4 w = d.omg[i];
@@ -167,7 +185,7 @@ __global__ void __launch_bounds__(BLK) k_initial(Dev d) {
                 d.omg[i] = w;
             }
         }
-        if (!already) {
+        if (!already && sp.precision == 0) {
             bool disp = false;
             if (sp.every == 0 || sp.check) {
                 const double4 b = d.lbp[i];
@@ -397,8 +415,14 @@ __global__ void __launch_bounds__(BLK) k_copyback(Dev d, int hcur) {
     // mixed-precision pair kernels); w = cutoff radius
     const double rx = x.x - sp.lo[0], ry = x.y - sp.lo[1], rz = x.z - sp.lo[2];
     const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
-    d.pos_hi[k] = make_float4(hx, hy, hz, (float)d.s_cutr[k]);
-    d.pos_lo[k] = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy), (float)(rz - (double)hz), 0.f);
+    const float4 ph = make_float4(hx, hy, hz, (float)d.s_cutr[k]);
+    const float4 pl = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy), (float)(rz - (double)hz), 0.f);
+    d.pos2[2 * k] = ph;
+    d.pos2[2 * k + 1] = pl;
+    if (sp.precision == 1) {
+        d.lbp2[2 * k] = ph;
+        d.lbp2[2 * k + 1] = pl;
+    }
     // ext cell in the new order, with a flag when a bin coordinate lies within
     // 1e-9 of a bin edge (the list build then recomputes image cells in fp64)
     const double ux = (x.x - sp.origin[0]) * sp.inv_bin[0];
@@ -455,149 +479,268 @@ __device__ __forceinline__ void ext_cell3(const SysParams& sp, double x, double 
     cz = ext_cell_1d(z, sp.origin[2], sp.inv_bin[2], sp.ext[2]);
 }
 
-// Neighbour list build.  For particle i, every periodic image of every
-// particle in the interior-cell window around it is screened with a two-float
-// fp32 separation; the reference's cutoff test (fp64, fma form) is evaluated
-// exactly only for the rare pairs within 1e-5 of the cutoff.  The reference's
-// owner rule is applied twice: `own` (i holds the pair in the reference's half
-// list) and `oth` (the partner holds it).  Both go into i's full row, so forces
-// are summed per particle without atomics while pair arithmetic stays in the
-// owner's frame.  Image cells are integer shifts of the bin index except for
-// particles flagged as sitting within 1e-9 of a bin edge, which are rebinned in
+// Owner-rule decisions that depend only on the pair of bins: for a tile of
+// candidates from source bin E (image shift s) seen from centre bin e.
+struct TileRule {
+    bool own;   // centre particle owns every pair of the tile
+    bool oth;   // every candidate owns its pair with the centre particle
+    bool same;  // same bin, no shift: ownership by index order
+};
+
+__device__ __forceinline__ TileRule tile_rule(const SysParams& sp, int ex, int ey, int ez, int Ex, int Ey, int Ez,
+                                              int sx, int sy, int sz) {
+    TileRule r{false, false, false};
+    if (!(sx | sy | sz)) {
+        const int dx = Ex - ex, dy = Ey - ey, dz = Ez - ez;
+        if (!stencil_ok(sp, dx, dy, dz)) return r;
+        const int flat = (dx * sp.ext[1] + dy) * sp.ext[2] + dz;
+        if (!sp.newton) {
+            r.own = true;  // full stencil; self excluded per pair
+            r.same = flat == 0;
+            return r;
+        }
+        r.own = flat > 0;
+        r.oth = flat < 0;
+        r.same = flat == 0;
+        return r;
+    }
+    // periodic image: image bin of the candidate g, image bin of the centre h
+    const int gx = min(max(Ex + sx * sp.nc[0], 0), sp.ext[0] - 1);
+    const int gy = min(max(Ey + sy * sp.nc[1], 0), sp.ext[1] - 1);
+    const int gz = min(max(Ez + sz * sp.nc[2], 0), sp.ext[2] - 1);
+    const int hx = min(max(ex - sx * sp.nc[0], 0), sp.ext[0] - 1);
+    const int hy = min(max(ey - sy * sp.nc[1], 0), sp.ext[1] - 1);
+    const int hz = min(max(ez - sz * sp.nc[2], 0), sp.ext[2] - 1);
+    r.own = owner_test(sp, ex, ey, ez, gx, gy, gz, true, 0, 1);
+    r.oth = sp.newton && owner_test(sp, Ex, Ey, Ez, hx, hy, hz, true, 0, 1);
+    return r;
+}
+
+// Neighbour list build, one warp per (ext) bin: the lanes are the bin's
+// particles (32 at a time); every neighbouring bin of the interior-cell window
+// (with its periodic image shift) is staged into shared memory 32 particles at
+// a time.  Each candidate is screened by a 10-instruction fp32 test on the hi
+// parts (conservative radius); survivors get the two-float separation, and
+// the reference's own fp64 cutoff test (fma form) only within 1e-5 of the
+// cutoff.  The reference's owner rule is applied twice: `own` (i holds the
+// pair in the reference's half list) and `oth` (the partner holds it); both go
+// into i's full row, so forces are summed per particle without atomics while
+// pair arithmetic stays in the owner's frame.  Owner decisions are per tile
+// (they depend only on the two bins) except for same-bin order and for
+// particles within 1e-9 of a bin edge, whose image bins are recomputed in
 // fp64.  Also saves last_build_pos (neighbor.rs:545-561).
-__global__ void __launch_bounds__(BLK) k_build(Dev d) {
-    const int s = d.blk_sys[blockIdx.x];
+constexpr int BUILD_WARPS = 4;
+
+__global__ void __launch_bounds__(BUILD_WARPS * 32) k_build(Dev d) {
+    __shared__ float4 tile_h[BUILD_WARPS][32], tile_l[BUILD_WARPS][32];
+    __shared__ int tile_e[BUILD_WARPS][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    constexpr int SUBS = BLK / BUILD_WARPS;  // blocks per 128-bin cell block
+    const int cblock = blockIdx.x / SUBS;
+    const int s = d.cblk_sys[cblock];
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
     if (!do_rebuild(st)) return;
-    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
-    if (li >= sp.n) return;
-    const long long i = (long long)sp.p0 + li;
-    const double4 xi = d.pos[i];
-    d.lbp[i] = xi;
-    const float4 hi = d.pos_hi[i];
-    const float4 lo = d.pos_lo[i];
-    const int ci = d.cell[i];
-    const bool edge_i = ci < 0;
-    const int flat_i = ci & 0x7fffffff;
-    const int ez = flat_i % sp.ext[2];
-    const int ey = (flat_i / sp.ext[2]) % sp.ext[1];
-    const int ex = flat_i / (sp.ext[2] * sp.ext[1]);
+    const int c = (cblock - d.cblk0[s]) * BLK + (blockIdx.x % SUBS) * BUILD_WARPS + warp;
+    if (c >= sp.ncell) return;
+    const int a0 = d.cstart[sp.c0 + c], a1 = d.cstart[sp.c0 + c + 1];
+    if (a0 == a1) return;
+    const int ez = c % sp.ext[2];
+    const int ey = (c / sp.ext[2]) % sp.ext[1];
+    const int ex = c / (sp.ext[2] * sp.ext[1]);
     const int qx0 = min(max(ex - sp.sl[0], 0), sp.nc[0] - 1);
     const int qy0 = min(max(ey - sp.sl[1], 0), sp.nc[1] - 1);
     const int qz0 = min(max(ez - sp.sl[2], 0), sp.nc[2] - 1);
     const float band_hi = 1.00001f, band_lo = 0.99999f;
-    int count = 0;
-    const long long base = sp.lst0 + li;
-    for (int ox = -sp.win[0]; ox <= sp.win[0]; ox++) {
-        int qx = qx0 + ox, sx = 0;
-        if (qx < 0) { qx += sp.nc[0]; sx = -1; } else if (qx >= sp.nc[0]) { qx -= sp.nc[0]; sx = 1; }
-        if (qx < 0 || qx >= sp.nc[0]) continue;
-        for (int oy = -sp.win[1]; oy <= sp.win[1]; oy++) {
-            int qy = qy0 + oy, sy = 0;
-            if (qy < 0) { qy += sp.nc[1]; sy = -1; } else if (qy >= sp.nc[1]) { qy -= sp.nc[1]; sy = 1; }
-            if (qy < 0 || qy >= sp.nc[1]) continue;
-            for (int oz = -sp.win[2]; oz <= sp.win[2]; oz++) {
-                int qz = qz0 + oz, sz = 0;
-                if (qz < 0) { qz += sp.nc[2]; sz = -1; } else if (qz >= sp.nc[2]) { qz -= sp.nc[2]; sz = 1; }
-                if (qz < 0 || qz >= sp.nc[2]) continue;
-                const bool shifted = (sx | sy | sz) != 0;
-                const uint32_t sc = (uint32_t)((sx + 1) * 9 + (sy + 1) * 3 + (sz + 1));
-                // source ext cells: the interior cell and the ghost-layer cells that
-                // clamp into it (particles whose bin coordinate rounded just outside)
-                const int axa = (qx == 0) ? -1 : 0, axb = (qx == sp.nc[0] - 1) ? 1 : 0;
-                const int aya = (qy == 0) ? -1 : 0, ayb = (qy == sp.nc[1] - 1) ? 1 : 0;
-                const int aza = (qz == 0) ? -1 : 0, azb = (qz == sp.nc[2] - 1) ? 1 : 0;
-                for (int ax = axa; ax <= axb; ax++)
-                    for (int ay = aya; ay <= ayb; ay++)
-                        for (int az = aza; az <= azb; az++) {
-                            const int Ex = qx + sp.sl[0] + ax, Ey = qy + sp.sl[1] + ay, Ez = qz + sp.sl[2] + az;
-                            const int flatE = (Ex * sp.ext[1] + Ey) * sp.ext[2] + Ez;
-                            const int m0 = d.cstart[sp.c0 + flatE], m1 = d.cstart[sp.c0 + flatE + 1];
-                            for (int m = m0; m < m1; m++) {
-                                const long long j = m;
-                                if (!shifted && j == i) continue;
-                                const float4 hj = d.pos_hi[j];
-                                const float4 lj = d.pos_lo[j];
-                                const float fx = two_float_sep(hj.x, lj.x, hi.x, lo.x, sx, sp.Lh[0], sp.Ll[0]);
-                                const float fy = two_float_sep(hj.y, lj.y, hi.y, lo.y, sy, sp.Lh[1], sp.Ll[1]);
-                                const float fz = two_float_sep(hj.z, lj.z, hi.z, lo.z, sz, sp.Lh[2], sp.Ll[2]);
-                                const float r2f = fx * fx + fy * fy + fz * fz;
-                                float c2f;
-                                if (sp.uniform) {
-                                    c2f = sp.ucut2f;
-                                } else {
-                                    const float ss = hi.w + hj.w;
-                                    c2f = ss * ss * sp.sf2f;
-                                }
-                                if (r2f > c2f * band_hi) continue;
-                                bool ok_i = true, ok_j = true;
-                                const bool band = r2f >= c2f * band_lo;
-                                double4 xj;
-                                if (band || (shifted && (edge_i || d.cell[j] < 0))) xj = d.pos[j];
-                                if (band) {
-                                    // the reference's own test, in its own arithmetic
-                                    const double si = d.cutr[i], sj = d.cutr[j];
-                                    const double dx = img_coord(xj.x, sx, sp.L[0]) - xi.x;
-                                    const double dy = img_coord(xj.y, sy, sp.L[1]) - xi.y;
-                                    const double dz = img_coord(xj.z, sz, sp.L[2]) - xi.z;
-                                    ok_i = cut_ok(sp, fma(dx, dx, fma(dy, dy, dz * dz)), si, sj);
-                                    if (shifted) {
-                                        const double ux = img_coord(xi.x, -sx, sp.L[0]) - xj.x;
-                                        const double uy = img_coord(xi.y, -sy, sp.L[1]) - xj.y;
-                                        const double uz = img_coord(xi.z, -sz, sp.L[2]) - xj.z;
-                                        ok_j = cut_ok(sp, fma(ux, ux, fma(uy, uy, uz * uz)), sj, si);
-                                    } else {
-                                        ok_j = ok_i;
+    const float brel = sp.band_rel;
+    for (int ib = a0; ib < a1; ib += 32) {
+        const long long i = ib + lane;
+        const bool act = i < a1;
+        float4 hi = make_float4(0, 0, 0, 0), lo = make_float4(0, 0, 0, 0);
+        bool edge_i = false;
+        if (act) {
+            d.lbp[i] = d.pos[i];
+            hi = d.pos2[2 * i];
+            lo = d.pos2[2 * i + 1];
+            edge_i = d.cell[i] < 0;
+        }
+        const long long base = sp.lst0 + (i - sp.p0);
+        int count = 0;
+        for (int ox = -sp.win[0]; ox <= sp.win[0]; ox++) {
+            int qx = qx0 + ox, sx = 0;
+            if (qx < 0) { qx += sp.nc[0]; sx = -1; } else if (qx >= sp.nc[0]) { qx -= sp.nc[0]; sx = 1; }
+            if (qx < 0 || qx >= sp.nc[0]) continue;
+            for (int oy = -sp.win[1]; oy <= sp.win[1]; oy++) {
+                int qy = qy0 + oy, sy = 0;
+                if (qy < 0) { qy += sp.nc[1]; sy = -1; } else if (qy >= sp.nc[1]) { qy -= sp.nc[1]; sy = 1; }
+                if (qy < 0 || qy >= sp.nc[1]) continue;
+                for (int oz = -sp.win[2]; oz <= sp.win[2]; oz++) {
+                    int qz = qz0 + oz, sz = 0;
+                    if (qz < 0) { qz += sp.nc[2]; sz = -1; } else if (qz >= sp.nc[2]) { qz -= sp.nc[2]; sz = 1; }
+                    if (qz < 0 || qz >= sp.nc[2]) continue;
+                    const bool shifted = (sx | sy | sz) != 0;
+                    const uint32_t sc = (uint32_t)((sx + 1) * 9 + (sy + 1) * 3 + (sz + 1));
+                    // centre position moved by -s L: the candidate's own hi part
+                    // then gives the prefilter separation directly
+                    const float hsx = hi.x - (float)sx * sp.Lh[0];
+                    const float hsy = hi.y - (float)sy * sp.Lh[1];
+                    const float hsz = hi.z - (float)sz * sp.Lh[2];
+                    const int axa = (qx == 0) ? -1 : 0, axb = (qx == sp.nc[0] - 1) ? 1 : 0;
+                    const int aya = (qy == 0) ? -1 : 0, ayb = (qy == sp.nc[1] - 1) ? 1 : 0;
+                    const int aza = (qz == 0) ? -1 : 0, azb = (qz == sp.nc[2] - 1) ? 1 : 0;
+                    for (int ax = axa; ax <= axb; ax++)
+                        for (int ay = aya; ay <= ayb; ay++)
+                            for (int az = aza; az <= azb; az++) {
+                                const int Ex = qx + sp.sl[0] + ax, Ey = qy + sp.sl[1] + ay, Ez = qz + sp.sl[2] + az;
+                                const int flatE = (Ex * sp.ext[1] + Ey) * sp.ext[2] + Ez;
+                                const int m0 = d.cstart[sp.c0 + flatE], m1 = d.cstart[sp.c0 + flatE + 1];
+                                if (m0 == m1) continue;
+                                const TileRule tr = tile_rule(sp, ex, ey, ez, Ex, Ey, Ez, sx, sy, sz);
+                                // nothing in this bin pair can enter the list unless a
+                                // bin-edge particle needs its image bin recomputed
+                                const bool maybe_edge = shifted;
+                                if (!tr.own && !tr.oth && !tr.same && !maybe_edge) continue;
+                                for (int t0 = m0; t0 < m1; t0 += 32) {
+                                    const int nt = min(32, m1 - t0);
+                                    __syncwarp();
+                                    if (lane < nt) {
+                                        tile_h[warp][lane] = d.pos2[2 * (long long)(t0 + lane)];
+                                        tile_l[warp][lane] = d.pos2[2 * (long long)(t0 + lane) + 1];
+                                        tile_e[warp][lane] = d.cell[t0 + lane] < 0;
                                     }
-                                    if (!ok_i && !ok_j) continue;
-                                }
-                                bool own, oth = false;
-                                if (!shifted) {
-                                    own = ok_i && owner_test(sp, ex, ey, ez, Ex, Ey, Ez, false, i, j);
-                                    if (sp.newton) oth = ok_j && owner_test(sp, Ex, Ey, Ez, ex, ey, ez, false, j, i);
-                                } else {
-                                    int gx, gy, gz, hx, hy, hz;
-                                    if (!edge_i && d.cell[j] >= 0) {
-                                        gx = min(max(Ex + sx * sp.nc[0], 0), sp.ext[0] - 1);
-                                        gy = min(max(Ey + sy * sp.nc[1], 0), sp.ext[1] - 1);
-                                        gz = min(max(Ez + sz * sp.nc[2], 0), sp.ext[2] - 1);
-                                        hx = min(max(ex - sx * sp.nc[0], 0), sp.ext[0] - 1);
-                                        hy = min(max(ey - sy * sp.nc[1], 0), sp.ext[1] - 1);
-                                        hz = min(max(ez - sz * sp.nc[2], 0), sp.ext[2] - 1);
-                                    } else {
-                                        ext_cell3(sp, img_coord(xj.x, sx, sp.L[0]), img_coord(xj.y, sy, sp.L[1]),
-                                                  img_coord(xj.z, sz, sp.L[2]), gx, gy, gz);
-                                        ext_cell3(sp, img_coord(xi.x, -sx, sp.L[0]), img_coord(xi.y, -sy, sp.L[1]),
-                                                  img_coord(xi.z, -sz, sp.L[2]), hx, hy, hz);
+                                    __syncwarp();
+                                    if (!act) continue;
+                                    // pass 1: hi-part fp32 screen of the whole tile into two bit
+                                    // masks: clearly inside the cutoff / near it (precise path)
+                                    unsigned int mask = 0u, near = 0u;
+#pragma unroll 4
+                                    for (int t = 0; t < nt; t++) {
+                                        const float4 hj = tile_h[warp][t];
+                                        const float px = hj.x - hsx, py = hj.y - hsy, pz = hj.z - hsz;
+                                        const float r2h = px * px + py * py + pz * pz;
+                                        float c2h;
+                                        if (sp.uniform) {
+                                            c2h = sp.ucut2f;
+                                        } else {
+                                            const float ssum = hi.w + hj.w;
+                                            c2h = ssum * ssum * sp.sf2f;
+                                        }
+                                        mask |= (r2h <= c2h * (1.f + brel) ? 1u : 0u) << t;
+                                        near |= (r2h > c2h * (1.f - brel) ? 1u : 0u) << t;
                                     }
-                                    own = ok_i && owner_test(sp, ex, ey, ez, gx, gy, gz, true, i, j);
-                                    if (sp.newton) oth = ok_j && owner_test(sp, Ex, Ey, Ez, hx, hy, hz, true, j, i);
-                                }
-                                const uint32_t jl = (uint32_t)(j - sp.p0);
-                                if (own) {
-                                    if (count < sp.ncap)
-                                        d.nlist[base + (long long)count * sp.npad] = jl | ((sc + 27u) << IDX_BITS);
-                                    count++;
-                                }
-                                if (oth) {
-                                    if (count < sp.ncap)
-                                        d.nlist[base + (long long)count * sp.npad] = jl | (sc << IDX_BITS);
-                                    count++;
+                                    if (!shifted && i >= t0 && i < t0 + nt) mask &= ~(1u << (int)(i - t0));
+                                    // pass 2: survivors only
+                                    while (mask) {
+                                        const int t = __ffs(mask) - 1;
+                                        mask &= mask - 1u;
+                                        const long long j = t0 + t;
+                                        bool ok_i = true, ok_j = true;
+                                        const bool edge = shifted && (edge_i || tile_e[warp][t] != 0);
+                                        if (!((near >> t) & 1u) && !edge) {
+                                            // clearly inside: owner decision only
+                                            const bool own = tr.own || (tr.same && (sp.newton ? j > i : true));
+                                            const bool oth = tr.oth || (tr.same && sp.newton && i > j);
+                                            const uint32_t jl = (uint32_t)(j - sp.p0);
+                                            if (own) {
+                                                if (count < sp.ncap)
+                                                    d.nlist[base + (long long)count * sp.npad] = jl | ((sc + 27u) << IDX_BITS);
+                                                count++;
+                                            }
+                                            if (oth) {
+                                                if (count < sp.ncap)
+                                                    d.nlist[base + (long long)count * sp.npad] = jl | (sc << IDX_BITS);
+                                                count++;
+                                            }
+                                            continue;
+                                        }
+                                        const float4 hj = tile_h[warp][t];
+                                        // near the cutoff: two-float separation, then the exact test
+                                        const float4 lj = tile_l[warp][t];
+                                        const float fx = two_float_sep(hj.x, lj.x, hi.x, lo.x, sx, sp.Lh[0], sp.Ll[0]);
+                                        const float fy = two_float_sep(hj.y, lj.y, hi.y, lo.y, sy, sp.Lh[1], sp.Ll[1]);
+                                        const float fz = two_float_sep(hj.z, lj.z, hi.z, lo.z, sz, sp.Lh[2], sp.Ll[2]);
+                                        const float r2f = fx * fx + fy * fy + fz * fz;
+                                        float c2f;
+                                        if (sp.uniform) {
+                                            c2f = sp.ucut2f;
+                                        } else {
+                                            const float ssum = hi.w + hj.w;
+                                            c2f = ssum * ssum * sp.sf2f;
+                                        }
+                                        if (r2f > c2f * band_hi) continue;
+                                        if (r2f >= c2f * band_lo || edge) {
+                                            const double4 xi = d.pos[i], xj = d.pos[j];
+                                            const double si = d.cutr[i], sj = d.cutr[j];
+                                            if (r2f >= c2f * band_lo) {
+                                                // the reference's own test, in its own arithmetic
+                                                const double dx = img_coord(xj.x, sx, sp.L[0]) - xi.x;
+                                                const double dy = img_coord(xj.y, sy, sp.L[1]) - xi.y;
+                                                const double dz = img_coord(xj.z, sz, sp.L[2]) - xi.z;
+                                                ok_i = cut_ok(sp, fma(dx, dx, fma(dy, dy, dz * dz)), si, sj);
+                                                if (shifted) {
+                                                    const double ux = img_coord(xi.x, -sx, sp.L[0]) - xj.x;
+                                                    const double uy = img_coord(xi.y, -sy, sp.L[1]) - xj.y;
+                                                    const double uz = img_coord(xi.z, -sz, sp.L[2]) - xj.z;
+                                                    ok_j = cut_ok(sp, fma(ux, ux, fma(uy, uy, uz * uz)), sj, si);
+                                                } else {
+                                                    ok_j = ok_i;
+                                                }
+                                                if (!ok_i && !ok_j) continue;
+                                            }
+                                            if (edge) {
+                                                int gx, gy, gz, hx, hy, hz;
+                                                ext_cell3(sp, img_coord(xj.x, sx, sp.L[0]), img_coord(xj.y, sy, sp.L[1]),
+                                                          img_coord(xj.z, sz, sp.L[2]), gx, gy, gz);
+                                                ext_cell3(sp, img_coord(xi.x, -sx, sp.L[0]),
+                                                          img_coord(xi.y, -sy, sp.L[1]),
+                                                          img_coord(xi.z, -sz, sp.L[2]), hx, hy, hz);
+                                                const bool own = ok_i && owner_test(sp, ex, ey, ez, gx, gy, gz, true, i, j);
+                                                const bool oth = sp.newton && ok_j &&
+                                                                 owner_test(sp, Ex, Ey, Ez, hx, hy, hz, true, j, i);
+                                                const uint32_t jl = (uint32_t)(j - sp.p0);
+                                                if (own) {
+                                                    if (count < sp.ncap)
+                                                        d.nlist[base + (long long)count * sp.npad] = jl | ((sc + 27u) << IDX_BITS);
+                                                    count++;
+                                                }
+                                                if (oth) {
+                                                    if (count < sp.ncap)
+                                                        d.nlist[base + (long long)count * sp.npad] = jl | (sc << IDX_BITS);
+                                                    count++;
+                                                }
+                                                continue;
+                                            }
+                                        }
+                                        const bool own = ok_i && (tr.own || (tr.same && (sp.newton ? j > i : true)));
+                                        const bool oth = ok_j && (tr.oth || (tr.same && sp.newton && i > j));
+                                        const uint32_t jl = (uint32_t)(j - sp.p0);
+                                        if (own) {
+                                            if (count < sp.ncap)
+                                                d.nlist[base + (long long)count * sp.npad] = jl | ((sc + 27u) << IDX_BITS);
+                                            count++;
+                                        }
+                                        if (oth) {
+                                            if (count < sp.ncap)
+                                                d.nlist[base + (long long)count * sp.npad] = jl | (sc << IDX_BITS);
+                                            count++;
+                                        }
+                                    }
                                 }
                             }
-                        }
+                }
             }
         }
+        if (act) {
+            if (count > sp.ncap) {
+                atomicOr(&st->status, ST_NBR_OVF);
+                atomicMax(&st->max_nbr, count);
+                count = sp.ncap;
+            } else {
+                atomicMax(&st->max_nbr, count);
+            }
+            d.nnum[i] = count;
+        }
     }
-    if (count > sp.ncap) {
-        atomicOr(&st->status, ST_NBR_OVF);
-        atomicMax(&st->max_nbr, count);
-        count = sp.ncap;
-    } else {
-        atomicMax(&st->max_nbr, count);
-    }
-    d.nnum[i] = count;
 }
 
 // ----------------------------------------------------------------------------
@@ -621,7 +764,7 @@ __global__ void __launch_bounds__(BLK) k_lj_fp64(Dev d) {
         const double4 xi = d.pos[i];
         const int nn = d.nnum[i];
         const long long base = sp.lst0 + li;
-        const double lj1 = sp.lj1, lj2 = sp.lj2, lj3 = sp.lj3, lj4 = sp.lj4, cut2 = sp.lj_cut2;
+        const double lj1 = sp.lj1, lj2 = sp.lj2, cut2 = sp.lj_cut2;
         const double half = sp.newton ? 1.0 : 0.5;
         for (int k = lane; k < nn; k += TPP) {
             const uint32_t e = d.nlist[base + (long long)k * sp.npad];
@@ -666,7 +809,6 @@ __global__ void __launch_bounds__(BLK) k_lj_fp64(Dev d) {
                     fx -= px; fy -= py; fz -= pz;
                 }
             }
-            if (own) pe += r6inv * (lj3 * r6inv - lj4) * half;
         }
     }
     if (TPP > 1) {
@@ -1051,7 +1193,6 @@ __global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
             d.vel[i] = v;
         }
         vals[0] = d.mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z);
-        vals[7] = f.w;
         if (sp.kind == 0 && integrate) {
             double4 w = d.omg[i];
             if (w.w != 0.0) {
@@ -1077,12 +1218,10 @@ __global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
     if (sp.virial) {
         last = system_reduce<8>(d, s, vals, out);
     } else {
-        // KE and PE only
-        const double v2[2] = {vals[0], vals[7]};
-        double o2[2];
-        last = system_reduce<2>(d, s, v2, o2);
-        out[0] = o2[0];
-        out[7] = o2[1];
+        const double v1[1] = {vals[0]};
+        double o1[1];
+        last = system_reduce<1>(d, s, v1, o1);
+        out[0] = o1[0];
     }
     if (last && threadIdx.x == 0) {
         const double ke = 0.5 * out[0];
@@ -1098,7 +1237,6 @@ __global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
         }
         if (sp.virial)
             for (int q = 0; q < 6; q++) st->vir[q] = out[1 + q];
-        st->pe = out[7];
         const bool rb = do_rebuild(st);
         if (integrate) {
             st->steps_since_build = rb ? 0 : st->steps_since_build + 1;
@@ -1189,6 +1327,39 @@ __global__ void __launch_bounds__(BLK) k_thermo2(Dev d, double* out16) {
     if (system_reduce<1>(d, s, vals, out) && threadIdx.x == 0) out16[(size_t)s * 16 + 4] = out[0] / (3.0 * o[8]);
 }
 
+// LJ potential energy per particle (owner entries of the full row; the sum
+// over particles is the sum over the reference's half-list pairs), fp64,
+// written to frc.w.  Launched on demand by the thermo query.
+__global__ void __launch_bounds__(BLK) k_lj_pe(Dev d) {
+    const int s = d.blk_sys[blockIdx.x];
+    const SysParams& sp = d.sp[s];
+    if (sp.kind != 1) return;
+    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    if (li >= sp.n) return;
+    const long long i = (long long)sp.p0 + li;
+    const double4 xi = d.pos[i];
+    const int nn = d.nnum[i];
+    const long long base = sp.lst0 + li;
+    double pe = 0.0;
+    for (int k = 0; k < nn; k++) {
+        const uint32_t e = d.nlist[base + (long long)k * sp.npad];
+        const uint32_t code = e >> IDX_BITS;
+        if (code < 27u) continue;
+        int sx, sy, sz;
+        decode_shift((int)(code - 27u), sx, sy, sz);
+        const double4 xj = d.pos[sp.p0 + (e & IDX_MASK)];
+        const double dx = img_coord(xj.x, sx, sp.L[0]) - xi.x;
+        const double dy = img_coord(xj.y, sy, sp.L[1]) - xi.y;
+        const double dz = img_coord(xj.z, sz, sp.L[2]) - xi.z;
+        const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
+        if (r2 >= sp.lj_cut2) continue;
+        const double r2inv = 1.0 / r2;
+        const double r6inv = r2inv * r2inv * r2inv;
+        pe += r6inv * (sp.lj3 * r6inv - sp.lj4) * (sp.newton ? 1.0 : 0.5);
+    }
+    d.frc[i].w = pe;
+}
+
 // ----------------------------------------------------------------------------
 // launchers
 // ----------------------------------------------------------------------------
@@ -1204,7 +1375,7 @@ int launch_rebuild(const Dev& d, int hcur, cudaStream_t st) {
     k_cellsort<<<d.ncblocks, BLK, 0, st>>>(d);
     k_gather<<<d.nblocks, BLK, 0, st>>>(d, hcur);
     k_copyback<<<d.nblocks, BLK, 0, st>>>(d, hcur);
-    k_build<<<d.nblocks, BLK, 0, st>>>(d);
+    k_build<<<d.ncblocks * (BLK / BUILD_WARPS), BUILD_WARPS * 32, 0, st>>>(d);
     return 7;
 }
 
@@ -1237,9 +1408,10 @@ int launch_ke_init(const Dev& d, cudaStream_t st) {
 }
 
 int launch_thermo(const Dev& d, double* out, cudaStream_t st) {
+    k_lj_pe<<<d.nblocks, BLK, 0, st>>>(d);
     k_thermo1<<<d.nblocks, BLK, 0, st>>>(d, out);
     k_thermo2<<<d.nblocks, BLK, 0, st>>>(d, out);
-    return 2;
+    return 3;
 }
 
 }  // namespace mdg
