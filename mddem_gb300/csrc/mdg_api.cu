@@ -604,7 +604,10 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
             p.hcap = 0;
         }
         if (k.virial) c->any_virial = true;
-        if (k.threads_per_particle > 1) c->tpp_lj = k.threads_per_particle;
+        // threads per particle of the LJ force kernel: explicit, or 4 for the
+        // mixed path (the measured best on GB300 for ~78-entry rows) and 1 for fp64
+        if (k.threads_per_particle > 0) c->tpp_lj = k.threads_per_particle;
+        else if (k.kind == MDG_KIND_LJ && k.precision == MDG_MIXED) c->tpp_lj = 4;
     }
     if (P > (long long)IDX_MASK * 8) {
         delete c;
