@@ -211,6 +211,21 @@ typedef struct mdg_step_timing {
 } mdg_step_timing;
 int  mdg_timed_steps(mdg_ctx* ctx, int64_t nsteps, size_t l2_flush_bytes, mdg_step_timing* per_step);
 
+/* Granular temperature without allocating.  No counterpart in the reference:
+ * it is the mdg_thermo reduction (print_granular_temperature + compute_ke) for
+ * callers that cannot call cudaMalloc -- e.g. a host that reserves all device
+ * memory for its own pool, or a latency-critical loop that must not risk an
+ * allocation's device synchronisation.  vel (n*3 interleaved) and mass (n) are
+ * device pointers; out3 (device, 3 doubles) receives
+ * [sum m|v-vbar|^2 / (3M), 0.5 sum m|v|^2, |sum m v|].  The only scratch is a
+ * static device array inside the library (about 256 KB, held on every GPU that
+ * loads the library until exit), which limits n to 1,048,576 particles
+ * (larger n returns MDG_ERR_ARG).  The first call on a device looks up that
+ * array's device address, so make the first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race.  Work is
+ * queued on `stream` (NULL = default stream); the call does not synchronise. */
+int  mdg_granular_temp_noalloc(const double* vel, const double* mass, size_t n, double* out3, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

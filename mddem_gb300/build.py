@@ -29,6 +29,7 @@ UNITS = [
     ("mdg_kernels_fp64.cu", ["-fmad=false"]),
     ("mdg_kernels_mixed.cu", []),
     ("mdg_api.cu", ["-fmad=false"]),
+    ("mdg_noalloc.cu", ["-fmad=false"]),
 ]
 
 

@@ -29,7 +29,7 @@ EXPORTS = [
     "mdg_abi_version", "mdg_status_string", "mdg_device_count", "mdg_create", "mdg_batch_create", "mdg_destroy",
     "mdg_num_systems", "mdg_upload_state", "mdg_download_state", "mdg_set_history", "mdg_get_history",
     "mdg_step", "mdg_force_only", "mdg_get_pairs", "mdg_thermo", "mdg_synchronize", "mdg_kernel_launches",
-    "mdg_set_graph_mode", "mdg_timed_steps",
+    "mdg_set_graph_mode", "mdg_timed_steps", "mdg_granular_temp_noalloc",
 ]
 
 
@@ -124,6 +124,7 @@ def load(path: str = LIB_PATH):
     lib.mdg_kernel_launches.restype = C.c_int64
     lib.mdg_set_graph_mode.argtypes = [C.c_void_p, C.c_int]
     lib.mdg_timed_steps.argtypes = [C.c_void_p, C.c_int64, C.c_size_t, C.POINTER(StepTiming)]
+    lib.mdg_granular_temp_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]
     _lib = lib
     return lib
 
