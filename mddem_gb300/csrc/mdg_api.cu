@@ -99,7 +99,7 @@ int validate_config(const mdg_config& c) {
         if (!(c.lj_epsilon > 0.0) || !(c.lj_sigma > 0.0) || !(c.lj_cutoff > 0.0)) return MDG_ERR_CONFIG;
     }
     if (c.nose_hoover && (!(c.nh_temperature > 0.0) || !(c.nh_coupling > 0.0))) return MDG_ERR_CONFIG;
-    if (c.precision == MDG_MIXED && (c.kind == MDG_KIND_DEM || c.virial)) return MDG_ERR_CONFIG;
+    if (c.precision == MDG_MIXED && c.virial) return MDG_ERR_CONFIG;
     const int t = c.threads_per_particle;
     if (!(t == 0 || t == 1 || t == 2 || t == 4 || t == 8)) return MDG_ERR_CONFIG;
     if (c.neighbor_capacity < 0 || c.history_capacity < 0) return MDG_ERR_CONFIG;
@@ -663,6 +663,7 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     c->d_sp = c->alloc<SysParams>(nsys, err);
     d.ss = c->alloc<SysState>(nsys, err);
     c->d_mat = c->alloc<double>(std::max<size_t>(mat_all.size(), 1), err);
+    float* d_matf = c->alloc<float>(std::max<size_t>(mat_all.size(), 1), err);
     c->d_thermo = c->alloc<double>((size_t)nsys * 16, err);
     d.grid_ctr = c->alloc<unsigned int>(1, err);
     if (err) {
@@ -670,8 +671,12 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
         return err;
     }
     cudaMemcpy(c->d_blk_sys, blk_sys.data(), blk_sys.size() * sizeof(int), cudaMemcpyHostToDevice);
-    if (!mat_all.empty())
+    if (!mat_all.empty()) {
         cudaMemcpy(c->d_mat, mat_all.data(), mat_all.size() * sizeof(double), cudaMemcpyHostToDevice);
+        std::vector<float> mf(mat_all.begin(), mat_all.end());
+        cudaMemcpy(d_matf, mf.data(), mf.size() * sizeof(float), cudaMemcpyHostToDevice);
+    }
+    d.matf = d_matf;
     d.blk_sys = c->d_blk_sys;
     d.sp = c->d_sp;
     d.mat = c->d_mat;

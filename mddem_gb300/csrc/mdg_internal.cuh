@@ -151,6 +151,7 @@ struct Dev {
     const SysParams* sp;
     SysState* ss;
     const double* mat;
+    const float* matf;   // fp32 copy of the material tables (mixed path)
     int nsys;
     int nblocks;
     long long P;       // total padded particles

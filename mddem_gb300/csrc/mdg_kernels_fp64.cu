@@ -415,8 +415,11 @@ __global__ void __launch_bounds__(BLK) k_copyback(Dev d, int hcur) {
     // mixed-precision pair kernels); w = cutoff radius
     const double rx = x.x - sp.lo[0], ry = x.y - sp.lo[1], rz = x.z - sp.lo[2];
     const float hx = (float)rx, hy = (float)ry, hz = (float)rz;
-    const float4 ph = make_float4(hx, hy, hz, (float)d.s_cutr[k]);
-    const float4 pl = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy), (float)(rz - (double)hz), 0.f);
+    const double cr = d.s_cutr[k];
+    const float crh = (float)cr;
+    const float4 ph = make_float4(hx, hy, hz, crh);
+    const float4 pl = make_float4((float)(rx - (double)hx), (float)(ry - (double)hy), (float)(rz - (double)hz),
+                                  (float)(cr - (double)crh));
     d.pos2[2 * k] = ph;
     d.pos2[2 * k + 1] = pl;
     if (sp.precision == 1) {

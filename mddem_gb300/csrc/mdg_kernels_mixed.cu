@@ -110,10 +110,372 @@ __global__ void __launch_bounds__(BLK, 8) k_lj_mixed(Dev d) {
     if (act && lane == 0) d.frc[i] = make_double4(kx.value(), ky.value(), kz.value(), 0.0);
 }
 
+// ----------------------------------------------------------------------------
+// Hertz-Mindlin / Hooke contact, mixed precision.
+//
+// Geometry: the overlap delta = (r1 + r2) - d cancels two millimetre-scale
+// numbers, so it is formed as ((r1 + r2)^2 - d^2) / ((r1 + r2) + d) with both
+// squares in double-float arithmetic (error-free fp32 transformations:
+// Knuth two-sum, two-product via fma; Dekker 1971), from two-float separations
+// and two-float radii.  Everything downstream (normal, damping, tangential
+// force, torques) is fp32; the tangential / rolling / twisting spring
+// integration (rotation into the tangent plane, v_t dt, Coulomb rescale) is
+// fp64; per-particle sums are Kahan-compensated.  Each pair is evaluated in
+// its owner's frame on both sides, so forces stay exactly antisymmetric.
+// Same laws and branches as hm_pair (contact.rs:103-615, 622-990).
+// ----------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
+    p = a * b;
+    e = fmaf(a, b, -p);
+}
+
+// separation component (x_p + s L) - x_o as an unevaluated sum dh + dl
+__device__ __forceinline__ void sep_df(float hp, float lp, float ho, float lo_, int s, float Lh, float Ll, float& dh,
+                                       float& dl) {
+    float a = hp, b = ho, al = lp, bl = lo_;
+    if (s > 0) {  // shift the owner (next to the crossed face) by -L
+        float t, te;
+        two_sum(ho, -Lh, t, te);
+        b = t;
+        bl = lo_ - Ll + te;
+    } else if (s < 0) {
+        float t, te;
+        two_sum(hp, -Lh, t, te);
+        a = t;
+        al = lp - Ll + te;
+    }
+    float e;
+    two_sum(a, -b, dh, e);
+    dl = (al - bl) + e;
+}
+
+struct Kahan3 {
+    Kahan x, y, z;
+    __device__ __forceinline__ void add(float a, float b, float c) {
+        x.add(a);
+        y.add(b);
+        z.add(c);
+    }
+};
+
+__device__ __forceinline__ float mtf(const Dev& d, const SysParams& sp, int tab, int a, int b) {
+    return d.matf[sp.mat0 + ((long long)tab * sp.nmat + a) * sp.nmat + b];
+}
+
+struct PairMixed {
+    float fn[3], ft[3], ti[3], tj[3], tr[3], tw[3];
+    double spring[7];
+    bool hit, tang, overlap;
+};
+
+// o = owner, p = partner; geometry as double-float separation (dxh + dxl ...)
+__device__ void hm_pair_mixed(const Dev& d, const SysParams& sp, const float (&dh)[3], const float (&dl)[3],
+                              float r1h, float r1l, float r2h, float r2l, const double4& v_i, const double4& v_j,
+                              const double4& w_i, const double4& w_j, int mi, int mj, uint32_t tag_i, uint32_t tag_j,
+                              const double* stored, PairMixed& o) {
+    const float kPi = 3.14159265358979f;
+    const float SQRT_5_3 = 0.9128709291752768f;
+    const float EPS = 1e-30f;
+    const bool hooke = sp.contact_model == 1;
+    const bool use_dmt = sp.adhesion_model == 1;
+    o.hit = o.tang = o.overlap = false;
+    // d^2 in double-float
+    float Sh = 0.f, Sl = 0.f;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        float p, e;
+        two_prod(dh[k], dh[k], p, e);
+        float t, te;
+        two_sum(Sh, p, t, te);
+        Sh = t;
+        Sl += te + e + 2.f * dh[k] * dl[k];
+    }
+    // r1 + r2 in double-float
+    float sh, se;
+    two_sum(r1h, r2h, sh, se);
+    const float sl = se + r1l + r2l;
+    const float sum_r = sh + sl;
+    const float surface_energy = hooke ? 0.f : mtf(d, sp, T_SURFACE, mi, mj);
+    const float r_eff = (r1h * r2h) / sum_r;
+    const float e_eff = mtf(d, sp, T_EEFF, mi, mj);
+    float pulloff = 0.f;
+    if (!hooke && surface_energy > 0.f && !use_dmt) {
+        const float g = surface_energy;
+        pulloff = cbrtf(kPi * kPi * g * g * r_eff / (4.f * e_eff * e_eff));
+    }
+    // (sum_r + pulloff)^2 - d^2 and (sum_r)^2 - d^2, double-float
+    float ih, il;
+    two_sum(sh, pulloff, ih, il);
+    il += sl;
+    float qh, qe;
+    two_prod(ih, ih, qh, qe);
+    float gap_h, gap_e;
+    two_sum(qh, -Sh, gap_h, gap_e);
+    const float range2 = gap_h + (gap_e + qe + 2.f * ih * il - Sl);
+    if (!(range2 > 0.f)) return;  // dist_sq >= interaction_r^2
+    const float dist_sq = Sh + Sl;
+    const float distance = sqrtf(dist_sq);
+    if (distance == 0.f) return;
+    float ph, pe;
+    two_prod(sh, sh, ph, pe);
+    float ch, ce;
+    two_sum(ph, -Sh, ch, ce);
+    const float diff = ch + (ce + pe + 2.f * sh * sl - Sl);  // (r1 + r2)^2 - d^2
+    const float r_min = fminf(r1h, r2h);
+    const float delta = fminf(diff / (sum_r + distance), 0.5f * r_min);
+    if (hooke && delta <= 0.f) return;
+    if (delta > 0.f && distance / sum_r < 0.90f) o.overlap = true;
+    if (!hooke && delta <= 0.f && surface_energy <= 0.f) return;
+    o.hit = true;
+    const float inv_dist = 1.f / distance;
+    const float nx = (dh[0] + dl[0]) * inv_dist, ny = (dh[1] + dl[1]) * inv_dist, nz = (dh[2] + dl[2]) * inv_dist;
+    const float g_eff = mtf(d, sp, T_GEFF, mi, mj);
+    const float inv_m_i = (float)v_i.w, inv_m_j = (float)v_j.w;
+    const float m_r = 1.f / (inv_m_i + inv_m_j);
+    const float beta = mtf(d, sp, T_BETA, mi, mj);
+    const float mu = mtf(d, sp, T_FRICTION, mi, mj);
+    const float mu_r = mtf(d, sp, T_ROLL_FRICTION, mi, mj);
+    const float mu_tw = mtf(d, sp, T_TWIST_FRICTION, mi, mj);
+    const float cohesion_energy = mtf(d, sp, T_COHESION, mi, mj);
+    const bool jkr_adhesion_only = !hooke && surface_energy > 0.f && !use_dmt && delta <= 0.f;
+    float s_n = 0.f, k_n = 0.f, k_t = 0.f, kn = 0.f, kt = 0.f, gamma_n = 0.f;
+    if (hooke) {
+        kn = mtf(d, sp, T_KN, mi, mj);
+        kt = mtf(d, sp, T_KT, mi, mj);
+        gamma_n = 2.f * beta * sqrtf(kn * m_r);
+    } else if (delta > 0.f) {
+        const float sdr = sqrtf(delta * r_eff);
+        s_n = 2.f * e_eff * sdr;
+        k_n = 4.f / 3.f * e_eff * sdr;
+        k_t = 8.f * g_eff * sdr;
+    }
+    const float r1 = r1h, r2 = r2h;
+    const float oix = (float)w_i.x, oiy = (float)w_i.y, oiz = (float)w_i.z;
+    const float ojx = (float)w_j.x, ojy = (float)w_j.y, ojz = (float)w_j.z;
+    const float r1nx = r1 * nx, r1ny = r1 * ny, r1nz = r1 * nz;
+    const float r2nx = r2 * nx, r2ny = r2 * ny, r2nz = r2 * nz;
+    // relative contact velocity: translational difference first (cancellation in fp64)
+    const float dvx = (float)(v_j.x - v_i.x), dvy = (float)(v_j.y - v_i.y), dvz = (float)(v_j.z - v_i.z);
+    const float vrx = dvx + (-ojy * r2nz + ojz * r2ny) - (oiy * r1nz - oiz * r1ny);
+    const float vry = dvy + (-ojz * r2nx + ojx * r2nz) - (oiz * r1nx - oix * r1nz);
+    const float vrz = dvz + (-ojx * r2ny + ojy * r2nx) - (oix * r1ny - oiy * r1nx);
+    const float v_n = vrx * nx + vry * ny + vrz * nz;
+    float f_n_mag;
+    if (hooke) {
+        if (cohesion_energy > 0.f) f_n_mag = kn * delta - gamma_n * v_n - cohesion_energy * kPi * delta * r_eff;
+        else f_n_mag = fmaxf(kn * delta - gamma_n * v_n, 0.f);
+    } else if (surface_energy > 0.f && use_dmt) {
+        f_n_mag = k_n * delta - 2.f * beta * SQRT_5_3 * sqrtf(s_n * m_r) * v_n - 2.f * kPi * surface_energy * r_eff;
+    } else if (surface_energy > 0.f) {
+        const float f_adh = 1.5f * kPi * surface_energy * r_eff;
+        if (jkr_adhesion_only) f_n_mag = -f_adh;
+        else f_n_mag = k_n * delta - 2.f * beta * SQRT_5_3 * sqrtf(s_n * m_r) * v_n - f_adh;
+    } else if (cohesion_energy > 0.f) {
+        f_n_mag = k_n * delta - 2.f * beta * SQRT_5_3 * sqrtf(s_n * m_r) * v_n - cohesion_energy * kPi * delta * r_eff;
+    } else {
+        f_n_mag = fmaxf(k_n * delta - 2.f * beta * SQRT_5_3 * sqrtf(s_n * m_r) * v_n, 0.f);
+    }
+    o.fn[0] = f_n_mag * nx;
+    o.fn[1] = f_n_mag * ny;
+    o.fn[2] = f_n_mag * nz;
+    if (jkr_adhesion_only) return;
+    o.tang = true;
+    const float vtx = vrx - v_n * nx, vty = vry - v_n * ny, vtz = vrz - v_n * nz;
+    const double sign = tag_i < tag_j ? 1.0 : -1.0;
+    const double dt = sp.dt;
+    const double ndx = nx, ndy = ny, ndz = nz;
+    // spring integration in fp64
+    double sx = sign * stored[0], sy = sign * stored[1], sz = sign * stored[2];
+    const double sdn = sx * ndx + sy * ndy + sz * ndz;
+    sx -= sdn * ndx;
+    sy -= sdn * ndy;
+    sz -= sdn * ndz;
+    sx += (double)vtx * dt;
+    sy += (double)vty * dt;
+    sz += (double)vtz * dt;
+    const float ktt = hooke ? kt : k_t;
+    const float s_mag = sqrtf((float)(sx * sx + sy * sy + sz * sz));
+    const float fts = ktt * s_mag;
+    const float ft_max = mu * fabsf(f_n_mag);
+    if (fts > ft_max && fts > EPS) {
+        const double sc = (double)(ft_max / fts);
+        sx *= sc;
+        sy *= sc;
+        sz *= sc;
+    }
+    const float gamma_t = 2.f * SQRT_5_3 * beta * sqrtf(ktt * m_r);
+    float ftx = ktt * (float)sx - gamma_t * vtx;
+    float fty = ktt * (float)sy - gamma_t * vty;
+    float ftz = ktt * (float)sz - gamma_t * vtz;
+    const float ftm = sqrtf(ftx * ftx + fty * fty + ftz * ftz);
+    if (ftm > ft_max && ftm > EPS) {
+        const float sc = ft_max / ftm;
+        ftx *= sc;
+        fty *= sc;
+        ftz *= sc;
+    }
+    o.ft[0] = ftx; o.ft[1] = fty; o.ft[2] = ftz;
+    o.ti[0] = r1ny * ftz - r1nz * fty; o.ti[1] = r1nz * ftx - r1nx * ftz; o.ti[2] = r1nx * fty - r1ny * ftx;
+    o.tj[0] = r2ny * ftz - r2nz * fty; o.tj[1] = r2nz * ftx - r2nx * ftz; o.tj[2] = r2nx * fty - r2ny * ftx;
+    // relative spin from the fp64 angular velocities
+    const float orx = (float)(w_i.x - w_j.x), ory = (float)(w_i.y - w_j.y), orz = (float)(w_i.z - w_j.z);
+    const float odn = orx * nx + ory * ny + orz * nz;
+    const float rollx = orx - odn * nx, rolly = ory - odn * ny, rollz = orz - odn * nz;
+    double rdx = sign * stored[3], rdy = sign * stored[4], rdz = sign * stored[5];
+    double twd = sign * stored[6];
+    o.tr[0] = o.tr[1] = o.tr[2] = 0.f;
+    o.tw[0] = o.tw[1] = o.tw[2] = 0.f;
+    if (mu_r > 0.f) {
+        const float roll_mag = sqrtf(rollx * rollx + rolly * rolly + rollz * rollz);
+        if (sp.rolling_model == 1) {
+            const float k_roll = mtf(d, sp, T_KROLL, mi, mj);
+            const float g_roll = mtf(d, sp, T_GROLL, mi, mj);
+            const double rdn = rdx * ndx + rdy * ndy + rdz * ndz;
+            rdx -= rdn * ndx; rdy -= rdn * ndy; rdz -= rdn * ndz;
+            rdx += (double)rollx * dt; rdy += (double)rolly * dt; rdz += (double)rollz * dt;
+            float tx = -k_roll * (float)rdx - g_roll * rollx;
+            float ty = -k_roll * (float)rdy - g_roll * rolly;
+            float tz = -k_roll * (float)rdz - g_roll * rollz;
+            const float trm = sqrtf(tx * tx + ty * ty + tz * tz);
+            const float tau_max = mu_r * fabsf(f_n_mag) * r_eff;
+            if (trm > tau_max && trm > EPS) {
+                const float sc = tau_max / trm;
+                tx *= sc; ty *= sc; tz *= sc;
+                if (k_roll > EPS) {
+                    rdx = (double)((tx + g_roll * rollx) / (-k_roll));
+                    rdy = (double)((ty + g_roll * rolly) / (-k_roll));
+                    rdz = (double)((tz + g_roll * rollz) / (-k_roll));
+                }
+            }
+            o.tr[0] = tx; o.tr[1] = ty; o.tr[2] = tz;
+        } else if (roll_mag > 1e-30f) {
+            const float inv_roll = mu_r * fabsf(f_n_mag) * r_eff / roll_mag;
+            o.tr[0] = -inv_roll * rollx; o.tr[1] = -inv_roll * rolly; o.tr[2] = -inv_roll * rollz;
+        }
+    }
+    if (mu_tw > 0.f) {
+        const float twist_vel = odn;
+        if (sp.twisting_model == 1) {
+            const float k_tw = mtf(d, sp, T_KTWIST, mi, mj);
+            const float g_tw = mtf(d, sp, T_GTWIST, mi, mj);
+            twd += (double)twist_vel * dt;
+            float tau_tw = -k_tw * (float)twd - g_tw * twist_vel;
+            const float tau_max = mu_tw * fabsf(f_n_mag) * r_eff;
+            if (fabsf(tau_tw) > tau_max) {
+                tau_tw = copysignf(1.f, tau_tw) * tau_max;
+                if (k_tw > EPS) twd = (double)((tau_tw + g_tw * twist_vel) / (-k_tw));
+            }
+            o.tw[0] = tau_tw * nx; o.tw[1] = tau_tw * ny; o.tw[2] = tau_tw * nz;
+        } else if (fabsf(twist_vel) > 1e-30f) {
+            const float tau = mu_tw * fabsf(f_n_mag) * r_eff;
+            const float sg = twist_vel > 0.f ? -1.f : 1.f;
+            o.tw[0] = sg * tau * nx; o.tw[1] = sg * tau * ny; o.tw[2] = sg * tau * nz;
+        }
+    }
+    o.spring[0] = sign * sx; o.spring[1] = sign * sy; o.spring[2] = sign * sz;
+    o.spring[3] = sign * rdx; o.spring[4] = sign * rdy; o.spring[5] = sign * rdz;
+    o.spring[6] = sign * twd;
+}
+
+__device__ __forceinline__ bool hist_find_m(const Dev& d, const SysParams& sp, int hc, long long p, int lp, uint32_t t,
+                                            double* out) {
+    const int n = d.hcnt[hc][p];
+    for (int c = 0; c < n; c++) {
+        if (d.htag[hc][sp.h0 + (long long)c * sp.npad + lp] == t) {
+            for (int q = 0; q < 7; q++) out[q] = d.hval[hc][sp.h0 * 7 + (long long)(c * 7 + q) * sp.npad + lp];
+            return true;
+        }
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(BLK) k_dem_mixed(Dev d, int hcur) {
+    const int s = d.blk_sys[blockIdx.x];
+    const SysParams& sp = d.sp[s];
+    if (sp.kind != 0) return;
+    SysState* st = d.ss + s;
+    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    if (li >= sp.n) return;
+    const long long i = (long long)sp.p0 + li;
+    const int hn = hcur ^ 1;
+    const float4 hi = d.pos2[2 * i], lo = d.pos2[2 * i + 1];
+    const double4 vi = d.vel[i];
+    const double4 wi = d.omg[i];
+    const int ti_ = (int)d.type[i];
+    const uint32_t tag_i = d.tag[i];
+    const int nn = d.nnum[i];
+    const long long base = sp.lst0 + li;
+    Kahan3 F, T;
+    int nh = 0, nover = 0;
+    PairMixed o;
+    for (int k = 0; k < nn; k++) {
+        const uint32_t e = d.nlist[base + (long long)k * sp.npad];
+        const int lj = (int)(e & IDX_MASK);
+        const long long j = sp.p0 + lj;
+        const uint32_t code = e >> IDX_BITS;
+        const bool own = code >= 27u;
+        const int sc = (int)(own ? code - 27u : code);
+        const int sx = sc / 9 - 1, sy = (sc / 3) % 3 - 1, sz = sc % 3 - 1;
+        const float4 hj = d.pos2[2 * j], lj4 = d.pos2[2 * j + 1];
+        const double4 vj = d.vel[j];
+        const double4 wj = d.omg[j];
+        const int tj_ = (int)d.type[j];
+        const uint32_t tag_j = d.tag[j];
+        double stored[7] = {0, 0, 0, 0, 0, 0, 0};
+        float dh[3], dl[3];
+        if (own) {
+            hist_find_m(d, sp, hcur, i, li, tag_j, stored);
+            sep_df(hj.x, lj4.x, hi.x, lo.x, sx, sp.Lh[0], sp.Ll[0], dh[0], dl[0]);
+            sep_df(hj.y, lj4.y, hi.y, lo.y, sy, sp.Lh[1], sp.Ll[1], dh[1], dl[1]);
+            sep_df(hj.z, lj4.z, hi.z, lo.z, sz, sp.Lh[2], sp.Ll[2], dh[2], dl[2]);
+            hm_pair_mixed(d, sp, dh, dl, hi.w, lo.w, hj.w, lj4.w, vi, vj, wi, wj, ti_, tj_, tag_i, tag_j, stored, o);
+            if (!o.hit) continue;
+            F.add(-o.fn[0], -o.fn[1], -o.fn[2]);
+            if (o.overlap) nover++;
+            if (!o.tang) continue;
+            F.add(o.ft[0], o.ft[1], o.ft[2]);
+            T.add(o.ti[0] + o.tr[0] + o.tw[0], o.ti[1] + o.tr[1] + o.tw[1], o.ti[2] + o.tr[2] + o.tw[2]);
+            if (nh < sp.hcap) {
+                d.htag[hn][sp.h0 + (long long)nh * sp.npad + li] = tag_j;
+                for (int q = 0; q < 7; q++)
+                    d.hval[hn][sp.h0 * 7 + (long long)(nh * 7 + q) * sp.npad + li] = o.spring[q];
+            }
+            nh++;
+        } else {
+            // owner frame: owner j, partner i's image -s
+            hist_find_m(d, sp, hcur, j, lj, tag_i, stored);
+            sep_df(hi.x, lo.x, hj.x, lj4.x, -sx, sp.Lh[0], sp.Ll[0], dh[0], dl[0]);
+            sep_df(hi.y, lo.y, hj.y, lj4.y, -sy, sp.Lh[1], sp.Ll[1], dh[1], dl[1]);
+            sep_df(hi.z, lo.z, hj.z, lj4.z, -sz, sp.Lh[2], sp.Ll[2], dh[2], dl[2]);
+            hm_pair_mixed(d, sp, dh, dl, hj.w, lj4.w, hi.w, lo.w, vj, vi, wj, wi, tj_, ti_, tag_j, tag_i, stored, o);
+            if (!o.hit) continue;
+            F.add(o.fn[0], o.fn[1], o.fn[2]);
+            if (!o.tang) continue;
+            F.add(-o.ft[0], -o.ft[1], -o.ft[2]);
+            T.add(o.tj[0] - o.tr[0] - o.tw[0], o.tj[1] - o.tr[1] - o.tw[1], o.tj[2] - o.tr[2] - o.tw[2]);
+        }
+    }
+    if (nh > sp.hcap) {
+        atomicOr(&st->status, ST_HIST_OVF);
+        nh = sp.hcap;
+    }
+    d.hcnt[hn][i] = nh;
+    if (nover) atomicAdd(&st->overlap, nover);
+    d.frc[i] = make_double4(F.x.value(), F.y.value(), F.z.value(), 0.0);
+    d.trq[i] = make_double4(T.x.value(), T.y.value(), T.z.value(), 0.0);
+}
+
 int launch_force_mixed(const Dev& d, int hcur, int has_lj, int has_dem, int tpp, cudaStream_t st) {
-    (void)hcur;
-    (void)has_dem;
     int n = 0;
+    if (has_dem) {
+        k_dem_mixed<<<d.nblocks, BLK, 0, st>>>(d, hcur);
+        n++;
+    }
     if (has_lj) {
         switch (tpp) {
             case 2: k_lj_mixed<2><<<d.nblocks * 2, BLK, 0, st>>>(d); break;

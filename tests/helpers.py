@@ -55,3 +55,26 @@ def overlapping_spheres(n, box, radius, seed, sep_factor=0.96, speed=0.5, omega=
     st = inputs._dem_state(pos, vel, r, 2500.0)
     st["omega"] = rng.normal(scale=omega, size=(n, 3))
     return st
+
+
+def dem_pair_force_scale(st_by_tag, box, pairs, e_eff):
+    """Per-tag sum of Hertz elastic normal-force magnitudes 4/3 E* sqrt(R*) d^1.5
+    over the particle's contacts: the per-pair force scale of the DEM
+    force-error metric.  ``st_by_tag``: dict with pos and radius indexed by tag."""
+    pos, rad = st_by_tag["pos"], st_by_tag["radius"]
+    n = pos.shape[0]
+    p = np.asarray(pairs, dtype=np.int64)
+    scale = np.zeros(n)
+    if len(p) == 0:
+        return scale
+    d = pos[p[:, 1]] - pos[p[:, 0]]
+    L = np.asarray(box)
+    d -= L * np.round(d / L)
+    dist = np.sqrt(np.einsum("ij,ij->i", d, d))
+    r1, r2 = rad[p[:, 0]], rad[p[:, 1]]
+    delta = np.clip(r1 + r2 - dist, 0.0, None)
+    reff = r1 * r2 / (r1 + r2)
+    f = 4.0 / 3.0 * e_eff * np.sqrt(reff) * delta ** 1.5
+    np.add.at(scale, p[:, 0], f)
+    np.add.at(scale, p[:, 1], f)
+    return scale

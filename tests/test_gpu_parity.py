@@ -216,3 +216,53 @@ def test_batch_equals_single(gpu_lib):
             (x,) = by_tag(g, f)
             (y,) = by_tag(alone[k], f)
             assert np.array_equal(x, y), (k, f)
+
+
+def test_mixed_dem_force_error(gpu_lib):
+    """Precision form, DEM: fp32 geometry/force with double-float overlap and
+    fp64 springs vs the fp64 path; per-particle force and torque error <= 1e-5
+    relative to max(|F|, sum of pair forces)."""
+    from helpers import dem_pair_force_scale
+
+    st = _dem_state(seed=8)
+    c64 = _dem_cfg()
+    cmx = _dem_cfg(precision="mixed")
+    o = _oracle(c64, st)
+    o.force_only()
+    keys, vals = o.history()
+    rng = np.random.default_rng(9)
+    vals = rng.normal(scale=1e-6, size=vals.shape)
+    a, b = _ctx(c64, st), _ctx(cmx, st)
+    a.set_history(keys, vals)
+    b.set_history(keys, vals)
+    a.force_only()
+    b.force_only()
+    ga, gb = a.download(), b.download()
+    fa, ta, pa, ra = by_tag(ga, "force", "torque", "pos", "radius")
+    fb, tb = by_tag(gb, "force", "torque")
+    E, nu = 8.7e9, 0.3
+    e_eff = 1.0 / (2 * (1 - nu * nu) / E)
+    scale = dem_pair_force_scale({"pos": pa, "radius": ra}, c64.box, a.pairs(), e_eff)
+    assert np.max(scale) > 0
+    assert rel_err(fb, fa, scale) <= 1e-5
+    assert rel_err(tb, ta, scale * ra) <= 1e-5
+    ka, va = a.history()
+    kb, vb = b.history()
+    assert pair_set(ka) == pair_set(kb)
+    db = {tuple(k): v for k, v in zip(kb.tolist(), vb)}
+    vmax = float(np.max(np.abs(va)))
+    for k, v in zip(ka.tolist(), va):
+        assert np.max(np.abs(db[tuple(k)] - v)) <= 1e-5 * vmax
+
+
+def test_mixed_dem_trajectory_close_to_fp64(gpu_lib):
+    st = _dem_state(seed=10)
+    a = _ctx(_dem_cfg(), st)
+    b = _ctx(_dem_cfg(precision="mixed"), st)
+    a.step(100)
+    b.step(100)
+    (pa,) = by_tag(a.download(), "pos")
+    (pb,) = by_tag(b.download(), "pos")
+    assert np.max(np.abs(pa - pb)) <= 1e-9 * 0.012
+    ta, tb = a.thermo(), b.thermo()
+    assert abs(ta["ke"] - tb["ke"]) <= 1e-5 * ta["ke"]
