@@ -169,6 +169,11 @@ int  mdg_device_count(int* count);
 int  mdg_create(const mdg_config* cfg, size_t capacity, mdg_ctx** out);
 int  mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, mdg_ctx** out);
 void mdg_destroy(mdg_ctx* ctx);
+/* Replace the physics of system `sys` (a slot) with `cfg`: contact laws,
+ * materials, LJ coefficients, timestep, [neighbor] settings.  The kind and
+ * precision must match the slot; memory stays allocated; other systems are
+ * untouched.  The slot is frozen until the next mdg_upload_state. */
+int  mdg_configure_system(mdg_ctx* ctx, int sys, const mdg_config* cfg);
 int  mdg_num_systems(const mdg_ctx* ctx);
 
 /* State transfer for system `sys` (0 for single-system contexts).
@@ -182,9 +187,18 @@ int  mdg_download_state(mdg_ctx* ctx, int sys, mdg_state_view* st);
 int  mdg_set_history(mdg_ctx* ctx, int sys, size_t n, const uint32_t* keys, const double* vals);
 int  mdg_get_history(mdg_ctx* ctx, int sys, uint32_t* keys, double* vals, size_t cap, size_t* n);
 
-/* Advance every system of the context by nsteps timesteps.  Returns the
- * first non-zero system status, if any. */
+/* Advance every active system of the context by nsteps timesteps (graph
+ * mode: one launch of a device-side loop).  Returns the first non-zero system
+ * status, if any. */
 int  mdg_step(mdg_ctx* ctx, int64_t nsteps);
+/* Step budget of one system: it advances `steps` more timesteps and then
+ * freezes (its kernels skip it) until given a new budget; -1 = unlimited (the
+ * default after upload).  Used by batching and serving to stop finished jobs
+ * inside one multi-step launch. */
+int  mdg_set_remaining(mdg_ctx* ctx, int sys, int64_t steps);
+int  mdg_get_remaining(mdg_ctx* ctx, int sys, int64_t* steps);
+/* Sticky device status word of one system (0 = healthy). */
+int  mdg_get_status(mdg_ctx* ctx, int sys, int32_t* status);
 /* Neighbor rebuild + force evaluation at the current state (no integration). */
 int  mdg_force_only(mdg_ctx* ctx);
 /* Half-list pairs at the last build as (owner tag, partner tag). */
@@ -225,6 +239,33 @@ int  mdg_timed_steps(mdg_ctx* ctx, int64_t nsteps, size_t l2_flush_bytes, mdg_st
  * All calls share the array: calls that overlap on the GPU race.  Work is
  * queued on `stream` (NULL = default stream); the call does not synchronise. */
 int  mdg_granular_temp_noalloc(const double* vel, const double* mass, size_t n, double* out3, void* stream);
+
+/* ---- Serving: continuous batching of independent jobs --------------------
+ * A server owns one batch context whose systems are slots (kind and particle
+ * capacity from slot_cfgs / slot_capacity).  Submitted jobs (config + initial
+ * state + step count) queue on the host; mdg_server_pump admits queued jobs
+ * into free slots of their kind while the resident jobs' estimated device
+ * footprint stays within hbm_budget bytes, advances all resident jobs with one
+ * multi-step device launch of at most max_steps steps (each job freezes at its
+ * own step count), and retires finished jobs (final state kept on the host
+ * until fetched).  Times are seconds since server creation. */
+typedef struct mdg_server mdg_server;
+typedef struct mdg_job_info {
+    int64_t id;
+    int32_t status;          /* MDG_OK or the job's error */
+    int32_t slot;
+    int64_t steps;
+    int64_t n;
+    double submit_s, start_s, end_s;
+} mdg_job_info;
+int  mdg_server_create(const mdg_config* slot_cfgs, const size_t* slot_capacity, int nslots, size_t hbm_budget,
+                       mdg_server** out);
+void mdg_server_destroy(mdg_server* srv);
+int  mdg_server_submit(mdg_server* srv, const mdg_config* cfg, const mdg_state_view* st, int64_t steps, int64_t* id);
+int  mdg_server_pump(mdg_server* srv, int64_t max_steps, int* active, int* pending);
+int  mdg_server_poll(mdg_server* srv, mdg_job_info* out, int cap, int* n);
+int  mdg_server_fetch(mdg_server* srv, int64_t id, mdg_state_view* out);
+int  mdg_server_context(mdg_server* srv, mdg_ctx** ctx);
 
 #ifdef __cplusplus
 }

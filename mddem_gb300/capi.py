@@ -29,7 +29,9 @@ EXPORTS = [
     "mdg_abi_version", "mdg_status_string", "mdg_device_count", "mdg_create", "mdg_batch_create", "mdg_destroy",
     "mdg_num_systems", "mdg_upload_state", "mdg_download_state", "mdg_set_history", "mdg_get_history",
     "mdg_step", "mdg_force_only", "mdg_get_pairs", "mdg_thermo", "mdg_synchronize", "mdg_kernel_launches",
-    "mdg_set_graph_mode", "mdg_timed_steps", "mdg_granular_temp_noalloc",
+    "mdg_set_graph_mode", "mdg_timed_steps", "mdg_granular_temp_noalloc", "mdg_set_remaining",
+    "mdg_get_remaining", "mdg_get_status", "mdg_configure_system", "mdg_server_create", "mdg_server_destroy",
+    "mdg_server_submit", "mdg_server_pump", "mdg_server_poll", "mdg_server_fetch", "mdg_server_context",
 ]
 
 
@@ -84,6 +86,11 @@ class Thermo(C.Structure):
     ]
 
 
+class JobInfo(C.Structure):
+    _fields_ = [("id", C.c_int64), ("status", C.c_int32), ("slot", C.c_int32), ("steps", C.c_int64),
+                ("n", C.c_int64), ("submit_s", C.c_double), ("start_s", C.c_double), ("end_s", C.c_double)]
+
+
 class StepTiming(C.Structure):
     _fields_ = [("step_ms", C.c_double), ("phase_ms", C.c_double * 4), ("kernels", C.c_int32),
                 ("rebuilt", C.c_int32)]
@@ -124,6 +131,20 @@ def load(path: str = LIB_PATH):
     lib.mdg_kernel_launches.restype = C.c_int64
     lib.mdg_set_graph_mode.argtypes = [C.c_void_p, C.c_int]
     lib.mdg_timed_steps.argtypes = [C.c_void_p, C.c_int64, C.c_size_t, C.POINTER(StepTiming)]
+    lib.mdg_set_remaining.argtypes = [C.c_void_p, C.c_int, C.c_int64]
+    lib.mdg_get_remaining.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int64)]
+    lib.mdg_get_status.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int32)]
+    lib.mdg_configure_system.argtypes = [C.c_void_p, C.c_int, C.POINTER(Config)]
+    lib.mdg_server_create.argtypes = [C.POINTER(Config), C.POINTER(C.c_size_t), C.c_int, C.c_size_t,
+                                      C.POINTER(C.c_void_p)]
+    lib.mdg_server_destroy.argtypes = [C.c_void_p]
+    lib.mdg_server_destroy.restype = None
+    lib.mdg_server_submit.argtypes = [C.c_void_p, C.POINTER(Config), C.POINTER(StateView), C.c_int64,
+                                      C.POINTER(C.c_int64)]
+    lib.mdg_server_pump.argtypes = [C.c_void_p, C.c_int64, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    lib.mdg_server_poll.argtypes = [C.c_void_p, C.POINTER(JobInfo), C.c_int, C.POINTER(C.c_int)]
+    lib.mdg_server_fetch.argtypes = [C.c_void_p, C.c_int64, C.POINTER(StateView)]
+    lib.mdg_server_context.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
     lib.mdg_granular_temp_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]
     _lib = lib
     return lib
@@ -173,6 +194,108 @@ def to_c_config(c: SimConfig):
     cc.neighbor_capacity = int(c.neighbor_capacity)
     cc.history_capacity = int(c.history_capacity)
     return cc, mats
+
+
+def _upload_view(state):
+    """StateView over a state dict (keeps the arrays alive in the returned dict)."""
+    n = len(state["tag"])
+    keep = {k: np.ascontiguousarray(v) for k, v in state.items() if isinstance(v, np.ndarray)}
+    keep["tag"] = keep["tag"].astype(np.uint32, copy=False)
+    if "type" in keep:
+        keep["type"] = keep["type"].astype(np.uint32, copy=False)
+    v = StateView()
+    v.n = n
+    v.tag = _ptr(keep["tag"], C.c_uint32)
+    v.type = _ptr(keep.get("type"), C.c_uint32)
+    for f in ("pos", "vel", "mass", "cutoff_radius", "radius", "inv_inertia", "omega", "quat", "force", "torque"):
+        if f in keep:
+            setattr(v, f, _ptr(keep[f], C.c_double))
+    if "image" in keep:
+        keep["image"] = keep["image"].astype(np.int32)
+        v.image = _ptr(keep["image"], C.c_int32)
+    return v, keep
+
+
+def _download_buffers(n, dem):
+    out = {
+        "tag": np.zeros(n, np.uint32), "type": np.zeros(n, np.uint32), "pos": np.zeros((n, 3)),
+        "vel": np.zeros((n, 3)), "force": np.zeros((n, 3)), "mass": np.zeros(n),
+        "cutoff_radius": np.zeros(n), "image": np.zeros((n, 3), np.int32),
+    }
+    if dem:
+        out.update(radius=np.zeros(n), inv_inertia=np.zeros(n), omega=np.zeros((n, 3)),
+                   torque=np.zeros((n, 3)), quat=np.zeros((n, 4)))
+    v = StateView()
+    v.n = n
+    v.tag = _ptr(out["tag"], C.c_uint32)
+    v.type = _ptr(out["type"], C.c_uint32)
+    v.image = _ptr(out["image"], C.c_int32)
+    for f in ("pos", "vel", "force", "mass", "cutoff_radius", "radius", "inv_inertia", "omega", "torque", "quat"):
+        if f in out:
+            setattr(v, f, _ptr(out[f], C.c_double))
+    return v, out
+
+
+class Server:
+    """Continuous-batching server (mdg_server_*): typed slots, HBM-budget
+    admission, one multi-step device launch per pump, retirement of finished
+    jobs."""
+
+    def __init__(self, slot_configs, slot_capacities, hbm_budget):
+        self.lib = load()
+        n = len(slot_configs)
+        arr = (Config * n)()
+        self._keep = []
+        for k, c in enumerate(slot_configs):
+            cc, mats = to_c_config(c)
+            arr[k] = cc
+            self._keep.append(mats)
+        caps = (C.c_size_t * n)(*[int(x) for x in slot_capacities])
+        h = C.c_void_p()
+        _check(self.lib.mdg_server_create(arr, caps, n, int(hbm_budget), C.byref(h)), "mdg_server_create")
+        self.h = h
+        self.meta = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.mdg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, cfg, state, steps):
+        cc, mats = to_c_config(cfg)
+        v, keep = _upload_view(state)
+        jid = C.c_int64()
+        _check(self.lib.mdg_server_submit(self.h, C.byref(cc), C.byref(v), int(steps), C.byref(jid)),
+               "mdg_server_submit")
+        self.meta[jid.value] = (cfg.kind == "dem", len(state["tag"]))
+        return jid.value
+
+    def pump(self, max_steps):
+        a, p = C.c_int(), C.c_int()
+        _check(self.lib.mdg_server_pump(self.h, int(max_steps), C.byref(a), C.byref(p)), "mdg_server_pump")
+        return a.value, p.value
+
+    def poll(self):
+        buf = (JobInfo * 256)()
+        out = []
+        while True:
+            n = C.c_int()
+            _check(self.lib.mdg_server_poll(self.h, buf, 256, C.byref(n)), "mdg_server_poll")
+            out += [{f: getattr(buf[k], f) for f, _ in JobInfo._fields_} for k in range(n.value)]
+            if n.value < 256:
+                return out
+
+    def fetch(self, jid):
+        dem, n = self.meta.pop(jid)
+        v, out = _download_buffers(n, dem)
+        _check(self.lib.mdg_server_fetch(self.h, int(jid), C.byref(v)), "mdg_server_fetch")
+        return out
 
 
 class Context:
@@ -304,6 +427,25 @@ class Context:
         _check(self.lib.mdg_timed_steps(self.h, int(nsteps), int(l2_flush_bytes), buf), "mdg_timed_steps")
         t = np.array([[b.step_ms, *b.phase_ms] for b in buf[:nsteps]])
         return t, np.array([b.kernels for b in buf[:nsteps]]), np.array([b.rebuilt for b in buf[:nsteps]])
+
+    def configure(self, cfg, sys=0):
+        cc, mats = to_c_config(cfg)
+        self._keep.append(mats)
+        _check(self.lib.mdg_configure_system(self.h, sys, C.byref(cc)), "mdg_configure_system")
+        self.configs[sys] = cfg
+
+    def status(self, sys=0):
+        v = C.c_int32()
+        _check(self.lib.mdg_get_status(self.h, sys, C.byref(v)), "mdg_get_status")
+        return v.value
+
+    def set_remaining(self, steps, sys=0):
+        _check(self.lib.mdg_set_remaining(self.h, sys, int(steps)), "mdg_set_remaining")
+
+    def remaining(self, sys=0):
+        v = C.c_int64()
+        _check(self.lib.mdg_get_remaining(self.h, sys, C.byref(v)), "mdg_get_remaining")
+        return v.value
 
     def set_graph_mode(self, on):
         _check(self.lib.mdg_set_graph_mode(self.h, int(on)), "mdg_set_graph_mode")

@@ -120,7 +120,6 @@ struct mdg_ctx {
     std::vector<int> uploaded;
     std::vector<int> ncap_sys;  // current list capacity per system
     Dev d{};
-    int hcur = 0;
     bool has_lj = false, has_dem = false, has_mixed = false, any_virial = false;
     int tpp_lj = 1;
     long long cells_alloc = 0, lst_alloc = 0;
@@ -129,24 +128,23 @@ struct mdg_ctx {
     int* d_cblk0 = nullptr;
     SysParams* d_sp = nullptr;
     double* d_mat = nullptr;
+    float* d_matf = nullptr;
     double* d_thermo = nullptr;
     std::vector<long long> mat_off;
     int graph_mode = 1;
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    cudaGraphExec_t tgraph[2] = {nullptr, nullptr};  // timed single-step graphs
+    cudaGraphExec_t wgraph = nullptr;                 // multi-step WHILE graph
+    cudaGraphExec_t tgraph = nullptr;                 // timed single-step graph
+    long long* d_loop = nullptr;                      // steps left in the WHILE graph
     cudaEvent_t tev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     int tkernels = 0;
     void* flush_buf = nullptr;
     size_t flush_bytes = 0;
-    int graph_steps = 0;
     long long launches = 0;
     std::vector<void*> allocs;
 
     ~mdg_ctx() {
-        for (int k = 0; k < 2; k++) {
-            if (graph[k]) cudaGraphExecDestroy(graph[k]);
-            if (tgraph[k]) cudaGraphExecDestroy(tgraph[k]);
-        }
+        if (wgraph) cudaGraphExecDestroy(wgraph);
+        if (tgraph) cudaGraphExecDestroy(tgraph);
         for (auto& e : tev)
             if (e) cudaEventDestroy(e);
         if (flush_buf) cudaFree(flush_buf);
@@ -167,20 +165,61 @@ struct mdg_ctx {
         cudaFree(p);
     }
     void drop_graphs() {
-        for (int k = 0; k < 2; k++) {
-            if (graph[k]) {
-                cudaGraphExecDestroy(graph[k]);
-                graph[k] = nullptr;
-            }
-            if (tgraph[k]) {
-                cudaGraphExecDestroy(tgraph[k]);
-                tgraph[k] = nullptr;
-            }
+        if (wgraph) {
+            cudaGraphExecDestroy(wgraph);
+            wgraph = nullptr;
+        }
+        if (tgraph) {
+            cudaGraphExecDestroy(tgraph);
+            tgraph = nullptr;
         }
     }
 };
 
 namespace {
+
+// The per-system physics a config sets: contact laws, materials (pair tables
+// into `tabs`), LJ coefficients, timestep and [neighbor] rebuild settings.
+// The slot's memory layout is left alone.
+void apply_physics(mdg_ctx* c, int s, const mdg_config& k, std::vector<double>& tabs) {
+    SysParams& p = c->sp[s];
+    c->cfg[s] = k;
+    p.contact_model = k.contact_model;
+    p.adhesion_model = k.adhesion_model;
+    p.rolling_model = k.rolling_model;
+    p.twisting_model = k.twisting_model;
+    p.dt = k.dt;
+    p.policy = k.rebuild_policy;
+    p.every = k.every;
+    p.check = k.check;
+    p.sort_every = k.sort_every;
+    p.newton = k.newton;
+    p.virial = k.virial;
+    p.tpp = k.threads_per_particle ? k.threads_per_particle : 1;
+    tabs.clear();
+    if (k.kind == MDG_KIND_DEM) {
+        c->mats[s].assign(k.materials, k.materials + k.n_materials);
+        c->cfg[s].materials = c->mats[s].data();
+        material_tables(k.materials, k.n_materials, tabs);
+        p.nmat = k.n_materials;
+    } else {
+        // LJPairCoeffs::from_params (crates/md_lj/src/lib.rs:230-239)
+        const double s2 = k.lj_sigma * k.lj_sigma;
+        const double sigma6 = s2 * s2 * s2;
+        p.lj1 = 48.0 * k.lj_epsilon * sigma6 * sigma6;
+        p.lj2 = 24.0 * k.lj_epsilon * sigma6;
+        p.lj3 = 4.0 * k.lj_epsilon * sigma6 * sigma6;
+        p.lj4 = 4.0 * k.lj_epsilon * sigma6;
+        const double rc = k.lj_cutoff * k.lj_sigma;
+        p.lj_cut2 = rc * rc;
+        p.lj1f = (float)p.lj1;
+        p.lj2f = (float)p.lj2;
+        p.lj3f = (float)p.lj3;
+        p.lj4f = (float)p.lj4;
+        p.lj_cut2f = (float)p.lj_cut2;
+        p.nmat = 1;
+    }
+}
 
 int cuda_err(cudaError_t e) {
     if (e == cudaSuccess) return MDG_OK;
@@ -352,17 +391,23 @@ int ensure_layout(mdg_ctx* c, int fresh = -1) {
     cudaMemcpy(c->d_cblk0, cblk0.data(), cblk0.size() * sizeof(int), cudaMemcpyHostToDevice);
     c->d.cblk_sys = c->d_cblk_sys;
     c->d.cblk0 = c->d_cblk0;
+    // captured graphs carry the cell-block count in their grid sizes
+    if (c->d.ncblocks != (int)(cells / BLK)) c->drop_graphs();
     c->d.ncblocks = (int)(cells / BLK);
     cudaMemcpy(c->d_sp, c->sp.data(), c->nsys * sizeof(SysParams), cudaMemcpyHostToDevice);
     return cuda_err(cudaGetLastError());
 }
 
-int enqueue_step(mdg_ctx* c, int hcur, cudaStream_t st) {
+int launch_force(mdg_ctx* c, const Dev& d, cudaStream_t st) {
+    if (c->has_mixed) return launch_force_mixed(d, c->has_lj, c->has_dem, c->tpp_lj, st);
+    return launch_force_fp64(d, c->has_lj, c->has_dem, c->tpp_lj, st);
+}
+
+int enqueue_step(mdg_ctx* c, cudaStream_t st) {
     int n = 0;
     n += launch_initial(c->d, st);
-    n += launch_rebuild(c->d, hcur, st);
-    if (c->has_mixed) n += launch_force_mixed(c->d, hcur, c->has_lj, c->has_dem, c->tpp_lj, st);
-    else n += launch_force_fp64(c->d, hcur, c->has_lj, c->has_dem, c->tpp_lj, st);
+    n += launch_rebuild(c->d, st);
+    n += launch_force(c, c->d, st);
     n += launch_final(c->d, st, 1);
     return n;
 }
@@ -371,7 +416,7 @@ int enqueue_step(mdg_ctx* c, int hcur, cudaStream_t st) {
 // pipeline sits in the body of an IF conditional node whose condition
 // k_initial sets on the device.  ev (optional) = 5 events bracketing the
 // phases.  Returns kernels in the step (rebuild kernels counted when run).
-int capture_step(mdg_ctx* c, int h, cudaEvent_t* ev, int* nk) {
+int capture_step(mdg_ctx* c, cudaEvent_t* ev, int* nk) {
     cudaStreamCaptureStatus cs;
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, nullptr, nullptr, nullptr);
@@ -403,13 +448,12 @@ int capture_step(mdg_ctx* c, int h, cudaEvent_t* ev, int* nk) {
     if (e != cudaSuccess) return cuda_err(e);
     e = cudaStreamBeginCaptureToGraph(c->stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_err(e);
-    n += launch_rebuild(d, h, c->stream2);
+    n += launch_rebuild(d, c->stream2);
     cudaGraph_t body_out = nullptr;
     e = cudaStreamEndCapture(c->stream2, &body_out);
     if (e != cudaSuccess) return cuda_err(e);
     if (ev) cudaEventRecordWithFlags(ev[2], c->stream, cudaEventRecordExternal);
-    if (c->has_mixed) n += launch_force_mixed(d, h, c->has_lj, c->has_dem, c->tpp_lj, c->stream);
-    else n += launch_force_fp64(d, h, c->has_lj, c->has_dem, c->tpp_lj, c->stream);
+    n += launch_force(c, d, c->stream);
     if (ev) cudaEventRecordWithFlags(ev[3], c->stream, cudaEventRecordExternal);
     n += launch_final(d, c->stream, 1);
     if (ev) cudaEventRecordWithFlags(ev[4], c->stream, cudaEventRecordExternal);
@@ -417,46 +461,85 @@ int capture_step(mdg_ctx* c, int h, cudaEvent_t* ev, int* nk) {
     return MDG_OK;
 }
 
-int build_graph(mdg_ctx* c, int hstart) {
+// Multi-step graph: a WHILE conditional node whose body is one step (with the
+// rebuild IF node inside) followed by the loop-control kernel, which counts
+// down d_loop and closes the loop when it reaches zero or no system is active.
+// One launch runs any number of steps without returning to the host.
+int build_while_graph(mdg_ctx* c) {
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_err(e);
-    int h = hstart;
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
     int r = MDG_OK;
-    for (int k = 0; k < c->graph_steps && !r; k++) {
-        r = capture_step(c, h, nullptr, nullptr);
-        h ^= 1;
+    cudaGraphConditionalHandle wh;
+    cudaGraphNode_t node;
+    cudaGraphNodeParams np{};
+    e = cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &cg, nullptr, nullptr, nullptr);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&wh, cg, 1, cudaGraphCondAssignDefault);
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if (e == cudaSuccess) e = cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &cg, &deps, nullptr, &nd);
+    if (e == cudaSuccess) {
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = wh;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        e = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np);
     }
-    e = cudaStreamEndCapture(c->stream, &g);
-    if (r) {
+    if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    cudaGraph_t g_end = nullptr;
+    e = e == cudaSuccess ? cudaStreamEndCapture(c->stream, &g) : (cudaStreamEndCapture(c->stream, &g_end), e);
+    if (e != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
-        return r;
+        if (g_end) cudaGraphDestroy(g_end);
+        return cuda_err(e);
     }
-    if (e != cudaSuccess) return cuda_err(e);
-    e = cudaGraphInstantiate(&c->graph[hstart], g, 0);
+    // body: capture on c->stream into the WHILE body graph
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        r = capture_step(c, nullptr, nullptr);
+        if (!r) launch_loop_ctl(c->d, c->d_loop, (unsigned long long)wh, c->stream);
+        cudaGraph_t bo = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(c->stream, &bo);
+        if (!r && e2 != cudaSuccess) r = cuda_err(e2);
+    } else {
+        r = cuda_err(e);
+    }
+    if (!r) {
+        e = cudaGraphInstantiate(&c->wgraph, g, 0);
+        if (e != cudaSuccess) r = cuda_err(e);
+    }
     cudaGraphDestroy(g);
-    return cuda_err(e);
+    return r;
 }
 
 // One step captured with event records between its phases.
-int build_timed_graph(mdg_ctx* c, int h) {
+int build_timed_graph(mdg_ctx* c) {
     for (auto& e : c->tev)
         if (!e && cudaEventCreate(&e) != cudaSuccess) return MDG_ERR_CUDA;
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_err(e);
     int n = 0;
-    int r = capture_step(c, h, c->tev, &n);
+    int r = capture_step(c, c->tev, &n);
     e = cudaStreamEndCapture(c->stream, &g);
     if (r) {
         if (g) cudaGraphDestroy(g);
         return r;
     }
     if (e != cudaSuccess) return cuda_err(e);
-    e = cudaGraphInstantiate(&c->tgraph[h], g, 0);
+    e = cudaGraphInstantiate(&c->tgraph, g, 0);
     cudaGraphDestroy(g);
     c->tkernels = n;
     return cuda_err(e);
+}
+
+int sys_hcur(mdg_ctx* c, int sys) {
+    SysState ss;
+    cudaMemcpy(&ss, c->d.ss + sys, sizeof(SysState), cudaMemcpyDeviceToHost);
+    return ss.hcur & 1;
 }
 
 int check_status(mdg_ctx* c) {
@@ -550,10 +633,7 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
             delete c;
             return MDG_ERR_CONFIG;  // one precision per context
         }
-        p.contact_model = k.contact_model;
-        p.adhesion_model = k.adhesion_model;
-        p.rolling_model = k.rolling_model;
-        p.twisting_model = k.twisting_model;
+        // memory layout of the slot (fixed for the context's lifetime)
         p.npad = (int)round_up((long long)capacity[s], BLK);
         p.p0 = (int)P;
         p.n = 0;
@@ -562,44 +642,18 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
         for (int b = 0; b < p.nb; b++) blk_sys.push_back(s);
         nblocks += p.nb;
         P += p.npad;
-        p.dt = k.dt;
-        p.policy = k.rebuild_policy;
-        p.every = k.every;
-        p.check = k.check;
-        p.sort_every = k.sort_every;
-        p.newton = k.newton;
-        p.virial = k.virial;
-        p.tpp = k.threads_per_particle ? k.threads_per_particle : 1;
         p.ncap = 0;
         if (k.kind == MDG_KIND_DEM) {
             c->has_dem = true;
-            c->mats[s].assign(k.materials, k.materials + k.n_materials);
-            c->cfg[s].materials = c->mats[s].data();
-            std::vector<double> tabs;
-            material_tables(k.materials, k.n_materials, tabs);
-            p.nmat = k.n_materials;
+            p.matcap = std::max(k.n_materials, 4);
             p.mat0 = (long long)mat_all.size();
-            mat_all.insert(mat_all.end(), tabs.begin(), tabs.end());
+            mat_all.resize(mat_all.size() + (size_t)NTAB * p.matcap * p.matcap, 0.0);
             p.hcap = k.history_capacity ? k.history_capacity : 24;
             p.h0 = hist_entries;
             hist_entries += (long long)p.hcap * p.npad;
         } else {
             c->has_lj = true;
-            // LJPairCoeffs::from_params (crates/md_lj/src/lib.rs:230-239)
-            const double s2 = k.lj_sigma * k.lj_sigma;
-            const double sigma6 = s2 * s2 * s2;
-            p.lj1 = 48.0 * k.lj_epsilon * sigma6 * sigma6;
-            p.lj2 = 24.0 * k.lj_epsilon * sigma6;
-            p.lj3 = 4.0 * k.lj_epsilon * sigma6 * sigma6;
-            p.lj4 = 4.0 * k.lj_epsilon * sigma6;
-            const double rc = k.lj_cutoff * k.lj_sigma;
-            p.lj_cut2 = rc * rc;
-            p.lj1f = (float)p.lj1;
-            p.lj2f = (float)p.lj2;
-            p.lj3f = (float)p.lj3;
-            p.lj4f = (float)p.lj4;
-            p.lj_cut2f = (float)p.lj_cut2;
-            p.nmat = 1;
+            p.matcap = 0;
             p.mat0 = 0;
             p.hcap = 0;
         }
@@ -608,6 +662,10 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
         // mixed path (the measured best on GB300 for ~78-entry rows) and 1 for fp64
         if (k.threads_per_particle > 0) c->tpp_lj = k.threads_per_particle;
         else if (k.kind == MDG_KIND_LJ && k.precision == MDG_MIXED) c->tpp_lj = 4;
+        // the physics of the slot (replaceable by mdg_configure_system)
+        std::vector<double> tabs;
+        apply_physics(c, s, k, tabs);
+        if (!tabs.empty()) std::copy(tabs.begin(), tabs.end(), mat_all.begin() + p.mat0);
     }
     if (P > (long long)IDX_MASK * 8) {
         delete c;
@@ -663,9 +721,11 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     c->d_sp = c->alloc<SysParams>(nsys, err);
     d.ss = c->alloc<SysState>(nsys, err);
     c->d_mat = c->alloc<double>(std::max<size_t>(mat_all.size(), 1), err);
-    float* d_matf = c->alloc<float>(std::max<size_t>(mat_all.size(), 1), err);
+    c->d_matf = c->alloc<float>(std::max<size_t>(mat_all.size(), 1), err);
     c->d_thermo = c->alloc<double>((size_t)nsys * 16, err);
     d.grid_ctr = c->alloc<unsigned int>(1, err);
+    d.stat_ctr = c->alloc<unsigned long long>(4, err);
+    c->d_loop = c->alloc<long long>(1, err);
     if (err) {
         delete c;
         return err;
@@ -674,9 +734,9 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     if (!mat_all.empty()) {
         cudaMemcpy(c->d_mat, mat_all.data(), mat_all.size() * sizeof(double), cudaMemcpyHostToDevice);
         std::vector<float> mf(mat_all.begin(), mat_all.end());
-        cudaMemcpy(d_matf, mf.data(), mf.size() * sizeof(float), cudaMemcpyHostToDevice);
+        cudaMemcpy(c->d_matf, mf.data(), mf.size() * sizeof(float), cudaMemcpyHostToDevice);
     }
-    d.matf = d_matf;
+    d.matf = c->d_matf;
     d.blk_sys = c->d_blk_sys;
     d.sp = c->d_sp;
     d.mat = c->d_mat;
@@ -696,9 +756,33 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
         delete c;
         return cuda_err(e);
     }
-    c->graph_steps = 2;
     *out = c;
     return MDG_OK;
+}
+
+int mdg_configure_system(mdg_ctx* c, int sys, const mdg_config* cfg) {
+    if (!c || !cfg || sys < 0 || sys >= c->nsys) return MDG_ERR_ARG;
+    int r = validate_config(*cfg);
+    if (r) return r;
+    SysParams& p = c->sp[sys];
+    if (cfg->kind != p.kind || cfg->precision != p.precision) return MDG_ERR_CONFIG;
+    if (cfg->kind == MDG_KIND_DEM && cfg->n_materials > p.matcap) return MDG_ERR_CONFIG;
+    if (cfg->virial && !c->d.vir) return MDG_ERR_CONFIG;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(e);
+    std::vector<double> tabs;
+    apply_physics(c, sys, *cfg, tabs);
+    if (!tabs.empty()) {
+        std::vector<float> tf(tabs.begin(), tabs.end());
+        cudaMemcpy(c->d_mat + p.mat0, tabs.data(), tabs.size() * sizeof(double), cudaMemcpyHostToDevice);
+        cudaMemcpy(c->d_matf + p.mat0, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice);
+    }
+    // freeze the slot until its next upload
+    long long zero = 0;
+    cudaMemcpy(&c->d.ss[sys].remaining, &zero, sizeof(zero), cudaMemcpyHostToDevice);
+    c->uploaded[sys] = 0;
+    e = cudaMemcpy(c->d_sp + sys, &p, sizeof(SysParams), cudaMemcpyHostToDevice);
+    return cuda_err(e);
 }
 
 int mdg_create(const mdg_config* cfg, size_t capacity, mdg_ctx** out) {
@@ -796,6 +880,7 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
     }
     SysState ss{};
     ss.rebuild = 1;  // the first step performs a full rebuild (CommState::FullRebuild)
+    ss.remaining = -1;
     cudaMemcpyAsync(d.ss + sys, &ss, sizeof(SysState), cudaMemcpyHostToDevice, s0);
     cudaError_t e = cudaStreamSynchronize(s0);
     if (e != cudaSuccess) return cuda_err(e);
@@ -891,7 +976,7 @@ int mdg_set_history(mdg_ctx* c, int sys, size_t nent, const uint32_t* keys, cons
         for (int q = 0; q < 7; q++) hv[(size_t)(cc * 7 + q) * np + i] = vals[7 * k + q];
         cnt[i] = cc + 1;
     }
-    const int h = c->hcur;
+    const int h = sys_hcur(c, sys);
     cudaMemcpy(d.hcnt[h] + o, cnt.data(), np * sizeof(int), cudaMemcpyHostToDevice);
     cudaMemcpy(d.htag[h] + p.h0, ht.data(), ht.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
     cudaMemcpy(d.hval[h] + p.h0 * 7, hv.data(), hv.size() * sizeof(double), cudaMemcpyHostToDevice);
@@ -912,7 +997,7 @@ int mdg_get_history(mdg_ctx* c, int sys, uint32_t* keys, double* vals, size_t ca
     std::vector<int> cnt(n);
     std::vector<uint32_t> ht((size_t)p.hcap * np);
     std::vector<double> hv((size_t)p.hcap * 7 * np);
-    const int h = c->hcur;
+    const int h = sys_hcur(c, sys);
     cudaMemcpy(tag.data(), d.tag + o, n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
     cudaMemcpy(cnt.data(), d.hcnt[h] + o, n * sizeof(int), cudaMemcpyDeviceToHost);
     cudaMemcpy(ht.data(), d.htag[h] + p.h0, ht.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost);
@@ -931,55 +1016,93 @@ int mdg_get_history(mdg_ctx* c, int sys, uint32_t* keys, double* vals, size_t ca
     return cuda_err(cudaGetLastError());
 }
 
+// Systems never uploaded (or reconfigured and not yet uploaded) hold a step
+// budget of zero -- set at creation and by mdg_configure_system, and
+// mdg_set_remaining refuses to lift it -- so every kernel skips them and a
+// batch may run with free slots.
+static bool any_uploaded(const mdg_ctx* c) {
+    for (int s = 0; s < c->nsys; s++)
+        if (c->uploaded[s]) return true;
+    return false;
+}
+
 int mdg_step(mdg_ctx* c, int64_t nsteps) {
     if (!c || nsteps < 0) return MDG_ERR_ARG;
-    for (int s = 0; s < c->nsys; s++)
-        if (!c->uploaded[s]) return MDG_ERR_STATE;
-    int64_t left = nsteps;
-    if (c->graph_mode && c->graph_steps > 0) {
-        while (left >= c->graph_steps) {
-            const int h = c->hcur;
-            if (!c->graph[h]) {
-                int r = build_graph(c, h);
-                if (r) return r;
-            }
-            cudaError_t e = cudaGraphLaunch(c->graph[h], c->stream);
-            if (e != cudaSuccess) return cuda_err(e);
-            c->launches += (long long)c->graph_steps * (3 + (c->has_lj && c->has_dem ? 1 : 0));
-            if (c->graph_steps % 2) c->hcur ^= 1;
-            left -= c->graph_steps;
+    if (!any_uploaded(c)) return MDG_ERR_STATE;
+    if (nsteps == 0) return MDG_OK;
+    unsigned long long rb0 = 0, rb1 = 0;
+    cudaMemcpy(&rb0, c->d.stat_ctr, sizeof(rb0), cudaMemcpyDeviceToHost);
+    if (c->graph_mode) {
+        // one launch: the WHILE graph counts the steps down on the device
+        if (!c->wgraph) {
+            int r = build_while_graph(c);
+            if (r) return r;
         }
-    }
-    for (int64_t k = 0; k < left; k++) {
-        c->launches += enqueue_step(c, c->hcur, c->stream);
-        c->hcur ^= 1;
+        long long n = nsteps;
+        cudaMemcpyAsync(c->d_loop, &n, sizeof(n), cudaMemcpyHostToDevice, c->stream);
+        cudaError_t e = cudaGraphLaunch(c->wgraph, c->stream);
+        if (e != cudaSuccess) return cuda_err(e);
+    } else {
+        for (int64_t k = 0; k < nsteps; k++) enqueue_step(c, c->stream);
     }
     cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(e);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(e);
+    cudaMemcpy(&rb1, c->d.stat_ctr, sizeof(rb1), cudaMemcpyDeviceToHost);
+    // kernels that ran: per step initial + force + final (+ loop control),
+    // plus the seven rebuild kernels on the steps whose rebuild branch opened
+    const long long base = 3 + (c->has_lj && c->has_dem ? 1 : 0) + (c->graph_mode ? 1 : 0);
+    c->launches += nsteps * base + 7LL * (long long)(c->graph_mode ? (rb1 - rb0) : nsteps);
+    return check_status(c);
+}
+
+int mdg_force_only(mdg_ctx* c) {
+    if (!c) return MDG_ERR_ARG;
+    if (!any_uploaded(c)) return MDG_ERR_STATE;
+    std::vector<SysState> ss(c->nsys);
+    cudaMemcpy(ss.data(), c->d.ss, c->nsys * sizeof(SysState), cudaMemcpyDeviceToHost);
+    for (auto& x : ss) x.rebuild = 1;
+    cudaMemcpy(c->d.ss, ss.data(), c->nsys * sizeof(SysState), cudaMemcpyHostToDevice);
+    cudaStream_t st = c->stream;
+    c->launches += launch_rebuild(c->d, st);
+    c->launches += launch_force(c, c->d, st);
+    c->launches += launch_final(c->d, st, 0);  // reductions + bookkeeping, no integration
+    cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_err(e);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(e);
     return check_status(c);
 }
 
-int mdg_force_only(mdg_ctx* c) {
-    if (!c) return MDG_ERR_ARG;
-    for (int s = 0; s < c->nsys; s++)
-        if (!c->uploaded[s]) return MDG_ERR_STATE;
-    std::vector<SysState> ss(c->nsys);
-    cudaMemcpy(ss.data(), c->d.ss, c->nsys * sizeof(SysState), cudaMemcpyDeviceToHost);
-    for (auto& x : ss) x.rebuild = 1;
-    cudaMemcpy(c->d.ss, ss.data(), c->nsys * sizeof(SysState), cudaMemcpyHostToDevice);
-    cudaStream_t st = c->stream;
-    c->launches += launch_rebuild(c->d, c->hcur, st);
-    if (c->has_mixed) c->launches += launch_force_mixed(c->d, c->hcur, c->has_lj, c->has_dem, c->tpp_lj, st);
-    else c->launches += launch_force_fp64(c->d, c->hcur, c->has_lj, c->has_dem, c->tpp_lj, st);
-    c->launches += launch_final(c->d, st, 0);  // reductions + bookkeeping, no integration
-    cudaError_t e = cudaStreamSynchronize(st);
+int mdg_get_status(mdg_ctx* c, int sys, int32_t* status) {
+    if (!c || sys < 0 || sys >= c->nsys || !status) return MDG_ERR_ARG;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_err(e);
-    c->hcur ^= 1;
-    e = cudaGetLastError();
+    int v = 0;
+    e = cudaMemcpy(&v, &c->d.ss[sys].status, sizeof(int), cudaMemcpyDeviceToHost);
+    *status = v;
+    return cuda_err(e);
+}
+
+int mdg_set_remaining(mdg_ctx* c, int sys, int64_t steps) {
+    if (!c || sys < 0 || sys >= c->nsys || steps < -1) return MDG_ERR_ARG;
+    if (steps != 0 && !c->uploaded[sys]) return MDG_ERR_STATE;  // nothing to run
+    cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_err(e);
-    return check_status(c);
+    long long v = steps;
+    e = cudaMemcpy(&c->d.ss[sys].remaining, &v, sizeof(v), cudaMemcpyHostToDevice);
+    return cuda_err(e);
+}
+
+int mdg_get_remaining(mdg_ctx* c, int sys, int64_t* steps) {
+    if (!c || sys < 0 || sys >= c->nsys || !steps) return MDG_ERR_ARG;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(e);
+    long long v = 0;
+    e = cudaMemcpy(&v, &c->d.ss[sys].remaining, sizeof(v), cudaMemcpyDeviceToHost);
+    *steps = v;
+    return cuda_err(e);
 }
 
 int mdg_get_pairs(mdg_ctx* c, int sys, uint32_t* pairs, size_t cap, size_t* nout) {
@@ -1045,8 +1168,7 @@ int64_t mdg_kernel_launches(const mdg_ctx* c) { return c ? c->launches : 0; }
 
 int mdg_timed_steps(mdg_ctx* c, int64_t nsteps, size_t l2_flush_bytes, mdg_step_timing* out) {
     if (!c || nsteps < 0 || (nsteps && !out)) return MDG_ERR_ARG;
-    for (int s = 0; s < c->nsys; s++)
-        if (!c->uploaded[s]) return MDG_ERR_STATE;
+    if (!any_uploaded(c)) return MDG_ERR_STATE;
     if (l2_flush_bytes > c->flush_bytes) {
         if (c->flush_buf) cudaFree(c->flush_buf);
         c->flush_buf = nullptr;
@@ -1061,15 +1183,14 @@ int mdg_timed_steps(mdg_ctx* c, int64_t nsteps, size_t l2_flush_bytes, mdg_step_
     for (auto& ev : c->tev)
         if (!ev && cudaEventCreate(&ev) != cudaSuccess) return MDG_ERR_CUDA;
     for (int64_t k = 0; k < nsteps; k++) {
-        const int h = c->hcur;
-        if (c->graph_mode && !c->tgraph[h]) {
-            int r = build_timed_graph(c, h);
+        if (c->graph_mode && !c->tgraph) {
+            int r = build_timed_graph(c);
             if (r) return r;
         }
         if (l2_flush_bytes) cudaMemsetAsync(c->flush_buf, (int)(k & 0xff), l2_flush_bytes, c->stream);
         cudaError_t e = cudaSuccess;
         if (c->graph_mode) {
-            e = cudaGraphLaunch(c->tgraph[h], c->stream);
+            e = cudaGraphLaunch(c->tgraph, c->stream);
         } else {
             // eager launches (profilers see every kernel); rebuild kernels always run
             cudaStream_t st = c->stream;
@@ -1077,10 +1198,9 @@ int mdg_timed_steps(mdg_ctx* c, int64_t nsteps, size_t l2_flush_bytes, mdg_step_
             cudaEventRecord(c->tev[0], st);
             n += launch_initial(c->d, st);
             cudaEventRecord(c->tev[1], st);
-            n += launch_rebuild(c->d, h, st);
+            n += launch_rebuild(c->d, st);
             cudaEventRecord(c->tev[2], st);
-            if (c->has_mixed) n += launch_force_mixed(c->d, h, c->has_lj, c->has_dem, c->tpp_lj, st);
-            else n += launch_force_fp64(c->d, h, c->has_lj, c->has_dem, c->tpp_lj, st);
+            n += launch_force(c, c->d, st);
             cudaEventRecord(c->tev[3], st);
             n += launch_final(c->d, st, 1);
             cudaEventRecord(c->tev[4], st);
@@ -1101,7 +1221,6 @@ int mdg_timed_steps(mdg_ctx* c, int64_t nsteps, size_t l2_flush_bytes, mdg_step_
         // the 7 rebuild-pipeline kernels run only when the conditional opened
         out[k].kernels = c->tkernels - ((rb || !c->graph_mode) ? 0 : 7);
         c->launches += out[k].kernels;
-        c->hcur ^= 1;
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(e);

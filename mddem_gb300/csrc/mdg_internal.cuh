@@ -66,6 +66,7 @@ struct SysParams {
     double dt;
     int policy, every, check, sort_every, newton;
     int nmat;
+    int matcap;          // material slots reserved in the packed tables
     long long mat0;      // offset into the packed material tables
     double lj1, lj2, lj3, lj4, lj_cut2;
     float lj1f, lj2f, lj3f, lj4f, lj_cut2f;
@@ -98,7 +99,14 @@ struct SysState {
     double vir[6];
     double pe;
     long long step;
+    long long remaining; // steps left before the system freezes; -1 = unlimited
+    int hcur;            // contact-history buffer holding the current springs
+    int pad_;
 };
+
+__device__ __forceinline__ bool sys_active(const SysState* st) {
+    return *((volatile const long long*)&st->remaining) != 0;
+}
 
 struct Dev {
     // per particle
@@ -161,6 +169,7 @@ struct Dev {
     unsigned long long cond;
     int use_cond;
     unsigned int* grid_ctr;
+    unsigned long long* stat_ctr;  // [0] steps whose rebuild branch opened
 };
 
 // Two-float separation (x_j + s L) - x_i from positions stored relative to
@@ -197,9 +206,11 @@ __device__ __forceinline__ void two_float_add(float& hi, float& lo, float t) {
 // ---- kernel launchers (mdg_kernels_fp64.cu / mdg_kernels_mixed.cu) ----------
 // Each returns the number of kernels it launched on `st`.
 int launch_initial(const Dev& d, cudaStream_t st);
-int launch_rebuild(const Dev& d, int hcur, cudaStream_t st);
-int launch_force_fp64(const Dev& d, int hcur, int has_lj, int has_dem, int tpp, cudaStream_t st);
-int launch_force_mixed(const Dev& d, int hcur, int has_lj, int has_dem, int tpp, cudaStream_t st);
+int launch_rebuild(const Dev& d, cudaStream_t st);
+int launch_force_fp64(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st);
+int launch_force_mixed(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st);
+// device-side loop control of a multi-step WHILE graph
+int launch_loop_ctl(const Dev& d, long long* counter, unsigned long long handle, cudaStream_t st);
 int launch_final(const Dev& d, cudaStream_t st, int integrate);
 int launch_ke_init(const Dev& d, cudaStream_t st);
 // thermo reduction for all systems into out[nsys][16] (device pointer)

@@ -106,13 +106,14 @@ __global__ void __launch_bounds__(BLK) k_initial(Dev d) {
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
     const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
-    const bool act = li < sp.n;
+    const bool live = sys_active(st);
+    const bool act = live && li < sp.n;
     const long long i = (long long)sp.p0 + li;
     const double dt = sp.dt;
     // exp(-dt/2 p_xi / Q) after the pre-initial half step of p_xi, computed
     // once per system by the previous step's reduction (k_final / k_ke_init)
     const double scale = sp.nh ? st->nh_scale : 1.0;
-    if (li == 0)
+    if (li == 0 && live)
         st->periodic_sort =
             (sp.policy == 0 && sp.sort_every > 0 && st->sort_counter + 1 >= sp.sort_every) ? 1 : 0;
     const int already = vload(&st->rebuild);
@@ -218,8 +219,10 @@ __global__ void __launch_bounds__(BLK) k_initial(Dev d) {
         if (last && threadIdx.x == 0) {
             __threadfence();
             unsigned int any = 0;
-            for (int q = 0; q < d.nsys; q++) any |= (unsigned)(vload(&d.ss[q].rebuild) | vload(&d.ss[q].periodic_sort));
+            for (int q = 0; q < d.nsys; q++)
+                if (sys_active(d.ss + q)) any |= (unsigned)(vload(&d.ss[q].rebuild) | vload(&d.ss[q].periodic_sort));
             *d.grid_ctr = 0;
+            if (any) d.stat_ctr[0] += 1;
             cudaGraphSetConditional((cudaGraphConditionalHandle)d.cond, any ? 1u : 0u);
         }
     }
@@ -229,10 +232,10 @@ __global__ void __launch_bounds__(BLK) k_initial(Dev d) {
 // rebuild pipeline
 // ----------------------------------------------------------------------------
 __device__ __forceinline__ bool do_sort(const SysState* st) {
-    return vload(&st->rebuild) || vload(&st->periodic_sort);
+    return sys_active(st) && (vload(&st->rebuild) || vload(&st->periodic_sort));
 }
 __device__ __forceinline__ bool do_rebuild(const SysState* st) {
-    return vload(&st->rebuild) || (vload(&st->periodic_sort) && vload(&st->nonid));
+    return sys_active(st) && (vload(&st->rebuild) || (vload(&st->periodic_sort) && vload(&st->nonid)));
 }
 
 // pbc (domain.rs:413-459, rebuild steps only) + bin key (neighbor.rs:721-738)
@@ -350,10 +353,11 @@ __global__ void __launch_bounds__(BLK) k_cellsort(Dev d) {
 // Atom::apply_permutation + AtomDataRegistry::apply_permutation_all +
 // ContactHistoryStore::apply_permutation (atom.rs:383-394, 197-202,
 // tangential.rs:92-96): gather every per-atom array into scratch.
-__global__ void __launch_bounds__(BLK) k_gather(Dev d, int hcur) {
+__global__ void __launch_bounds__(BLK) k_gather(Dev d) {
     const int s = d.blk_sys[blockIdx.x];
     const SysParams& sp = d.sp[s];
     if (!do_rebuild(d.ss + s)) return;
+    const int hcur = d.ss[s].hcur;
     const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
     if (li >= sp.n) return;
     const long long k = (long long)sp.p0 + li;
@@ -382,10 +386,11 @@ __global__ void __launch_bounds__(BLK) k_gather(Dev d, int hcur) {
     }
 }
 
-__global__ void __launch_bounds__(BLK) k_copyback(Dev d, int hcur) {
+__global__ void __launch_bounds__(BLK) k_copyback(Dev d) {
     const int s = d.blk_sys[blockIdx.x];
     const SysParams& sp = d.sp[s];
     if (!do_rebuild(d.ss + s)) return;
+    const int hcur = d.ss[s].hcur;
     const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
     if (li >= sp.n) return;
     const long long k = (long long)sp.p0 + li;
@@ -756,7 +761,7 @@ __global__ void __launch_bounds__(BLK) k_lj_fp64(Dev d) {
     const int sub = blockIdx.x % TPP;
     const int s = d.blk_sys[pb];
     const SysParams& sp = d.sp[s];
-    if (sp.kind != 1) return;
+    if (sp.kind != 1 || !sys_active(d.ss + s)) return;
     const int lane = threadIdx.x % TPP;
     const int li = (pb - sp.b0) * BLK + sub * (BLK / TPP) + threadIdx.x / TPP;
     const bool act = li < sp.n;
@@ -1080,11 +1085,12 @@ __device__ __forceinline__ bool hist_find(const Dev& d, const SysParams& sp, int
     return false;
 }
 
-__global__ void __launch_bounds__(BLK) k_dem_fp64(Dev d, int hcur) {
+__global__ void __launch_bounds__(BLK) k_dem_fp64(Dev d) {
     const int s = d.blk_sys[blockIdx.x];
     const SysParams& sp = d.sp[s];
-    if (sp.kind != 0) return;
     SysState* st = d.ss + s;
+    if (sp.kind != 0 || !sys_active(st)) return;
+    const int hcur = st->hcur;
     const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
     if (li >= sp.n) return;
     const long long i = (long long)sp.p0 + li;
@@ -1173,6 +1179,7 @@ __global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
     const int s = d.blk_sys[blockIdx.x];
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
+    if (!sys_active(st)) return;  // every block of a frozen system returns
     const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
     const bool act = li < sp.n;
     const long long i = (long long)sp.p0 + li;
@@ -1245,9 +1252,11 @@ __global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
             st->steps_since_build = rb ? 0 : st->steps_since_build + 1;
             st->sort_counter = st->periodic_sort ? 0 : st->sort_counter + 1;
             st->step += 1;
+            if (st->remaining > 0) st->remaining -= 1;
         } else if (rb) {
             st->steps_since_build = 0;
         }
+        if (sp.kind == 0) st->hcur ^= 1;  // the force kernel wrote the other history buffer
         if (rb) st->nbuilds += 1;
         if (st->overlap > 500) st->status |= ST_OVERLAP;
         st->overlap = 0;
@@ -1371,18 +1380,18 @@ int launch_initial(const Dev& d, cudaStream_t st) {
     return 1;
 }
 
-int launch_rebuild(const Dev& d, int hcur, cudaStream_t st) {
+int launch_rebuild(const Dev& d, cudaStream_t st) {
     k_cells<<<d.nblocks, BLK, 0, st>>>(d);
     k_scan<<<d.nsys, 1024, 0, st>>>(d);
     k_scatter<<<d.nblocks, BLK, 0, st>>>(d);
     k_cellsort<<<d.ncblocks, BLK, 0, st>>>(d);
-    k_gather<<<d.nblocks, BLK, 0, st>>>(d, hcur);
-    k_copyback<<<d.nblocks, BLK, 0, st>>>(d, hcur);
+    k_gather<<<d.nblocks, BLK, 0, st>>>(d);
+    k_copyback<<<d.nblocks, BLK, 0, st>>>(d);
     k_build<<<d.ncblocks * (BLK / BUILD_WARPS), BUILD_WARPS * 32, 0, st>>>(d);
     return 7;
 }
 
-int launch_force_fp64(const Dev& d, int hcur, int has_lj, int has_dem, int tpp, cudaStream_t st) {
+int launch_force_fp64(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st) {
     int n = 0;
     if (has_lj) {
         switch (tpp) {
@@ -1394,10 +1403,26 @@ int launch_force_fp64(const Dev& d, int hcur, int has_lj, int has_dem, int tpp, 
         n++;
     }
     if (has_dem) {
-        k_dem_fp64<<<d.nblocks, BLK, 0, st>>>(d, hcur);
+        k_dem_fp64<<<d.nblocks, BLK, 0, st>>>(d);
         n++;
     }
     return n;
+}
+
+// WHILE-graph loop control: one step done; continue while steps remain and
+// some system is still active.
+__global__ void k_loop_ctl(Dev d, long long* counter, unsigned long long handle) {
+    if (threadIdx.x != 0) return;
+    const long long left = *counter - 1;
+    *counter = left;
+    unsigned int any = 0;
+    for (int q = 0; q < d.nsys && !any; q++) any = sys_active(d.ss + q) ? 1u : 0u;
+    cudaGraphSetConditional((cudaGraphConditionalHandle)handle, (left > 0 && any) ? 1u : 0u);
+}
+
+int launch_loop_ctl(const Dev& d, long long* counter, unsigned long long handle, cudaStream_t st) {
+    k_loop_ctl<<<1, 32, 0, st>>>(d, counter, handle);
+    return 1;
 }
 
 int launch_final(const Dev& d, cudaStream_t st, int integrate) {

@@ -31,7 +31,7 @@ __global__ void __launch_bounds__(BLK, 8) k_lj_mixed(Dev d) {
     const int sub = blockIdx.x % TPP;
     const int s = d.blk_sys[pb];
     const SysParams& sp = d.sp[s];
-    if (sp.kind != 1) return;
+    if (sp.kind != 1 || !sys_active(d.ss + s)) return;
     const int lane = threadIdx.x % TPP;
     const int li = (pb - sp.b0) * BLK + sub * (BLK / TPP) + threadIdx.x / TPP;
     const bool act = li < sp.n;
@@ -394,11 +394,12 @@ __device__ __forceinline__ bool hist_find_m(const Dev& d, const SysParams& sp, i
     return false;
 }
 
-__global__ void __launch_bounds__(BLK) k_dem_mixed(Dev d, int hcur) {
+__global__ void __launch_bounds__(BLK) k_dem_mixed(Dev d) {
     const int s = d.blk_sys[blockIdx.x];
     const SysParams& sp = d.sp[s];
-    if (sp.kind != 0) return;
     SysState* st = d.ss + s;
+    if (sp.kind != 0 || !sys_active(st)) return;
+    const int hcur = st->hcur;
     const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
     if (li >= sp.n) return;
     const long long i = (long long)sp.p0 + li;
@@ -470,10 +471,10 @@ __global__ void __launch_bounds__(BLK) k_dem_mixed(Dev d, int hcur) {
     d.trq[i] = make_double4(T.x.value(), T.y.value(), T.z.value(), 0.0);
 }
 
-int launch_force_mixed(const Dev& d, int hcur, int has_lj, int has_dem, int tpp, cudaStream_t st) {
+int launch_force_mixed(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st) {
     int n = 0;
     if (has_dem) {
-        k_dem_mixed<<<d.nblocks, BLK, 0, st>>>(d, hcur);
+        k_dem_mixed<<<d.nblocks, BLK, 0, st>>>(d);
         n++;
     }
     if (has_lj) {

@@ -1,0 +1,111 @@
+"""Batching and serving forms on the GPU.
+
+* per-system step budgets inside one multi-step launch: a system with a
+  budget of k steps ends exactly where a standalone k-step run ends;
+* serving: jobs of both kinds and different sizes are queued, admitted into
+  typed slots as slots and HBM budget free up, advanced together on the device,
+  retired, and every job's final state equals the same job run alone
+  (identical kernels and per-system arithmetic: bitwise);
+* slot reuse: a slot reconfigured for a new job carries nothing over.
+"""
+import numpy as np
+import pytest
+
+from helpers import by_tag
+
+pytestmark = pytest.mark.gpu
+
+
+def _alone(cfg, st, steps):
+    from mddem_gb300 import capi
+
+    with capi.Context(cfg, len(st["tag"])) as c:
+        c.upload(st)
+        c.step(steps)
+        return c.download()
+
+
+def _same(a, b, fields=("pos", "vel")):
+    for f in fields:
+        (x,) = by_tag(a, f)
+        (y,) = by_tag(b, f)
+        if not np.array_equal(x, y):
+            return False
+    return True
+
+
+def test_step_budgets_freeze_systems(gpu_lib):
+    from mddem_gb300 import capi, config, inputs
+
+    c1 = config.lj_fluid_config()
+    s1 = inputs.lj_fcc(6, 10.06, 0.85, 0.85, seed=21)
+    c2 = config.granular_gas_config(box=0.02, dt=2e-7)
+    s2 = inputs.dem_granular_gas(400, box=0.02, seed=22)
+    b = capi.Context([c1, c2], [864, 400])
+    b.upload(s1, 0)
+    b.upload(s2, 1)
+    b.set_remaining(13, 0)
+    b.set_remaining(37, 1)
+    b.step(50)
+    assert b.remaining(0) == 0 and b.remaining(1) == 0
+    assert b.thermo(0)["step"] == 13 and b.thermo(1)["step"] == 37
+    assert _same(b.download(0), _alone(c1, s1, 13))
+    assert _same(b.download(1), _alone(c2, s2, 37), ("pos", "vel", "omega"))
+
+
+def _jobs(precision):
+    from mddem_gb300 import config, inputs
+
+    jobs = []
+    for k, (n, steps) in enumerate([(300, 40), (900, 120), (1500, 80), (600, 60)]):
+        box = (n * 4.19e-9 / 0.15) ** (1 / 3)
+        cfg = config.granular_gas_config(box=box, dt=2e-7, precision=precision)
+        cfg.materials[0].restitution = 0.8 + 0.05 * k
+        jobs.append((cfg, inputs.dem_granular_gas(n, box=box, seed=30 + k), steps))
+    for k, (nc, box, steps) in enumerate([(6, 10.06, 70), (5, 8.4, 150)]):
+        cfg = config.lj_fluid_config(box=box, precision=precision)
+        jobs.append((cfg, inputs.lj_fcc(nc, box, 0.85, 0.85 + 0.1 * k, seed=40 + k), steps))
+    return jobs
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_server_results_equal_alone(gpu_lib, precision):
+    from mddem_gb300 import capi, config
+
+    jobs = _jobs(precision)
+    slots = [config.granular_gas_config(precision=precision)] * 2 + [config.lj_fluid_config(precision=precision)] * 2
+    caps = [2000, 2000, 1000, 1000]
+    # budget for about two resident DEM jobs: forces queueing and slot reuse
+    srv = capi.Server(slots, caps, hbm_budget=16 << 20)
+    ids = [srv.submit(c, s, n) for c, s, n in jobs[:3]]
+    srv.pump(25)
+    ids += [srv.submit(c, s, n) for c, s, n in jobs[3:]]
+    done = {}
+    for _ in range(1000):
+        active, pending = srv.pump(25)
+        for info in srv.poll():
+            done[info["id"]] = info
+        if active == 0 and pending == 0:
+            break
+    done.update({i["id"]: i for i in srv.poll()})
+    assert sorted(done) == sorted(ids)
+    for jid, (cfg, st, steps) in zip(ids, jobs):
+        info = done[jid]
+        assert info["status"] == 0 and info["steps"] == steps
+        assert info["submit_s"] <= info["start_s"] <= info["end_s"]
+        got = srv.fetch(jid)
+        ref = _alone(cfg, st, steps)
+        f = ("pos", "vel", "omega") if cfg.kind == "dem" else ("pos", "vel")
+        assert _same(got, ref, f), (jid, cfg.kind, len(st["tag"]))
+    srv.close()
+
+
+def test_server_rejects_jobs_without_a_slot(gpu_lib):
+    from mddem_gb300 import capi, config, inputs
+
+    srv = capi.Server([config.granular_gas_config()], [200], hbm_budget=1 << 30)
+    st = inputs.dem_granular_gas(500, seed=1)
+    with pytest.raises(capi.MdgError) as e:
+        srv.submit(config.granular_gas_config(), st, 10)
+    assert e.value.status == 4  # MDG_ERR_BUDGET
+    srv.close()
