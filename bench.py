@@ -1,18 +1,25 @@
-"""Throughput benchmark: particle-steps/s of the hot path on one GB300.
+"""Throughput benchmark of the particle hot path on one GB300.
 
-Default workload (N=1): LJ fluid, 256,000 atoms (40^3 FCC cells, box 67.06,
-rho* = 0.85, T* = 0.85), Nose-Hoover (T = 0.85, tau = 1), dt = 0.005, list
-cutoff 2.8 (rc 2.5 x skin 1.12), mixed-precision forces (FP32 geometry and
-arithmetic with Kahan sums, FP64 integration).  A "step" is one MD timestep
-of the whole system.  Each timed step is bracketed by CUDA events on the
-library's stream; L2 is flushed (512 MB write) before every step outside the
-events.
+Default workload (N=1): the served job stream -- Poisson-arriving jobs
+(50 % granular cooling gases of 100..200000 spheres, 25 % two-sphere Hertz
+rebounds, 25 % LJ FCC melts of 500..100000 atoms; 1000..50000 steps each)
+advanced by the continuous-batching server (mdg_server_*) in mixed precision.
+A "step" is one server pump: admission of the jobs that arrived, one
+multi-step device launch (200 timesteps) over every resident job, retirement
+of finished jobs.  value = particle-steps advanced inside the K timed pumps
+/ CUDA-event time on the server's stream over them.  Reported beside it:
+p50/p99 job latency (arrival to retirement) over the whole trace, and the
+same jobs run one by one on the plain FP64 path (particle-steps/s).
+
+Other workloads (--workload): lj256k, lj864, dem500, gas200k, poly1m (one
+system; a step is one timestep, L2 flushed before each), ens256 (256 gas
+replicas in one batch context; a step is one timestep of all).
 
 --impl reference times the CPU FP64 restatement of the reference's path (the
-oracle) on the same workload, one independent copy per host core.
+oracle) on the same workload with every host core.
 
-Multi-GPU (--gpus N under torchrun): replicas only; every rank advances its
-own copy of the workload; value = all ranks' particle-steps / max rank time.
+Multi-GPU (--gpus N under torchrun): replicas only; every rank runs its own
+copy of the workload; value = all ranks' particle-steps / max rank time.
 """
 from __future__ import annotations
 
@@ -44,6 +51,16 @@ def workload(name):
     if name == "dem500":
         cfg = config.granular_gas_config()
         return "DEM granular gas 500 glass spheres r=1mm box 0.025", cfg, lambda: inputs.dem_granular_gas(500, seed=0)
+    from mddem_gb300 import workloads as w
+
+    if name == "gas200k":
+        cfg = config.granular_gas_config(box=w.gas_box(200000, 0.15), dt=w.DT_GAS)
+        return ("DEM granular gas 200000 glass spheres r=1mm solid fraction 0.15", cfg,
+                lambda: w.gas(200000, phi=0.15, seed=2024)[1])
+    if name == "poly1m":
+        cfg = w.polydisperse_config()
+        return ("DEM polydisperse gas 1000000 glass spheres r~U[0.8,1.2]mm solid fraction 0.30 Maxwellian", cfg,
+                lambda: w.polydisperse_gas(seed=2024)[1])
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -82,10 +99,17 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
-    def summary(self):
+    def mark(self):
+        """Index of the next sample: bracket a window with two marks."""
+        return len(self.lines)
+
+    def summary(self, i0=0, i1=None):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines[i0:i1]
+        if i0 and len(lines) < 2:  # window shorter than the sampling period
+            lines = self.lines[max(0, i0 - 2):(i1 or len(self.lines)) + 2]
+        for ln in lines:
             p = [x.strip() for x in ln.split(",")]
             if len(p) < 7:
                 continue
@@ -176,10 +200,54 @@ def _ref_worker(args):
     return len(st["tag"]) * done, time.perf_counter() - t0, done
 
 
+def _ref_serve_worker(args):
+    idx, njobs, budget = args
+    import types
+
+    trace = serve_trace(types.SimpleNamespace(jobs=njobs))
+    work = secs = 0.0
+    for k in idx:
+        if secs > budget:
+            break
+        cfg, st = trace[k].make("fp64", "reference")
+        w_, s_ = _oracle_job(cfg, st, max(1, min(trace[k].steps, int(4e6 // trace[k].n))), budget - secs + 1.0)
+        work += w_
+        secs += s_
+    return work, secs
+
+
+def run_reference_serve(a):
+    import multiprocessing as mp
+
+    trace = serve_trace(a)
+    cores = os.cpu_count() or 1
+    order = sorted(range(len(trace)), key=lambda k: trace[k].arrival)
+    parts = [order[c::cores] for c in range(cores)]
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_ref_serve_worker, [(p, a.jobs, 45.0) for p in parts if p])
+    work = sum(r[0] for r in res)
+    wall = max(r[1] for r in res)
+    val = work / wall
+    sample = (f"the stream's jobs dealt round-robin to {len(res)} cores, each job up to 4e6 particle-steps "
+              "after 1 warm-up step, at most 45 s per core")
+    line = {
+        "impl": "reference", "metric": "particle-steps/s served", "value": val, "unit": "particle-steps/s",
+        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": serve_desc(trace), "precision": "fp64", "parallelism": f"{len(res)} host cores"},
+        "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": len(res), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(a):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    if a.workload == "serve":
+        return run_reference_serve(a)
     import multiprocessing as mp
 
     desc, cfg, make = workload(a.workload)
@@ -203,13 +271,294 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# served job stream
+# ---------------------------------------------------------------------------
+SERVE_PUMP = 200            # timesteps per pump (one bench step)
+SERVE_JOBS = 128
+SERVE_BACKLOG = 48          # jobs already queued when the stream starts
+SERVE_RATE = 2.0            # Poisson arrivals per pump tick after the backlog
+SERVE_HBM_BUDGET = 12 << 30  # admission budget of resident jobs' device bytes
+PLAIN_SAMPLE_STEPS = 200
+
+
+def serve_trace(a):
+    from mddem_gb300 import workloads as w
+
+    trace = w.serve_trace(njobs=a.jobs, rate=SERVE_RATE, seed=2024)
+    t0 = trace[SERVE_BACKLOG].arrival if len(trace) > SERVE_BACKLOG else 0.0
+    for k, j in enumerate(trace):  # the backlog arrives at tick 0, the rest keep their gaps
+        j.arrival = 0.0 if k < SERVE_BACKLOG else j.arrival - t0 + 1.0
+    return trace
+
+
+def serve_desc(trace):
+    kinds = {}
+    for j in trace:
+        kinds[j.kind] = kinds.get(j.kind, 0) + 1
+    return (f"served stream: {len(trace)} jobs ({kinds.get('gas', 0)} cooling gases N 100-200000, "
+            f"{kinds.get('rebound', 0)} two-sphere rebounds, {kinds.get('lj', 0)} LJ FCC melts N 500-100000), "
+            f"steps 1000-50000 log-uniform, {SERVE_BACKLOG} queued at start then Poisson {SERVE_RATE}/pump, "
+            f"{SERVE_PUMP} timesteps per pump")
+
+
+def state_bytes(st):
+    import numpy as np
+
+    return sum(v.nbytes for v in st.values() if isinstance(v, np.ndarray))
+
+
+def replay(a, srv, trace, made, clk):
+    """Submit each job at its arrival tick, pump until the stream drains.
+    Pumps [warmup, warmup + steps) are the timed window (CUDA events on the
+    server's stream); steps = 0: every pump from warmup until the drain.  Returns window and whole-run figures and job infos."""
+    import torch
+
+    order = sorted(range(len(trace)), key=lambda k: trace[k].arrival)
+    stream = torch.cuda.ExternalStream(srv.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    nxt, tick, infos, sid = 0, 0, {}, {}
+    h2d = d2h = 0
+    win = {}
+    t_all = time.perf_counter()
+    while True:
+        while nxt < len(order) and trace[order[nxt]].arrival <= tick:
+            k = order[nxt]
+            cfg, st = made[k]
+            sid[srv.submit(cfg, st, trace[k].steps)] = k
+            h2d += state_bytes(st)
+            nxt += 1
+        if tick == a.warmup:
+            win.update(s0=srv.stats(), l0=srv.launches(), c0=clk.mark(), w0=time.perf_counter())
+            e0.record(stream)
+        active, pending = srv.pump(SERVE_PUMP)
+        tick += 1
+        mid = a.warmup + (a.steps // 2 if a.steps else 10)
+        if tick >= mid and "mix" not in win:
+            win["mix"] = [sid[r["id"]] for r in srv.resident()]
+        drained = nxt == len(order) and active == 0 and pending == 0
+        if "s0" in win and "s1" not in win and ((a.steps and tick == a.warmup + a.steps) or drained):
+            e1.record(stream)
+            e1.synchronize()
+            win.update(s1=srv.stats(), l1=srv.launches(), c1=clk.mark(), w1=time.perf_counter(),
+                       ms=e0.elapsed_time(e1), pumps=tick - a.warmup)
+        for info in srv.poll():
+            out = srv.fetch(info["id"])
+            d2h += state_bytes(out)
+            infos[sid[info["id"]]] = info
+        if drained:
+            break
+    wall = time.perf_counter() - t_all
+    return win, infos, {"wall_s": wall, "pumps": tick, "h2d": h2d, "d2h": d2h}
+
+
+def plain_job_by_job(trace, made):
+    """The same jobs on the plain FP64 path, one context per job, one after
+    another: create + upload + steps + download.  Steps are timed on a sample
+    of each job (up to PLAIN_SAMPLE_STEPS after one warm-up step) and scaled to
+    the job's step count."""
+    from mddem_gb300 import capi
+
+    work = secs = 0.0
+    for j, (cfg, st) in zip(trace, made):
+        n = len(st["tag"])
+        t0 = time.perf_counter()
+        ctx = capi.Context(cfg.replace(precision="fp64"), n)
+        ctx.upload(st)
+        ctx.step(1)
+        t1 = time.perf_counter()
+        m = max(1, min(j.steps - 1, PLAIN_SAMPLE_STEPS))
+        ctx.step(m)
+        t2 = time.perf_counter()
+        ctx.download()
+        t3 = time.perf_counter()
+        ctx.close()
+        work += n * j.steps
+        secs += (t1 - t0) + (t3 - t2) + (t2 - t1) * (j.steps - 1) / m + (t2 - t1) / m
+    return {"value": work / secs, "unit": "particle-steps/s", "jobs": len(trace),
+            "sample": f"each job's step time measured over up to {PLAIN_SAMPLE_STEPS} steps after 1 warm-up step, "
+                      "scaled to its step count; setup, upload and download timed in full"}
+
+
+# Compulsory DRAM bytes per particle of the per-particle kernels (each array
+# touched once per launch; neighbours' rows assumed L2-resident), by kind and
+# precision.  k_initial: v, f, x (+ two-float x, build-time x for the mixed
+# rebuild test; fp64: build-time x) (+ DEM: omega, torque, quaternion) read,
+# v, x (+ two-float x) (+ omega, quaternion) written.  k_final: f, v, m, x
+# (+ omega, torque) read, v (+ omega) written.
+INIT_BYTES = {("dem", "mixed"): 416, ("dem", "fp64"): 352, ("lj", "mixed"): 256, ("lj", "fp64"): 192}
+FINAL_BYTES = {"dem": 232, "lj": 136}
+
+
+def force_bytes(kind, nfull, contacts):
+    """k_lj_* / k_dem_*: row length 4 + entries 4 each + own geometry 32 +
+    force 32 written; DEM adds v and omega 64, torque 32, and per contact the
+    partner tag and 7 spring values read and written (2 x 60)."""
+    b = 4 + 4 * nfull + 32 + 32
+    if kind == "dem":
+        b += 64 + 32 + 4 + 120 * contacts
+    return b
+
+
+def serve_roofline(a, trace, made, mix):
+    """Per-kernel device times of the resident mix at the middle of the timed
+    window, re-created from the jobs' initial states in a batch context per
+    kind (eager launches, L2 flushed before each step, CUDA events on the
+    library's stream); the dominant kernel's algorithmic bytes / time."""
+    from mddem_gb300 import capi
+
+    per = {}
+    for kind in ("dem", "lj"):
+        ks = [k for k in mix if (trace[k].kind == "lj") == (kind == "lj")]
+        if not ks:
+            continue
+        cfgs = [made[k][0] for k in ks]
+        sts = [made[k][1] for k in ks]
+        ctx = capi.Context(cfgs, [len(s["tag"]) for s in sts])
+        for q, st in enumerate(sts):
+            ctx.upload(st, q)
+        ctx.set_graph_mode(0)
+        ctx.timed_steps(3, L2_FLUSH)
+        t, _, _ = ctx.timed_steps(5, L2_FLUSH)
+        n = sum(len(s["tag"]) for s in sts)
+        nfull = sum(2.0 * len(ctx.pairs(q)) for q in range(len(sts))) / n
+        contacts = sum(len(ctx.history(q)[0]) for q in range(len(sts))) / n if kind == "dem" else 0.0
+        ctx.close()
+        per[kind] = dict(n=n, init=float(t[:, 1].mean()), force=float(t[:, 3].mean()),
+                         final=float(t[:, 4].mean()), nfull=nfull, contacts=contacts)
+    prec = a.precision
+    cands = {
+        "k_initial": (sum(p["init"] for p in per.values()),
+                      sum(p["n"] * INIT_BYTES[(k, prec)] for k, p in per.items())),
+        "k_final": (sum(p["final"] for p in per.values()),
+                    sum(p["n"] * FINAL_BYTES[k] for k, p in per.items())),
+    }
+    for k, p in per.items():
+        name = ("k_dem_" if k == "dem" else "k_lj_") + prec
+        cands[name] = (p["force"], p["n"] * force_bytes(k, p["nfull"], p["contacts"]))
+    name = max(cands, key=lambda q: cands[q][0])
+    ms, nbytes = cands[name]
+    peak, src = peak_hbm()
+    achieved = nbytes / (ms / 1e3) / 1e9
+    traffic = ncu_traffic(name + "/serve")
+    return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": src, "traffic": traffic,
+            "algorithmic_bytes_per_launch": nbytes, "launch_ms": ms,
+            "kernels_ms": {q: v[0] for q, v in cands.items()},
+            "mix": {k: {"particles": p["n"], "avg_full_neighbors": p["nfull"], "contacts_per_particle": p["contacts"]}
+                    for k, p in per.items()}}
+
+
+def _oracle_job(cfg, st, steps_cap, budget):
+    from oracle.oracle import Oracle
+
+    o = Oracle(cfg.replace(precision="fp64"))
+    o.load(st)
+    o.step(1)
+    n, done, t0 = len(st["tag"]), 0, time.perf_counter()
+    while done < steps_cap and time.perf_counter() - t0 < budget:
+        o.step(1)
+        done += 1
+    return n * done, time.perf_counter() - t0
+
+
+def serve_cpu_sample(trace, made, budget=15.0):
+    """The oracle (single thread) on the stream's jobs in arrival order, each
+    for up to 2e6 particle-steps after one warm-up step, until `budget` s."""
+    work = secs = 0.0
+    used = 0
+    for j, (cfg, st) in sorted(zip(trace, made), key=lambda q: q[0].arrival):
+        if secs > budget:
+            break
+        w_, s_ = _oracle_job(cfg, st, max(1, min(j.steps, int(2e6 // j.n))), budget - secs + 1.0)
+        work += w_
+        secs += s_
+        used += 1
+    return {"value": work / secs, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+            "sample": f"first {used} jobs of the stream in arrival order, each up to 2e6 particle-steps "
+                      "after 1 warm-up step, single thread"}
+
+
+def bench_serve(a, world, rank, local, dist):
+    import numpy as np
+    from mddem_gb300 import build, capi, workloads as w
+
+    build.build()
+    trace = serve_trace(a)
+    made = [j.make(a.precision, a.policy) for j in trace]
+    cfgs, caps = w.serve_slots(a.precision, a.policy)
+    srv = capi.Server(cfgs, caps, SERVE_HBM_BUDGET)
+    # warm-up jobs (one of each kind), drained before the stream starts
+    for j in (w.Job("gas", 300, 2 * SERVE_PUMP, 0, dict(phi=0.1, e=0.9, seed=7)),
+              w.Job("rebound", 2, 2 * SERVE_PUMP, 0, dict(speed=1.0)),
+              w.Job("lj", 500, 2 * SERVE_PUMP, 0, dict(cells=5, rho=0.85, T=1.0, seed=7))):
+        c, s = j.make(a.precision, a.policy)
+        srv.submit(c, s, j.steps)
+    while True:
+        act, pen = srv.pump(SERVE_PUMP)
+        for info in srv.poll():
+            srv.fetch(info["id"])
+        if not act and not pen:
+            break
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        win, infos, run = replay(a, srv, trace, made, clk)
+    ps = win["s1"]["particle_steps"] - win["s0"]["particle_steps"]
+    ms = win["ms"]
+    if dist:
+        import torch
+
+        tt = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        tp = torch.tensor([ps], dtype=torch.float64)
+        dist.all_reduce(tp, op=dist.ReduceOp.SUM)
+        ms, ps = float(tt.item()), float(tp.item())
+    lat = np.array([infos[k]["end_s"] - infos[k]["submit_s"] for k in sorted(infos)])
+    failed = [k for k in infos if infos[k]["status"] != 0]
+    total_ps = float(sum(j.n * j.steps for j in trace))
+    line = {
+        "metric": "particle-steps/s served", "value": ps / (ms / 1e3), "unit": "particle-steps/s",
+        "n_gpus": world, "steps": win["pumps"], "warmup": a.warmup, "ms_per_step": ms / win["pumps"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if a.precision == "mixed" else "f64", "data": "synthetic",
+        "config": {"workload": serve_desc(trace), "precision": a.precision, "rebuild_policy": a.policy,
+                   "pump_timesteps": SERVE_PUMP, "slots": {"dem": w.SERVE_DEM_SLOTS, "lj": w.SERVE_LJ_SLOTS},
+                   "hbm_budget_bytes": SERVE_HBM_BUDGET,
+                   "l2": "inputs larger than L2 (resident state of all jobs, > 129 MB)",
+                   "parallelism": f"replicas x{world}"},
+        "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                      "max": float(lat.max()), "jobs": int(len(lat)), "failed": len(failed)},
+        "trace": {"particle_steps": total_ps, "wall_s": run["wall_s"], "pumps": run["pumps"],
+                  "host_split_s": {q: win["s1"][q] - win["s0"][q] for q in ("admit_s", "step_s", "retire_s")}},
+        "gpu_launches": int(win["l1"] - win["l0"]),
+        "clocks": clk.summary(win["c0"], win["c1"]),
+        "e2e": {"value": total_ps / run["wall_s"], "unit": "particle-steps/s",
+                "h2d_bytes_per_step": run["h2d"] / run["pumps"], "d2h_bytes_per_step": run["d2h"] / run["pumps"],
+                "note": "whole stream through mdg_server_* with host buffers: submit, pumps, poll, fetch"},
+    }
+    srv.close()
+    if rank == 0:
+        line["roofline"] = serve_roofline(a, trace, made, win.get("mix", []))
+        line["plain_fp64_job_by_job"] = plain_job_by_job(trace, made)
+        line["served_vs_plain"] = line["value"] / world / line["plain_fp64_job_by_job"]["value"]
+        if not a.no_cpu_baseline:
+            line["cpu_baseline"] = serve_cpu_sample(trace, made)
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 50; served stream: every pump until it drains)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300")
-    ap.add_argument("--workload", default="lj256k")
+    ap.add_argument("--workload", default="serve")
+    ap.add_argument("--jobs", type=int, default=SERVE_JOBS, help="jobs in the served stream")
     ap.add_argument("--precision", default="mixed")
     ap.add_argument("--policy", default="displacement")
     ap.add_argument("--tpp", type=int, default=0, help="threads per particle in the force kernel (0 = auto)")
@@ -218,6 +567,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     a = ap.parse_args()
     a.warmup = max(3, a.warmup)
+    if a.steps is None:
+        a.steps = 0 if a.workload == "serve" else 50
     if a.impl == "reference":
         return run_reference(a)
 
@@ -231,6 +582,8 @@ def main():
 
         dist.init_process_group("gloo")
 
+    if a.workload == "serve":
+        return bench_serve(a, world, rank, local, dist)
     from mddem_gb300 import build, capi
 
     build.build()

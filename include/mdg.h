@@ -197,6 +197,13 @@ int  mdg_step(mdg_ctx* ctx, int64_t nsteps);
  * inside one multi-step launch. */
 int  mdg_set_remaining(mdg_ctx* ctx, int sys, int64_t steps);
 int  mdg_get_remaining(mdg_ctx* ctx, int sys, int64_t* steps);
+/* The context's CUDA stream (cudaStream_t): all of the context's device work
+ * is ordered on it, so a caller may record events on it or make its own
+ * streams wait for it. */
+int  mdg_get_stream(mdg_ctx* ctx, void** stream);
+/* Every system's step budget, status word and step counter in one device
+ * read (arrays of mdg_num_systems entries; any may be NULL). */
+int  mdg_get_progress(mdg_ctx* ctx, int64_t* remaining, int32_t* status, int64_t* steps);
 /* Sticky device status word of one system (0 = healthy). */
 int  mdg_get_status(mdg_ctx* ctx, int sys, int32_t* status);
 /* Neighbor rebuild + force evaluation at the current state (no integration). */
@@ -266,6 +273,38 @@ int  mdg_server_pump(mdg_server* srv, int64_t max_steps, int* active, int* pendi
 int  mdg_server_poll(mdg_server* srv, mdg_job_info* out, int cap, int* n);
 int  mdg_server_fetch(mdg_server* srv, int64_t id, mdg_state_view* out);
 int  mdg_server_context(mdg_server* srv, mdg_ctx** ctx);
+/* Running totals: particle-steps advanced by all pumps, pumps that launched
+ * work, jobs retired; resident and queued jobs and their estimated device
+ * bytes now; seconds since creation; host seconds spent in admission
+ * (configure + upload), in the multi-step launches (to completion) and in
+ * retirement (progress read + download). */
+typedef struct mdg_server_stats_t {
+    double particle_steps;
+    int64_t pumps, retired;
+    int32_t resident, pending;
+    size_t hbm_used;
+    double time_s;
+    double admit_s, step_s, retire_s;
+} mdg_server_stats_t;
+int  mdg_server_stats(mdg_server* srv, mdg_server_stats_t* out);
+/* The jobs resident in slots now (steps = steps done so far, end_s = -1);
+ * *n receives the count, of which min(cap, count) are written. */
+int  mdg_server_resident(mdg_server* srv, mdg_job_info* out, int cap, int* n);
+
+/* ---- seeded initial conditions ---------------------------------------------
+ * Random sequential addition of non-overlapping spheres in a periodic box:
+ * replaces the rejection loop of insert.rs:523-571 (candidate centre uniform in
+ * the box, inset by the largest radius when `inset`; radius uniform in
+ * [rmin, rmax]; rejected when any placed sphere lies within
+ * sep_factor * (r_i + r_j) under the minimum image) with a cell grid so that
+ * 1e6 spheres place in seconds.  The random stream is xoshiro256** seeded by
+ * splitmix64(seed): same seed, same spheres on every host.  pos_out (n*3) and
+ * rad_out (n) are host buffers; *placed receives the count placed, and the
+ * call returns MDG_ERR_ARG when fewer than n fit within max_attempts
+ * (0 = 20000 n). */
+int  mdg_rsa_spheres(size_t n, const double box_lo[3], const double box_hi[3], double rmin, double rmax,
+                     double sep_factor, int inset, uint64_t seed, uint64_t max_attempts, double* pos_out,
+                     double* rad_out, size_t* placed);
 
 #ifdef __cplusplus
 }

@@ -31,6 +31,7 @@ UNITS = [
     ("mdg_api.cu", ["-fmad=false"]),
     ("mdg_noalloc.cu", ["-fmad=false"]),
     ("mdg_serve.cpp", []),
+    ("mdg_insert.cpp", []),
 ]
 
 

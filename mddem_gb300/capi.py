@@ -32,6 +32,8 @@ EXPORTS = [
     "mdg_set_graph_mode", "mdg_timed_steps", "mdg_granular_temp_noalloc", "mdg_set_remaining",
     "mdg_get_remaining", "mdg_get_status", "mdg_configure_system", "mdg_server_create", "mdg_server_destroy",
     "mdg_server_submit", "mdg_server_pump", "mdg_server_poll", "mdg_server_fetch", "mdg_server_context",
+    "mdg_rsa_spheres", "mdg_get_progress", "mdg_get_stream", "mdg_server_stats",
+    "mdg_server_resident",
 ]
 
 
@@ -91,6 +93,12 @@ class JobInfo(C.Structure):
                 ("n", C.c_int64), ("submit_s", C.c_double), ("start_s", C.c_double), ("end_s", C.c_double)]
 
 
+class ServerStats(C.Structure):
+    _fields_ = [("particle_steps", C.c_double), ("pumps", C.c_int64), ("retired", C.c_int64),
+                ("resident", C.c_int32), ("pending", C.c_int32), ("hbm_used", C.c_size_t), ("time_s", C.c_double),
+                ("admit_s", C.c_double), ("step_s", C.c_double), ("retire_s", C.c_double)]
+
+
 class StepTiming(C.Structure):
     _fields_ = [("step_ms", C.c_double), ("phase_ms", C.c_double * 4), ("kernels", C.c_int32),
                 ("rebuilt", C.c_int32)]
@@ -145,6 +153,13 @@ def load(path: str = LIB_PATH):
     lib.mdg_server_poll.argtypes = [C.c_void_p, C.POINTER(JobInfo), C.c_int, C.POINTER(C.c_int)]
     lib.mdg_server_fetch.argtypes = [C.c_void_p, C.c_int64, C.POINTER(StateView)]
     lib.mdg_server_context.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+    lib.mdg_get_progress.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
+    lib.mdg_server_resident.argtypes = [C.c_void_p, C.POINTER(JobInfo), C.c_int, C.POINTER(C.c_int)]
+    lib.mdg_server_stats.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
+    lib.mdg_get_stream.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+    lib.mdg_rsa_spheres.argtypes = [C.c_size_t, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double,
+                                    C.c_double, C.c_double, C.c_int, C.c_uint64, C.c_uint64,
+                                    C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_size_t)]
     lib.mdg_granular_temp_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]
     _lib = lib
     return lib
@@ -236,6 +251,21 @@ def _download_buffers(n, dem):
     return v, out
 
 
+def rsa_spheres(n, box_lo, box_hi, rmin, rmax, sep_factor=1.1, inset=True, seed=0, max_attempts=0):
+    """mdg_rsa_spheres: seeded random sequential addition (host, native)."""
+    lib = load()
+    pos = np.zeros((n, 3))
+    rad = np.zeros(n)
+    lo = (C.c_double * 3)(*box_lo)
+    hi = (C.c_double * 3)(*box_hi)
+    placed = C.c_size_t()
+    st = lib.mdg_rsa_spheres(n, lo, hi, rmin, rmax, sep_factor, int(inset), seed, max_attempts,
+                             _ptr(pos, C.c_double), _ptr(rad, C.c_double), C.byref(placed))
+    if st != MDG_OK:
+        raise MdgError(st, f"mdg_rsa_spheres placed {placed.value}/{n}")
+    return pos, rad
+
+
 class Server:
     """Continuous-batching server (mdg_server_*): typed slots, HBM-budget
     admission, one multi-step device launch per pump, retirement of finished
@@ -254,6 +284,8 @@ class Server:
         h = C.c_void_p()
         _check(self.lib.mdg_server_create(arr, caps, n, int(hbm_budget), C.byref(h)), "mdg_server_create")
         self.h = h
+        self.nslots = n
+        self.slot_configs = list(slot_configs)
         self.meta = {}
 
     def close(self):
@@ -291,6 +323,39 @@ class Server:
             if n.value < 256:
                 return out
 
+    def context(self):
+        """The server's batch context as a non-owning Context (diagnostics:
+        timed steps, thermo, pairs of a resident slot)."""
+        ctx = C.c_void_p()
+        _check(self.lib.mdg_server_context(self.h, C.byref(ctx)), "mdg_server_context")
+        c = Context.__new__(Context)
+        c.lib, c.h, c.nsys, c.owner = self.lib, ctx, self.nslots, False
+        c.configs, c._keep, c.n = list(self.slot_configs), [], [0] * self.nslots
+        return c
+
+    def launches(self):
+        ctx = C.c_void_p()
+        _check(self.lib.mdg_server_context(self.h, C.byref(ctx)), "mdg_server_context")
+        return int(self.lib.mdg_kernel_launches(ctx))
+
+    def resident(self):
+        buf = (JobInfo * 1024)()
+        n = C.c_int()
+        _check(self.lib.mdg_server_resident(self.h, buf, 1024, C.byref(n)), "mdg_server_resident")
+        return [{f: getattr(buf[k], f) for f, _ in JobInfo._fields_} for k in range(min(n.value, 1024))]
+
+    def stats(self):
+        v = ServerStats()
+        _check(self.lib.mdg_server_stats(self.h, C.byref(v)), "mdg_server_stats")
+        return {f: getattr(v, f) for f, _ in ServerStats._fields_}
+
+    def stream(self):
+        ctx = C.c_void_p()
+        _check(self.lib.mdg_server_context(self.h, C.byref(ctx)), "mdg_server_context")
+        v = C.c_void_p()
+        _check(self.lib.mdg_get_stream(ctx, C.byref(v)), "mdg_get_stream")
+        return v.value or 0
+
     def fetch(self, jid):
         dem, n = self.meta.pop(jid)
         v, out = _download_buffers(n, dem)
@@ -317,12 +382,13 @@ class Context:
         h = C.c_void_p()
         _check(self.lib.mdg_batch_create(arr, caps, n, C.byref(h)), "mdg_batch_create")
         self.h = h
+        self.nsys = n
         self.n = [0] * n
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and getattr(self, "owner", True):
             self.lib.mdg_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -438,6 +504,21 @@ class Context:
         v = C.c_int32()
         _check(self.lib.mdg_get_status(self.h, sys, C.byref(v)), "mdg_get_status")
         return v.value
+
+    def stream(self):
+        """The context's CUDA stream handle (as an int), for events and
+        ordering with the caller's own work."""
+        v = C.c_void_p()
+        _check(self.lib.mdg_get_stream(self.h, C.byref(v)), "mdg_get_stream")
+        return v.value or 0
+
+    def progress(self):
+        """(remaining, status, step) arrays over all systems, one device read."""
+        n = self.nsys
+        rem, sta, stp = np.zeros(n, np.int64), np.zeros(n, np.int32), np.zeros(n, np.int64)
+        _check(self.lib.mdg_get_progress(self.h, _ptr(rem, C.c_int64), _ptr(sta, C.c_int32), _ptr(stp, C.c_int64)),
+               "mdg_get_progress")
+        return rem, sta, stp
 
     def set_remaining(self, steps, sys=0):
         _check(self.lib.mdg_set_remaining(self.h, sys, int(steps)), "mdg_set_remaining")

@@ -119,6 +119,15 @@ struct mdg_ctx {
     std::vector<size_t> capacity;
     std::vector<int> uploaded;
     std::vector<int> ncap_sys;  // current list capacity per system
+    // step budget of each system as the device counts it (-1 unlimited):
+    // every running system advances every step until its budget reaches 0
+    std::vector<long long> rem_host;
+    std::vector<int> run_sys;      // systems in the current run maps
+    bool maps_dirty = true;
+    std::vector<int> cblk0_host, cseg_blocks;  // cell segment of each system
+    int* d_blk_run = nullptr;
+    int* d_cblk_run = nullptr;
+    int* d_run_sys = nullptr;
     Dev d{};
     bool has_lj = false, has_dem = false, has_mixed = false, any_virial = false;
     int tpp_lj = 1;
@@ -348,6 +357,8 @@ int ensure_layout(mdg_ctx* c, int fresh = -1) {
         p.c0 = (int)cells;
         const long long seg = round_up((long long)p.ncell + 1, BLK);
         cblk0[s] = (int)(cells / BLK);
+        c->cseg_blocks[s] = (int)(seg / BLK);
+        p.ncb = (int)(seg / BLK);
         for (long long b = 0; b < seg / BLK; b++) cblk_sys.push_back(s);
         cells += seg;
         old_lst0[s] = p.lst0;
@@ -363,9 +374,11 @@ int ensure_layout(mdg_ctx* c, int fresh = -1) {
         c->free_ptr(c->d.cnt);
         c->free_ptr(c->d.cstart);
         c->free_ptr(c->d_cblk_sys);
+        c->free_ptr(c->d_cblk_run);
         c->d.cnt = c->alloc<int>(cells, err);
         c->d.cstart = c->alloc<int>(cells, err);
         c->d_cblk_sys = c->alloc<int>(cells / BLK, err);
+        c->d_cblk_run = c->alloc<int>(cells / BLK, err);
         if (err) return err;
         c->cells_alloc = cells;
         c->drop_graphs();
@@ -387,15 +400,57 @@ int ensure_layout(mdg_ctx* c, int fresh = -1) {
         c->lst_alloc = cap;
         c->drop_graphs();
     }
+    // the per-cell kernels run over every allocated cell block, so captured
+    // graphs stay valid while the systems' cell grids change inside the
+    // allocation; blocks past the systems' cells find -1 and return
+    cblk_sys.resize((size_t)(c->cells_alloc / BLK), -1);
     cudaMemcpy(c->d_cblk_sys, cblk_sys.data(), cblk_sys.size() * sizeof(int), cudaMemcpyHostToDevice);
     cudaMemcpy(c->d_cblk0, cblk0.data(), cblk0.size() * sizeof(int), cudaMemcpyHostToDevice);
     c->d.cblk_sys = c->d_cblk_sys;
     c->d.cblk0 = c->d_cblk0;
-    // captured graphs carry the cell-block count in their grid sizes
-    if (c->d.ncblocks != (int)(cells / BLK)) c->drop_graphs();
-    c->d.ncblocks = (int)(cells / BLK);
+    c->cblk0_host = cblk0;
+    c->maps_dirty = true;
+    c->d.ncblocks = (int)(c->cells_alloc / BLK);
     cudaMemcpy(c->d_sp, c->sp.data(), c->nsys * sizeof(SysParams), cudaMemcpyHostToDevice);
     return cuda_err(cudaGetLastError());
+}
+
+// Run maps for the next launch: the particle and cell blocks of the systems
+// that will advance (uploaded, budget not exhausted).  Captured graphs carry
+// the maps' lengths as grid sizes, so they are dropped when the set changes.
+// Returns the number of running systems, or -MDG_ERR_CUDA.
+int update_run_maps(mdg_ctx* c) {
+    std::vector<int> run;
+    for (int s = 0; s < c->nsys; s++)
+        if (c->uploaded[s] && c->rem_host[s] != 0) run.push_back(s);
+    if (!c->maps_dirty && run == c->run_sys) return (int)run.size();
+    std::vector<int> pb, cb;
+    for (int s : run) {
+        const SysParams& p = c->sp[s];
+        for (int b = 0; b < p.nb; b++) pb.push_back(p.b0 + b);
+        for (int b = 0; b < c->cseg_blocks[s]; b++) cb.push_back(c->cblk0_host[s] + b);
+    }
+    if (!pb.empty() &&
+        (cudaMemcpy(c->d_blk_run, pb.data(), pb.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+         cudaMemcpy(c->d_cblk_run, cb.data(), cb.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
+         cudaMemcpy(c->d_run_sys, run.data(), run.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess))
+        return -MDG_ERR_CUDA;
+    c->drop_graphs();  // grid sizes follow the maps
+    c->d.blk_run = c->d_blk_run;
+    c->d.cblk_run = c->d_cblk_run;
+    c->d.nrun = (int)pb.size();
+    c->d.ncrun = (int)cb.size();
+    c->d.run_sys = c->d_run_sys;
+    c->d.nrun_sys = (int)run.size();
+    c->run_sys = run;
+    c->maps_dirty = false;
+    return (int)run.size();
+}
+
+// Budgets after n more steps of the running systems.
+void advance_budgets(mdg_ctx* c, int64_t n) {
+    for (int s : c->run_sys)
+        if (c->rem_host[s] > 0) c->rem_host[s] = c->rem_host[s] > n ? c->rem_host[s] - n : 0;
 }
 
 int launch_force(mdg_ctx* c, const Dev& d, cudaStream_t st) {
@@ -617,6 +672,8 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     c->sp.assign(nsys, SysParams{});
     c->capacity.assign(capacity, capacity + nsys);
     c->uploaded.assign(nsys, 0);
+    c->rem_host.assign(nsys, 0);
+    c->cseg_blocks.assign(nsys, 0);
     long long P = 0;
     int nblocks = 0;
     long long hist_entries = 0;
@@ -638,9 +695,9 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
         p.p0 = (int)P;
         p.n = 0;
         p.b0 = nblocks;
-        p.nb = p.npad / BLK;
-        for (int b = 0; b < p.nb; b++) blk_sys.push_back(s);
-        nblocks += p.nb;
+        p.nb = 0;  // blocks in use: set by each upload
+        for (int b = 0; b < p.npad / BLK; b++) blk_sys.push_back(s);
+        nblocks += p.npad / BLK;
         P += p.npad;
         p.ncap = 0;
         if (k.kind == MDG_KIND_DEM) {
@@ -717,6 +774,12 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     if (c->any_virial) d.vir = c->alloc<double>(6 * P, err);
     d.blkpart = c->alloc<double>((size_t)nblocks * 8, err);
     c->d_blk_sys = c->alloc<int>(nblocks, err);
+    c->d_blk_run = c->alloc<int>(nblocks, err);
+    c->d_run_sys = c->alloc<int>(nsys, err);
+    d.rb_sys = c->alloc<int>(nsys + 1, err);
+    d.rb_poff = c->alloc<int>(nsys + 1, err);
+    d.rb_coff = c->alloc<int>(nsys + 1, err);
+    d.rb_n = c->alloc<int>(1, err);
     c->d_cblk0 = c->alloc<int>(nsys, err);
     c->d_sp = c->alloc<SysParams>(nsys, err);
     d.ss = c->alloc<SysState>(nsys, err);
@@ -781,6 +844,7 @@ int mdg_configure_system(mdg_ctx* c, int sys, const mdg_config* cfg) {
     long long zero = 0;
     cudaMemcpy(&c->d.ss[sys].remaining, &zero, sizeof(zero), cudaMemcpyHostToDevice);
     c->uploaded[sys] = 0;
+    c->rem_host[sys] = 0;
     e = cudaMemcpy(c->d_sp + sys, &p, sizeof(SysParams), cudaMemcpyHostToDevice);
     return cuda_err(e);
 }
@@ -810,6 +874,8 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
     int r = setup_grid(k, st->cutoff_radius, n, p);
     if (r) return r;
     p.n = (int)n;
+    p.nb = (int)((n + BLK - 1) / BLK);
+    c->maps_dirty = true;
     const int ncap = auto_ncap(k, p, n);
     p.ncap = ncap;
     if (k.nose_hoover) {
@@ -890,6 +956,7 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(e);
     c->uploaded[sys] = 1;
+    c->rem_host[sys] = -1;
     return MDG_OK;
 }
 
@@ -1030,6 +1097,9 @@ int mdg_step(mdg_ctx* c, int64_t nsteps) {
     if (!c || nsteps < 0) return MDG_ERR_ARG;
     if (!any_uploaded(c)) return MDG_ERR_STATE;
     if (nsteps == 0) return MDG_OK;
+    const int nrun = update_run_maps(c);
+    if (nrun < 0) return -nrun;
+    if (nrun == 0) return MDG_OK;  // every system's budget is spent
     unsigned long long rb0 = 0, rb1 = 0;
     cudaMemcpy(&rb0, c->d.stat_ctr, sizeof(rb0), cudaMemcpyDeviceToHost);
     if (c->graph_mode) {
@@ -1050,16 +1120,20 @@ int mdg_step(mdg_ctx* c, int64_t nsteps) {
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(e);
     cudaMemcpy(&rb1, c->d.stat_ctr, sizeof(rb1), cudaMemcpyDeviceToHost);
+    advance_budgets(c, nsteps);
     // kernels that ran: per step initial + force + final (+ loop control),
-    // plus the seven rebuild kernels on the steps whose rebuild branch opened
+    // plus the eight rebuild kernels on the steps whose rebuild branch opened
     const long long base = 3 + (c->has_lj && c->has_dem ? 1 : 0) + (c->graph_mode ? 1 : 0);
-    c->launches += nsteps * base + 7LL * (long long)(c->graph_mode ? (rb1 - rb0) : nsteps);
+    c->launches += nsteps * base + 8LL * (long long)(c->graph_mode ? (rb1 - rb0) : nsteps);
     return check_status(c);
 }
 
 int mdg_force_only(mdg_ctx* c) {
     if (!c) return MDG_ERR_ARG;
     if (!any_uploaded(c)) return MDG_ERR_STATE;
+    const int nrun = update_run_maps(c);
+    if (nrun < 0) return -nrun;
+    if (nrun == 0) return MDG_OK;
     std::vector<SysState> ss(c->nsys);
     cudaMemcpy(ss.data(), c->d.ss, c->nsys * sizeof(SysState), cudaMemcpyDeviceToHost);
     for (auto& x : ss) x.rebuild = 1;
@@ -1092,7 +1166,29 @@ int mdg_set_remaining(mdg_ctx* c, int sys, int64_t steps) {
     if (e != cudaSuccess) return cuda_err(e);
     long long v = steps;
     e = cudaMemcpy(&c->d.ss[sys].remaining, &v, sizeof(v), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) c->rem_host[sys] = steps;
     return cuda_err(e);
+}
+
+int mdg_get_stream(mdg_ctx* c, void** stream) {
+    if (!c || !stream) return MDG_ERR_ARG;
+    *stream = (void*)c->stream;
+    return MDG_OK;
+}
+
+int mdg_get_progress(mdg_ctx* c, int64_t* remaining, int32_t* status, int64_t* steps) {
+    if (!c) return MDG_ERR_ARG;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(e);
+    std::vector<SysState> ss(c->nsys);
+    e = cudaMemcpy(ss.data(), c->d.ss, c->nsys * sizeof(SysState), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(e);
+    for (int s = 0; s < c->nsys; s++) {
+        if (remaining) remaining[s] = ss[s].remaining;
+        if (status) status[s] = ss[s].status;
+        if (steps) steps[s] = ss[s].step;
+    }
+    return MDG_OK;
 }
 
 int mdg_get_remaining(mdg_ctx* c, int sys, int64_t* steps) {
@@ -1169,6 +1265,12 @@ int64_t mdg_kernel_launches(const mdg_ctx* c) { return c ? c->launches : 0; }
 int mdg_timed_steps(mdg_ctx* c, int64_t nsteps, size_t l2_flush_bytes, mdg_step_timing* out) {
     if (!c || nsteps < 0 || (nsteps && !out)) return MDG_ERR_ARG;
     if (!any_uploaded(c)) return MDG_ERR_STATE;
+    const int nrun = update_run_maps(c);
+    if (nrun < 0) return -nrun;
+    if (nrun == 0) {  // every system's budget is spent: nothing runs
+        for (int64_t k = 0; k < nsteps; k++) out[k] = mdg_step_timing{};
+        return MDG_OK;
+    }
     if (l2_flush_bytes > c->flush_bytes) {
         if (c->flush_buf) cudaFree(c->flush_buf);
         c->flush_buf = nullptr;
@@ -1216,12 +1318,13 @@ int mdg_timed_steps(mdg_ctx* c, int64_t nsteps, size_t l2_flush_bytes, mdg_step_
         for (int q = 0; q < 4; q++) out[k].phase_ms[q] = ms[1 + q];
         cudaMemcpy(ss.data(), c->d.ss, c->nsys * sizeof(SysState), cudaMemcpyDeviceToHost);
         int rb = 0;
-        for (int s = 0; s < c->nsys; s++) rb |= (ss[s].steps_since_build == 0);
+        for (int s : c->run_sys) rb |= (ss[s].steps_since_build == 0);
         out[k].rebuilt = rb;
-        // the 7 rebuild-pipeline kernels run only when the conditional opened
-        out[k].kernels = c->tkernels - ((rb || !c->graph_mode) ? 0 : 7);
+        // the 8 rebuild-pipeline kernels run only when the conditional opened
+        out[k].kernels = c->tkernels - ((rb || !c->graph_mode) ? 0 : 8);
         c->launches += out[k].kernels;
     }
+    advance_budgets(c, nsteps);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(e);
     return check_status(c);

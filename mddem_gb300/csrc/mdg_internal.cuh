@@ -43,7 +43,8 @@ struct SysParams {
     int precision;       // 0 fp64, 1 mixed
     int contact_model, adhesion_model, rolling_model, twisting_model;
     int p0, n, npad;     // particle segment
-    int b0, nb;          // block segment
+    int b0, nb;          // first particle block; blocks holding the n particles
+    int ncb;             // cell blocks of the system's cell segment
     int c0, ncell;       // ext-cell segment
     int nc[3];           // interior cells per axis
     int ext[3];          // extended grid (interior + 2*layers)
@@ -153,9 +154,26 @@ struct Dev {
     // reductions
     double* blkpart;   // [nblocks][8]
     const int* blk_sys;   // particle block -> system
-    const int* cblk_sys;  // cell block -> system
+    const int* cblk_sys;  // cell block -> system (-1 past the systems' cells)
     const int* cblk0;     // first cell block of each system
-    int ncblocks;
+    int ncblocks;         // allocated cell blocks
+    // Run maps: the particle / cell blocks of the systems that advance in this
+    // launch (uploaded, step budget not exhausted).  The step kernels' grids
+    // cover only these, so idle slots of a batch cost nothing.
+    const int* blk_run;   // global particle block ids
+    int nrun;
+    const int* cblk_run;  // global cell block ids
+    int ncrun;
+    const int* run_sys;   // the running systems, ascending
+    int nrun_sys;
+    // Rebuild work list, written on the device by k_rb_plan when a step
+    // rebuilds: the systems that sort or rebuild, with prefix offsets of their
+    // particle blocks and cell blocks (rb_poff / rb_coff have rb_n + 1 entries).
+    // The rebuild kernels walk these virtual blocks with grid-stride loops.
+    int* rb_sys;
+    int* rb_poff;
+    int* rb_coff;
+    int* rb_n;
     const SysParams* sp;
     SysState* ss;
     const double* mat;

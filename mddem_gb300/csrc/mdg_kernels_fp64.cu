@@ -7,9 +7,9 @@
 // the reference's scatter-then-reverse-comm order, hence a 1e-12 relative
 // bound on forces rather than bit equality.
 //
-// One timestep = k_initial -> [rebuild: k_cells, k_scan, k_scatter,
-// k_cellsort, k_gather, k_copyback, k_build] -> force -> k_final.  Rebuild
-// kernels return at once for systems that do not rebuild this step.
+// One timestep = k_initial -> [rebuild: k_rb_plan, k_cells, k_scan,
+// k_scatter, k_cellsort, k_gather, k_copyback, k_build] -> force -> k_final.
+// The rebuild kernels visit only the systems that sort or rebuild this step.
 #include "mdg_internal.cuh"
 
 namespace mdg {
@@ -35,13 +35,13 @@ __device__ __forceinline__ void decode_shift(int sc, int& sx, int& sy, int& sz) 
     sz = sc % 3 - 1;
 }
 
-// Per-system reduction of NV doubles.  Every block of the system contributes a
-// partial; the last block to arrive sums the partials with a fixed order
+// Per-system reduction of NV doubles.  Every block of the system (gb = its
+// global particle block id) contributes a partial; the last block to arrive sums the partials with a fixed order
 // (strided lanes, then a fixed tree) so the result is deterministic.  Returns
 // true on the last block (all threads), totals valid in out[] on thread 0.
-// The grid must be exactly the particle-block grid.
+// Every block of the system must be in the launch.
 template <int NV>
-__device__ bool system_reduce(const Dev& d, int s, const double (&v)[NV], double (&out)[NV]) {
+__device__ bool system_reduce(const Dev& d, int s, int gb, const double (&v)[NV], double (&out)[NV]) {
     static_assert(NV <= 8, "blkpart holds 8 doubles per block");
     __shared__ double sh[NV][BLK];
     __shared__ int last;
@@ -59,7 +59,7 @@ __device__ bool system_reduce(const Dev& d, int s, const double (&v)[NV], double
     }
     if (t == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; k++) d.blkpart[(size_t)blockIdx.x * 8 + k] = sh[k][0];
+        for (int k = 0; k < NV; k++) d.blkpart[(size_t)gb * 8 + k] = sh[k][0];
         __threadfence();
         unsigned int prev = atomicAdd(&d.ss[s].red_count, 1u);
         last = (prev == (unsigned)(sp.nb - 1)) ? 1 : 0;
@@ -102,10 +102,11 @@ __device__ __forceinline__ int vload(const int* p) { return *((const volatile in
 // (mddem_verlet/src/lib.rs:97-123) + initial_rotation (rotational.rs:59-84),
 // fused with decide_rebuild's per-atom tests (neighbor.rs:564-674).
 __global__ void __launch_bounds__(BLK) k_initial(Dev d) {
-    const int s = d.blk_sys[blockIdx.x];
+    const int gb = d.blk_run[blockIdx.x];
+    const int s = d.blk_sys[gb];
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
-    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    const int li = (gb - sp.b0) * BLK + threadIdx.x;
     const bool live = sys_active(st);
     const bool act = live && li < sp.n;
     const long long i = (long long)sp.p0 + li;
@@ -238,13 +239,102 @@ __device__ __forceinline__ bool do_rebuild(const SysState* st) {
     return sys_active(st) && (vload(&st->rebuild) || (vload(&st->periodic_sort) && vload(&st->nonid)));
 }
 
+// Exclusive block-wide scan (1024 threads) of one int; total to `tot`.
+__device__ __forceinline__ int block_scan1024(int v, int* wsum, int& tot) {
+    const int t = threadIdx.x;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if ((t & 31) >= o) x += y;
+    }
+    if ((t & 31) == 31) wsum[t >> 5] = x;
+    __syncthreads();
+    if (t < 32) {
+        int w = wsum[t];
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, w, o);
+            if (t >= o) w += y;
+        }
+        wsum[t] = w;
+    }
+    __syncthreads();
+    const int incl = x + ((t >> 5) ? wsum[(t >> 5) - 1] : 0);
+    tot = wsum[31];
+    __syncthreads();
+    return incl - v;
+}
+
+// Rebuild work list of this step (one block of 1024 threads): the running
+// systems that sort or rebuild, in ascending order, with the prefix offsets
+// of their particle blocks and cell blocks.
+__global__ void __launch_bounds__(1024) k_rb_plan(Dev d) {
+    __shared__ int wsum[32];
+    const int t = threadIdx.x;
+    int cn = 0, cp = 0, cc = 0;  // carries (uniform across the block)
+    for (int base = 0; base < d.nrun_sys; base += 1024) {
+        const int k = base + t;
+        const int s = k < d.nrun_sys ? d.run_sys[k] : -1;
+        const bool f = s >= 0 && do_sort(d.ss + s);
+        const int np = f ? d.sp[s].nb : 0, nc = f ? d.sp[s].ncb : 0;
+        int tn, tp, tc;
+        const int en = block_scan1024(f ? 1 : 0, wsum, tn);
+        const int ep = block_scan1024(np, wsum, tp);
+        const int ec = block_scan1024(nc, wsum, tc);
+        if (f) {
+            d.rb_sys[cn + en] = s;
+            d.rb_poff[cn + en] = cp + ep;
+            d.rb_coff[cn + en] = cc + ec;
+        }
+        cn += tn;
+        cp += tp;
+        cc += tc;
+    }
+    if (t == 0) {
+        d.rb_poff[cn] = cp;
+        d.rb_coff[cn] = cc;
+        *d.rb_n = cn;
+    }
+}
+
+// entry k of a prefix array off[0..n] with off[k] <= v < off[k+1]
+__device__ __forceinline__ int rb_find(const int* off, int n, int v) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= v) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Grid-stride loop over the particle blocks (s = system, lb = block within
+// it) or cell blocks of the rebuild work list.
+#define RB_FOR_PARTICLE_BLOCKS(BODY)                                  \
+    {                                                                 \
+        const int rbn_ = *d.rb_n;                                     \
+        const int tot_ = d.rb_poff[rbn_];                             \
+        for (int v_ = blockIdx.x; v_ < tot_; v_ += gridDim.x) {       \
+            const int k_ = rb_find(d.rb_poff, rbn_, v_);              \
+            BODY(d, d.rb_sys[k_], v_ - d.rb_poff[k_]);                \
+        }                                                             \
+    }
+#define RB_FOR_CELL_BLOCKS(BODY, SUB)                                 \
+    {                                                                 \
+        const int rbn_ = *d.rb_n;                                     \
+        const int tot_ = d.rb_coff[rbn_] * (SUB);                     \
+        for (int v_ = blockIdx.x; v_ < tot_; v_ += gridDim.x) {       \
+            const int cv_ = v_ / (SUB);                               \
+            const int k_ = rb_find(d.rb_coff, rbn_, cv_);             \
+            BODY(d, d.rb_sys[k_], cv_ - d.rb_coff[k_], v_ % (SUB));   \
+        }                                                             \
+    }
+
 // pbc (domain.rs:413-459, rebuild steps only) + bin key (neighbor.rs:721-738)
-__global__ void __launch_bounds__(BLK) k_cells(Dev d) {
-    const int s = d.blk_sys[blockIdx.x];
+__device__ __forceinline__ void cells_block(const Dev& d, int s, int lb) {
     const SysParams& sp = d.sp[s];
     const SysState* st = d.ss + s;
     if (!do_sort(st)) return;
-    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    const int li = lb * BLK + threadIdx.x;
     if (li >= sp.n) return;
     const long long i = (long long)sp.p0 + li;
     double4 x = d.pos[i];
@@ -264,11 +354,11 @@ __global__ void __launch_bounds__(BLK) k_cells(Dev d) {
     d.cell[i] = flat;
     atomicAdd(&d.cnt[sp.c0 + flat], 1);
 }
+__global__ void __launch_bounds__(BLK) k_cells(Dev d) RB_FOR_PARTICLE_BLOCKS(cells_block)
 
 // exclusive scan of one system's cell counts -> absolute starts (+ sentinel);
-// counts are reset for use as scatter cursors.  One block per system.
-__global__ void __launch_bounds__(1024) k_scan(Dev d) {
-    const int s = blockIdx.x;
+// counts are reset for use as scatter cursors.  One block per listed system.
+__device__ void scan_system(const Dev& d, int s) {
     const SysParams& sp = d.sp[s];
     if (!do_sort(d.ss + s)) return;
     __shared__ int wsum[32];
@@ -306,30 +396,34 @@ __global__ void __launch_bounds__(1024) k_scan(Dev d) {
         __syncthreads();
     }
     if (t == 0) d.cstart[sp.c0 + sp.ncell] = carry;
+    __syncthreads();
+}
+__global__ void __launch_bounds__(1024) k_scan(Dev d) {
+    const int rbn = *d.rb_n;
+    for (int k = blockIdx.x; k < rbn; k += gridDim.x) scan_system(d, d.rb_sys[k]);
 }
 
-__global__ void __launch_bounds__(BLK) k_scatter(Dev d) {
-    const int s = d.blk_sys[blockIdx.x];
+__device__ __forceinline__ void scatter_block(const Dev& d, int s, int lb) {
     const SysParams& sp = d.sp[s];
     if (!do_sort(d.ss + s)) return;
-    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    const int li = lb * BLK + threadIdx.x;
     if (li >= sp.n) return;
     const long long i = (long long)sp.p0 + li;
     const int c = d.cell[i];
     const int slot = d.cstart[sp.c0 + c] + atomicAdd(&d.cnt[sp.c0 + c], 1);
     d.perm[slot] = (int)i;
 }
+__global__ void __launch_bounds__(BLK) k_scatter(Dev d) RB_FOR_PARTICLE_BLOCKS(scatter_block)
 
 // Stable order inside each cell (by old index): the sort of sort_atoms_by_bin
 // made stable (documented deviation from sort_unstable_by_key,
 // neighbor.rs:740).  Also detects a non-identity permutation, which turns a
 // periodic sort into a rebuild (neighbor.rs:784-793).
-__global__ void __launch_bounds__(BLK) k_cellsort(Dev d) {
-    const int s = d.cblk_sys[blockIdx.x];
+__device__ __forceinline__ void cellsort_block(const Dev& d, int s, int lcb, int) {
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
     if (!do_sort(st)) return;
-    const int c = (blockIdx.x - d.cblk0[s]) * BLK + threadIdx.x;
+    const int c = lcb * BLK + threadIdx.x;
     if (c >= sp.ncell) return;
     const int start = d.cstart[sp.c0 + c];
     const int m = d.cnt[sp.c0 + c];
@@ -349,16 +443,16 @@ __global__ void __launch_bounds__(BLK) k_cellsort(Dev d) {
     d.cnt[sp.c0 + c] = 0;
     if (!ident) atomicOr(&st->nonid, 1);
 }
+__global__ void __launch_bounds__(BLK) k_cellsort(Dev d) RB_FOR_CELL_BLOCKS(cellsort_block, 1)
 
 // Atom::apply_permutation + AtomDataRegistry::apply_permutation_all +
 // ContactHistoryStore::apply_permutation (atom.rs:383-394, 197-202,
 // tangential.rs:92-96): gather every per-atom array into scratch.
-__global__ void __launch_bounds__(BLK) k_gather(Dev d) {
-    const int s = d.blk_sys[blockIdx.x];
+__device__ __forceinline__ void gather_block(const Dev& d, int s, int lb) {
     const SysParams& sp = d.sp[s];
     if (!do_rebuild(d.ss + s)) return;
     const int hcur = d.ss[s].hcur;
-    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    const int li = lb * BLK + threadIdx.x;
     if (li >= sp.n) return;
     const long long k = (long long)sp.p0 + li;
     const long long o = d.perm[k];
@@ -386,12 +480,13 @@ __global__ void __launch_bounds__(BLK) k_gather(Dev d) {
     }
 }
 
-__global__ void __launch_bounds__(BLK) k_copyback(Dev d) {
-    const int s = d.blk_sys[blockIdx.x];
+__global__ void __launch_bounds__(BLK) k_gather(Dev d) RB_FOR_PARTICLE_BLOCKS(gather_block)
+
+__device__ __forceinline__ void copyback_block(const Dev& d, int s, int lb) {
     const SysParams& sp = d.sp[s];
     if (!do_rebuild(d.ss + s)) return;
     const int hcur = d.ss[s].hcur;
-    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    const int li = lb * BLK + threadIdx.x;
     if (li >= sp.n) return;
     const long long k = (long long)sp.p0 + li;
     const double4 x = d.s_pos[k];
@@ -443,6 +538,7 @@ __global__ void __launch_bounds__(BLK) k_copyback(Dev d) {
     const bool edge = fx < 1e-9 || fx > 1.0 - 1e-9 || fy < 1e-9 || fy > 1.0 - 1e-9 || fz < 1e-9 || fz > 1.0 - 1e-9;
     d.cell[k] = ((cx * sp.ext[1] + cy) * sp.ext[2] + cz) | (edge ? (int)0x80000000u : 0);
 }
+__global__ void __launch_bounds__(BLK) k_copyback(Dev d) RB_FOR_PARTICLE_BLOCKS(copyback_block)
 
 // Stencil membership of a cell offset (compute_bin_grid's distance test,
 // neighbor.rs:341-361, tabulated on the host).
@@ -539,17 +635,18 @@ __device__ __forceinline__ TileRule tile_rule(const SysParams& sp, int ex, int e
 // fp64.  Also saves last_build_pos (neighbor.rs:545-561).
 constexpr int BUILD_WARPS = 4;
 
-__global__ void __launch_bounds__(BUILD_WARPS * 32) k_build(Dev d) {
+constexpr int BUILD_SUBS = BLK / BUILD_WARPS;  // blocks per 128-bin cell block
+
+// One warp per bin: bin `sub * BUILD_WARPS + warp` of cell block `lcb` of
+// system s.  Warp-synchronous only (no block barrier), so warps may leave early.
+__device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
     __shared__ float4 tile_h[BUILD_WARPS][32], tile_l[BUILD_WARPS][32];
     __shared__ int tile_e[BUILD_WARPS][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    constexpr int SUBS = BLK / BUILD_WARPS;  // blocks per 128-bin cell block
-    const int cblock = blockIdx.x / SUBS;
-    const int s = d.cblk_sys[cblock];
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
     if (!do_rebuild(st)) return;
-    const int c = (cblock - d.cblk0[s]) * BLK + (blockIdx.x % SUBS) * BUILD_WARPS + warp;
+    const int c = lcb * BLK + sub * BUILD_WARPS + warp;
     if (c >= sp.ncell) return;
     const int a0 = d.cstart[sp.c0 + c], a1 = d.cstart[sp.c0 + c + 1];
     if (a0 == a1) return;
@@ -751,13 +848,15 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32) k_build(Dev d) {
     }
 }
 
+__global__ void __launch_bounds__(BUILD_WARPS * 32) k_build(Dev d) RB_FOR_CELL_BLOCKS(build_cells, BUILD_SUBS)
+
 // ----------------------------------------------------------------------------
 // LJ 12-6 force (lj_force, md_lj/src/lib.rs:488-633) over the full list.
 // TPP lanes share one particle's row and combine with warp shuffles.
 // ----------------------------------------------------------------------------
 template <int TPP>
 __global__ void __launch_bounds__(BLK) k_lj_fp64(Dev d) {
-    const int pb = blockIdx.x / TPP;
+    const int pb = d.blk_run[blockIdx.x / TPP];
     const int sub = blockIdx.x % TPP;
     const int s = d.blk_sys[pb];
     const SysParams& sp = d.sp[s];
@@ -1086,12 +1185,13 @@ __device__ __forceinline__ bool hist_find(const Dev& d, const SysParams& sp, int
 }
 
 __global__ void __launch_bounds__(BLK) k_dem_fp64(Dev d) {
-    const int s = d.blk_sys[blockIdx.x];
+    const int gb = d.blk_run[blockIdx.x];
+    const int s = d.blk_sys[gb];
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
     if (sp.kind != 0 || !sys_active(st)) return;
     const int hcur = st->hcur;
-    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    const int li = (gb - sp.b0) * BLK + threadIdx.x;
     if (li >= sp.n) return;
     const long long i = (long long)sp.p0 + li;
     const int hn = hcur ^ 1;
@@ -1176,11 +1276,12 @@ __global__ void __launch_bounds__(BLK) k_dem_fp64(Dev d) {
 // (rotational.rs:87-100), nh_post_final (md_thermostat/src/lib.rs:313-353).
 // integrate = 0: reductions and rebuild bookkeeping only (force-only evaluation).
 __global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
-    const int s = d.blk_sys[blockIdx.x];
+    const int gb = d.blk_run[blockIdx.x];
+    const int s = d.blk_sys[gb];
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
     if (!sys_active(st)) return;  // every block of a frozen system returns
-    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    const int li = (gb - sp.b0) * BLK + threadIdx.x;
     const bool act = li < sp.n;
     const long long i = (long long)sp.p0 + li;
     const double dt = sp.dt;
@@ -1226,11 +1327,11 @@ __global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
     double out[8];
     bool last;
     if (sp.virial) {
-        last = system_reduce<8>(d, s, vals, out);
+        last = system_reduce<8>(d, s, gb, vals, out);
     } else {
         const double v1[1] = {vals[0]};
         double o1[1];
-        last = system_reduce<1>(d, s, v1, o1);
+        last = system_reduce<1>(d, s, gb, v1, o1);
         out[0] = o1[0];
     }
     if (last && threadIdx.x == 0) {
@@ -1268,9 +1369,11 @@ __global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
 
 // KE of the uploaded velocities (the first nh_pre_initial's compute_ke).
 __global__ void __launch_bounds__(BLK) k_ke_init(Dev d) {
-    const int s = d.blk_sys[blockIdx.x];
+    const int gb = blockIdx.x;
+    const int s = d.blk_sys[gb];
     const SysParams& sp = d.sp[s];
-    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    if (gb - sp.b0 >= sp.nb) return;  // past the particles: not in the reduction
+    const int li = (gb - sp.b0) * BLK + threadIdx.x;
     double vals[1] = {0.0};
     if (li < sp.n) {
         const long long i = (long long)sp.p0 + li;
@@ -1278,7 +1381,7 @@ __global__ void __launch_bounds__(BLK) k_ke_init(Dev d) {
         vals[0] = d.mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z);
     }
     double out[1];
-    if (system_reduce<1>(d, s, vals, out) && threadIdx.x == 0) {
+    if (system_reduce<1>(d, s, gb, vals, out) && threadIdx.x == 0) {
         SysState* st = d.ss + s;
         const double ke = 0.5 * out[0];
         st->ke = ke;
@@ -1293,9 +1396,11 @@ __global__ void __launch_bounds__(BLK) k_ke_init(Dev d) {
 
 // thermo pass 1: sum m, sum m v, compute_ke sum, pe  (granular_temp.rs:62-101, atom.rs:489-502)
 __global__ void __launch_bounds__(BLK) k_thermo1(Dev d, double* out16) {
-    const int s = d.blk_sys[blockIdx.x];
+    const int gb = blockIdx.x;
+    const int s = d.blk_sys[gb];
     const SysParams& sp = d.sp[s];
-    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    if (gb - sp.b0 >= sp.nb) return;  // past the particles: not in the reduction
+    const int li = (gb - sp.b0) * BLK + threadIdx.x;
     double vals[6] = {0, 0, 0, 0, 0, 0};
     if (li < sp.n) {
         const long long i = (long long)sp.p0 + li;
@@ -1309,7 +1414,7 @@ __global__ void __launch_bounds__(BLK) k_thermo1(Dev d, double* out16) {
         vals[5] = d.frc[i].w;
     }
     double out[6];
-    if (system_reduce<6>(d, s, vals, out) && threadIdx.x == 0) {
+    if (system_reduce<6>(d, s, gb, vals, out) && threadIdx.x == 0) {
         double* o = out16 + (size_t)s * 16;
         o[0] = 0.5 * out[4];
         o[1] = out[5];
@@ -1323,9 +1428,11 @@ __global__ void __launch_bounds__(BLK) k_thermo1(Dev d, double* out16) {
 
 // thermo pass 2: sum m |v - vbar|^2 -> granular temperature
 __global__ void __launch_bounds__(BLK) k_thermo2(Dev d, double* out16) {
-    const int s = d.blk_sys[blockIdx.x];
+    const int gb = blockIdx.x;
+    const int s = d.blk_sys[gb];
     const SysParams& sp = d.sp[s];
-    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    if (gb - sp.b0 >= sp.nb) return;  // past the particles: not in the reduction
+    const int li = (gb - sp.b0) * BLK + threadIdx.x;
     const double* o = out16 + (size_t)s * 16;
     double vals[1] = {0.0};
     if (li < sp.n) {
@@ -1336,17 +1443,19 @@ __global__ void __launch_bounds__(BLK) k_thermo2(Dev d, double* out16) {
         vals[0] = m * (dx * dx) + m * (dy * dy) + m * (dz * dz);
     }
     double out[1];
-    if (system_reduce<1>(d, s, vals, out) && threadIdx.x == 0) out16[(size_t)s * 16 + 4] = out[0] / (3.0 * o[8]);
+    if (system_reduce<1>(d, s, gb, vals, out) && threadIdx.x == 0) out16[(size_t)s * 16 + 4] = out[0] / (3.0 * o[8]);
 }
 
 // LJ potential energy per particle (owner entries of the full row; the sum
 // over particles is the sum over the reference's half-list pairs), fp64,
 // written to frc.w.  Launched on demand by the thermo query.
 __global__ void __launch_bounds__(BLK) k_lj_pe(Dev d) {
-    const int s = d.blk_sys[blockIdx.x];
+    const int gb = blockIdx.x;
+    const int s = d.blk_sys[gb];
     const SysParams& sp = d.sp[s];
+    if (gb - sp.b0 >= sp.nb) return;  // past the particles: not in the reduction
     if (sp.kind != 1) return;
-    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    const int li = (gb - sp.b0) * BLK + threadIdx.x;
     if (li >= sp.n) return;
     const long long i = (long long)sp.p0 + li;
     const double4 xi = d.pos[i];
@@ -1376,34 +1485,43 @@ __global__ void __launch_bounds__(BLK) k_lj_pe(Dev d) {
 // launchers
 // ----------------------------------------------------------------------------
 int launch_initial(const Dev& d, cudaStream_t st) {
-    k_initial<<<d.nblocks, BLK, 0, st>>>(d);
+    k_initial<<<d.nrun, BLK, 0, st>>>(d);
     return 1;
 }
 
+// The rebuild kernels walk the device-built work list with grid-stride
+// loops; their grids (fixed when a graph is captured) are the running blocks,
+// capped at a few waves of the GPU.
 int launch_rebuild(const Dev& d, cudaStream_t st) {
-    k_cells<<<d.nblocks, BLK, 0, st>>>(d);
-    k_scan<<<d.nsys, 1024, 0, st>>>(d);
-    k_scatter<<<d.nblocks, BLK, 0, st>>>(d);
-    k_cellsort<<<d.ncblocks, BLK, 0, st>>>(d);
-    k_gather<<<d.nblocks, BLK, 0, st>>>(d);
-    k_copyback<<<d.nblocks, BLK, 0, st>>>(d);
-    k_build<<<d.ncblocks * (BLK / BUILD_WARPS), BUILD_WARPS * 32, 0, st>>>(d);
-    return 7;
+    constexpr int CAP = 152 * 16;
+    const int gp = d.nrun < CAP ? d.nrun : CAP;
+    const int gc = d.ncrun < CAP ? d.ncrun : CAP;
+    const int gb = d.ncrun * BUILD_SUBS < 2 * CAP ? d.ncrun * BUILD_SUBS : 2 * CAP;
+    const int gs = d.nrun_sys < 304 ? d.nrun_sys : 304;
+    k_rb_plan<<<1, 1024, 0, st>>>(d);
+    k_cells<<<gp, BLK, 0, st>>>(d);
+    k_scan<<<gs, 1024, 0, st>>>(d);
+    k_scatter<<<gp, BLK, 0, st>>>(d);
+    k_cellsort<<<gc, BLK, 0, st>>>(d);
+    k_gather<<<gp, BLK, 0, st>>>(d);
+    k_copyback<<<gp, BLK, 0, st>>>(d);
+    k_build<<<gb, BUILD_WARPS * 32, 0, st>>>(d);
+    return 8;
 }
 
 int launch_force_fp64(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st) {
     int n = 0;
     if (has_lj) {
         switch (tpp) {
-            case 2: k_lj_fp64<2><<<d.nblocks * 2, BLK, 0, st>>>(d); break;
-            case 4: k_lj_fp64<4><<<d.nblocks * 4, BLK, 0, st>>>(d); break;
-            case 8: k_lj_fp64<8><<<d.nblocks * 8, BLK, 0, st>>>(d); break;
-            default: k_lj_fp64<1><<<d.nblocks, BLK, 0, st>>>(d); break;
+            case 2: k_lj_fp64<2><<<d.nrun * 2, BLK, 0, st>>>(d); break;
+            case 4: k_lj_fp64<4><<<d.nrun * 4, BLK, 0, st>>>(d); break;
+            case 8: k_lj_fp64<8><<<d.nrun * 8, BLK, 0, st>>>(d); break;
+            default: k_lj_fp64<1><<<d.nrun, BLK, 0, st>>>(d); break;
         }
         n++;
     }
     if (has_dem) {
-        k_dem_fp64<<<d.nblocks, BLK, 0, st>>>(d);
+        k_dem_fp64<<<d.nrun, BLK, 0, st>>>(d);
         n++;
     }
     return n;
@@ -1426,7 +1544,7 @@ int launch_loop_ctl(const Dev& d, long long* counter, unsigned long long handle,
 }
 
 int launch_final(const Dev& d, cudaStream_t st, int integrate) {
-    k_final<<<d.nblocks, BLK, 0, st>>>(d, integrate);
+    k_final<<<d.nrun, BLK, 0, st>>>(d, integrate);
     return 1;
 }
 

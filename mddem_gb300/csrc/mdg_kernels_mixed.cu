@@ -27,7 +27,7 @@ struct Kahan {
 // frames as the FP64 kernel).
 template <int TPP>
 __global__ void __launch_bounds__(BLK, 8) k_lj_mixed(Dev d) {
-    const int pb = blockIdx.x / TPP;
+    const int pb = d.blk_run[blockIdx.x / TPP];
     const int sub = blockIdx.x % TPP;
     const int s = d.blk_sys[pb];
     const SysParams& sp = d.sp[s];
@@ -395,12 +395,13 @@ __device__ __forceinline__ bool hist_find_m(const Dev& d, const SysParams& sp, i
 }
 
 __global__ void __launch_bounds__(BLK) k_dem_mixed(Dev d) {
-    const int s = d.blk_sys[blockIdx.x];
+    const int gb = d.blk_run[blockIdx.x];
+    const int s = d.blk_sys[gb];
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
     if (sp.kind != 0 || !sys_active(st)) return;
     const int hcur = st->hcur;
-    const int li = (blockIdx.x - sp.b0) * BLK + threadIdx.x;
+    const int li = (gb - sp.b0) * BLK + threadIdx.x;
     if (li >= sp.n) return;
     const long long i = (long long)sp.p0 + li;
     const int hn = hcur ^ 1;
@@ -474,15 +475,15 @@ __global__ void __launch_bounds__(BLK) k_dem_mixed(Dev d) {
 int launch_force_mixed(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st) {
     int n = 0;
     if (has_dem) {
-        k_dem_mixed<<<d.nblocks, BLK, 0, st>>>(d);
+        k_dem_mixed<<<d.nrun, BLK, 0, st>>>(d);
         n++;
     }
     if (has_lj) {
         switch (tpp) {
-            case 2: k_lj_mixed<2><<<d.nblocks * 2, BLK, 0, st>>>(d); break;
-            case 4: k_lj_mixed<4><<<d.nblocks * 4, BLK, 0, st>>>(d); break;
-            case 8: k_lj_mixed<8><<<d.nblocks * 8, BLK, 0, st>>>(d); break;
-            default: k_lj_mixed<1><<<d.nblocks, BLK, 0, st>>>(d); break;
+            case 2: k_lj_mixed<2><<<d.nrun * 2, BLK, 0, st>>>(d); break;
+            case 4: k_lj_mixed<4><<<d.nrun * 4, BLK, 0, st>>>(d); break;
+            case 8: k_lj_mixed<8><<<d.nrun * 8, BLK, 0, st>>>(d); break;
+            default: k_lj_mixed<1><<<d.nrun, BLK, 0, st>>>(d); break;
         }
         n++;
     }

@@ -96,6 +96,7 @@ struct Job {
     std::vector<mdg_material> mats;
     HostState state;
     int64_t steps = 0;
+    int64_t left = 0;  // steps still to run while resident
     size_t bytes = 0;
     int slot = -1;
     int status = MDG_OK;
@@ -124,6 +125,9 @@ struct mdg_server {
     std::deque<int64_t> pending;
     std::map<int64_t, std::unique_ptr<Job>> jobs;
     std::vector<int64_t> finished;  // not yet polled
+    double particle_steps = 0;  // work done by all pumps
+    double admit_s = 0, step_s = 0, retire_s = 0;
+    int64_t pumps = 0, retired = 0;
     clk::time_point t0 = clk::now();
     double now() const { return std::chrono::duration<double>(clk::now() - t0).count(); }
 };
@@ -187,6 +191,7 @@ int mdg_server_submit(mdg_server* s, const mdg_config* cfg, const mdg_state_view
 // after the call.
 int mdg_server_pump(mdg_server* s, int64_t max_steps, int* active, int* pending) {
     if (!s || max_steps < 0) return MDG_ERR_ARG;
+    const double ta = s->now();
     // admission: FIFO, skipping jobs that do not fit yet (no head-of-line blocking)
     for (auto it = s->pending.begin(); it != s->pending.end();) {
         Job* j = s->jobs[*it].get();
@@ -214,6 +219,7 @@ int mdg_server_pump(mdg_server* s, int64_t max_steps, int* active, int* pending)
             continue;
         }
         j->slot = slot;
+        j->left = j->steps;
         j->t_start = s->now();
         s->slot_job[slot] = j->id;
         s->used += j->bytes;
@@ -223,22 +229,39 @@ int mdg_server_pump(mdg_server* s, int64_t max_steps, int* active, int* pending)
     int64_t most = 0;
     for (int k = 0; k < s->nslots; k++)
         if (s->slot_job[k] >= 0) {
-            int64_t left = 0;
-            mdg_get_remaining(s->ctx, k, &left);
+            // a resident job's budget is exactly its steps left: the host
+            // tracks it, the device counts it down
+            const int64_t left = s->jobs[s->slot_job[k]]->left;
             most = left > most ? left : most;
             nactive++;
         }
+    const double tb = s->now();
+    s->admit_s += tb - ta;
     int rstep = MDG_OK;
-    if (nactive && most > 0) rstep = mdg_step(s->ctx, most < max_steps ? most : max_steps);
-    // retirement
+    const int64_t adv = most < max_steps ? most : max_steps;
+    if (nactive && adv > 0) {
+        rstep = mdg_step(s->ctx, adv);
+        for (int k = 0; k < s->nslots; k++)
+            if (s->slot_job[k] >= 0) {
+                const Job* j = s->jobs[s->slot_job[k]].get();
+                s->particle_steps += (double)j->state.n * (double)(j->left < adv ? j->left : adv);
+            }
+        s->pumps++;
+    }
+    const double tc = s->now();
+    s->step_s += tc - tb;
+    // retirement: one read of every slot's budget and status
+    std::vector<int64_t> left(s->nslots, 0);
+    std::vector<int32_t> stw(s->nslots, 0);
+    if (nactive) {
+        const int r = mdg_get_progress(s->ctx, left.data(), stw.data(), nullptr);
+        if (r) return r;
+    }
     for (int k = 0; k < s->nslots; k++) {
         if (s->slot_job[k] < 0) continue;
-        int64_t left = 0;
-        mdg_get_remaining(s->ctx, k, &left);
-        int32_t stw = 0;
-        mdg_get_status(s->ctx, k, &stw);
-        const bool failed = stw != 0;
-        if (left != 0 && !failed) continue;
+        s->jobs[s->slot_job[k]]->left = left[k];
+        const bool failed = stw[k] != 0;
+        if (left[k] != 0 && !failed) continue;
         Job* j = s->jobs[s->slot_job[k]].get();
         j->state.alloc(j->state.n, j->cfg.kind == MDG_KIND_DEM);
         mdg_state_view v = j->state.view();
@@ -246,15 +269,57 @@ int mdg_server_pump(mdg_server* s, int64_t max_steps, int* active, int* pending)
         j->status = failed ? (rstep != MDG_OK ? rstep : MDG_ERR_STATE) : rd;
         j->t_end = s->now();
         s->finished.push_back(j->id);
+        s->retired++;
         s->used -= j->bytes;
         s->slot_job[k] = -1;
         mdg_set_remaining(s->ctx, k, 0);
         nactive--;
     }
+    s->retire_s += s->now() - tc;
     if (active) *active = nactive;
     if (pending) *pending = (int)s->pending.size();
     return (rstep == MDG_OK || rstep == MDG_ERR_OVERLAP_LIMIT || rstep == MDG_ERR_NAN ||
             rstep == MDG_ERR_LIST_OVERFLOW) ? MDG_OK : rstep;
+}
+
+int mdg_server_stats(mdg_server* s, mdg_server_stats_t* out) {
+    if (!s || !out) return MDG_ERR_ARG;
+    out->particle_steps = s->particle_steps;
+    out->pumps = s->pumps;
+    out->retired = s->retired;
+    int resident = 0;
+    for (int k = 0; k < s->nslots; k++) resident += s->slot_job[k] >= 0;
+    out->resident = resident;
+    out->pending = (int)s->pending.size();
+    out->hbm_used = s->used;
+    out->time_s = s->now();
+    out->admit_s = s->admit_s;
+    out->step_s = s->step_s;
+    out->retire_s = s->retire_s;
+    return MDG_OK;
+}
+
+int mdg_server_resident(mdg_server* s, mdg_job_info* out, int cap, int* n) {
+    if (!s || !n || (cap > 0 && !out)) return MDG_ERR_ARG;
+    int m = 0;
+    for (int k = 0; k < s->nslots; k++) {
+        if (s->slot_job[k] < 0) continue;
+        if (m < cap) {
+            const Job* j = s->jobs[s->slot_job[k]].get();
+            mdg_job_info& o = out[m];
+            o.id = j->id;
+            o.status = j->status;
+            o.slot = k;
+            o.steps = j->steps - j->left;  // steps done so far
+            o.n = (int64_t)j->state.n;
+            o.submit_s = j->t_submit;
+            o.start_s = j->t_start;
+            o.end_s = -1.0;
+        }
+        m++;
+    }
+    *n = m;
+    return MDG_OK;
 }
 
 int mdg_server_poll(mdg_server* s, mdg_job_info* out, int cap, int* n) {
