@@ -216,6 +216,44 @@ def _ref_serve_worker(args):
     return work, secs
 
 
+def _ref_ens_worker(args):
+    idx, budget = args
+    from mddem_gb300 import workloads as w
+
+    ens = w.ensemble(precision="fp64", policy="reference")
+    work = secs = 0.0
+    for k in idx:
+        if secs > budget:
+            break
+        cfg, st = ens[k]
+        n = len(st["tag"])
+        w_, s_ = _oracle_job(cfg, st, max(1, min(5000, int(4e6 // n))), budget - secs + 1.0)
+        work += w_
+        secs += s_
+    return work, secs
+
+
+def run_reference_ensemble(a):
+    import multiprocessing as mp
+
+    cores = os.cpu_count() or 1
+    parts = [list(range(c, 256, cores)) for c in range(cores)]
+    with mp.get_context("spawn").Pool(cores) as pool:
+        res = pool.map(_ref_ens_worker, [(p, 45.0) for p in parts if p])
+    val = sum(r[0] for r in res) / max(r[1] for r in res)
+    line = {
+        "impl": "reference", "metric": "particle-steps/s", "value": val, "unit": "particle-steps/s",
+        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": ENS_DESC, "precision": "fp64", "parallelism": f"{len(res)} host cores"},
+        "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": len(res), "kind": "port",
+                         "sample": f"the 256 replicas dealt round-robin to {len(res)} cores, each up to "
+                                   "4e6 particle-steps after 1 warm-up step, at most 45 s per core"},
+        "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference_serve(a):
     import multiprocessing as mp
 
@@ -248,6 +286,8 @@ def run_reference(a):
         return
     if a.workload == "serve":
         return run_reference_serve(a)
+    if a.workload == "ens256":
+        return run_reference_ensemble(a)
     import multiprocessing as mp
 
     desc, cfg, make = workload(a.workload)
@@ -550,6 +590,130 @@ def bench_serve(a, world, rank, local, dist):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# replica ensemble in one batch context
+# ---------------------------------------------------------------------------
+ENS_DESC = ("ensemble: 256 periodic granular-gas replicas, N log-uniform [500, 50000], solid fraction U[0.1,0.3], "
+            "restitution U[0.70,0.99], friction U[0,0.5], r = 1 mm, dt = 2.934e-7 s, one batch context")
+
+
+def bench_ensemble(a, world, rank, local, dist):
+    import numpy as np
+    import torch
+    from mddem_gb300 import build, capi, workloads as w
+
+    build.build()
+    ens = w.ensemble(precision=a.precision, policy=a.policy)
+    cfgs = [e[0] for e in ens]
+    sts = [e[1] for e in ens]
+    n = sum(len(s["tag"]) for s in sts)
+    ctx = capi.Context(cfgs, [len(s["tag"]) for s in sts])
+    for q, s in enumerate(sts):
+        ctx.upload(s, q)
+    tune = ctx.autotune(steps=20) if not a.no_tune else None
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    ctx.step(a.warmup)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = ctx.launches()
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        c0 = clk.mark()
+        e0.record(stream)
+        ctx.step(a.steps)  # one launch: a device-side loop over the K steps
+        e1.record(stream)
+        e1.synchronize()
+        c1 = clk.mark()
+    ms = e0.elapsed_time(e1)
+    l1 = ctx.launches()
+    if dist:
+        tt = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    line = {
+        "metric": "particle-steps/s", "value": world * n * a.steps / (ms / 1e3), "unit": "particle-steps/s",
+        "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if a.precision == "mixed" else "f64", "data": "synthetic",
+        "config": {"workload": ENS_DESC, "particles": n, "precision": a.precision, "rebuild_policy": a.policy,
+                   "autotune": tune, "l2": "inputs larger than L2 (1.5 GB of particle state)",
+                   "launch": "one CUDA-graph launch runs all K steps (device-side WHILE loop)",
+                   "parallelism": f"replicas x{world}"},
+        "gpu_launches": int(l1 - l0),
+        "clocks": clk.summary(c0, c1),
+    }
+    if rank == 0:
+        # per-kernel phases (eager launches, CUDA events) for the roofline
+        ctx.set_graph_mode(0)
+        t, _, _ = ctx.timed_steps(5, 0)
+        ctx.set_graph_mode(1)
+        contacts = sum(len(ctx.history(q)[0]) for q in range(len(sts))) / n
+        nfull = sum(2.0 * len(ctx.pairs(q)) for q in range(len(sts))) / n
+        cands = {"k_initial": (float(t[:, 1].mean()), n * INIT_BYTES[("dem", a.precision)]),
+                 "k_dem_" + a.precision: (float(t[:, 3].mean()), n * force_bytes("dem", nfull, contacts)),
+                 "k_final": (float(t[:, 4].mean()), n * FINAL_BYTES["dem"])}
+        name = max(cands, key=lambda q: cands[q][0])
+        kms, nbytes = cands[name]
+        peak, src = peak_hbm()
+        ach = nbytes / (kms / 1e3) / 1e9
+        line["roofline"] = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "unit": "GB/s",
+                            "frac": ach / peak, "peak_source": src, "traffic": ncu_traffic(name + "/ens256"),
+                            "algorithmic_bytes_per_launch": nbytes, "launch_ms": kms,
+                            "kernels_ms": {q: v[0] for q, v in cands.items()}}
+        if not a.no_e2e:
+            line["e2e"] = ensemble_e2e(cfgs, sts, a.steps)
+        line["plain_fp64_replica_by_replica"] = plain_replicas(cfgs, sts)
+        line["batched_vs_plain"] = line["value"] / world / line["plain_fp64_replica_by_replica"]["value"]
+        if not a.no_cpu_baseline:
+            import types
+
+            tr = [types.SimpleNamespace(n=len(s["tag"]), steps=5000, arrival=float(q)) for q, s in enumerate(sts)]
+            line["cpu_baseline"] = serve_cpu_sample(tr, list(zip(cfgs, sts)))
+            line["cpu_baseline"]["sample"] = line["cpu_baseline"]["sample"].replace("jobs of the stream", "replicas")
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def ensemble_e2e(cfgs, sts, steps):
+    """Upload of every replica from host arrays, K steps (one launch), thermo
+    read-back of every replica, download of every replica; wall clock."""
+    from mddem_gb300 import capi
+
+    ctx = capi.Context(cfgs, [len(s["tag"]) for s in sts])
+    for q, s in enumerate(sts):
+        ctx.upload(s, q)
+    ctx.step(3)
+    t0 = time.perf_counter()
+    up = down = 0
+    for q, s in enumerate(sts):
+        ctx.upload(s, q)
+        up += state_bytes(s)
+    ctx.step(steps)
+    for q in range(len(sts)):
+        ctx.thermo(q)
+        down += state_bytes(ctx.download(q)) + 8 * 16
+    el = time.perf_counter() - t0
+    ctx.close()
+    n = sum(len(s["tag"]) for s in sts)
+    return {"value": n * steps / el, "unit": "particle-steps/s", "h2d_bytes_per_step": up / steps,
+            "d2h_bytes_per_step": down / steps}
+
+
+def plain_replicas(cfgs, sts):
+    """Every replica on the plain FP64 path, one context each, one after
+    another (step time sampled over up to PLAIN_SAMPLE_STEPS steps, scaled to
+    the replicas' 5000 steps)."""
+    import types
+
+    tr = [types.SimpleNamespace(n=len(s["tag"]), steps=5000) for s in sts]
+    r = plain_job_by_job(tr, list(zip(cfgs, sts)))
+    r["sample"] = r["sample"].replace("each job's", "each replica's") + "; 5000 steps per replica"
+    return r
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -565,6 +729,7 @@ def main():
     ap.add_argument("--eager", action="store_true", help="launch kernels one by one (for profilers)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (ensemble)")
     a = ap.parse_args()
     a.warmup = max(3, a.warmup)
     if a.steps is None:
@@ -584,6 +749,8 @@ def main():
 
     if a.workload == "serve":
         return bench_serve(a, world, rank, local, dist)
+    if a.workload == "ens256":
+        return bench_ensemble(a, world, rank, local, dist)
     from mddem_gb300 import build, capi
 
     build.build()

@@ -153,6 +153,8 @@ typedef struct mdg_thermo_t {
     int64_t n;
     int32_t status;          /* sticky device status word for this system */
     int32_t max_neighbors;   /* largest full-list row seen at the last build */
+    double e_tail, p_tail;   /* LJ long-range tail corrections (setup_lj_tails,
+                                md_lj/src/lib.rs:397-445); 0 for DEM */
 } mdg_thermo_t;
 
 typedef struct mdg_ctx mdg_ctx;
@@ -197,6 +199,42 @@ int  mdg_step(mdg_ctx* ctx, int64_t nsteps);
  * inside one multi-step launch. */
 int  mdg_set_remaining(mdg_ctx* ctx, int sys, int64_t steps);
 int  mdg_get_remaining(mdg_ctx* ctx, int sys, int64_t* steps);
+/* A copy of system sys's current config (its materials pointer refers to the
+ * context's own copy, valid until the next mdg_configure_system of sys). */
+int  mdg_get_config(mdg_ctx* ctx, int sys, mdg_config* out);
+/* Lanes per particle row of the LJ force kernel (1, 2, 4 or 8), for the whole
+ * context; changes the per-particle summation order, not the physics. */
+int  mdg_set_threads_per_particle(mdg_ctx* ctx, int tpp);
+int  mdg_get_threads_per_particle(const mdg_ctx* ctx);
+
+/* ---- autotuner -----------------------------------------------------------------
+ * Picks, by timing short trial runs on the context's own systems, the LJ
+ * force kernel's threads per particle, and per particle kind (DEM, LJ) the
+ * skin fraction (the rebuild cadence: list cutoff 2 r skin, rebuild when a
+ * particle moved (skin - 1) r_min) and the bin size (a multiple of the list
+ * cutoff).  All three leave the physics unchanged: forces use the contact /
+ * LJ cutoff, not the list cutoff.  Call after uploading and before the first
+ * step: every trial restarts from the uploaded state (and contact history),
+ * and the call ends with that state uploaded again under the chosen
+ * parameters, so the simulation is exactly as uploaded.  Coordinate descent
+ * over the candidates; a trial's cost is its mean step time over `steps`
+ * graph-launched steps (extended until two rebuilds were seen, at most
+ * 8 x steps), plus the measured full-rebuild time over the trial's steps
+ * when no rebuild occurred in them. */
+typedef struct mdg_tune_opts {
+    int steps;              /* steps per trial (0 = 40) */
+    int tune_tpp, tune_skin, tune_bin;  /* 0 = keep that parameter */
+} mdg_tune_opts;
+typedef struct mdg_tune_result {
+    int tpp;
+    double skin_fraction[2];    /* [DEM, LJ] chosen (0 = kind absent) */
+    double bin_factor[2];       /* bin size / list cutoff chosen (>= 1: bins are
+                                   never smaller than the list cutoff) */
+    double ms_before, ms_after; /* modelled ms per step, first and chosen */
+    int trials;
+} mdg_tune_result;
+int  mdg_autotune(mdg_ctx* ctx, const mdg_tune_opts* opts, mdg_tune_result* out);
+
 /* The context's CUDA stream (cudaStream_t): all of the context's device work
  * is ordered on it, so a caller may record events on it or make its own
  * streams wait for it. */

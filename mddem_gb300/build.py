@@ -32,6 +32,7 @@ UNITS = [
     ("mdg_noalloc.cu", ["-fmad=false"]),
     ("mdg_serve.cpp", []),
     ("mdg_insert.cpp", []),
+    ("mdg_tune.cpp", []),
 ]
 
 

@@ -33,7 +33,8 @@ EXPORTS = [
     "mdg_get_remaining", "mdg_get_status", "mdg_configure_system", "mdg_server_create", "mdg_server_destroy",
     "mdg_server_submit", "mdg_server_pump", "mdg_server_poll", "mdg_server_fetch", "mdg_server_context",
     "mdg_rsa_spheres", "mdg_get_progress", "mdg_get_stream", "mdg_server_stats",
-    "mdg_server_resident",
+    "mdg_server_resident", "mdg_get_config", "mdg_set_threads_per_particle", "mdg_get_threads_per_particle",
+    "mdg_autotune",
 ]
 
 
@@ -84,7 +85,7 @@ class Thermo(C.Structure):
         ("ke", C.c_double), ("pe", C.c_double), ("temp", C.c_double), ("p_xi", C.c_double),
         ("granular_temp", C.c_double), ("momentum", C.c_double), ("virial", C.c_double * 6),
         ("step", C.c_int64), ("nbuilds", C.c_int64), ("n", C.c_int64), ("status", C.c_int32),
-        ("max_neighbors", C.c_int32),
+        ("max_neighbors", C.c_int32), ("e_tail", C.c_double), ("p_tail", C.c_double),
     ]
 
 
@@ -97,6 +98,15 @@ class ServerStats(C.Structure):
     _fields_ = [("particle_steps", C.c_double), ("pumps", C.c_int64), ("retired", C.c_int64),
                 ("resident", C.c_int32), ("pending", C.c_int32), ("hbm_used", C.c_size_t), ("time_s", C.c_double),
                 ("admit_s", C.c_double), ("step_s", C.c_double), ("retire_s", C.c_double)]
+
+
+class TuneOpts(C.Structure):
+    _fields_ = [("steps", C.c_int), ("tune_tpp", C.c_int), ("tune_skin", C.c_int), ("tune_bin", C.c_int)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("tpp", C.c_int), ("skin_fraction", C.c_double * 2), ("bin_factor", C.c_double * 2),
+                ("ms_before", C.c_double), ("ms_after", C.c_double), ("trials", C.c_int)]
 
 
 class StepTiming(C.Structure):
@@ -154,6 +164,9 @@ def load(path: str = LIB_PATH):
     lib.mdg_server_fetch.argtypes = [C.c_void_p, C.c_int64, C.POINTER(StateView)]
     lib.mdg_server_context.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
     lib.mdg_get_progress.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
+    lib.mdg_set_threads_per_particle.argtypes = [C.c_void_p, C.c_int]
+    lib.mdg_get_threads_per_particle.argtypes = [C.c_void_p]
+    lib.mdg_autotune.argtypes = [C.c_void_p, C.POINTER(TuneOpts), C.POINTER(TuneResult)]
     lib.mdg_server_resident.argtypes = [C.c_void_p, C.POINTER(JobInfo), C.c_int, C.POINTER(C.c_int)]
     lib.mdg_server_stats.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
     lib.mdg_get_stream.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
@@ -504,6 +517,20 @@ class Context:
         v = C.c_int32()
         _check(self.lib.mdg_get_status(self.h, sys, C.byref(v)), "mdg_get_status")
         return v.value
+
+    def autotune(self, steps=40, tpp=True, skin=True, bins=True):
+        """mdg_autotune: pick threads per particle, skin fraction and bin size
+        by trial runs; call after upload, before the first step."""
+        o = TuneOpts(steps, int(tpp), int(skin), int(bins))
+        r = TuneResult()
+        _check(self.lib.mdg_autotune(self.h, C.byref(o), C.byref(r)), "mdg_autotune")
+        return {"tpp": r.tpp, "skin_fraction": list(r.skin_fraction), "bin_factor": list(r.bin_factor),
+                "ms_before": r.ms_before, "ms_after": r.ms_after, "trials": r.trials}
+
+    def threads_per_particle(self, tpp=None):
+        if tpp is not None:
+            _check(self.lib.mdg_set_threads_per_particle(self.h, int(tpp)), "mdg_set_threads_per_particle")
+        return int(self.lib.mdg_get_threads_per_particle(self.h))
 
     def stream(self):
         """The context's CUDA stream handle (as an int), for events and

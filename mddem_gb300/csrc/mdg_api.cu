@@ -1170,6 +1170,23 @@ int mdg_set_remaining(mdg_ctx* c, int sys, int64_t steps) {
     return cuda_err(e);
 }
 
+int mdg_get_config(mdg_ctx* c, int sys, mdg_config* out) {
+    if (!c || !out || sys < 0 || sys >= c->nsys) return MDG_ERR_ARG;
+    *out = c->cfg[sys];
+    return MDG_OK;
+}
+
+int mdg_set_threads_per_particle(mdg_ctx* c, int tpp) {
+    if (!c || !(tpp == 1 || tpp == 2 || tpp == 4 || tpp == 8)) return MDG_ERR_ARG;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(e);
+    if (c->tpp_lj != tpp) c->drop_graphs();
+    c->tpp_lj = tpp;
+    return MDG_OK;
+}
+
+int mdg_get_threads_per_particle(const mdg_ctx* c) { return c ? c->tpp_lj : 0; }
+
 int mdg_get_stream(mdg_ctx* c, void** stream) {
     if (!c || !stream) return MDG_ERR_ARG;
     *stream = (void*)c->stream;
@@ -1252,6 +1269,23 @@ int mdg_thermo(mdg_ctx* c, int sys, mdg_thermo_t* out) {
     out->n = p.n;
     out->status = ss.status;
     out->max_neighbors = ss.max_nbr;
+    out->e_tail = out->p_tail = 0.0;
+    if (p.kind == MDG_KIND_LJ) {
+        // setup_lj_tails (md_lj/src/lib.rs:397-445), one type: rho = N / V,
+        // V = the product of the box sides, rc = sqrt((cutoff sigma)^2)
+        const mdg_config& k = c->cfg[sys];
+        const double n = (double)p.n;
+        const double rho = n / (p.L[0] * p.L[1] * p.L[2]);
+        const double cs = k.lj_cutoff * k.lj_sigma;
+        const double rc = std::sqrt(cs * cs);
+        const double sigma3 = (k.lj_sigma * k.lj_sigma) * k.lj_sigma;
+        const double rc3 = (rc * rc) * rc, rc9 = (rc3 * rc3) * rc3;
+        const double sigma9 = (sigma3 * sigma3) * sigma3;
+        const double pi = 3.141592653589793;
+        out->e_tail = (8.0 / 3.0) * pi * n * rho * k.lj_epsilon * sigma3 * (sigma9 / (3.0 * rc9) - sigma3 / rc3);
+        out->p_tail =
+            (16.0 / 3.0) * pi * rho * rho * k.lj_epsilon * sigma3 * (2.0 * sigma9 / (3.0 * rc9) - sigma3 / rc3);
+    }
     return cuda_err(cudaGetLastError());
 }
 

@@ -1243,4 +1243,27 @@ int orc_thermo(void* h, double* out) {
 
 long orc_overlap_count(void* h) { return static_cast<Sim*>(h)->overlap_total; }
 
+// setup_lj_tails (md_lj/src/lib.rs:397-445), single type: rho = N / V with
+// V = size_x size_y size_z (domain.rs:153); rc = sqrt((cutoff sigma)^2);
+// powi(3) as (x x) x.
+int orc_lj_tails(void* h, double* e_tail, double* p_tail) {
+    Sim* s = static_cast<Sim*>(h);
+    const double n = (double)s->nlocal;
+    const double v = s->size[0] * s->size[1] * s->size[2];
+    const double rho = n / v;
+    const double eps = s->cfg.lj_epsilon, sig = s->cfg.lj_sigma;
+    const double cs = s->cfg.lj_cutoff * sig;
+    const double rc = std::sqrt(cs * cs);
+    const double sigma3 = (sig * sig) * sig;
+    const double rc3 = (rc * rc) * rc;
+    const double rc9 = (rc3 * rc3) * rc3;
+    const double sigma6 = sigma3 * sigma3;
+    const double sigma9 = sigma6 * sigma3;
+    const double w = 1.0 * 1.0;
+    const double PI = 3.141592653589793;
+    *e_tail = 0.0 + w * (8.0 / 3.0) * PI * n * rho * eps * sigma3 * (sigma9 / (3.0 * rc9) - sigma3 / rc3);
+    *p_tail = 0.0 + w * (16.0 / 3.0) * PI * rho * rho * eps * sigma3 * (2.0 * sigma9 / (3.0 * rc9) - sigma3 / rc3);
+    return 0;
+}
+
 }  // extern "C"

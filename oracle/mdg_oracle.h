@@ -85,6 +85,8 @@ int    orc_set_history(void* h, size_t n, const uint32_t* keys, const double* va
  *          vxx, vyy, vzz, vxy, vxz, vyz, nbuilds, step, ndof, q_mass] */
 int    orc_thermo(void* h, double* out16);
 long   orc_overlap_count(void* h);
+/* LJ long-range tail corrections E_tail, P_tail (single type). */
+int    orc_lj_tails(void* h, double* e_tail, double* p_tail);
 
 #ifdef __cplusplus
 }

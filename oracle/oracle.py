@@ -214,5 +214,10 @@ class Oracle:
         d["step"] = int(out[13])
         return d
 
+    def lj_tails(self):
+        e, p = C.c_double(), C.c_double()
+        self.lib.orc_lj_tails(self.h, C.byref(e), C.byref(p))
+        return e.value, p.value
+
     def overlaps(self):
         return int(self.lib.orc_overlap_count(self.h))

@@ -182,3 +182,33 @@ def test_csv_roundtrip(tmp_path):
     b = inputs.read_csv(p)
     for k in ("pos", "vel", "radius", "mass", "inv_inertia"):
         assert np.array_equal(a[k], b[k]), k
+
+
+def test_rsa_spheres_seeded_and_non_overlapping(lib):
+    """mdg_rsa_spheres: same seed, same spheres; every pair under the minimum
+    image keeps sep_factor * (r_i + r_j); radii within [rmin, rmax]; centres
+    inset by rmax."""
+    from mddem_gb300 import capi
+
+    L = 0.03
+    a = capi.rsa_spheres(1500, (0, 0, 0), (L, L, L), 0.8e-3, 1.2e-3, sep_factor=1.1, seed=7)
+    b = capi.rsa_spheres(1500, (0, 0, 0), (L, L, L), 0.8e-3, 1.2e-3, sep_factor=1.1, seed=7)
+    c = capi.rsa_spheres(1500, (0, 0, 0), (L, L, L), 0.8e-3, 1.2e-3, sep_factor=1.1, seed=8)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert not np.array_equal(a[0], c[0])
+    pos, rad = a
+    assert rad.min() >= 0.8e-3 and rad.max() <= 1.2e-3
+    assert pos.min() >= 1.2e-3 and pos.max() <= L - 1.2e-3
+    d = pos[:, None, :] - pos[None, :, :]
+    d -= L * np.round(d / L)
+    r = np.sqrt(np.einsum("ijk,ijk->ij", d, d))
+    np.fill_diagonal(r, np.inf)
+    assert np.all(r > 1.1 * (rad[:, None] + rad[None, :]))
+
+
+def test_rsa_spheres_reports_unplaceable(lib):
+    from mddem_gb300 import capi
+
+    with pytest.raises(capi.MdgError):  # solid fraction far above the RSA limit
+        capi.rsa_spheres(5000, (0, 0, 0), (0.02, 0.02, 0.02), 1e-3, 1e-3, sep_factor=1.0, seed=1,
+                         max_attempts=200000)

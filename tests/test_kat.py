@@ -255,3 +255,32 @@ def test_lj_sign_cutoff_and_newton3(backend):
     f, s = two(0.9, virial=True)
     v = s.thermo()["virial"]
     assert v[0] + v[1] + v[2] < 0
+
+
+def test_lj_tail_corrections(backend):
+    """setup_lj_tails (md_lj/src/lib.rs:397-445): E_tail = 8/3 pi N rho eps
+    sigma^3 [sigma^9/(3 rc^9) - sigma^3/rc^3], P_tail = 16/3 pi rho^2 eps
+    sigma^3 [2 sigma^9/(3 rc^9) - sigma^3/rc^3], rho = N / V; both negative
+    for rc = 2.5 sigma."""
+    from mddem_gb300 import config, inputs
+
+    cfg = config.lj_fluid_config(box=10.06)
+    st = inputs.lj_fcc(6, 10.06, 0.85, 0.85, seed=1)
+    s = Sim(backend, cfg, st)
+    if backend == "oracle":
+        e, p = s.o.lj_tails()
+    else:
+        t = s.thermo()
+        e, p = t["e_tail"], t["p_tail"]
+    n, rho, rc = 864.0, 864.0 / 10.06 ** 3, 2.5
+    e_ref = 8.0 / 3.0 * math.pi * n * rho * (1.0 / (3.0 * rc ** 9) - 1.0 / rc ** 3)
+    p_ref = 16.0 / 3.0 * math.pi * rho * rho * (2.0 / (3.0 * rc ** 9) - 1.0 / rc ** 3)
+    assert e < 0 and p < 0
+    assert abs(e - e_ref) <= 1e-13 * abs(e_ref)
+    assert abs(p - p_ref) <= 1e-13 * abs(p_ref)
+    if backend == "gpu":
+        from oracle.oracle import Oracle
+
+        o = Oracle(cfg)
+        o.load(st)
+        assert (e, p) == o.lj_tails()  # same formula, same operation order
