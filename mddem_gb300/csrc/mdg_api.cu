@@ -460,7 +460,7 @@ int launch_force(mdg_ctx* c, const Dev& d, cudaStream_t st) {
 
 int enqueue_step(mdg_ctx* c, cudaStream_t st) {
     int n = 0;
-    n += launch_initial(c->d, st);
+    n += c->has_mixed ? launch_initial_mixed(c->d, st) : launch_initial(c->d, st);
     n += launch_rebuild(c->d, st);
     n += launch_force(c, c->d, st);
     n += launch_final(c->d, st, 1);
@@ -484,7 +484,7 @@ int capture_step(mdg_ctx* c, cudaEvent_t* ev, int* nk) {
     d.use_cond = 1;
     int n = 0;
     if (ev) cudaEventRecordWithFlags(ev[0], c->stream, cudaEventRecordExternal);
-    n += launch_initial(d, c->stream);
+    n += c->has_mixed ? launch_initial_mixed(d, c->stream) : launch_initial(d, c->stream);
     if (ev) cudaEventRecordWithFlags(ev[1], c->stream, cudaEventRecordExternal);
     const cudaGraphNode_t* deps = nullptr;
     size_t nd = 0;
@@ -1332,7 +1332,7 @@ int mdg_timed_steps(mdg_ctx* c, int64_t nsteps, size_t l2_flush_bytes, mdg_step_
             cudaStream_t st = c->stream;
             int n = 0;
             cudaEventRecord(c->tev[0], st);
-            n += launch_initial(c->d, st);
+            n += c->has_mixed ? launch_initial_mixed(c->d, st) : launch_initial(c->d, st);
             cudaEventRecord(c->tev[1], st);
             n += launch_rebuild(c->d, st);
             cudaEventRecord(c->tev[2], st);

@@ -224,6 +224,7 @@ __device__ __forceinline__ void two_float_add(float& hi, float& lo, float t) {
 // ---- kernel launchers (mdg_kernels_fp64.cu / mdg_kernels_mixed.cu) ----------
 // Each returns the number of kernels it launched on `st`.
 int launch_initial(const Dev& d, cudaStream_t st);
+int launch_initial_mixed(const Dev& d, cudaStream_t st);
 int launch_rebuild(const Dev& d, cudaStream_t st);
 int launch_force_fp64(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st);
 int launch_force_mixed(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st);

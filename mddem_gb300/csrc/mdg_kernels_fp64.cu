@@ -1303,7 +1303,8 @@ __global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
             }
             d.vel[i] = v;
         }
-        vals[0] = d.mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z);
+        // KE feeds only the thermostat (thermo output has its own reduction)
+        if (sp.nh) vals[0] = d.mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z);
         if (sp.kind == 0 && integrate) {
             double4 w = d.omg[i];
             if (w.w != 0.0) {
@@ -1316,12 +1317,11 @@ __global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
         }
         if (sp.virial)
             for (int q = 0; q < 6; q++) vals[1 + q] = d.vir[q * d.P + i];
-        // non-finite test on the exponent bits (integer ops only)
-        const double4 x = d.pos[i];
+        // non-finite test on the exponent bits of v (integer ops only): a
+        // non-finite force or position shows in v by the next step
         const int ex = 0x7ff00000;
         bad = ((__double2hiint(v.x) & ex) == ex) | ((__double2hiint(v.y) & ex) == ex) |
-              ((__double2hiint(v.z) & ex) == ex) | ((__double2hiint(x.x) & ex) == ex) |
-              ((__double2hiint(x.y) & ex) == ex) | ((__double2hiint(x.z) & ex) == ex);
+              ((__double2hiint(v.z) & ex) == ex);
     }
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&st->status, ST_NAN);
     double out[8];
@@ -1378,7 +1378,8 @@ __global__ void __launch_bounds__(BLK) k_ke_init(Dev d) {
     if (li < sp.n) {
         const long long i = (long long)sp.p0 + li;
         const double4 v = d.vel[i];
-        vals[0] = d.mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z);
+        // KE feeds only the thermostat (thermo output has its own reduction)
+        if (sp.nh) vals[0] = d.mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z);
     }
     double out[1];
     if (system_reduce<1>(d, s, gb, vals, out) && threadIdx.x == 0) {

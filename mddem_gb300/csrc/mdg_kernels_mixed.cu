@@ -405,12 +405,18 @@ __global__ void __launch_bounds__(BLK) k_dem_mixed(Dev d) {
     if (li >= sp.n) return;
     const long long i = (long long)sp.p0 + li;
     const int hn = hcur ^ 1;
+    const int nn = d.nnum[i];
+    if (nn == 0) {  // no listed partner (most particles of a dilute gas)
+        d.hcnt[hn][i] = 0;
+        d.frc[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+        d.trq[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+        return;
+    }
     const float4 hi = d.pos2[2 * i], lo = d.pos2[2 * i + 1];
     const double4 vi = d.vel[i];
     const double4 wi = d.omg[i];
     const int ti_ = (int)d.type[i];
     const uint32_t tag_i = d.tag[i];
-    const int nn = d.nnum[i];
     const long long base = sp.lst0 + li;
     Kahan3 F, T;
     int nh = 0, nover = 0;
@@ -470,6 +476,128 @@ __global__ void __launch_bounds__(BLK) k_dem_mixed(Dev d) {
     if (nover) atomicAdd(&st->overlap, nover);
     d.frc[i] = make_double4(F.x.value(), F.y.value(), F.z.value(), 0.0);
     d.trq[i] = make_double4(T.x.value(), T.y.value(), T.z.value(), 0.0);
+}
+
+// Initial integration of the mixed path: the same update as k_initial (NH
+// scale, half kick, drift, two-float drift copy, fp32 rebuild test, half
+// spin kick, quaternion update) with FP64 kept for x, v, omega and q, FMA
+// contraction, and the rotation increment of initial_rotation
+// (rotational.rs:59-84) formed in FP32: |omega|, sin and cos of the half angle
+// are fp32, cos as 1 - 2 sin^2(angle/4) so its tiny deviation from 1 keeps
+// full relative precision, and the Hamilton product dq * q runs in FP64.  Per
+// step this perturbs q by about 1e-7 x angle/2 (angle = |omega| dt).
+__global__ void __launch_bounds__(BLK) k_initial_mixed(Dev d) {
+    const int gb = d.blk_run[blockIdx.x];
+    const int s = d.blk_sys[gb];
+    const SysParams& sp = d.sp[s];
+    SysState* st = d.ss + s;
+    const int li = (gb - sp.b0) * BLK + threadIdx.x;
+    const bool live = sys_active(st);
+    const bool act = live && li < sp.n;
+    const long long i = (long long)sp.p0 + li;
+    const double dt = sp.dt;
+    const double scale = sp.nh ? st->nh_scale : 1.0;
+    if (li == 0 && live)
+        st->periodic_sort =
+            (sp.policy == 0 && sp.sort_every > 0 && st->sort_counter + 1 >= sp.sort_every) ? 1 : 0;
+    const int already = *((const volatile int*)&st->rebuild);
+    int need = 0;
+    if (act) {
+        double4 v = d.vel[i];
+        const double4 f = d.frc[i];
+        double4 x = d.pos[i];
+        if (sp.nh) {
+            v.x *= scale;
+            v.y *= scale;
+            v.z *= scale;
+        }
+        const double h = 0.5 * dt * v.w;
+        v.x = fma(h, f.x, v.x);
+        v.y = fma(h, f.y, v.y);
+        v.z = fma(h, f.z, v.z);
+        const double tx = v.x * dt, ty = v.y * dt, tz = v.z * dt;
+        x.x += tx;
+        x.y += ty;
+        x.z += tz;
+        d.vel[i] = v;
+        d.pos[i] = x;
+        float4 ph = d.pos2[2 * i], pl = d.pos2[2 * i + 1];
+        two_float_add(ph.x, pl.x, (float)tx);
+        two_float_add(ph.y, pl.y, (float)ty);
+        two_float_add(ph.z, pl.z, (float)tz);
+        d.pos2[2 * i] = ph;
+        d.pos2[2 * i + 1] = pl;
+        if (!already) {
+            const float4 bh = d.lbp2[2 * i], bl = d.lbp2[2 * i + 1];
+            const float dx = (ph.x - bh.x) + (pl.x - bl.x);
+            const float dy = (ph.y - bh.y) + (pl.y - bl.y);
+            const float dz = (ph.z - bh.z) + (pl.z - bl.z);
+            bool nd = dx * dx + dy * dy + dz * dz > sp.disp_thr2f;
+            if (sp.every > 0) nd = (sp.check && nd) || st->steps_since_build >= sp.every;
+            if (!nd && sp.policy == 0) {
+                const float rx = ph.x + pl.x, ry = ph.y + pl.y, rz = ph.z + pl.z;
+                nd = rx < 0.f || rx >= sp.Lh[0] || ry < 0.f || ry >= sp.Lh[1] || rz < 0.f || rz >= sp.Lh[2];
+            }
+            need = nd;
+        }
+        if (sp.kind == 0) {
+            double4 w = d.omg[i];
+            if (w.w != 0.0) {
+                const double4 tq = d.trq[i];
+                const double hw = 0.5 * dt * w.w;
+                w.x = fma(hw, tq.x, w.x);
+                w.y = fma(hw, tq.y, w.y);
+                w.z = fma(hw, tq.z, w.z);
+                const float wx = (float)w.x, wy = (float)w.y, wz = (float)w.z;
+                const float om = sqrtf(wx * wx + wy * wy + wz * wz);
+                const float angle = om * (float)dt;
+                if (angle > 1e-14f) {
+                    const float half = 0.5f * angle;
+                    const float sq = sinf(0.5f * half);
+                    const double c1 = (double)(-2.f * sq * sq);  // cos(half) - 1
+                    const float k = sinf(half) / om;
+                    const double a1 = (double)(wx * k), a2 = (double)(wy * k), a3 = (double)(wz * k);
+                    const double4 q = d.quat[i];
+                    double4 r;  // (1 + c1, a) * q, Hamilton product (rotational.rs:34-41)
+                    r.x = fma(c1, q.x, q.x) - (a1 * q.y + a2 * q.z + a3 * q.w);
+                    r.y = fma(c1, q.y, q.y) + (a1 * q.x + a2 * q.w - a3 * q.z);
+                    r.z = fma(c1, q.z, q.z) + (a2 * q.x + a3 * q.y - a1 * q.w);
+                    r.w = fma(c1, q.w, q.w) + (a3 * q.x + a1 * q.z - a2 * q.y);
+                    d.quat[i] = r;
+                }
+                d.omg[i] = w;
+            }
+        }
+    }
+    if (__any_sync(0xffffffffu, need) && (threadIdx.x & 31) == 0) atomicOr(&st->rebuild, 1);
+    if (d.use_cond) {
+        // grid-wide last block: open the rebuild branch of the step graph only
+        // when some running system rebuilds or sorts
+        __shared__ int last;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            last = atomicAdd(d.grid_ctr, 1u) == (unsigned)(gridDim.x - 1);
+        }
+        __syncthreads();
+        if (last && threadIdx.x == 0) {
+            __threadfence();
+            unsigned int any = 0;
+            for (int q = 0; q < d.nrun_sys; q++) {
+                const SysState* o = d.ss + d.run_sys[q];
+                if (sys_active(o))
+                    any |= (unsigned)(*((const volatile int*)&o->rebuild) | *((const volatile int*)&o->periodic_sort));
+            }
+            *d.grid_ctr = 0;
+            if (any) d.stat_ctr[0] += 1;
+            cudaGraphSetConditional((cudaGraphConditionalHandle)d.cond, any ? 1u : 0u);
+        }
+    }
+}
+
+int launch_initial_mixed(const Dev& d, cudaStream_t st) {
+    k_initial_mixed<<<d.nrun, BLK, 0, st>>>(d);
+    return 1;
 }
 
 int launch_force_mixed(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st) {

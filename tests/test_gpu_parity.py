@@ -261,8 +261,29 @@ def test_mixed_dem_trajectory_close_to_fp64(gpu_lib):
     b = _ctx(_dem_cfg(precision="mixed"), st)
     a.step(100)
     b.step(100)
-    (pa,) = by_tag(a.download(), "pos")
-    (pb,) = by_tag(b.download(), "pos")
+    pa, qa, wa = by_tag(a.download(), "pos", "quat", "omega")
+    pb, qb, wb = by_tag(b.download(), "pos", "quat", "omega")
     assert np.max(np.abs(pa - pb)) <= 1e-9 * 0.012
+    # fp32 rotation increment: about 1e-7 x angle/2 per step on q
+    assert np.max(np.abs(qa - qb)) <= 1e-8
+    assert np.max(np.abs(wa - wb)) <= 1e-5 * np.max(np.abs(wa))
     ta, tb = a.thermo(), b.thermo()
     assert abs(ta["ke"] - tb["ke"]) <= 1e-5 * ta["ke"]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_non_finite_state_reports_nan(gpu_lib, precision):
+    """Two LJ atoms at the same point: r = 0 makes the pair force non-finite;
+    the step returns MDG_ERR_NAN and the system's status word keeps the bit."""
+    from mddem_gb300 import capi, config
+
+    st = {"tag": np.arange(3, dtype=np.uint32), "type": np.zeros(3, np.uint32),
+          "pos": np.array([[5.0, 5.0, 5.0], [5.0, 5.0, 5.0], [7.0, 7.0, 7.0]]), "vel": np.zeros((3, 3)),
+          "mass": np.ones(3), "cutoff_radius": np.full(3, 1.25)}
+    cfg = config.lj_fluid_config(box=12.0, nose_hoover=False, precision=precision)
+    ctx = capi.Context(cfg, 3)
+    ctx.upload(st)
+    with pytest.raises(capi.MdgError) as e:
+        ctx.step(2)
+    assert e.value.status == 6  # MDG_ERR_NAN
+    assert ctx.status() != 0
