@@ -453,6 +453,16 @@ void advance_budgets(mdg_ctx* c, int64_t n) {
         if (c->rem_host[s] > 0) c->rem_host[s] = c->rem_host[s] > n ? c->rem_host[s] - n : 0;
 }
 
+// Rebuild pipeline (+ the mixed DEM worklist) and final kernel of the
+// context's precision.
+int launch_rb(mdg_ctx* c, const Dev& d, cudaStream_t st) {
+    return launch_rebuild(d, st) + (c->has_mixed ? launch_rebuild_tail_mixed(d, c->has_dem, st) : 0);
+}
+int rb_kernels(const mdg_ctx* c) { return 8 + (c->has_mixed && c->has_dem ? 1 : 0); }
+int launch_fin(mdg_ctx* c, const Dev& d, cudaStream_t st, int integrate) {
+    return c->has_mixed ? launch_final_mixed(d, st, integrate) : launch_final(d, st, integrate);
+}
+
 int launch_force(mdg_ctx* c, const Dev& d, cudaStream_t st) {
     if (c->has_mixed) return launch_force_mixed(d, c->has_lj, c->has_dem, c->tpp_lj, st);
     return launch_force_fp64(d, c->has_lj, c->has_dem, c->tpp_lj, st);
@@ -461,9 +471,9 @@ int launch_force(mdg_ctx* c, const Dev& d, cudaStream_t st) {
 int enqueue_step(mdg_ctx* c, cudaStream_t st) {
     int n = 0;
     n += c->has_mixed ? launch_initial_mixed(c->d, st) : launch_initial(c->d, st);
-    n += launch_rebuild(c->d, st);
+    n += launch_rb(c, c->d, st);
     n += launch_force(c, c->d, st);
-    n += launch_final(c->d, st, 1);
+    n += launch_fin(c, c->d, st, 1);
     return n;
 }
 
@@ -503,14 +513,14 @@ int capture_step(mdg_ctx* c, cudaEvent_t* ev, int* nk) {
     if (e != cudaSuccess) return cuda_err(e);
     e = cudaStreamBeginCaptureToGraph(c->stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_err(e);
-    n += launch_rebuild(d, c->stream2);
+    n += launch_rb(c, d, c->stream2);
     cudaGraph_t body_out = nullptr;
     e = cudaStreamEndCapture(c->stream2, &body_out);
     if (e != cudaSuccess) return cuda_err(e);
     if (ev) cudaEventRecordWithFlags(ev[2], c->stream, cudaEventRecordExternal);
     n += launch_force(c, d, c->stream);
     if (ev) cudaEventRecordWithFlags(ev[3], c->stream, cudaEventRecordExternal);
-    n += launch_final(d, c->stream, 1);
+    n += launch_fin(c, d, c->stream, 1);
     if (ev) cudaEventRecordWithFlags(ev[4], c->stream, cudaEventRecordExternal);
     if (nk) *nk = n;
     return MDG_OK;
@@ -780,6 +790,10 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     d.rb_poff = c->alloc<int>(nsys + 1, err);
     d.rb_coff = c->alloc<int>(nsys + 1, err);
     d.rb_n = c->alloc<int>(1, err);
+    if (c->has_mixed && c->has_dem) {
+        d.dem_wl = c->alloc<int>(P, err);
+        d.dem_wl_n = c->alloc<int>(nsys, err);
+    }
     c->d_cblk0 = c->alloc<int>(nsys, err);
     c->d_sp = c->alloc<SysParams>(nsys, err);
     d.ss = c->alloc<SysState>(nsys, err);
@@ -1122,9 +1136,9 @@ int mdg_step(mdg_ctx* c, int64_t nsteps) {
     cudaMemcpy(&rb1, c->d.stat_ctr, sizeof(rb1), cudaMemcpyDeviceToHost);
     advance_budgets(c, nsteps);
     // kernels that ran: per step initial + force + final (+ loop control),
-    // plus the eight rebuild kernels on the steps whose rebuild branch opened
+    // plus the rebuild kernels on the steps whose rebuild branch opened
     const long long base = 3 + (c->has_lj && c->has_dem ? 1 : 0) + (c->graph_mode ? 1 : 0);
-    c->launches += nsteps * base + 8LL * (long long)(c->graph_mode ? (rb1 - rb0) : nsteps);
+    c->launches += nsteps * base + (long long)rb_kernels(c) * (long long)(c->graph_mode ? (rb1 - rb0) : nsteps);
     return check_status(c);
 }
 
@@ -1139,9 +1153,9 @@ int mdg_force_only(mdg_ctx* c) {
     for (auto& x : ss) x.rebuild = 1;
     cudaMemcpy(c->d.ss, ss.data(), c->nsys * sizeof(SysState), cudaMemcpyHostToDevice);
     cudaStream_t st = c->stream;
-    c->launches += launch_rebuild(c->d, st);
+    c->launches += launch_rb(c, c->d, st);
     c->launches += launch_force(c, c->d, st);
-    c->launches += launch_final(c->d, st, 0);  // reductions + bookkeeping, no integration
+    c->launches += launch_fin(c, c->d, st, 0);  // reductions + bookkeeping, no integration
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_err(e);
     e = cudaGetLastError();
@@ -1334,11 +1348,11 @@ int mdg_timed_steps(mdg_ctx* c, int64_t nsteps, size_t l2_flush_bytes, mdg_step_
             cudaEventRecord(c->tev[0], st);
             n += c->has_mixed ? launch_initial_mixed(c->d, st) : launch_initial(c->d, st);
             cudaEventRecord(c->tev[1], st);
-            n += launch_rebuild(c->d, st);
+            n += launch_rb(c, c->d, st);
             cudaEventRecord(c->tev[2], st);
             n += launch_force(c, c->d, st);
             cudaEventRecord(c->tev[3], st);
-            n += launch_final(c->d, st, 1);
+            n += launch_fin(c, c->d, st, 1);
             cudaEventRecord(c->tev[4], st);
             c->tkernels = n;
         }
@@ -1354,8 +1368,8 @@ int mdg_timed_steps(mdg_ctx* c, int64_t nsteps, size_t l2_flush_bytes, mdg_step_
         int rb = 0;
         for (int s : c->run_sys) rb |= (ss[s].steps_since_build == 0);
         out[k].rebuilt = rb;
-        // the 8 rebuild-pipeline kernels run only when the conditional opened
-        out[k].kernels = c->tkernels - ((rb || !c->graph_mode) ? 0 : 8);
+        // the rebuild-pipeline kernels run only when the conditional opened
+        out[k].kernels = c->tkernels - ((rb || !c->graph_mode) ? 0 : rb_kernels(c));
         c->launches += out[k].kernels;
     }
     advance_budgets(c, nsteps);

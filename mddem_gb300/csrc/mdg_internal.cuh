@@ -174,6 +174,11 @@ struct Dev {
     int* rb_poff;
     int* rb_coff;
     int* rb_n;
+    // Mixed DEM contexts: per system, the particles that have list partners
+    // (indices within the system, at the system's particle offset), built at
+    // each rebuild; the force kernel visits only these.
+    int* dem_wl;
+    int* dem_wl_n;
     const SysParams* sp;
     SysState* ss;
     const double* mat;
@@ -223,8 +228,166 @@ __device__ __forceinline__ void two_float_add(float& hi, float& lo, float t) {
 
 // ---- kernel launchers (mdg_kernels_fp64.cu / mdg_kernels_mixed.cu) ----------
 // Each returns the number of kernels it launched on `st`.
+// Per-system reduction of NV doubles.  Every block of the system (gb = its
+// global particle block id) contributes a partial; the last block to arrive sums the partials with a fixed order
+// (strided lanes, then a fixed tree) so the result is deterministic.  Returns
+// true on the last block (all threads), totals valid in out[] on thread 0.
+// Every block of the system must be in the launch.
+template <int NV>
+__device__ bool system_reduce(const Dev& d, int s, int gb, const double (&v)[NV], double (&out)[NV]) {
+    static_assert(NV <= 8, "blkpart holds 8 doubles per block");
+    __shared__ double sh[NV][BLK];
+    __shared__ int last;
+    const SysParams& sp = d.sp[s];
+    const int t = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < NV; k++) sh[k][t] = v[k];
+    __syncthreads();
+    for (int w = BLK / 2; w > 0; w >>= 1) {
+        if (t < w) {
+#pragma unroll
+            for (int k = 0; k < NV; k++) sh[k][t] = sh[k][t] + sh[k][t + w];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) d.blkpart[(size_t)gb * 8 + k] = sh[k][0];
+        __threadfence();
+        unsigned int prev = atomicAdd(&d.ss[s].red_count, 1u);
+        last = (prev == (unsigned)(sp.nb - 1)) ? 1 : 0;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; k++) acc[k] = 0.0;
+    for (int b = t; b < sp.nb; b += BLK) {
+        const volatile double* p = d.blkpart + (size_t)(sp.b0 + b) * 8;
+#pragma unroll
+        for (int k = 0; k < NV; k++) acc[k] = acc[k] + p[k];
+    }
+#pragma unroll
+    for (int k = 0; k < NV; k++) sh[k][t] = acc[k];
+    __syncthreads();
+    for (int w = BLK / 2; w > 0; w >>= 1) {
+        if (t < w) {
+#pragma unroll
+            for (int k = 0; k < NV; k++) sh[k][t] = sh[k][t] + sh[k][t + w];
+        }
+        __syncthreads();
+    }
+    if (t == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) out[k] = sh[k][0];
+        d.ss[s].red_count = 0;
+    }
+    return true;
+}
+
+__device__ __forceinline__ int vload(const int* p) { return *((const volatile int*)p); }
+
+// The system sorts its particles this step / rebuilds its list this step.
+__device__ __forceinline__ bool do_sort(const SysState* st) {
+    return sys_active(st) && (vload(&st->rebuild) || vload(&st->periodic_sort));
+}
+__device__ __forceinline__ bool do_rebuild(const SysState* st) {
+    return sys_active(st) && (vload(&st->rebuild) || (vload(&st->periodic_sort) && vload(&st->nonid)));
+}
+
+// End of a step for one system (one thread, after the system's last block
+// of the final kernel): nh_post_final's half step of p_xi from the kinetic
+// energy (m|v|^2 summed in ke2), then the next nh_pre_initial's half step
+// (its compute_ke sees the same velocities) and its exp scale
+// (md_thermostat/src/lib.rs:254-353); the virial; the rebuild / sort
+// counters, step, step budget and history buffer flip; the overlap limit
+// (contact.rs:197-216).
+__device__ __forceinline__ void step_end(const SysParams& sp, SysState* st, double ke2, const double* vir,
+                                         int integrate) {
+    const double ke = 0.5 * ke2;
+    const double dt = sp.dt;
+    st->ke = ke;
+    if (sp.nh && integrate) {
+        const double post = st->p_xi_pre + (dt / 2.0) * (2.0 * ke - sp.nh_ndof * sp.nh_T);
+        st->p_xi_post = post;
+        const double pre = post + (dt / 2.0) * (2.0 * ke - sp.nh_ndof * sp.nh_T);
+        st->p_xi_pre = pre;
+        st->nh_scale = exp(-dt / 2.0 * pre / sp.nh_Q);
+    }
+    if (vir)
+        for (int q = 0; q < 6; q++) st->vir[q] = vir[q];
+    const bool rb = do_rebuild(st);
+    if (integrate) {
+        st->steps_since_build = rb ? 0 : st->steps_since_build + 1;
+        st->sort_counter = st->periodic_sort ? 0 : st->sort_counter + 1;
+        st->step += 1;
+        if (st->remaining > 0) st->remaining -= 1;
+    } else if (rb) {
+        st->steps_since_build = 0;
+    }
+    if (sp.kind == 0) st->hcur ^= 1;  // the force kernel wrote the other history buffer
+    if (rb) st->nbuilds += 1;
+    if (st->overlap > 500) st->status |= ST_OVERLAP;
+    st->overlap = 0;
+    st->rebuild = 0;
+    st->periodic_sort = 0;
+    st->nonid = 0;
+}
+
+// True on the last block of system s to arrive (all threads); the block
+// counter is reset there.  Every block of the system must call it.
+__device__ __forceinline__ bool system_last(const Dev& d, int s) {
+    __shared__ int last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned int prev = atomicAdd(&d.ss[s].red_count, 1u);
+        last = prev == (unsigned)(d.sp[s].nb - 1);
+        if (last) d.ss[s].red_count = 0;
+    }
+    __syncthreads();
+    if (last) __threadfence();
+    return last;
+}
+
+// entry k of a prefix array off[0..n] with off[k] <= v < off[k+1]
+__device__ __forceinline__ int rb_find(const int* off, int n, int v) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= v) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Grid-stride loop over the particle blocks (s = system, lb = block within
+// it) or cell blocks of the rebuild work list.
+#define RB_FOR_PARTICLE_BLOCKS(BODY)                                  \
+    {                                                                 \
+        const int rbn_ = *d.rb_n;                                     \
+        const int tot_ = d.rb_poff[rbn_];                             \
+        for (int v_ = blockIdx.x; v_ < tot_; v_ += gridDim.x) {       \
+            const int k_ = rb_find(d.rb_poff, rbn_, v_);              \
+            BODY(d, d.rb_sys[k_], v_ - d.rb_poff[k_]);                \
+        }                                                             \
+    }
+#define RB_FOR_CELL_BLOCKS(BODY, SUB)                                 \
+    {                                                                 \
+        const int rbn_ = *d.rb_n;                                     \
+        const int tot_ = d.rb_coff[rbn_] * (SUB);                     \
+        for (int v_ = blockIdx.x; v_ < tot_; v_ += gridDim.x) {       \
+            const int cv_ = v_ / (SUB);                               \
+            const int k_ = rb_find(d.rb_coff, rbn_, cv_);             \
+            BODY(d, d.rb_sys[k_], cv_ - d.rb_coff[k_], v_ % (SUB));   \
+        }                                                             \
+    }
+
 int launch_initial(const Dev& d, cudaStream_t st);
 int launch_initial_mixed(const Dev& d, cudaStream_t st);
+int launch_rebuild_tail_mixed(const Dev& d, int has_dem, cudaStream_t st);
+int launch_final_mixed(const Dev& d, cudaStream_t st, int integrate);
 int launch_rebuild(const Dev& d, cudaStream_t st);
 int launch_force_fp64(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st);
 int launch_force_mixed(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st);

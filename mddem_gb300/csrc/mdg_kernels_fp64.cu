@@ -35,65 +35,7 @@ __device__ __forceinline__ void decode_shift(int sc, int& sx, int& sy, int& sz) 
     sz = sc % 3 - 1;
 }
 
-// Per-system reduction of NV doubles.  Every block of the system (gb = its
-// global particle block id) contributes a partial; the last block to arrive sums the partials with a fixed order
-// (strided lanes, then a fixed tree) so the result is deterministic.  Returns
-// true on the last block (all threads), totals valid in out[] on thread 0.
-// Every block of the system must be in the launch.
-template <int NV>
-__device__ bool system_reduce(const Dev& d, int s, int gb, const double (&v)[NV], double (&out)[NV]) {
-    static_assert(NV <= 8, "blkpart holds 8 doubles per block");
-    __shared__ double sh[NV][BLK];
-    __shared__ int last;
-    const SysParams& sp = d.sp[s];
-    const int t = threadIdx.x;
-#pragma unroll
-    for (int k = 0; k < NV; k++) sh[k][t] = v[k];
-    __syncthreads();
-    for (int w = BLK / 2; w > 0; w >>= 1) {
-        if (t < w) {
-#pragma unroll
-            for (int k = 0; k < NV; k++) sh[k][t] = sh[k][t] + sh[k][t + w];
-        }
-        __syncthreads();
-    }
-    if (t == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; k++) d.blkpart[(size_t)gb * 8 + k] = sh[k][0];
-        __threadfence();
-        unsigned int prev = atomicAdd(&d.ss[s].red_count, 1u);
-        last = (prev == (unsigned)(sp.nb - 1)) ? 1 : 0;
-    }
-    __syncthreads();
-    if (!last) return false;
-    __threadfence();
-    double acc[NV];
-#pragma unroll
-    for (int k = 0; k < NV; k++) acc[k] = 0.0;
-    for (int b = t; b < sp.nb; b += BLK) {
-        const volatile double* p = d.blkpart + (size_t)(sp.b0 + b) * 8;
-#pragma unroll
-        for (int k = 0; k < NV; k++) acc[k] = acc[k] + p[k];
-    }
-#pragma unroll
-    for (int k = 0; k < NV; k++) sh[k][t] = acc[k];
-    __syncthreads();
-    for (int w = BLK / 2; w > 0; w >>= 1) {
-        if (t < w) {
-#pragma unroll
-            for (int k = 0; k < NV; k++) sh[k][t] = sh[k][t] + sh[k][t + w];
-        }
-        __syncthreads();
-    }
-    if (t == 0) {
-#pragma unroll
-        for (int k = 0; k < NV; k++) out[k] = sh[k][0];
-        d.ss[s].red_count = 0;
-    }
-    return true;
-}
 
-__device__ __forceinline__ int vload(const int* p) { return *((const volatile int*)p); }
 
 // ----------------------------------------------------------------------------
 // initial integration + rebuild decision
@@ -232,12 +174,7 @@ __global__ void __launch_bounds__(BLK) k_initial(Dev d) {
 // ----------------------------------------------------------------------------
 // rebuild pipeline
 // ----------------------------------------------------------------------------
-__device__ __forceinline__ bool do_sort(const SysState* st) {
-    return sys_active(st) && (vload(&st->rebuild) || vload(&st->periodic_sort));
-}
-__device__ __forceinline__ bool do_rebuild(const SysState* st) {
-    return sys_active(st) && (vload(&st->rebuild) || (vload(&st->periodic_sort) && vload(&st->nonid)));
-}
+
 
 // Exclusive block-wide scan (1024 threads) of one int; total to `tot`.
 __device__ __forceinline__ int block_scan1024(int v, int* wsum, int& tot) {
@@ -295,39 +232,6 @@ __global__ void __launch_bounds__(1024) k_rb_plan(Dev d) {
         *d.rb_n = cn;
     }
 }
-
-// entry k of a prefix array off[0..n] with off[k] <= v < off[k+1]
-__device__ __forceinline__ int rb_find(const int* off, int n, int v) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (off[mid] <= v) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
-// Grid-stride loop over the particle blocks (s = system, lb = block within
-// it) or cell blocks of the rebuild work list.
-#define RB_FOR_PARTICLE_BLOCKS(BODY)                                  \
-    {                                                                 \
-        const int rbn_ = *d.rb_n;                                     \
-        const int tot_ = d.rb_poff[rbn_];                             \
-        for (int v_ = blockIdx.x; v_ < tot_; v_ += gridDim.x) {       \
-            const int k_ = rb_find(d.rb_poff, rbn_, v_);              \
-            BODY(d, d.rb_sys[k_], v_ - d.rb_poff[k_]);                \
-        }                                                             \
-    }
-#define RB_FOR_CELL_BLOCKS(BODY, SUB)                                 \
-    {                                                                 \
-        const int rbn_ = *d.rb_n;                                     \
-        const int tot_ = d.rb_coff[rbn_] * (SUB);                     \
-        for (int v_ = blockIdx.x; v_ < tot_; v_ += gridDim.x) {       \
-            const int cv_ = v_ / (SUB);                               \
-            const int k_ = rb_find(d.rb_coff, rbn_, cv_);             \
-            BODY(d, d.rb_sys[k_], cv_ - d.rb_coff[k_], v_ % (SUB));   \
-        }                                                             \
-    }
 
 // pbc (domain.rs:413-459, rebuild steps only) + bin key (neighbor.rs:721-738)
 __device__ __forceinline__ void cells_block(const Dev& d, int s, int lb) {
@@ -453,6 +357,7 @@ __device__ __forceinline__ void gather_block(const Dev& d, int s, int lb) {
     if (!do_rebuild(d.ss + s)) return;
     const int hcur = d.ss[s].hcur;
     const int li = lb * BLK + threadIdx.x;
+    if (li == 0 && d.dem_wl_n) d.dem_wl_n[s] = 0;  // the worklist is rebuilt after the list
     if (li >= sp.n) return;
     const long long k = (long long)sp.p0 + li;
     const long long o = d.perm[k];
@@ -1334,37 +1239,7 @@ __global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
         last = system_reduce<1>(d, s, gb, v1, o1);
         out[0] = o1[0];
     }
-    if (last && threadIdx.x == 0) {
-        const double ke = 0.5 * out[0];
-        st->ke = ke;
-        if (sp.nh && integrate) {
-            // nh_post_final's half step, then the next nh_pre_initial's half step
-            // (its compute_ke sees the same velocities) and its exp scale
-            const double post = st->p_xi_pre + (dt / 2.0) * (2.0 * ke - sp.nh_ndof * sp.nh_T);
-            st->p_xi_post = post;
-            const double pre = post + (dt / 2.0) * (2.0 * ke - sp.nh_ndof * sp.nh_T);
-            st->p_xi_pre = pre;
-            st->nh_scale = exp(-dt / 2.0 * pre / sp.nh_Q);
-        }
-        if (sp.virial)
-            for (int q = 0; q < 6; q++) st->vir[q] = out[1 + q];
-        const bool rb = do_rebuild(st);
-        if (integrate) {
-            st->steps_since_build = rb ? 0 : st->steps_since_build + 1;
-            st->sort_counter = st->periodic_sort ? 0 : st->sort_counter + 1;
-            st->step += 1;
-            if (st->remaining > 0) st->remaining -= 1;
-        } else if (rb) {
-            st->steps_since_build = 0;
-        }
-        if (sp.kind == 0) st->hcur ^= 1;  // the force kernel wrote the other history buffer
-        if (rb) st->nbuilds += 1;
-        if (st->overlap > 500) st->status |= ST_OVERLAP;
-        st->overlap = 0;
-        st->rebuild = 0;
-        st->periodic_sort = 0;
-        st->nonid = 0;
-    }
+    if (last && threadIdx.x == 0) step_end(sp, st, out[0], sp.virial ? out + 1 : nullptr, integrate);
 }
 
 // KE of the uploaded velocities (the first nh_pre_initial's compute_ke).

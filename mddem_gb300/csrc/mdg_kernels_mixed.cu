@@ -401,17 +401,14 @@ __global__ void __launch_bounds__(BLK) k_dem_mixed(Dev d) {
     SysState* st = d.ss + s;
     if (sp.kind != 0 || !sys_active(st)) return;
     const int hcur = st->hcur;
-    const int li = (gb - sp.b0) * BLK + threadIdx.x;
-    if (li >= sp.n) return;
+    // the system's worklist: particles with listed partners (the others keep
+    // the zero force, torque and history written at the build)
+    const int k = (gb - sp.b0) * BLK + threadIdx.x;
+    if (k >= d.dem_wl_n[s]) return;
+    const int li = d.dem_wl[sp.p0 + k];
     const long long i = (long long)sp.p0 + li;
     const int hn = hcur ^ 1;
     const int nn = d.nnum[i];
-    if (nn == 0) {  // no listed partner (most particles of a dilute gas)
-        d.hcnt[hn][i] = 0;
-        d.frc[i] = make_double4(0.0, 0.0, 0.0, 0.0);
-        d.trq[i] = make_double4(0.0, 0.0, 0.0, 0.0);
-        return;
-    }
     const float4 hi = d.pos2[2 * i], lo = d.pos2[2 * i + 1];
     const double4 vi = d.vel[i];
     const double4 wi = d.omg[i];
@@ -593,6 +590,108 @@ __global__ void __launch_bounds__(BLK) k_initial_mixed(Dev d) {
             cudaGraphSetConditional((cudaGraphConditionalHandle)d.cond, any ? 1u : 0u);
         }
     }
+}
+
+// After a DEM system's list build: particles with no listed partner get zero
+// force, torque and contact-history count in both buffers (nothing writes
+// them again until the next build); the others are appended to the system's
+// worklist (warp-aggregated; any order: each particle's force is computed
+// independently, so results do not depend on it).
+__device__ __forceinline__ void dem_wl_block(const Dev& d, int s, int lb) {
+    const SysParams& sp = d.sp[s];
+    if (sp.kind != 0 || !do_rebuild(d.ss + s)) return;
+    const int li = lb * BLK + threadIdx.x;
+    const bool in = li < sp.n;
+    const long long i = (long long)sp.p0 + li;
+    const bool has = in && d.nnum[i] > 0;
+    if (in && !has) {
+        d.frc[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+        d.trq[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+        d.hcnt[0][i] = 0;
+        d.hcnt[1][i] = 0;
+    }
+    const unsigned int m = __ballot_sync(0xffffffffu, has);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&d.dem_wl_n[s], __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (has) d.dem_wl[sp.p0 + base + __popc(m & ((1u << lane) - 1u))] = li;
+}
+__global__ void __launch_bounds__(BLK) k_dem_wl(Dev d) RB_FOR_PARTICLE_BLOCKS(dem_wl_block)
+
+int launch_rebuild_tail_mixed(const Dev& d, int has_dem, cudaStream_t st) {
+    if (!has_dem) return 0;
+    constexpr int CAP = 152 * 16;
+    k_dem_wl<<<d.nrun < CAP ? d.nrun : CAP, BLK, 0, st>>>(d);
+    return 1;
+}
+
+// final_integration + final_rotation (mddem_verlet/src/lib.rs:136-154,
+// rotational.rs:87-100) and nh_post_final for the mixed path: FP64 state with
+// FMA; the kinetic-energy reduction only for thermostatted systems (mixed
+// contexts carry no virial).
+__global__ void __launch_bounds__(BLK) k_final_mixed(Dev d, int integrate) {
+    const int gb = d.blk_run[blockIdx.x];
+    const int s = d.blk_sys[gb];
+    const SysParams& sp = d.sp[s];
+    SysState* st = d.ss + s;
+    if (!sys_active(st)) return;  // every block of a frozen system returns
+    const int li = (gb - sp.b0) * BLK + threadIdx.x;
+    const bool act = li < sp.n;
+    const long long i = (long long)sp.p0 + li;
+    const double dt = sp.dt;
+    double ke2 = 0.0;
+    int bad = 0;
+    if (act) {
+        const double4 f = d.frc[i];
+        double4 v = d.vel[i];
+        if (integrate) {
+            const double h = 0.5 * dt * v.w;
+            v.x = fma(h, f.x, v.x);
+            v.y = fma(h, f.y, v.y);
+            v.z = fma(h, f.z, v.z);
+            if (sp.nh) {
+                const double scale = st->nh_scale;
+                v.x *= scale;
+                v.y *= scale;
+                v.z *= scale;
+            }
+            d.vel[i] = v;
+        }
+        if (sp.nh) ke2 = d.mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z);
+        if (sp.kind == 0 && integrate) {
+            double4 w = d.omg[i];
+            if (w.w != 0.0) {
+                const double4 tq = d.trq[i];
+                const double hw = 0.5 * dt * w.w;
+                w.x = fma(hw, tq.x, w.x);
+                w.y = fma(hw, tq.y, w.y);
+                w.z = fma(hw, tq.z, w.z);
+                d.omg[i] = w;
+            }
+        }
+        const int ex = 0x7ff00000;
+        bad = ((__double2hiint(v.x) & ex) == ex) | ((__double2hiint(v.y) & ex) == ex) |
+              ((__double2hiint(v.z) & ex) == ex);
+    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&st->status, ST_NAN);
+    bool last;
+    double tot = 0.0;
+    if (sp.nh) {
+        const double v1[1] = {ke2};
+        double o1[1];
+        last = system_reduce<1>(d, s, gb, v1, o1);
+        tot = o1[0];
+    } else {
+        last = system_last(d, s);
+    }
+    if (last && threadIdx.x == 0) step_end(sp, st, tot, nullptr, integrate);
+}
+
+int launch_final_mixed(const Dev& d, cudaStream_t st, int integrate) {
+    k_final_mixed<<<d.nrun, BLK, 0, st>>>(d, integrate);
+    return 1;
 }
 
 int launch_initial_mixed(const Dev& d, cudaStream_t st) {
