@@ -528,6 +528,8 @@ def bench_serve(a, world, rank, local, dist):
     made = [j.make(a.precision, a.policy) for j in trace]
     cfgs, caps = w.serve_slots(a.precision, a.policy)
     srv = capi.Server(cfgs, caps, SERVE_HBM_BUDGET)
+    if a.eager:
+        srv.context().set_graph_mode(0)
     # warm-up jobs (one of each kind), drained before the stream starts
     for j in (w.Job("gas", 300, 2 * SERVE_PUMP, 0, dict(phi=0.1, e=0.9, seed=7)),
               w.Job("rebound", 2, 2 * SERVE_PUMP, 0, dict(speed=1.0)),
@@ -611,6 +613,8 @@ def bench_ensemble(a, world, rank, local, dist):
     for q, s in enumerate(sts):
         ctx.upload(s, q)
     tune = ctx.autotune(steps=20) if not a.no_tune else None
+    if a.eager:
+        ctx.set_graph_mode(0)
     stream = torch.cuda.ExternalStream(ctx.stream())
     ctx.step(a.warmup)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -646,7 +650,7 @@ def bench_ensemble(a, world, rank, local, dist):
         # per-kernel phases (eager launches, CUDA events) for the roofline
         ctx.set_graph_mode(0)
         t, _, _ = ctx.timed_steps(5, 0)
-        ctx.set_graph_mode(1)
+        ctx.set_graph_mode(0 if a.eager else 1)
         contacts = sum(len(ctx.history(q)[0]) for q in range(len(sts))) / n
         nfull = sum(2.0 * len(ctx.pairs(q)) for q in range(len(sts))) / n
         cands = {"k_initial": (float(t[:, 1].mean()), n * INIT_BYTES[("dem", a.precision)]),
