@@ -151,14 +151,6 @@ def ncu_traffic(kernel):
         return None
 
 
-def force_bytes_per_particle(nfull, precision):
-    """Algorithmic DRAM bytes per particle of one force launch: row length (4),
-    the row's list entries (4 each), the particle's own geometry read once
-    (fp64 row 32 B, or the two-float copy 32 B), and the force row written
-    (32 B)."""
-    return 4 + 4 * nfull + 32 + 32
-
-
 def cpu_baseline_sample(wl, max_seconds=15.0):
     """Single-core oracle on a bounded sample of the workload (steps until
     ~max_seconds of CPU time)."""
@@ -326,19 +318,22 @@ def serve_trace(a):
     from mddem_gb300 import workloads as w
 
     trace = w.serve_trace(njobs=a.jobs, rate=SERVE_RATE, seed=2024)
+    scale = getattr(a, "job_steps_scale", 1.0)
+    for j in trace:
+        j.steps = max(1, int(round(j.steps * scale)))
     t0 = trace[SERVE_BACKLOG].arrival if len(trace) > SERVE_BACKLOG else 0.0
     for k, j in enumerate(trace):  # the backlog arrives at tick 0, the rest keep their gaps
         j.arrival = 0.0 if k < SERVE_BACKLOG else j.arrival - t0 + 1.0
     return trace
 
 
-def serve_desc(trace):
+def serve_desc(trace, scale=1.0):
     kinds = {}
     for j in trace:
         kinds[j.kind] = kinds.get(j.kind, 0) + 1
     return (f"served stream: {len(trace)} jobs ({kinds.get('gas', 0)} cooling gases N 100-200000, "
             f"{kinds.get('rebound', 0)} two-sphere rebounds, {kinds.get('lj', 0)} LJ FCC melts N 500-100000), "
-            f"steps 1000-50000 log-uniform, {SERVE_BACKLOG} queued at start then Poisson {SERVE_RATE}/pump, "
+            f"steps {1000 * scale:g}-{50000 * scale:g} log-uniform, {SERVE_BACKLOG} queued at start then Poisson {SERVE_RATE}/pump, "
             f"{SERVE_PUMP} timesteps per pump")
 
 
@@ -355,6 +350,10 @@ def replay(a, srv, trace, made, clk):
     import torch
 
     order = sorted(range(len(trace)), key=lambda k: trace[k].arrival)
+    # warm-up pumps of the stream itself; a stream shorter than that (small
+    # cases for launch lists) keeps its last pumps timed
+    est = int(max(j.arrival + j.steps / SERVE_PUMP for j in trace))
+    warm = min(a.warmup, max(0, est - 2))
     stream = torch.cuda.ExternalStream(srv.stream())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     nxt, tick, infos, sid = 0, 0, {}, {}
@@ -368,20 +367,20 @@ def replay(a, srv, trace, made, clk):
             sid[srv.submit(cfg, st, trace[k].steps)] = k
             h2d += state_bytes(st)
             nxt += 1
-        if tick == a.warmup:
-            win.update(s0=srv.stats(), l0=srv.launches(), c0=clk.mark(), w0=time.perf_counter())
+        if tick == warm:
+            win.update(s0=srv.stats(), l0=srv.launches(), c0=clk.mark(), w0=time.perf_counter(), warm=warm)
             e0.record(stream)
         active, pending = srv.pump(SERVE_PUMP)
         tick += 1
-        mid = a.warmup + (a.steps // 2 if a.steps else 10)
+        mid = warm + (a.steps // 2 if a.steps else min(10, max(0, est - warm) // 2))
         if tick >= mid and "mix" not in win:
             win["mix"] = [sid[r["id"]] for r in srv.resident()]
         drained = nxt == len(order) and active == 0 and pending == 0
-        if "s0" in win and "s1" not in win and ((a.steps and tick == a.warmup + a.steps) or drained):
+        if "s0" in win and "s1" not in win and ((a.steps and tick == warm + a.steps) or drained):
             e1.record(stream)
             e1.synchronize()
             win.update(s1=srv.stats(), l1=srv.launches(), c1=clk.mark(), w1=time.perf_counter(),
-                       ms=e0.elapsed_time(e1), pumps=tick - a.warmup)
+                       ms=e0.elapsed_time(e1), pumps=tick - warm)
         for info in srv.poll():
             out = srv.fetch(info["id"])
             d2h += state_bytes(out)
@@ -531,9 +530,10 @@ def bench_serve(a, world, rank, local, dist):
     if a.eager:
         srv.context().set_graph_mode(0)
     # warm-up jobs (one of each kind), drained before the stream starts
-    for j in (w.Job("gas", 300, 2 * SERVE_PUMP, 0, dict(phi=0.1, e=0.9, seed=7)),
-              w.Job("rebound", 2, 2 * SERVE_PUMP, 0, dict(speed=1.0)),
-              w.Job("lj", 500, 2 * SERVE_PUMP, 0, dict(cells=5, rho=0.85, T=1.0, seed=7))):
+    wsteps = 2 * SERVE_PUMP if a.job_steps_scale >= 1.0 else SERVE_PUMP // 4
+    for j in (w.Job("gas", 300, wsteps, 0, dict(phi=0.1, e=0.9, seed=7)),
+              w.Job("rebound", 2, wsteps, 0, dict(speed=1.0)),
+              w.Job("lj", 500, wsteps, 0, dict(cells=5, rho=0.85, T=1.0, seed=7))):
         c, s = j.make(a.precision, a.policy)
         srv.submit(c, s, j.steps)
     while True:
@@ -561,10 +561,10 @@ def bench_serve(a, world, rank, local, dist):
     total_ps = float(sum(j.n * j.steps for j in trace))
     line = {
         "metric": "particle-steps/s served", "value": ps / (ms / 1e3), "unit": "particle-steps/s",
-        "n_gpus": world, "steps": win["pumps"], "warmup": a.warmup, "ms_per_step": ms / win["pumps"],
+        "n_gpus": world, "steps": win["pumps"], "warmup": win["warm"], "ms_per_step": ms / win["pumps"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if a.precision == "mixed" else "f64", "data": "synthetic",
-        "config": {"workload": serve_desc(trace), "precision": a.precision, "rebuild_policy": a.policy,
+        "config": {"workload": serve_desc(trace, a.job_steps_scale), "precision": a.precision, "rebuild_policy": a.policy,
                    "pump_timesteps": SERVE_PUMP, "slots": {"dem": w.SERVE_DEM_SLOTS, "lj": w.SERVE_LJ_SLOTS},
                    "hbm_budget_bytes": SERVE_HBM_BUDGET,
                    "l2": "inputs larger than L2 (resident state of all jobs, > 129 MB)",
@@ -582,8 +582,9 @@ def bench_serve(a, world, rank, local, dist):
     srv.close()
     if rank == 0:
         line["roofline"] = serve_roofline(a, trace, made, win.get("mix", []))
-        line["plain_fp64_job_by_job"] = plain_job_by_job(trace, made)
-        line["served_vs_plain"] = line["value"] / world / line["plain_fp64_job_by_job"]["value"]
+        if not a.no_plain:
+            line["plain_fp64_job_by_job"] = plain_job_by_job(trace, made)
+            line["served_vs_plain"] = line["value"] / world / line["plain_fp64_job_by_job"]["value"]
         if not a.no_cpu_baseline:
             line["cpu_baseline"] = serve_cpu_sample(trace, made)
         print(json.dumps(line), flush=True)
@@ -666,8 +667,9 @@ def bench_ensemble(a, world, rank, local, dist):
                             "kernels_ms": {q: v[0] for q, v in cands.items()}}
         if not a.no_e2e:
             line["e2e"] = ensemble_e2e(cfgs, sts, a.steps)
-        line["plain_fp64_replica_by_replica"] = plain_replicas(cfgs, sts)
-        line["batched_vs_plain"] = line["value"] / world / line["plain_fp64_replica_by_replica"]["value"]
+        if not a.no_plain:
+            line["plain_fp64_replica_by_replica"] = plain_replicas(cfgs, sts)
+            line["batched_vs_plain"] = line["value"] / world / line["plain_fp64_replica_by_replica"]["value"]
         if not a.no_cpu_baseline:
             import types
 
@@ -734,6 +736,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (ensemble)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison (serve, ensemble)")
+    ap.add_argument("--job-steps-scale", type=float, default=1.0,
+                    help="scale the served jobs' step counts (small cases for launch lists)")
     a = ap.parse_args()
     a.warmup = max(3, a.warmup)
     if a.steps is None:
@@ -784,11 +789,21 @@ def main():
     pairs = len(ctx.pairs())
     nfull_avg = 2.0 * pairs / n
     force_ms = float(t[:, 3].mean())
-    bpp = force_bytes_per_particle(nfull_avg, a.precision)
-    achieved = bpp * n / (force_ms / 1e3) / 1e9
+    kind = cfg.kind
+    contacts = len(ctx.history()[0]) / n if kind == "dem" else 0.0
+    suffix = "mixed" if a.precision == "mixed" else "fp64"
+    # the dominant per-particle kernel of the step: force, initial or final
+    # integration (phases timed by CUDA events; rebuild steps averaged in)
+    cands = {("k_dem_" if kind == "dem" else "k_lj_") + suffix: (force_ms, force_bytes(kind, nfull_avg, contacts)),
+             ("k_initial_mixed" if a.precision == "mixed" else "k_initial"):
+                 (float(t[:, 1].mean()), INIT_BYTES[(kind, a.precision)]),
+             ("k_final_mixed" if a.precision == "mixed" else "k_final"):
+                 (float(t[:, 4].mean()), FINAL_BYTES[kind])}
+    kname = max(cands, key=lambda q: cands[q][0])
+    kms, bpp = cands[kname]
+    achieved = bpp * n / (kms / 1e3) / 1e9
     peak, src = peak_hbm()
-    kname = "k_lj_mixed" if a.precision == "mixed" else "k_lj_fp64"
-    traffic = ncu_traffic(kname)
+    traffic = ncu_traffic(kname + "/" + a.workload) or (ncu_traffic(kname) if a.workload == "lj256k" else None)
     line = {
         "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": total_ms / a.steps, "higher_is_better": True,
@@ -802,7 +817,8 @@ def main():
         "gpu_launches": int(kernels.sum()),
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": src, "traffic": traffic,
-                     "algorithmic_bytes_per_particle": bpp, "avg_full_neighbors": nfull_avg},
+                     "algorithmic_bytes_per_particle": bpp, "avg_full_neighbors": nfull_avg, "launch_ms": kms,
+                     "kernels_ms": {q: v[0] for q, v in cands.items()}},
         "clocks": clk.summary(),
     }
     if rank == 0 and not a.no_e2e:
