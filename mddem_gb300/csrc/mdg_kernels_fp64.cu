@@ -540,6 +540,65 @@ __device__ __forceinline__ TileRule tile_rule(const SysParams& sp, int ex, int e
 // fp64.  Also saves last_build_pos (neighbor.rs:545-561).
 constexpr int BUILD_WARPS = 4;
 
+// The survivors of the fp32 screen that lie near the cutoff, or that involve
+// a particle within 1e-9 of a bin edge under a periodic shift: two-float
+// separation, the reference's own fp64 cutoff test (fma form) inside the
+// band, and image bins recomputed in fp64 for edge particles.  Returns bit 0
+// when i owns the pair in the reference's half list, bit 1 when j does.
+// Kept out of line: it is rare, and inlined it would set the register count
+// of the whole build loop.
+__device__ __noinline__ int near_pair(const Dev& d, const SysParams& sp, long long i, long long j, float4 hi, float4 lo,
+                                      float4 hj, float4 lj, int sx, int sy, int sz, bool edge, int ex, int ey, int ez,
+                                      int Ex, int Ey, int Ez, TileRule tr) {
+    const float band_hi = 1.00001f, band_lo = 0.99999f;
+    bool ok_i = true, ok_j = true;
+    const float fx = two_float_sep(hj.x, lj.x, hi.x, lo.x, sx, sp.Lh[0], sp.Ll[0]);
+    const float fy = two_float_sep(hj.y, lj.y, hi.y, lo.y, sy, sp.Lh[1], sp.Ll[1]);
+    const float fz = two_float_sep(hj.z, lj.z, hi.z, lo.z, sz, sp.Lh[2], sp.Ll[2]);
+    const float r2f = fx * fx + fy * fy + fz * fz;
+    float c2f;
+    if (sp.uniform) {
+        c2f = sp.ucut2f;
+    } else {
+        const float ssum = hi.w + hj.w;
+        c2f = ssum * ssum * sp.sf2f;
+    }
+    if (r2f > c2f * band_hi) return 0;
+    if (r2f >= c2f * band_lo || edge) {
+        const double4 xi = d.pos[i], xj = d.pos[j];
+        const double si = d.cutr[i], sj = d.cutr[j];
+        if (r2f >= c2f * band_lo) {
+            // the reference's own test, in its own arithmetic
+            const double dx = img_coord(xj.x, sx, sp.L[0]) - xi.x;
+            const double dy = img_coord(xj.y, sy, sp.L[1]) - xi.y;
+            const double dz = img_coord(xj.z, sz, sp.L[2]) - xi.z;
+            ok_i = cut_ok(sp, fma(dx, dx, fma(dy, dy, dz * dz)), si, sj);
+            if (sx | sy | sz) {
+                const double ux = img_coord(xi.x, -sx, sp.L[0]) - xj.x;
+                const double uy = img_coord(xi.y, -sy, sp.L[1]) - xj.y;
+                const double uz = img_coord(xi.z, -sz, sp.L[2]) - xj.z;
+                ok_j = cut_ok(sp, fma(ux, ux, fma(uy, uy, uz * uz)), sj, si);
+            } else {
+                ok_j = ok_i;
+            }
+            if (!ok_i && !ok_j) return 0;
+        }
+        if (edge) {
+            int gx, gy, gz, hx, hy, hz;
+            ext_cell3(sp, img_coord(xj.x, sx, sp.L[0]), img_coord(xj.y, sy, sp.L[1]), img_coord(xj.z, sz, sp.L[2]),
+                      gx, gy, gz);
+            ext_cell3(sp, img_coord(xi.x, -sx, sp.L[0]), img_coord(xi.y, -sy, sp.L[1]), img_coord(xi.z, -sz, sp.L[2]),
+                      hx, hy, hz);
+            const bool own = ok_i && owner_test(sp, ex, ey, ez, gx, gy, gz, true, i, j);
+            const bool oth = sp.newton && ok_j && owner_test(sp, Ex, Ey, Ez, hx, hy, hz, true, j, i);
+            return (own ? 1 : 0) | (oth ? 2 : 0);
+        }
+    }
+    const bool own = ok_i && (tr.own || (tr.same && (sp.newton ? j > i : true)));
+    const bool oth = ok_j && (tr.oth || (tr.same && sp.newton && i > j));
+    return (own ? 1 : 0) | (oth ? 2 : 0);
+}
+
 constexpr int BUILD_SUBS = BLK / BUILD_WARPS;  // blocks per 128-bin cell block
 
 // One warp per bin: bin `sub * BUILD_WARPS + warp` of cell block `lcb` of
@@ -561,7 +620,6 @@ __device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
     const int qx0 = min(max(ex - sp.sl[0], 0), sp.nc[0] - 1);
     const int qy0 = min(max(ey - sp.sl[1], 0), sp.nc[1] - 1);
     const int qz0 = min(max(ez - sp.sl[2], 0), sp.nc[2] - 1);
-    const float band_hi = 1.00001f, band_lo = 0.99999f;
     const float brel = sp.band_rel;
     for (int ib = a0; ib < a1; ib += 32) {
         const long long i = ib + lane;
@@ -644,92 +702,23 @@ __device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
                                         const int t = __ffs(mask) - 1;
                                         mask &= mask - 1u;
                                         const long long j = t0 + t;
-                                        bool ok_i = true, ok_j = true;
                                         const bool edge = shifted && (edge_i || tile_e[warp][t] != 0);
+                                        int bits;
                                         if (!((near >> t) & 1u) && !edge) {
                                             // clearly inside: owner decision only
-                                            const bool own = tr.own || (tr.same && (sp.newton ? j > i : true));
-                                            const bool oth = tr.oth || (tr.same && sp.newton && i > j);
-                                            const uint32_t jl = (uint32_t)(j - sp.p0);
-                                            if (own) {
-                                                if (count < sp.ncap)
-                                                    d.nlist[base + (long long)count * sp.npad] = jl | ((sc + 27u) << IDX_BITS);
-                                                count++;
-                                            }
-                                            if (oth) {
-                                                if (count < sp.ncap)
-                                                    d.nlist[base + (long long)count * sp.npad] = jl | (sc << IDX_BITS);
-                                                count++;
-                                            }
-                                            continue;
-                                        }
-                                        const float4 hj = tile_h[warp][t];
-                                        // near the cutoff: two-float separation, then the exact test
-                                        const float4 lj = tile_l[warp][t];
-                                        const float fx = two_float_sep(hj.x, lj.x, hi.x, lo.x, sx, sp.Lh[0], sp.Ll[0]);
-                                        const float fy = two_float_sep(hj.y, lj.y, hi.y, lo.y, sy, sp.Lh[1], sp.Ll[1]);
-                                        const float fz = two_float_sep(hj.z, lj.z, hi.z, lo.z, sz, sp.Lh[2], sp.Ll[2]);
-                                        const float r2f = fx * fx + fy * fy + fz * fz;
-                                        float c2f;
-                                        if (sp.uniform) {
-                                            c2f = sp.ucut2f;
+                                            bits = ((tr.own || (tr.same && (sp.newton ? j > i : true))) ? 1 : 0) |
+                                                   ((tr.oth || (tr.same && sp.newton && i > j)) ? 2 : 0);
                                         } else {
-                                            const float ssum = hi.w + hj.w;
-                                            c2f = ssum * ssum * sp.sf2f;
+                                            bits = near_pair(d, sp, i, j, hi, lo, tile_h[warp][t], tile_l[warp][t], sx, sy,
+                                                             sz, edge, ex, ey, ez, Ex, Ey, Ez, tr);
                                         }
-                                        if (r2f > c2f * band_hi) continue;
-                                        if (r2f >= c2f * band_lo || edge) {
-                                            const double4 xi = d.pos[i], xj = d.pos[j];
-                                            const double si = d.cutr[i], sj = d.cutr[j];
-                                            if (r2f >= c2f * band_lo) {
-                                                // the reference's own test, in its own arithmetic
-                                                const double dx = img_coord(xj.x, sx, sp.L[0]) - xi.x;
-                                                const double dy = img_coord(xj.y, sy, sp.L[1]) - xi.y;
-                                                const double dz = img_coord(xj.z, sz, sp.L[2]) - xi.z;
-                                                ok_i = cut_ok(sp, fma(dx, dx, fma(dy, dy, dz * dz)), si, sj);
-                                                if (shifted) {
-                                                    const double ux = img_coord(xi.x, -sx, sp.L[0]) - xj.x;
-                                                    const double uy = img_coord(xi.y, -sy, sp.L[1]) - xj.y;
-                                                    const double uz = img_coord(xi.z, -sz, sp.L[2]) - xj.z;
-                                                    ok_j = cut_ok(sp, fma(ux, ux, fma(uy, uy, uz * uz)), sj, si);
-                                                } else {
-                                                    ok_j = ok_i;
-                                                }
-                                                if (!ok_i && !ok_j) continue;
-                                            }
-                                            if (edge) {
-                                                int gx, gy, gz, hx, hy, hz;
-                                                ext_cell3(sp, img_coord(xj.x, sx, sp.L[0]), img_coord(xj.y, sy, sp.L[1]),
-                                                          img_coord(xj.z, sz, sp.L[2]), gx, gy, gz);
-                                                ext_cell3(sp, img_coord(xi.x, -sx, sp.L[0]),
-                                                          img_coord(xi.y, -sy, sp.L[1]),
-                                                          img_coord(xi.z, -sz, sp.L[2]), hx, hy, hz);
-                                                const bool own = ok_i && owner_test(sp, ex, ey, ez, gx, gy, gz, true, i, j);
-                                                const bool oth = sp.newton && ok_j &&
-                                                                 owner_test(sp, Ex, Ey, Ez, hx, hy, hz, true, j, i);
-                                                const uint32_t jl = (uint32_t)(j - sp.p0);
-                                                if (own) {
-                                                    if (count < sp.ncap)
-                                                        d.nlist[base + (long long)count * sp.npad] = jl | ((sc + 27u) << IDX_BITS);
-                                                    count++;
-                                                }
-                                                if (oth) {
-                                                    if (count < sp.ncap)
-                                                        d.nlist[base + (long long)count * sp.npad] = jl | (sc << IDX_BITS);
-                                                    count++;
-                                                }
-                                                continue;
-                                            }
-                                        }
-                                        const bool own = ok_i && (tr.own || (tr.same && (sp.newton ? j > i : true)));
-                                        const bool oth = ok_j && (tr.oth || (tr.same && sp.newton && i > j));
                                         const uint32_t jl = (uint32_t)(j - sp.p0);
-                                        if (own) {
+                                        if (bits & 1) {
                                             if (count < sp.ncap)
                                                 d.nlist[base + (long long)count * sp.npad] = jl | ((sc + 27u) << IDX_BITS);
                                             count++;
                                         }
-                                        if (oth) {
+                                        if (bits & 2) {
                                             if (count < sp.ncap)
                                                 d.nlist[base + (long long)count * sp.npad] = jl | (sc << IDX_BITS);
                                             count++;
@@ -753,7 +742,14 @@ __device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
     }
 }
 
-__global__ void __launch_bounds__(BUILD_WARPS * 32) k_build(Dev d) RB_FOR_CELL_BLOCKS(build_cells, BUILD_SUBS)
+// Minimum resident blocks per SM asked of ptxas for k_build: 5 caps it at
+// 96 registers (from 125) with ~100 B of spills and runs 22 % faster on GB300
+// (LJ 256k) than no cap; a compile-time tuning knob.
+#ifndef MDG_BUILD_MINB
+#define MDG_BUILD_MINB 5
+#endif
+__global__ void __launch_bounds__(BUILD_WARPS * 32, MDG_BUILD_MINB) k_build(Dev d)
+    RB_FOR_CELL_BLOCKS(build_cells, BUILD_SUBS)
 
 // ----------------------------------------------------------------------------
 // LJ 12-6 force (lj_force, md_lj/src/lib.rs:488-633) over the full list.
