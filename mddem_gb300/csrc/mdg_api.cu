@@ -143,7 +143,8 @@ struct mdg_ctx {
     int graph_mode = 1;
     cudaGraphExec_t wgraph = nullptr;                 // multi-step WHILE graph
     cudaGraphExec_t tgraph = nullptr;                 // timed single-step graph
-    long long* d_loop = nullptr;                      // steps left in the WHILE graph
+    long long* d_loop = nullptr;  // {iterations left, iterations of the launch} of the WHILE graph
+    bool run_nh = false;          // some running system is thermostatted
     cudaEvent_t tev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     int tkernels = 0;
     void* flush_buf = nullptr;
@@ -443,6 +444,8 @@ int update_run_maps(mdg_ctx* c) {
     c->d.run_sys = c->d_run_sys;
     c->d.nrun_sys = (int)run.size();
     c->run_sys = run;
+    c->run_nh = false;
+    for (int s : run) c->run_nh = c->run_nh || c->sp[s].nh;
     c->maps_dirty = false;
     return (int)run.size();
 }
@@ -526,10 +529,53 @@ int capture_step(mdg_ctx* c, cudaEvent_t* ev, int* nk) {
     return MDG_OK;
 }
 
+// The WHILE body of a mixed-precision context: the fused step kernel (final
+// half of the previous step + initial half of this one), the thermostatted
+// systems' initial half, the rebuild IF node, the force kernels.
+int capture_body_mixed(mdg_ctx* c, int* nk) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, nullptr, nullptr, nullptr);
+    if (e != cudaSuccess) return cuda_err(e);
+    cudaGraphConditionalHandle hd;
+    e = cudaGraphConditionalHandleCreate(&hd, g, 0, cudaGraphCondAssignDefault);
+    if (e != cudaSuccess) return cuda_err(e);
+    Dev d = c->d;
+    d.cond = (unsigned long long)hd;
+    d.use_cond = 1;
+    int n = launch_step_mixed(d, c->d_loop, c->stream);
+    if (c->run_nh) n += launch_initial_mixed(d, c->stream, 1, c->d_loop);
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    e = cudaStreamGetCaptureInfo(c->stream, &cs, nullptr, &g, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return cuda_err(e);
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = hd;
+    np.conditional.type = cudaGraphCondTypeIf;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &np);
+    if (e != cudaSuccess) return cuda_err(e);
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    e = cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return cuda_err(e);
+    e = cudaStreamBeginCaptureToGraph(c->stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_err(e);
+    n += launch_rb(c, d, c->stream2);
+    cudaGraph_t body_out = nullptr;
+    e = cudaStreamEndCapture(c->stream2, &body_out);
+    if (e != cudaSuccess) return cuda_err(e);
+    n += launch_force(c, d, c->stream);
+    if (nk) *nk = n;
+    return MDG_OK;
+}
+
 // Multi-step graph: a WHILE conditional node whose body is one step (with the
 // rebuild IF node inside) followed by the loop-control kernel, which counts
 // down d_loop and closes the loop when it reaches zero or no system is active.
-// One launch runs any number of steps without returning to the host.
+// One launch runs any number of steps without returning to the host.  Mixed
+// contexts loop over the fused body and finish the last step after the loop.
 int build_while_graph(mdg_ctx* c) {
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal);
@@ -553,6 +599,9 @@ int build_while_graph(mdg_ctx* c) {
         e = cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np);
     }
     if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(c->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+    // mixed path: the loop's fused kernels leave the last step's final half,
+    // done once after the loop
+    if (e == cudaSuccess && c->has_mixed) launch_fin(c, c->d, c->stream, 1);
     cudaGraph_t g_end = nullptr;
     e = e == cudaSuccess ? cudaStreamEndCapture(c->stream, &g) : (cudaStreamEndCapture(c->stream, &g_end), e);
     if (e != cudaSuccess) {
@@ -564,7 +613,7 @@ int build_while_graph(mdg_ctx* c) {
     cudaGraph_t body = np.conditional.phGraph_out[0];
     e = cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
     if (e == cudaSuccess) {
-        r = capture_step(c, nullptr, nullptr);
+        r = c->has_mixed ? capture_body_mixed(c, nullptr) : capture_step(c, nullptr, nullptr);
         if (!r) launch_loop_ctl(c->d, c->d_loop, (unsigned long long)wh, c->stream);
         cudaGraph_t bo = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(c->stream, &bo);
@@ -802,7 +851,7 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     c->d_thermo = c->alloc<double>((size_t)nsys * 16, err);
     d.grid_ctr = c->alloc<unsigned int>(1, err);
     d.stat_ctr = c->alloc<unsigned long long>(4, err);
-    c->d_loop = c->alloc<long long>(1, err);
+    c->d_loop = c->alloc<long long>(2, err);
     if (err) {
         delete c;
         return err;
@@ -1123,7 +1172,8 @@ int mdg_step(mdg_ctx* c, int64_t nsteps) {
             if (r) return r;
         }
         long long n = nsteps;
-        cudaMemcpyAsync(c->d_loop, &n, sizeof(n), cudaMemcpyHostToDevice, c->stream);
+        const long long nn[2] = {n, n};
+        cudaMemcpyAsync(c->d_loop, nn, sizeof(nn), cudaMemcpyHostToDevice, c->stream);
         cudaError_t e = cudaGraphLaunch(c->wgraph, c->stream);
         if (e != cudaSuccess) return cuda_err(e);
     } else {
@@ -1137,7 +1187,14 @@ int mdg_step(mdg_ctx* c, int64_t nsteps) {
     advance_budgets(c, nsteps);
     // kernels that ran: per step initial + force + final (+ loop control),
     // plus the rebuild kernels on the steps whose rebuild branch opened
-    const long long base = 3 + (c->has_lj && c->has_dem ? 1 : 0) + (c->graph_mode ? 1 : 0);
+    const long long nforce = (c->has_lj ? 1 : 0) + (c->has_dem ? 1 : 0);
+    long long base = 2 + nforce + (c->graph_mode ? 1 : 0);
+    if (c->graph_mode && c->has_mixed) {
+        // fused step kernel (+ thermostatted initial) per iteration, the
+        // epilogue final once per launch
+        base = 1 + (c->run_nh ? 1 : 0) + nforce + 1;
+        c->launches += 1;
+    }
     c->launches += nsteps * base + (long long)rb_kernels(c) * (long long)(c->graph_mode ? (rb1 - rb0) : nsteps);
     return check_status(c);
 }

@@ -102,7 +102,8 @@ struct SysState {
     long long step;
     long long remaining; // steps left before the system freezes; -1 = unlimited
     int hcur;            // contact-history buffer holding the current springs
-    int pad_;
+    int rb_next;         // rebuild requests for the next step, gathered by the fused
+                         // final + initial kernel while this step's flags are still read
 };
 
 __device__ __forceinline__ bool sys_active(const SysState* st) {
@@ -385,7 +386,8 @@ __device__ __forceinline__ int rb_find(const int* off, int n, int v) {
     }
 
 int launch_initial(const Dev& d, cudaStream_t st);
-int launch_initial_mixed(const Dev& d, cudaStream_t st);
+int launch_initial_mixed(const Dev& d, cudaStream_t st, int nh_only = 0, const long long* loop = nullptr);
+int launch_step_mixed(const Dev& d, const long long* loop, cudaStream_t st);
 int launch_rebuild_tail_mixed(const Dev& d, int has_dem, cudaStream_t st);
 int launch_final_mixed(const Dev& d, cudaStream_t st, int integrate);
 int launch_rebuild(const Dev& d, cudaStream_t st);

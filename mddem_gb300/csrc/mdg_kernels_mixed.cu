@@ -124,13 +124,17 @@ __global__ void __launch_bounds__(BLK, 8) k_lj_mixed(Dev d) {
 // its owner's frame on both sides, so forces stay exactly antisymmetric.
 // Same laws and branches as hm_pair (contact.rs:103-615, 622-990).
 // ----------------------------------------------------------------------------
+// The error-free transformations use round-to-nearest intrinsics: ptxas may
+// otherwise contract a product with the sum that consumes it into one FMA
+// (its choice depends on scheduling and register pressure), which keeps the
+// rounded product in the error term but not in the sum and breaks exactness.
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-    s = a + b;
-    const float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
 }
 __device__ __forceinline__ void two_prod(float a, float b, float& p, float& e) {
-    p = a * b;
+    p = __fmul_rn(a, b);
     e = fmaf(a, b, -p);
 }
 
@@ -489,13 +493,18 @@ __global__ void __launch_bounds__(BLK, MDG_DEM_MINB) k_dem_mixed(Dev d) {
 // are fp32, cos as 1 - 2 sin^2(angle/4) so its tiny deviation from 1 keeps
 // full relative precision, and the Hamilton product dq * q runs in FP64.  Per
 // step this perturbs q by about 1e-7 x angle/2 (angle = |omega| dt).
-__global__ void __launch_bounds__(BLK) k_initial_mixed(Dev d) {
+//
+// nh_only: only thermostatted systems (the multi-step graph's fused kernel
+// below does the others), and nothing on the first iteration of a launch
+// (loop[0] == loop[1]), where the fused kernel does every system.
+__global__ void __launch_bounds__(BLK) k_initial_mixed(Dev d, int nh_only, const long long* loop) {
+    if (nh_only && loop[0] == loop[1]) return;  // uniform over the grid
     const int gb = d.blk_run[blockIdx.x];
     const int s = d.blk_sys[gb];
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
     const int li = (gb - sp.b0) * BLK + threadIdx.x;
-    const bool live = sys_active(st);
+    const bool live = sys_active(st) && (!nh_only || sp.nh);
     const bool act = live && li < sp.n;
     const long long i = (long long)sp.p0 + li;
     const double dt = sp.dt;
@@ -700,8 +709,182 @@ int launch_final_mixed(const Dev& d, cudaStream_t st, int integrate) {
     return 1;
 }
 
-int launch_initial_mixed(const Dev& d, cudaStream_t st) {
-    k_initial_mixed<<<d.nrun, BLK, 0, st>>>(d);
+// One iteration of the multi-step graph, mixed path: the final half of the
+// previous step (k_final_mixed's update, step bookkeeping) fused with the
+// initial half of this step (k_initial_mixed's update, rebuild test) in one
+// pass over the particle arrays -- 424 instead of 648 bytes per DEM particle.
+// The arithmetic is the same FMA sequence as the two kernels, so the state is
+// bitwise identical.  loop = {iterations left, iterations of this launch}:
+// the first iteration has no previous step to finish (the state is at a step
+// boundary), and the launch's last step is finished by k_final_mixed after
+// the loop.  Thermostatted systems get only the final half here: their
+// initial half needs the system's kinetic energy after it, so
+// k_initial_mixed (nh_only) follows.  A system whose step budget runs out with
+// the finished step is not started again.
+__global__ void __launch_bounds__(BLK) k_step_mixed(Dev d, const long long* loop) {
+    const int gb = d.blk_run[blockIdx.x];
+    const int s = d.blk_sys[gb];
+    const SysParams& sp = d.sp[s];
+    SysState* st = d.ss + s;
+    const int li = (gb - sp.b0) * BLK + threadIdx.x;
+    const long long i = (long long)sp.p0 + li;
+    const double dt = sp.dt;
+    const bool first = loop[0] == loop[1];
+    // read before this system's last block updates the bookkeeping
+    const long long rem = *((volatile const long long*)&st->remaining);
+    const bool was = rem != 0;
+    const bool fin = !first && was;
+    const long long rem_after = (fin && rem > 0) ? rem - 1 : rem;
+    const bool ini = rem_after != 0 && !(fin && sp.nh);
+    int ssb = 0;
+    if (ini && sp.every > 0) ssb = fin ? (do_rebuild(st) ? 0 : st->steps_since_build + 1) : st->steps_since_build;
+    double ke2 = 0.0;
+    int bad = 0, need = 0;
+    if (li < sp.n && (fin || ini)) {
+        double4 v = d.vel[i];
+        const double4 f = d.frc[i];
+        const double h = 0.5 * dt * v.w;
+        if (fin) {
+            v.x = fma(h, f.x, v.x);
+            v.y = fma(h, f.y, v.y);
+            v.z = fma(h, f.z, v.z);
+            if (sp.nh) {
+                const double scale = st->nh_scale;
+                v.x *= scale;
+                v.y *= scale;
+                v.z *= scale;
+                ke2 = d.mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z);
+            }
+            const int ex = 0x7ff00000;
+            bad = ((__double2hiint(v.x) & ex) == ex) | ((__double2hiint(v.y) & ex) == ex) |
+                  ((__double2hiint(v.z) & ex) == ex);
+        }
+        if (ini) {
+            if (sp.nh) {  // first iteration only (fin && nh excludes ini)
+                const double scale = st->nh_scale;
+                v.x *= scale;
+                v.y *= scale;
+                v.z *= scale;
+            }
+            v.x = fma(h, f.x, v.x);
+            v.y = fma(h, f.y, v.y);
+            v.z = fma(h, f.z, v.z);
+            const double tx = v.x * dt, ty = v.y * dt, tz = v.z * dt;
+            double4 x = d.pos[i];
+            x.x += tx;
+            x.y += ty;
+            x.z += tz;
+            d.pos[i] = x;
+            float4 ph = d.pos2[2 * i], pl = d.pos2[2 * i + 1];
+            two_float_add(ph.x, pl.x, (float)tx);
+            two_float_add(ph.y, pl.y, (float)ty);
+            two_float_add(ph.z, pl.z, (float)tz);
+            d.pos2[2 * i] = ph;
+            d.pos2[2 * i + 1] = pl;
+            const float4 bh = d.lbp2[2 * i], bl = d.lbp2[2 * i + 1];
+            const float dx = (ph.x - bh.x) + (pl.x - bl.x);
+            const float dy = (ph.y - bh.y) + (pl.y - bl.y);
+            const float dz = (ph.z - bh.z) + (pl.z - bl.z);
+            bool nd = dx * dx + dy * dy + dz * dz > sp.disp_thr2f;
+            if (sp.every > 0) nd = (sp.check && nd) || ssb >= sp.every;
+            if (!nd && sp.policy == 0) {
+                const float rx = ph.x + pl.x, ry = ph.y + pl.y, rz = ph.z + pl.z;
+                nd = rx < 0.f || rx >= sp.Lh[0] || ry < 0.f || ry >= sp.Lh[1] || rz < 0.f || rz >= sp.Lh[2];
+            }
+            need = nd;
+        }
+        d.vel[i] = v;
+        if (sp.kind == 0) {
+            double4 w = d.omg[i];
+            if (w.w != 0.0) {
+                const double4 tq = d.trq[i];
+                const double hw = 0.5 * dt * w.w;
+                if (fin) {
+                    w.x = fma(hw, tq.x, w.x);
+                    w.y = fma(hw, tq.y, w.y);
+                    w.z = fma(hw, tq.z, w.z);
+                }
+                if (ini) {
+                    w.x = fma(hw, tq.x, w.x);
+                    w.y = fma(hw, tq.y, w.y);
+                    w.z = fma(hw, tq.z, w.z);
+                    const float wx = (float)w.x, wy = (float)w.y, wz = (float)w.z;
+                    const float om = sqrtf(wx * wx + wy * wy + wz * wz);
+                    const float angle = om * (float)dt;
+                    if (angle > 1e-14f) {
+                        const float half = 0.5f * angle;
+                        const float sq = sinf(0.5f * half);
+                        const double c1 = (double)(-2.f * sq * sq);
+                        const float k = sinf(half) / om;
+                        const double a1 = (double)(wx * k), a2 = (double)(wy * k), a3 = (double)(wz * k);
+                        const double4 q = d.quat[i];
+                        double4 r;
+                        r.x = fma(c1, q.x, q.x) - (a1 * q.y + a2 * q.z + a3 * q.w);
+                        r.y = fma(c1, q.y, q.y) + (a1 * q.x + a2 * q.w - a3 * q.z);
+                        r.z = fma(c1, q.z, q.z) + (a2 * q.x + a3 * q.y - a1 * q.w);
+                        r.w = fma(c1, q.w, q.w) + (a3 * q.x + a1 * q.z - a2 * q.y);
+                        d.quat[i] = r;
+                    }
+                }
+                d.omg[i] = w;
+            }
+        }
+    }
+    if (__any_sync(0xffffffffu, need) && (threadIdx.x & 31) == 0) atomicOr(&st->rb_next, 1);
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&st->status, ST_NAN);
+    if (was) {  // uniform over the system's blocks
+        bool last;
+        double tot = 0.0;
+        if (fin && sp.nh) {
+            const double v1[1] = {ke2};
+            double o1[1];
+            last = system_reduce<1>(d, s, gb, v1, o1);
+            tot = o1[0];
+        } else {
+            last = system_last(d, s);
+        }
+        if (last && threadIdx.x == 0) {
+            if (fin) step_end(sp, st, tot, nullptr, 1);  // clears this step's flags
+            if (ini) {
+                st->rebuild |= st->rb_next;
+                st->periodic_sort =
+                    (sp.policy == 0 && sp.sort_every > 0 && st->sort_counter + 1 >= sp.sort_every) ? 1 : 0;
+            }
+            st->rb_next = 0;
+        }
+    }
+    if (d.use_cond) {
+        // grid-wide last block: open the rebuild branch when some running
+        // system rebuilds or sorts in the step that starts now
+        __shared__ int glast;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            glast = atomicAdd(d.grid_ctr, 1u) == (unsigned)(gridDim.x - 1);
+        }
+        __syncthreads();
+        if (glast && threadIdx.x == 0) {
+            __threadfence();
+            unsigned int any = 0;
+            for (int q = 0; q < d.nrun_sys; q++) {
+                const SysState* o = d.ss + d.run_sys[q];
+                if (sys_active(o))
+                    any |= (unsigned)(*((const volatile int*)&o->rebuild) | *((const volatile int*)&o->periodic_sort));
+            }
+            *d.grid_ctr = 0;
+            if (any) d.stat_ctr[0] += 1;
+            cudaGraphSetConditional((cudaGraphConditionalHandle)d.cond, any ? 1u : 0u);
+        }
+    }
+}
+
+int launch_step_mixed(const Dev& d, const long long* loop, cudaStream_t st) {
+    k_step_mixed<<<d.nrun, BLK, 0, st>>>(d, loop);
+    return 1;
+}
+
+int launch_initial_mixed(const Dev& d, cudaStream_t st, int nh_only, const long long* loop) {
+    k_initial_mixed<<<d.nrun, BLK, 0, st>>>(d, nh_only, loop);
     return 1;
 }
 

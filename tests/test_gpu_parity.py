@@ -287,3 +287,36 @@ def test_non_finite_state_reports_nan(gpu_lib, precision):
         ctx.step(2)
     assert e.value.status == 6  # MDG_ERR_NAN
     assert ctx.status() != 0
+
+
+def test_fused_multistep_equals_unfused(gpu_lib):
+    """The multi-step graph of a mixed context fuses each step's final half
+    with the next step's initial half (one pass over the particle arrays); the
+    result must be bitwise the eager launches' (separate initial and final
+    kernels): a thermostatted LJ melt and two DEM gases in one batch, one gas
+    with a step budget that ends inside a launch, over several launches."""
+    from mddem_gb300 import capi, config, inputs
+
+    cfgs = [config.lj_fluid_config(precision="mixed", policy="displacement"),
+            config.granular_gas_config(box=0.02, dt=2e-7, precision="mixed", policy="displacement"),
+            config.granular_gas_config(box=0.012, dt=1e-7, precision="mixed")]
+    sts = [inputs.lj_fcc(6, 10.06, 0.85, 0.85, seed=31), inputs.dem_granular_gas(400, box=0.02, seed=32),
+           _dem_state(seed=33, n=600)]
+    out = []
+    for graph in (1, 0):
+        c = capi.Context(cfgs, [len(s["tag"]) for s in sts])
+        for k, s in enumerate(sts):
+            c.upload(s, k)
+        c.set_graph_mode(graph)
+        c.set_remaining(23, 1)
+        for n in (1, 17, 40, 5):
+            c.step(n)
+        out.append([c.download(k) for k in range(3)] + [[c.thermo(k) for k in range(3)]])
+    for k in range(3):
+        for f in ("pos", "vel") + (("omega", "quat") if k else ()):
+            (a,) = by_tag(out[0][k], f)
+            (b,) = by_tag(out[1][k], f)
+            assert np.array_equal(a, b), (k, f)
+    for ta, tb in zip(out[0][3], out[1][3]):
+        assert ta["step"] == tb["step"] and ta["nbuilds"] == tb["nbuilds"] and ta["p_xi"] == tb["p_xi"]
+    assert out[0][3][1]["step"] == 23
