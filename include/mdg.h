@@ -155,6 +155,10 @@ typedef struct mdg_thermo_t {
     int32_t max_neighbors;   /* largest full-list row seen at the last build */
     double e_tail, p_tail;   /* LJ long-range tail corrections (setup_lj_tails,
                                 md_lj/src/lib.rs:397-445); 0 for DEM */
+    double rot_temp;         /* DEM: sum 0.4 m r^2 |omega|^2 / (3 M)
+                                (examples/bench_sphere_haff_cooling/main.rs:88-105) */
+    double pressure;         /* rho T - tr(virial) / (3 V) + P_tail (compute_pressure,
+                                md_measure/src/lib.rs:605-652; virial 0 unless enabled) */
 } mdg_thermo_t;
 
 typedef struct mdg_ctx mdg_ctx;
@@ -234,6 +238,19 @@ typedef struct mdg_tune_result {
     int trials;
 } mdg_tune_result;
 int  mdg_autotune(mdg_ctx* ctx, const mdg_tune_opts* opts, mdg_tune_result* out);
+
+/* ---- measurements (md_measure/src/lib.rs) ----------------------------------
+ * mdg_rdf: pair counts per bin of width r_max / nbins over all pairs of one
+ * system under the minimum image (accumulate_rdf's single-rank loop,
+ * lib.rs:333-410, same fp64 arithmetic: the counts equal the reference's on
+ * the same positions); counts (nbins <= 4096 entries, host) are overwritten.
+ * g(r) = counts_k V / (N (N - 1) / 2 x 4/3 pi (r_{k+1}^3 - r_k^3)).
+ * mdg_msd_reset records every particle's unwrapped position (x + image L) by
+ * tag; mdg_msd returns the mean of |unwrapped - recorded|^2 (track_msd,
+ * lib.rs:459-600). */
+int  mdg_rdf(mdg_ctx* ctx, int sys, double r_max, int nbins, uint64_t* counts);
+int  mdg_msd_reset(mdg_ctx* ctx, int sys);
+int  mdg_msd(mdg_ctx* ctx, int sys, double* msd);
 
 /* The context's CUDA stream (cudaStream_t): all of the context's device work
  * is ordered on it, so a caller may record events on it or make its own

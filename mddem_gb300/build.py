@@ -30,6 +30,7 @@ UNITS = [
     ("mdg_kernels_mixed.cu", []),
     ("mdg_api.cu", ["-fmad=false"]),
     ("mdg_noalloc.cu", ["-fmad=false"]),
+    ("mdg_measure.cu", ["-fmad=false"]),
     ("mdg_serve.cpp", []),
     ("mdg_insert.cpp", []),
     ("mdg_tune.cpp", []),

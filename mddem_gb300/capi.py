@@ -34,7 +34,7 @@ EXPORTS = [
     "mdg_server_submit", "mdg_server_pump", "mdg_server_poll", "mdg_server_fetch", "mdg_server_context",
     "mdg_rsa_spheres", "mdg_get_progress", "mdg_get_stream", "mdg_server_stats",
     "mdg_server_resident", "mdg_get_config", "mdg_set_threads_per_particle", "mdg_get_threads_per_particle",
-    "mdg_autotune",
+    "mdg_autotune", "mdg_rdf", "mdg_msd_reset", "mdg_msd",
 ]
 
 
@@ -86,6 +86,7 @@ class Thermo(C.Structure):
         ("granular_temp", C.c_double), ("momentum", C.c_double), ("virial", C.c_double * 6),
         ("step", C.c_int64), ("nbuilds", C.c_int64), ("n", C.c_int64), ("status", C.c_int32),
         ("max_neighbors", C.c_int32), ("e_tail", C.c_double), ("p_tail", C.c_double),
+        ("rot_temp", C.c_double), ("pressure", C.c_double),
     ]
 
 
@@ -164,6 +165,9 @@ def load(path: str = LIB_PATH):
     lib.mdg_server_fetch.argtypes = [C.c_void_p, C.c_int64, C.POINTER(StateView)]
     lib.mdg_server_context.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
     lib.mdg_get_progress.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
+    lib.mdg_rdf.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_uint64)]
+    lib.mdg_msd_reset.argtypes = [C.c_void_p, C.c_int]
+    lib.mdg_msd.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
     lib.mdg_set_threads_per_particle.argtypes = [C.c_void_p, C.c_int]
     lib.mdg_get_threads_per_particle.argtypes = [C.c_void_p]
     lib.mdg_autotune.argtypes = [C.c_void_p, C.POINTER(TuneOpts), C.POINTER(TuneResult)]
@@ -526,6 +530,29 @@ class Context:
         _check(self.lib.mdg_autotune(self.h, C.byref(o), C.byref(r)), "mdg_autotune")
         return {"tpp": r.tpp, "skin_fraction": list(r.skin_fraction), "bin_factor": list(r.bin_factor),
                 "ms_before": r.ms_before, "ms_after": r.ms_after, "trials": r.trials}
+
+    def rdf(self, sys=0, r_max=3.0, nbins=200):
+        """mdg_rdf: (r_low, g, counts) with the reference's normalisation
+        g_k = counts_k V / (N (N-1)/2 x shell_k) (md_measure/src/lib.rs:420-440)."""
+        counts = np.zeros(nbins, np.uint64)
+        _check(self.lib.mdg_rdf(self.h, sys, float(r_max), int(nbins), _ptr(counts, C.c_uint64)), "mdg_rdf")
+        cfg = self.configs[sys]
+        vol = float(np.prod(cfg.box))
+        n = float(self.thermo(sys)["n"])
+        dr = r_max / nbins
+        k = np.arange(nbins, dtype=np.float64)
+        shell = (4.0 / 3.0) * np.pi * (((k + 1) * dr) ** 3 - (k * dr) ** 3)
+        npairs = n * (n - 1.0) / 2.0
+        g = counts.astype(np.float64) * vol / (npairs * shell)
+        return k * dr, g, counts
+
+    def msd_reset(self, sys=0):
+        _check(self.lib.mdg_msd_reset(self.h, sys), "mdg_msd_reset")
+
+    def msd(self, sys=0):
+        v = C.c_double()
+        _check(self.lib.mdg_msd(self.h, sys, C.byref(v)), "mdg_msd")
+        return v.value
 
     def threads_per_particle(self, tpp=None):
         if tpp is not None:

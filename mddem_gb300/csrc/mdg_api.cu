@@ -145,6 +145,15 @@ struct mdg_ctx {
     cudaGraphExec_t tgraph = nullptr;                 // timed single-step graph
     long long* d_loop = nullptr;  // {iterations left, iterations of the launch} of the WHILE graph
     bool run_nh = false;          // some running system is thermostatted
+    // measurement scratch (allocated on first use, grown when needed)
+    float4* rdf_posf = nullptr;
+    long long rdf_posf_n = 0;
+    unsigned long long* rdf_counts = nullptr;
+    int rdf_counts_n = 0;
+    std::vector<double*> msd_ref;       // per system: unwrapped positions by tag
+    std::vector<long long> msd_ntag;    // per system: tags covered (max tag + 1)
+    double* msd_part = nullptr;
+    long long msd_part_n = 0;
     cudaEvent_t tev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     int tkernels = 0;
     void* flush_buf = nullptr;
@@ -1258,6 +1267,81 @@ int mdg_set_threads_per_particle(mdg_ctx* c, int tpp) {
 
 int mdg_get_threads_per_particle(const mdg_ctx* c) { return c ? c->tpp_lj : 0; }
 
+int mdg_rdf(mdg_ctx* c, int sys, double r_max, int nbins, uint64_t* counts) {
+    if (!c || !counts || sys < 0 || sys >= c->nsys || nbins < 1 || nbins > rdf_max_bins() || !(r_max > 0.0))
+        return MDG_ERR_ARG;
+    if (!c->uploaded[sys]) return MDG_ERR_STATE;
+    const SysParams& p = c->sp[sys];
+    int err = 0;
+    if (c->rdf_posf_n < p.n) {
+        c->free_ptr(c->rdf_posf);
+        c->rdf_posf = c->alloc<float4>(p.n, err);
+        if (err) return err;
+        c->rdf_posf_n = p.n;
+    }
+    if (c->rdf_counts_n < nbins) {
+        c->free_ptr(c->rdf_counts);
+        c->rdf_counts = c->alloc<unsigned long long>(nbins, err);
+        if (err) return err;
+        c->rdf_counts_n = nbins;
+    }
+    cudaMemsetAsync(c->rdf_counts, 0, nbins * sizeof(unsigned long long), c->stream);
+    c->launches += launch_rdf(c->d, sys, p, c->rdf_posf, r_max, nbins, c->rdf_counts, c->stream);
+    cudaError_t e = cudaMemcpyAsync(counts, c->rdf_counts, nbins * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                    c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    return cuda_err(e == cudaSuccess ? cudaGetLastError() : e);
+}
+
+int mdg_msd_reset(mdg_ctx* c, int sys) {
+    if (!c || sys < 0 || sys >= c->nsys) return MDG_ERR_ARG;
+    if (!c->uploaded[sys]) return MDG_ERR_STATE;
+    const SysParams& p = c->sp[sys];
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(e);
+    std::vector<uint32_t> tag(p.n);
+    e = cudaMemcpy(tag.data(), c->d.tag + p.p0, p.n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(e);
+    long long ntag = 0;
+    for (uint32_t t : tag) ntag = std::max(ntag, (long long)t + 1);
+    if (c->msd_ref.empty()) {
+        c->msd_ref.assign(c->nsys, nullptr);
+        c->msd_ntag.assign(c->nsys, 0);
+    }
+    int err = 0;
+    if (c->msd_ntag[sys] < ntag) {
+        c->free_ptr(c->msd_ref[sys]);
+        c->msd_ref[sys] = c->alloc<double>(3 * ntag, err);
+        if (err) return err;
+        c->msd_ntag[sys] = ntag;
+    }
+    c->launches += launch_msd_ref(c->d, sys, p.n, c->msd_ref[sys], c->stream);
+    return cuda_err(cudaStreamSynchronize(c->stream));
+}
+
+int mdg_msd(mdg_ctx* c, int sys, double* msd) {
+    if (!c || !msd || sys < 0 || sys >= c->nsys) return MDG_ERR_ARG;
+    if (!c->uploaded[sys] || c->msd_ref.empty() || !c->msd_ref[sys]) return MDG_ERR_STATE;
+    const SysParams& p = c->sp[sys];
+    const long long nb = (p.n + BLK - 1) / BLK;
+    int err = 0;
+    if (c->msd_part_n < nb) {
+        c->free_ptr(c->msd_part);
+        c->msd_part = c->alloc<double>(nb, err);
+        if (err) return err;
+        c->msd_part_n = nb;
+    }
+    c->launches += launch_msd(c->d, sys, p.n, c->msd_ref[sys], c->msd_part, c->stream);
+    std::vector<double> part(nb);
+    cudaError_t e = cudaMemcpyAsync(part.data(), c->msd_part, nb * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(e);
+    double sum = 0.0;
+    for (double x : part) sum += x;
+    *msd = sum / (double)p.n;
+    return cuda_err(cudaGetLastError());
+}
+
 int mdg_get_stream(mdg_ctx* c, void** stream) {
     if (!c || !stream) return MDG_ERR_ARG;
     *stream = (void*)c->stream;
@@ -1340,6 +1424,7 @@ int mdg_thermo(mdg_ctx* c, int sys, mdg_thermo_t* out) {
     out->n = p.n;
     out->status = ss.status;
     out->max_neighbors = ss.max_nbr;
+    out->rot_temp = t[6];
     out->e_tail = out->p_tail = 0.0;
     if (p.kind == MDG_KIND_LJ) {
         // setup_lj_tails (md_lj/src/lib.rs:397-445), one type: rho = N / V,
@@ -1356,6 +1441,12 @@ int mdg_thermo(mdg_ctx* c, int sys, mdg_thermo_t* out) {
         out->e_tail = (8.0 / 3.0) * pi * n * rho * k.lj_epsilon * sigma3 * (sigma9 / (3.0 * rc9) - sigma3 / rc3);
         out->p_tail =
             (16.0 / 3.0) * pi * rho * rho * k.lj_epsilon * sigma3 * (2.0 * sigma9 / (3.0 * rc9) - sigma3 / rc3);
+    }
+    {
+        // compute_pressure (md_measure/src/lib.rs:605-652): rho T - tr(W) / (3V) + P_tail
+        const double v = p.L[0] * p.L[1] * p.L[2];
+        const double trace = out->virial[0] + out->virial[1] + out->virial[2];
+        out->pressure = (double)p.n / v * out->temp - trace / (3.0 * v) + out->p_tail;
     }
     return cuda_err(cudaGetLastError());
 }

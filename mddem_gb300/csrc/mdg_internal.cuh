@@ -388,6 +388,11 @@ __device__ __forceinline__ int rb_find(const int* off, int n, int v) {
 int launch_initial(const Dev& d, cudaStream_t st);
 int launch_initial_mixed(const Dev& d, cudaStream_t st, int nh_only = 0, const long long* loop = nullptr);
 int launch_step_mixed(const Dev& d, const long long* loop, cudaStream_t st);
+int launch_rdf(const Dev& d, int s, const SysParams& sp, float4* posf, double r_max, int nbins,
+               unsigned long long* counts, cudaStream_t st);
+int launch_msd_ref(const Dev& d, int s, int n, double* ref, cudaStream_t st);
+int launch_msd(const Dev& d, int s, int n, const double* ref, double* part, cudaStream_t st);
+int rdf_max_bins();
 int launch_rebuild_tail_mixed(const Dev& d, int has_dem, cudaStream_t st);
 int launch_final_mixed(const Dev& d, cudaStream_t st, int integrate);
 int launch_rebuild(const Dev& d, cudaStream_t st);

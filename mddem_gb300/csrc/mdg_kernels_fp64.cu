@@ -1273,7 +1273,7 @@ __global__ void __launch_bounds__(BLK) k_thermo1(Dev d, double* out16) {
     const SysParams& sp = d.sp[s];
     if (gb - sp.b0 >= sp.nb) return;  // past the particles: not in the reduction
     const int li = (gb - sp.b0) * BLK + threadIdx.x;
-    double vals[6] = {0, 0, 0, 0, 0, 0};
+    double vals[7] = {0, 0, 0, 0, 0, 0, 0};
     if (li < sp.n) {
         const long long i = (long long)sp.p0 + li;
         const double4 v = d.vel[i];
@@ -1284,13 +1284,22 @@ __global__ void __launch_bounds__(BLK) k_thermo1(Dev d, double* out16) {
         vals[3] = m * v.z;
         vals[4] = m * (v.x * v.x + v.y * v.y + v.z * v.z);
         vals[5] = d.frc[i].w;
+        if (sp.kind == 0) {
+            // rotational term I |omega|^2 with I = 0.4 m r^2
+            // (examples/bench_sphere_haff_cooling/main.rs:88-100)
+            const double r = d.pos[i].w;
+            const double4 w = d.omg[i];
+            const double inertia = 0.4 * m * r * r;
+            vals[6] = inertia * (w.x * w.x + w.y * w.y + w.z * w.z);
+        }
     }
-    double out[6];
-    if (system_reduce<6>(d, s, gb, vals, out) && threadIdx.x == 0) {
+    double out[7];
+    if (system_reduce<7>(d, s, gb, vals, out) && threadIdx.x == 0) {
         double* o = out16 + (size_t)s * 16;
         o[0] = 0.5 * out[4];
         o[1] = out[5];
         o[5] = sqrt(out[1] * out[1] + out[2] * out[2] + out[3] * out[3]);
+        o[6] = out[0] > 0.0 ? out[6] / (3.0 * out[0]) : 0.0;  // T_rot = sum I w^2 / (3 M)
         o[8 + 0] = out[0];
         o[8 + 1] = out[1] / out[0];
         o[8 + 2] = out[2] / out[0];
