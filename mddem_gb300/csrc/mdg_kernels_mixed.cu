@@ -25,8 +25,13 @@ struct Kahan {
 
 // LJ 12-6 in FP32 with compensated per-particle sums (same list, same owner
 // frames as the FP64 kernel).
+// Minimum resident blocks per SM asked of ptxas for k_lj_mixed (a compile-time
+// tuning knob; 8 caps it at 64 registers).
+#ifndef MDG_LJ_MINB
+#define MDG_LJ_MINB 8
+#endif
 template <int TPP>
-__global__ void __launch_bounds__(BLK, 8) k_lj_mixed(Dev d) {
+__global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
     const int pb = d.blk_run[blockIdx.x / TPP];
     const int sub = blockIdx.x % TPP;
     const int s = d.blk_sys[pb];

@@ -1,0 +1,190 @@
+"""Run a reference TOML config on the GPU path: ``python -m mddem_gb300.run config.toml``.
+
+The host side of the reference's ``App`` for this path (examples/*/main.rs with
+CorePlugins + GranularDefaultPlugins or LJDefaultPlugins): the TOML sections
+the hot path reads (``config.from_toml``), the initial state from ``[lattice]``
+(FCC, crates/md_lattice/src/lib.rs:232-471) or ``[[particles.insert]]``
+(random insertion, crates/dem_atom/src/insert.rs:417-614: region = domain
+inset by the radius, rejection at 1.1 (r_i + r_j), per-component Gaussian
+velocities of std ``velocity`` plus ``velocity_x/y/z``; or ``source = "file"``
+CSV, insert.rs:652-776), the timestep (``[run] dt``, else 0.15 Rayleigh time
+of the smallest sphere, insert.rs:1392-1431, or 0.005 for a lattice), then
+``[run] steps`` steps with a thermo line every ``[run] thermo`` steps,
+``[measure]`` RDF / MSD sampling (md_measure) written at the end, and
+``[restart]`` files in the reference's format every ``interval`` steps.
+The state lives on the GPU throughout; the host only sees thermo values and
+the states it writes.
+"""
+from __future__ import annotations
+
+import argparse
+import math
+import os
+import sys
+import time
+import tomllib
+
+import numpy as np
+
+from . import capi, config, inputs, restart
+
+
+class RunError(ValueError):
+    pass
+
+
+def _insert(doc, cfg, seed):
+    blocks = doc.get("particles", {}).get("insert", [])
+    if not blocks:
+        raise RunError("a DEM config needs [[particles.insert]]")
+    names = [m.name for m in cfg.materials]
+    states = []
+    for k, b in enumerate(blocks):
+        if b.get("source", "random") == "file":
+            if b.get("format", "csv") != "csv":
+                raise RunError(f"insert source format {b.get('format')!r}: only csv is supported")
+            states.append(inputs.read_csv(b["file"], density=float(b.get("density", 2500.0))))
+            continue
+        if "rate" in b:
+            raise RunError("rate-based insertion is not supported")
+        n = int(b["count"])
+        rad = b["radius"]
+        if isinstance(rad, dict):
+            if rad.get("distribution") != "uniform":
+                raise RunError(f"radius distribution {rad.get('distribution')!r}: fixed or uniform only")
+            rmin, rmax = float(rad["min"]), float(rad["max"])
+        else:
+            rmin = rmax = float(rad)
+        lo = cfg.box_lo
+        hi = cfg.box_hi
+        if b.get("region"):
+            raise RunError("insertion regions other than the domain are not supported")
+        pos, r = capi.rsa_spheres(n, lo, hi, rmin, rmax, sep_factor=1.1, inset=True, seed=seed + k)
+        rng = np.random.default_rng(seed + 7919 * (k + 1))
+        v = float(b.get("velocity", 0.0))
+        vel = rng.normal(0.0, v, size=(n, 3)) if v > 0.0 else np.zeros((n, 3))
+        vel += np.array([float(b.get("velocity_x", 0.0)), float(b.get("velocity_y", 0.0)),
+                         float(b.get("velocity_z", 0.0))])
+        mat = b.get("material", names[0])
+        if mat not in names:
+            raise RunError(f"material {mat!r} is not in [[dem.materials]]")
+        st = inputs._dem_state(pos, vel, r, float(b["density"]), mtype=np.full(n, names.index(mat)))
+        states.append(st)
+    if len(states) == 1:
+        return states[0]
+    out = {}
+    for key in states[0]:
+        if isinstance(states[0][key], np.ndarray):
+            out[key] = np.concatenate([s[key] for s in states])
+    out["tag"] = np.arange(len(out["tag"]), dtype=np.uint32)
+    return out
+
+
+def setup(text, seed=0, precision=None):
+    """(config, initial state, run settings) from a reference TOML text."""
+    doc = tomllib.loads(text)
+    cfg = config.from_toml(text)
+    if precision:
+        cfg = cfg.replace(precision=precision)
+    run = doc.get("run", {})
+    if isinstance(run, list):
+        run = run[0] if run else {}
+    if cfg.kind == "lj":
+        lat = doc.get("lattice")
+        if not lat or lat.get("style", "fcc") != "fcc":
+            raise RunError("an LJ config needs [lattice] style = \"fcc\"")
+        L = cfg.box[0]
+        rho = float(lat.get("density", 0.85))
+        ncell = int(math.floor(L / (4.0 / rho) ** (1.0 / 3.0)))
+        st = inputs.lj_fcc(ncell, L, rho, float(lat.get("temperature", 0.85)), mass=float(lat.get("mass", 1.0)),
+                           skin=float(lat.get("skin", 1.25)), seed=seed, lo=cfg.box_lo[0])
+    else:
+        st = _insert(doc, cfg, seed)
+        if cfg.dt == 0.0:
+            m = cfg.materials[0]
+            dens = np.asarray(st.get("density", np.full(len(st["tag"]), 2500.0)))
+            cfg = cfg.replace(dt=config.rayleigh_dt(float(np.min(st["radius"])), float(np.max(dens)),
+                                                    m.youngs_mod, m.poisson_ratio))
+    settings = {
+        "steps": int(run.get("steps", 1000)),
+        "thermo": int(run.get("thermo", 100)),
+        "measure": doc.get("measure", {}),
+        "restart": doc.get("restart", {}),
+        "output": doc.get("output", {}).get("dir", "output"),
+    }
+    return cfg, st, settings
+
+
+def thermo_line(step, t, kind):
+    if kind == "lj":
+        return (f"{step:10d} T {t['temp']:.6f} KE {t['ke']:.6e} PE {t['pe']:.6e} E {t['ke'] + t['pe']:.6e} "
+                f"P {t['pressure']:.5f}")
+    return (f"{step:10d} T_g {t['granular_temp']:.6e} T_rot {t['rot_temp']:.6e} KE {t['ke']:.6e} "
+            f"|P| {t['momentum']:.3e}")
+
+
+def run(text, seed=0, precision=None, steps=None, out=sys.stdout):
+    cfg, st, s = setup(text, seed, precision)
+    nsteps = s["steps"] if steps is None else steps
+    n = len(st["tag"])
+    ctx = capi.Context(cfg, n)
+    ctx.upload(st)
+    meas = s["measure"]
+    rdf_every = int(meas.get("rdf_interval", 0)) if cfg.kind == "lj" and meas else 0
+    msd_every = int(meas.get("msd_interval", 0)) if cfg.kind == "lj" and meas else 0
+    nbins, rmax = int(meas.get("rdf_bins", 200)), float(meas.get("rdf_cutoff", 3.0))
+    rs = s["restart"]
+    rst_every = int(rs.get("interval", 0)) if rs else 0
+    fmt = rs.get("format", "bincode") if rs else "bincode"
+    if rst_every or rdf_every or msd_every:
+        os.makedirs(s["output"], exist_ok=True)
+    g_sum, g_n, msd = None, 0, []
+    if msd_every:
+        ctx.msd_reset()
+    marks = sorted({k for every in (s["thermo"], rdf_every, msd_every, rst_every) if every
+                    for k in range(every, nsteps + 1, every)} | {nsteps})
+    print(f"# {cfg.kind} N={n} dt={cfg.dt:.6e} steps={nsteps} precision={cfg.precision}", file=out)
+    print(thermo_line(0, ctx.thermo(), cfg.kind), file=out)
+    done, t0 = 0, time.perf_counter()
+    for k in marks:
+        ctx.step(k - done)  # one graph launch for all the steps up to the next mark
+        done = k
+        if s["thermo"] and k % s["thermo"] == 0 or k == nsteps:
+            print(thermo_line(k, ctx.thermo(), cfg.kind), file=out)
+        if rdf_every and k % rdf_every == 0:
+            r, g, _ = ctx.rdf(r_max=rmax, nbins=nbins)
+            g_sum = g if g_sum is None else g_sum + g
+            g_n += 1
+        if msd_every and k % msd_every == 0:
+            msd.append((k, ctx.msd()))
+        if rst_every and k % rst_every == 0:
+            p = os.path.join(s["output"], restart.restart_filename(k, 0, fmt))
+            hist = ctx.history() if cfg.kind == "dem" else None
+            restart.write_restart(p, ctx.download(), hist, step=k, dt=cfg.dt, fmt=fmt)
+    el = time.perf_counter() - t0
+    print(f"# {nsteps} steps in {el:.3f} s: {n * nsteps / max(el, 1e-9):.4e} particle-steps/s", file=out)
+    if g_n:
+        with open(os.path.join(s["output"], "rdf.txt"), "w") as f:
+            for rr, gg in zip((np.arange(nbins) + 0.5) * rmax / nbins, g_sum / g_n):
+                f.write(f"{rr:.6f} {gg:.6f}\n")
+    if msd:
+        with open(os.path.join(s["output"], "msd.txt"), "w") as f:
+            for k, v in msd:
+                f.write(f"{k} {v:.10e}\n")
+    return ctx
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description="Run a reference TOML config on the GB300 hot path")
+    ap.add_argument("config")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default=None)
+    ap.add_argument("--steps", type=int, default=None)
+    a = ap.parse_args(argv)
+    with open(a.config, "rb") as f:
+        text = f.read().decode()
+    run(text, a.seed, a.precision, a.steps)
+
+
+if __name__ == "__main__":
+    main()
