@@ -118,6 +118,14 @@ typedef struct mdg_config {
     int threads_per_particle;    /* 0 = auto; 1,2,4,8,16,32 for the force kernels */
     int neighbor_capacity;       /* 0 = auto: max full-list entries per particle */
     int history_capacity;        /* 0 = auto: max stored contacts per particle */
+    /* [langevin] (crates/md_thermostat/src/lib.rs:380-581): at PostForce
+     * F += -gamma m v + sqrt(2 gamma m kT / dt) N(0,1) per component.  The
+     * reference draws from one ChaCha8 stream in atom order; here N(0,1) comes
+     * from a counter-based stream keyed by (seed, step, tag, component), so a
+     * run is reproducible and independent of particle order and batching. */
+    int langevin;
+    double lv_temperature, lv_damping;
+    uint64_t lv_seed;
 } mdg_config;
 
 /* SoA view of one system's particles (caller-owned, n particles). */

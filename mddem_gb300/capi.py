@@ -65,6 +65,7 @@ class Config(C.Structure):
         ("virial", C.c_int),
         ("rebuild_policy", C.c_int), ("threads_per_particle", C.c_int), ("neighbor_capacity", C.c_int),
         ("history_capacity", C.c_int),
+        ("langevin", C.c_int), ("lv_temperature", C.c_double), ("lv_damping", C.c_double), ("lv_seed", C.c_uint64),
     ]
 
 
@@ -225,6 +226,8 @@ def to_c_config(c: SimConfig):
     cc.threads_per_particle = int(c.threads_per_particle)
     cc.neighbor_capacity = int(c.neighbor_capacity)
     cc.history_capacity = int(c.history_capacity)
+    cc.langevin = int(c.langevin)
+    cc.lv_temperature, cc.lv_damping, cc.lv_seed = float(c.lv_temperature), float(c.lv_damping), int(c.lv_seed)
     return cc, mats
 
 

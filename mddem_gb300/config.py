@@ -74,6 +74,10 @@ class SimConfig:
     threads_per_particle: int = 0
     neighbor_capacity: int = 0
     history_capacity: int = 0
+    langevin: bool = False
+    lv_temperature: float = 0.85
+    lv_damping: float = 1.0
+    lv_seed: int = 12345
 
     def replace(self, **kw) -> "SimConfig":
         return dataclasses.replace(self, **kw)
@@ -89,6 +93,7 @@ _SECTIONS = {
     "neighbor": {"skin_fraction", "bin_size", "every", "check", "sort_every", "newton"},
     "lj": {"epsilon", "sigma", "cutoff", "mixing", "types", "pair_coeffs"},
     "thermostat": {"temperature", "coupling", "group"},
+    "langevin": {"temperature", "damping", "seed", "group"},
     "gpu": {"precision", "rebuild_policy", "threads_per_particle", "neighbor_capacity", "history_capacity",
             "virial"},
 }
@@ -163,6 +168,15 @@ def from_toml(text: str, kind: str | None = None) -> SimConfig:
             c.nose_hoover = True
             c.nh_temperature = float(th.get("temperature", 0.85))
             c.nh_coupling = float(th.get("coupling", 1.0))
+    lv = doc.get("langevin")
+    if lv is not None:
+        _check_keys("langevin", lv, _SECTIONS["langevin"])
+        if lv.get("group"):
+            raise ConfigError("thermostat groups are not supported by the GPU path")
+        c.langevin = True
+        c.lv_temperature = float(lv.get("temperature", 0.85))
+        c.lv_damping = float(lv.get("damping", 1.0))
+        c.lv_seed = int(lv.get("seed", 12345))
     gpu = doc.get("gpu", {})
     _check_keys("gpu", gpu, _SECTIONS["gpu"])
     for k in ("precision", "rebuild_policy", "threads_per_particle", "neighbor_capacity", "history_capacity",

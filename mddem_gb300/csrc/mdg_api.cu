@@ -99,6 +99,7 @@ int validate_config(const mdg_config& c) {
         if (!(c.lj_epsilon > 0.0) || !(c.lj_sigma > 0.0) || !(c.lj_cutoff > 0.0)) return MDG_ERR_CONFIG;
     }
     if (c.nose_hoover && (!(c.nh_temperature > 0.0) || !(c.nh_coupling > 0.0))) return MDG_ERR_CONFIG;
+    if (c.langevin && (c.nose_hoover || !(c.lv_temperature >= 0.0) || !(c.lv_damping >= 0.0))) return MDG_ERR_CONFIG;
     if (c.precision == MDG_MIXED && c.virial) return MDG_ERR_CONFIG;
     const int t = c.threads_per_particle;
     if (!(t == 0 || t == 1 || t == 2 || t == 4 || t == 8)) return MDG_ERR_CONFIG;
@@ -214,6 +215,10 @@ void apply_physics(mdg_ctx* c, int s, const mdg_config& k, std::vector<double>& 
     p.sort_every = k.sort_every;
     p.newton = k.newton;
     p.virial = k.virial;
+    p.lv = k.langevin && k.lv_damping > 0.0;  // gamma = 0: no forces (langevin_force's early return)
+    p.lv_gamma = k.lv_damping;
+    p.lv_kT = k.lv_temperature;
+    p.lv_seed = (unsigned long long)k.lv_seed;
     p.tpp = k.threads_per_particle ? k.threads_per_particle : 1;
     tabs.clear();
     if (k.kind == MDG_KIND_DEM) {

@@ -45,6 +45,10 @@ struct SysParams {
     int p0, n, npad;     // particle segment
     int b0, nb;          // first particle block; blocks holding the n particles
     int ncb;             // cell blocks of the system's cell segment
+    // Langevin ([langevin]): drag gamma, noise kT, seed of the counter-based stream
+    int lv;
+    double lv_gamma, lv_kT;
+    unsigned long long lv_seed;
     int c0, ncell;       // ext-cell segment
     int nc[3];           // interior cells per axis
     int ext[3];          // extended grid (interior + 2*layers)
@@ -350,6 +354,42 @@ __device__ __forceinline__ bool system_last(const Dev& d, int s) {
     __syncthreads();
     if (last) __threadfence();
     return last;
+}
+
+// Langevin force at PostForce (langevin_force, md_thermostat/src/lib.rs:529-564):
+// f += -gamma m v + sqrt(2 gamma m kT / dt) N(0,1) per component, with m the
+// mass and v the half-kicked velocity.  N(0,1) by the Box-Muller cos branch
+// of normal_sample (lib.rs:571-577) from two uniforms of a counter-based
+// stream: the SplitMix64 finaliser (Steele, Lea & Flood 2014) over (seed,
+// step, tag, draw), so each particle's noise is independent of its storage
+// order.
+__device__ __forceinline__ unsigned long long lv_mix(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double lv_uniform(unsigned long long seed, long long step, unsigned int tag, int draw) {
+    const unsigned long long h =
+        lv_mix(seed + lv_mix((unsigned long long)step * 0x9e3779b97f4a7c15ull + lv_mix(((unsigned long long)tag << 3) + draw)));
+    return (double)(h >> 11) * 0x1.0p-53;
+}
+__device__ __forceinline__ double lv_normal(unsigned long long seed, long long step, unsigned int tag, int k) {
+    const double u1 = lv_uniform(seed, step, tag, 2 * k), u2 = lv_uniform(seed, step, tag, 2 * k + 1);
+    return sqrt(-2.0 * log(fmax(u1, 1e-300))) * cos(6.283185307179586 * u2);
+}
+__device__ __forceinline__ void langevin_add(const Dev& d, const SysParams& sp, const SysState* st, long long i,
+                                             const double4& v, double4& f) {
+    const double drag = sp.lv_gamma * d.mass[i];
+    const double rc = sqrt(2.0 * drag * sp.lv_kT / sp.dt);
+    const unsigned int tag = d.tag[i];
+    const long long step = st->step;
+    f.x = f.x - drag * v.x;
+    f.y = f.y - drag * v.y;
+    f.z = f.z - drag * v.z;
+    f.x = f.x + rc * lv_normal(sp.lv_seed, step, tag, 0);
+    f.y = f.y + rc * lv_normal(sp.lv_seed, step, tag, 1);
+    f.z = f.z + rc * lv_normal(sp.lv_seed, step, tag, 2);
+    d.frc[i] = f;  // the reference changes atoms.force: the next initial kick uses it
 }
 
 // entry k of a prefix array off[0..n] with off[k] <= v < off[k+1]

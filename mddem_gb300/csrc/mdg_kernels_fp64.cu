@@ -1189,8 +1189,9 @@ __global__ void __launch_bounds__(BLK) k_final(Dev d, int integrate) {
     double vals[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     int bad = 0;
     if (act) {
-        const double4 f = d.frc[i];
+        double4 f = d.frc[i];
         double4 v = d.vel[i];
+        if (integrate && sp.lv) langevin_add(d, sp, st, i, v, f);
         if (integrate) {
             const double h = 0.5 * dt * v.w;
             v.x += h * f.x;

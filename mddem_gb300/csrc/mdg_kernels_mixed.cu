@@ -664,8 +664,9 @@ __global__ void __launch_bounds__(BLK) k_final_mixed(Dev d, int integrate) {
     double ke2 = 0.0;
     int bad = 0;
     if (act) {
-        const double4 f = d.frc[i];
+        double4 f = d.frc[i];
         double4 v = d.vel[i];
+        if (integrate && sp.lv) langevin_add(d, sp, st, i, v, f);
         if (integrate) {
             const double h = 0.5 * dt * v.w;
             v.x = fma(h, f.x, v.x);
@@ -747,8 +748,9 @@ __global__ void __launch_bounds__(BLK) k_step_mixed(Dev d, const long long* loop
     int bad = 0, need = 0;
     if (li < sp.n && (fin || ini)) {
         double4 v = d.vel[i];
-        const double4 f = d.frc[i];
+        double4 f = d.frc[i];
         const double h = 0.5 * dt * v.w;
+        if (fin && sp.lv) langevin_add(d, sp, st, i, v, f);
         if (fin) {
             v.x = fma(h, f.x, v.x);
             v.y = fma(h, f.y, v.y);

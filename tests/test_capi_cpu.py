@@ -212,3 +212,24 @@ def test_rsa_spheres_reports_unplaceable(lib):
     with pytest.raises(capi.MdgError):  # solid fraction far above the RSA limit
         capi.rsa_spheres(5000, (0, 0, 0), (0.02, 0.02, 0.02), 1e-3, 1e-3, sep_factor=1.0, seed=1,
                          max_attempts=200000)
+
+
+def test_toml_langevin_section():
+    from mddem_gb300 import config
+
+    txt = """
+[domain]
+x_high = 10.06
+y_high = 10.06
+z_high = 10.06
+[lattice]
+density = 0.85
+[langevin]
+temperature = 1.1
+damping = 0.5
+seed = 9
+"""
+    c = config.from_toml(txt)
+    assert c.langevin and c.lv_temperature == 1.1 and c.lv_damping == 0.5 and c.lv_seed == 9
+    with pytest.raises(config.ConfigError):
+        config.from_toml(txt.replace("seed = 9", "seed = 9\nfriction = 1.0"))
