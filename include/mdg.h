@@ -72,7 +72,9 @@ enum {
     MDG_ERR_TIMEOUT = 8,       /* a bounded device wait gave up */
     MDG_ERR_ARG = 9,           /* bad argument (null pointer, index, size) */
     MDG_ERR_STATE = 10,        /* call out of order (e.g. step before upload) */
-    MDG_ERR_NODEVICE = 11      /* no CUDA device */
+    MDG_ERR_NODEVICE = 11,     /* no CUDA device */
+    MDG_ERR_LOST = 12          /* a particle left the box across a fixed boundary
+                                  (the reference removes it, domain.rs:434-452) */
 };
 
 enum { MDG_KIND_DEM = 0, MDG_KIND_LJ = 1 };
@@ -95,10 +97,24 @@ typedef struct mdg_material {
 } mdg_material;
 
 /* One simulation (a "system"): the TOML sections the plugins read. */
+/* Plane wall ([[wall]] type = "plane", crates/dem_wall/src/lib.rs:171-347):
+ * the plane through `point` with outward `normal` (normalised on use); active
+ * for particles inside [bound_lo, bound_hi] (use +-HUGE_VAL for unbounded);
+ * `velocity` a constant wall velocity; `material` an index into the config's
+ * materials.  Sphere-wall Hertz normal force with damping and adhesion and a
+ * twisting torque (wall_contact_force, lib.rs:848-990). */
+typedef struct mdg_wall {
+    double point[3], normal[3];
+    double bound_lo[3], bound_hi[3];
+    double velocity[3];
+    int material;
+} mdg_wall;
+#define MDG_MAX_WALLS 6
+
 typedef struct mdg_config {
     int kind;                    /* MDG_KIND_* */
     int precision;               /* MDG_FP64 or MDG_MIXED ([gpu] precision) */
-    double box_lo[3], box_hi[3]; /* [domain]; all three axes periodic */
+    double box_lo[3], box_hi[3]; /* [domain]; periodic unless `fixed` below */
     double dt;                   /* [run] dt (> 0) */
     /* [neighbor] (crates/mddem_core/src/neighbor.rs:44-80) */
     double skin_fraction, bin_size;
@@ -126,7 +142,14 @@ typedef struct mdg_config {
     int langevin;
     double lv_temperature, lv_damping;
     uint64_t lv_seed;
+    /* [domain] boundary_x/y/z = "fixed": no periodic images along that axis
+     * (0 = periodic, the default); particles must stay inside the box there. */
+    int fixed[3];
+    /* [[wall]] plane walls (DEM), at most MDG_MAX_WALLS */
+    int n_walls;
+    const mdg_wall* walls;
 } mdg_config;
+
 
 /* SoA view of one system's particles (caller-owned, n particles). */
 typedef struct mdg_state_view {

@@ -21,7 +21,7 @@ MDG_OK = 0
 STATUS_NAMES = {
     0: "MDG_OK", 1: "MDG_ERR_CONFIG", 2: "MDG_ERR_CUDA", 3: "MDG_ERR_OOM", 4: "MDG_ERR_BUDGET",
     5: "MDG_ERR_OVERLAP_LIMIT", 6: "MDG_ERR_NAN", 7: "MDG_ERR_LIST_OVERFLOW", 8: "MDG_ERR_TIMEOUT",
-    9: "MDG_ERR_ARG", 10: "MDG_ERR_STATE", 11: "MDG_ERR_NODEVICE",
+    9: "MDG_ERR_ARG", 10: "MDG_ERR_STATE", 11: "MDG_ERR_NODEVICE", 12: "MDG_ERR_LOST",
 }
 
 # every symbol include/mdg.h declares
@@ -51,6 +51,11 @@ class Material(C.Structure):
         "twisting_stiffness", "twisting_damping")]
 
 
+class Wall(C.Structure):
+    _fields_ = [("point", C.c_double * 3), ("normal", C.c_double * 3), ("bound_lo", C.c_double * 3),
+                ("bound_hi", C.c_double * 3), ("velocity", C.c_double * 3), ("material", C.c_int)]
+
+
 class Config(C.Structure):
     _fields_ = [
         ("kind", C.c_int), ("precision", C.c_int),
@@ -66,6 +71,7 @@ class Config(C.Structure):
         ("rebuild_policy", C.c_int), ("threads_per_particle", C.c_int), ("neighbor_capacity", C.c_int),
         ("history_capacity", C.c_int),
         ("langevin", C.c_int), ("lv_temperature", C.c_double), ("lv_damping", C.c_double), ("lv_seed", C.c_uint64),
+        ("fixed", C.c_int * 3), ("n_walls", C.c_int), ("walls", C.POINTER(Wall)),
     ]
 
 
@@ -228,7 +234,18 @@ def to_c_config(c: SimConfig):
     cc.history_capacity = int(c.history_capacity)
     cc.langevin = int(c.langevin)
     cc.lv_temperature, cc.lv_damping, cc.lv_seed = float(c.lv_temperature), float(c.lv_damping), int(c.lv_seed)
-    return cc, mats
+    cc.fixed[:] = [int(x) for x in c.fixed]
+    walls = (Wall * max(1, len(c.walls)))()
+    for k, w in enumerate(c.walls):
+        walls[k].point[:] = [float(x) for x in w.point]
+        walls[k].normal[:] = [float(x) for x in w.normal]
+        walls[k].bound_lo[:] = [float(x) for x in w.bound_lo]
+        walls[k].bound_hi[:] = [float(x) for x in w.bound_hi]
+        walls[k].velocity[:] = [float(x) for x in w.velocity]
+        walls[k].material = int(w.material)
+    cc.n_walls = len(c.walls)
+    cc.walls = C.cast(walls, C.POINTER(Wall))
+    return cc, (mats, walls)
 
 
 def _upload_view(state):

@@ -41,6 +41,17 @@ class Material:
 
 
 @dataclass
+class Wall:
+    """Plane wall ([[wall]], crates/dem_wall/src/lib.rs:171-262)."""
+    point: tuple = (0.0, 0.0, 0.0)
+    normal: tuple = (0.0, 0.0, 1.0)
+    bound_lo: tuple = (-math.inf, -math.inf, -math.inf)
+    bound_hi: tuple = (math.inf, math.inf, math.inf)
+    velocity: tuple = (0.0, 0.0, 0.0)
+    material: int = 0
+
+
+@dataclass
 class SimConfig:
     kind: str = "dem"                         # "dem" | "lj"
     box_lo: tuple = (0.0, 0.0, 0.0)
@@ -78,6 +89,8 @@ class SimConfig:
     lv_temperature: float = 0.85
     lv_damping: float = 1.0
     lv_seed: int = 12345
+    fixed: tuple = (0, 0, 0)
+    walls: list = field(default_factory=list)
 
     def replace(self, **kw) -> "SimConfig":
         return dataclasses.replace(self, **kw)
@@ -98,6 +111,10 @@ _SECTIONS = {
             "virial"},
 }
 _MATERIAL_KEYS = {f.name for f in dataclasses.fields(Material)}
+_WALL_KEYS = {"type", "point_x", "point_y", "point_z", "normal_x", "normal_y", "normal_z", "material", "name",
+              "bound_x_low", "bound_x_high", "bound_y_low", "bound_y_high", "bound_z_low", "bound_z_high",
+              "velocity", "oscillate", "servo", "axis", "center", "radius", "lo", "hi", "inside", "region",
+              "temperature"}
 
 
 def _check_keys(section: str, table: dict, allowed: set):
@@ -118,10 +135,13 @@ def from_toml(text: str, kind: str | None = None) -> SimConfig:
     c.kind = kind
     dom = doc.get("domain", {})
     _check_keys("domain", dom, _SECTIONS["domain"])
+    fixed = []
     for ax in ("x", "y", "z"):
         bt = dom.get(f"boundary_{ax}", "periodic")
-        if bt != "periodic":
-            raise ConfigError(f"boundary_{ax} = {bt!r}: the GPU path supports periodic boxes only")
+        if bt not in ("periodic", "fixed"):
+            raise ConfigError(f"boundary_{ax} = {bt!r}: the GPU path supports periodic and fixed boundaries")
+        fixed.append(1 if bt == "fixed" else 0)
+    c.fixed = tuple(fixed)
     lo = [float(dom.get(f"{a}_low", dom.get(f"{a}_lo", 0.0))) for a in "xyz"]
     hi = [float(dom.get(f"{a}_high", dom.get(f"{a}_hi", 1.0))) for a in "xyz"]
     c.box_lo, c.box_hi = tuple(lo), tuple(hi)
@@ -146,6 +166,25 @@ def from_toml(text: str, kind: str | None = None) -> SimConfig:
         if not mats:
             raise ConfigError("[[dem.materials]] requires at least one material")
         c.materials = mats
+        c.walls = []
+        for w in doc.get("wall", []) or []:
+            _check_keys("wall", w, _WALL_KEYS)
+            if w.get("type", "plane") != "plane":
+                raise ConfigError(f"wall type {w.get('type')!r}: the GPU path supports plane walls only")
+            if w.get("oscillate") or w.get("servo"):
+                raise ConfigError("oscillating and servo walls are not supported by the GPU path")
+            if w.get("temperature") is not None:
+                raise ConfigError("wall heat transfer is not supported by the GPU path")
+            names = [m.name for m in mats]
+            if w.get("material") not in names:
+                raise ConfigError(f"wall material {w.get('material')!r} is not in [[dem.materials]]")
+            c.walls.append(Wall(
+                point=tuple(float(w.get(f"point_{a}", 0.0)) for a in "xyz"),
+                normal=tuple(float(w.get(f"normal_{a}", 0.0)) for a in "xyz"),
+                bound_lo=tuple(float(w.get(f"bound_{a}_low", -math.inf)) for a in "xyz"),
+                bound_hi=tuple(float(w.get(f"bound_{a}_high", math.inf)) for a in "xyz"),
+                velocity=tuple(float(x) for x in (w.get("velocity") or (0.0, 0.0, 0.0))),
+                material=names.index(w["material"])))
         c.contact_model = dem.get("contact_model", "hertz")
         c.adhesion_model = dem.get("adhesion_model", "jkr")
         c.rolling_model = dem.get("rolling_model", "constant")

@@ -100,6 +100,13 @@ int validate_config(const mdg_config& c) {
     }
     if (c.nose_hoover && (!(c.nh_temperature > 0.0) || !(c.nh_coupling > 0.0))) return MDG_ERR_CONFIG;
     if (c.langevin && (c.nose_hoover || !(c.lv_temperature >= 0.0) || !(c.lv_damping >= 0.0))) return MDG_ERR_CONFIG;
+    if (c.n_walls < 0 || c.n_walls > MDG_MAX_WALLS || (c.n_walls > 0 && (!c.walls || c.kind != MDG_KIND_DEM)))
+        return MDG_ERR_CONFIG;
+    for (int w = 0; w < c.n_walls; w++) {
+        const mdg_wall& q = c.walls[w];
+        const double mag = sqrt(q.normal[0] * q.normal[0] + q.normal[1] * q.normal[1] + q.normal[2] * q.normal[2]);
+        if (!(mag > 1e-15) || q.material < 0 || q.material >= c.n_materials) return MDG_ERR_CONFIG;
+    }
     if (c.precision == MDG_MIXED && c.virial) return MDG_ERR_CONFIG;
     const int t = c.threads_per_particle;
     if (!(t == 0 || t == 1 || t == 2 || t == 4 || t == 8)) return MDG_ERR_CONFIG;
@@ -146,6 +153,7 @@ struct mdg_ctx {
     cudaGraphExec_t tgraph = nullptr;                 // timed single-step graph
     long long* d_loop = nullptr;  // {iterations left, iterations of the launch} of the WHILE graph
     bool run_nh = false;          // some running system is thermostatted
+    bool has_walls = false;       // some system has plane walls (once set, stays)
     // measurement scratch (allocated on first use, grown when needed)
     float4* rdf_posf = nullptr;
     long long rdf_posf_n = 0;
@@ -215,6 +223,26 @@ void apply_physics(mdg_ctx* c, int s, const mdg_config& k, std::vector<double>& 
     p.sort_every = k.sort_every;
     p.newton = k.newton;
     p.virial = k.virial;
+    for (int d = 0; d < 3; d++) p.per[d] = k.fixed[d] ? 0 : 1;
+    p.nwall = k.n_walls;
+    if (k.n_walls > 0) {
+        if (!c->has_walls) c->drop_graphs();
+        c->has_walls = true;
+    }
+    for (int w = 0; w < k.n_walls; w++) {
+        // WallPlugin's plane set-up (dem_wall/src/lib.rs:675-685): unit normal
+        const mdg_wall& q = k.walls[w];
+        WallP& o = p.walls[w];
+        const double mag = sqrt(q.normal[0] * q.normal[0] + q.normal[1] * q.normal[1] + q.normal[2] * q.normal[2]);
+        for (int d = 0; d < 3; d++) {
+            o.p[d] = q.point[d];
+            o.nrm[d] = q.normal[d] / mag;
+            o.lo[d] = q.bound_lo[d];
+            o.hi[d] = q.bound_hi[d];
+            o.vel[d] = q.velocity[d];
+        }
+        o.mat = q.material;
+    }
     p.lv = k.langevin && k.lv_damping > 0.0;  // gamma = 0: no forces (langevin_force's early return)
     p.lv_gamma = k.lv_damping;
     p.lv_kT = k.lv_temperature;
@@ -284,7 +312,7 @@ int setup_grid(const mdg_config& c, const double* cutr, size_t n, SysParams& p) 
         p.win[d] = sr;
         ncell *= p.ext[d];
         // one periodic image per neighbour: the box must exceed twice the list cutoff
-        if (!(p.L[d] > 2.0 * max_cutoff)) return MDG_ERR_CONFIG;
+        if (!c.fixed[d] && !(p.L[d] > 2.0 * max_cutoff)) return MDG_ERR_CONFIG;
         if (p.win[d] > xi) return MDG_ERR_CONFIG;
     }
     if (ncell > (1LL << 30)) return MDG_ERR_CONFIG;
@@ -353,6 +381,7 @@ int sys_status_to_err(int st) {
     if (st & ST_NAN) return MDG_ERR_NAN;
     if (st & (ST_NBR_OVF | ST_HIST_OVF)) return MDG_ERR_LIST_OVERFLOW;
     if (st & ST_TIMEOUT) return MDG_ERR_TIMEOUT;
+    if (st & ST_LOST) return MDG_ERR_LOST;
     return MDG_OK;
 }
 
@@ -480,9 +509,11 @@ int launch_fin(mdg_ctx* c, const Dev& d, cudaStream_t st, int integrate) {
     return c->has_mixed ? launch_final_mixed(d, st, integrate) : launch_final(d, st, integrate);
 }
 
-int launch_force(mdg_ctx* c, const Dev& d, cudaStream_t st) {
-    if (c->has_mixed) return launch_force_mixed(d, c->has_lj, c->has_dem, c->tpp_lj, st);
-    return launch_force_fp64(d, c->has_lj, c->has_dem, c->tpp_lj, st);
+int launch_force(mdg_ctx* c, const Dev& d, cudaStream_t st, int integrating = 1) {
+    int n = c->has_mixed ? launch_force_mixed(d, c->has_lj, c->has_dem, c->tpp_lj, st)
+                         : launch_force_fp64(d, c->has_lj, c->has_dem, c->tpp_lj, st);
+    if (c->has_walls) n += launch_walls(d, integrating, st);  // added after the pair forces
+    return n;
 }
 
 int enqueue_step(mdg_ctx* c, cudaStream_t st) {
@@ -701,6 +732,7 @@ const char* mdg_status_string(int s) {
         case MDG_ERR_ARG: return "bad argument";
         case MDG_ERR_STATE: return "call out of order";
         case MDG_ERR_NODEVICE: return "no CUDA device";
+        case MDG_ERR_LOST: return "a particle left the box across a fixed boundary";
         default: return "unknown status";
     }
 }
@@ -1201,7 +1233,7 @@ int mdg_step(mdg_ctx* c, int64_t nsteps) {
     advance_budgets(c, nsteps);
     // kernels that ran: per step initial + force + final (+ loop control),
     // plus the rebuild kernels on the steps whose rebuild branch opened
-    const long long nforce = (c->has_lj ? 1 : 0) + (c->has_dem ? 1 : 0);
+    const long long nforce = (c->has_lj ? 1 : 0) + (c->has_dem ? 1 : 0) + (c->has_walls ? 1 : 0);
     long long base = 2 + nforce + (c->graph_mode ? 1 : 0);
     if (c->graph_mode && c->has_mixed) {
         // fused step kernel (+ thermostatted initial) per iteration, the
@@ -1225,7 +1257,7 @@ int mdg_force_only(mdg_ctx* c) {
     cudaMemcpy(c->d.ss, ss.data(), c->nsys * sizeof(SysState), cudaMemcpyHostToDevice);
     cudaStream_t st = c->stream;
     c->launches += launch_rb(c, c->d, st);
-    c->launches += launch_force(c, c->d, st);
+    c->launches += launch_force(c, c->d, st, 0);
     c->launches += launch_fin(c, c->d, st, 0);  // reductions + bookkeeping, no integration
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_err(e);

@@ -16,6 +16,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "../../include/mdg.h"  // MDG_MAX_WALLS, status and kind codes
+
 namespace mdg {
 
 constexpr int BLK = 128;               // particles per block (segment padding unit)
@@ -30,12 +32,20 @@ enum : int {
     ST_NBR_OVF = 4,
     ST_HIST_OVF = 8,
     ST_TIMEOUT = 16,
+    ST_LOST = 32,
 };
 
 // material pair table ids (MaterialTable::build_pair_tables order)
 enum : int {
     T_BETA = 0, T_FRICTION, T_ROLL_FRICTION, T_COHESION, T_SURFACE, T_EEFF, T_GEFF,
     T_TWIST_FRICTION, T_KN, T_KT, T_KROLL, T_GROLL, T_KTWIST, T_GTWIST
+};
+
+// A plane wall: a point on it, the unit outward normal, the active box,
+// the wall velocity and its material index.
+struct WallP {
+    double p[3], nrm[3], lo[3], hi[3], vel[3];
+    int mat;
 };
 
 struct SysParams {
@@ -45,6 +55,10 @@ struct SysParams {
     int p0, n, npad;     // particle segment
     int b0, nb;          // first particle block; blocks holding the n particles
     int ncb;             // cell blocks of the system's cell segment
+    // periodic axes (fixed axes: no images, no wrap) and plane walls
+    int per[3];
+    int nwall;
+    WallP walls[MDG_MAX_WALLS];
     // Langevin ([langevin]): drag gamma, noise kT, seed of the counter-based stream
     int lv;
     double lv_gamma, lv_kT;
@@ -428,6 +442,7 @@ __device__ __forceinline__ int rb_find(const int* off, int n, int v) {
 int launch_initial(const Dev& d, cudaStream_t st);
 int launch_initial_mixed(const Dev& d, cudaStream_t st, int nh_only = 0, const long long* loop = nullptr);
 int launch_step_mixed(const Dev& d, const long long* loop, cudaStream_t st);
+int launch_walls(const Dev& d, int integrating, cudaStream_t st);
 int launch_rdf(const Dev& d, int s, const SysParams& sp, float4* posf, double r_max, int nbins,
                unsigned long long* counts, cudaStream_t st);
 int launch_msd_ref(const Dev& d, int s, int n, double* ref, cudaStream_t st);

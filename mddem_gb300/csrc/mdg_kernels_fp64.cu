@@ -99,7 +99,8 @@ __global__ void __launch_bounds__(BLK) k_initial(Dev d) {
                 if (sp.every > 0) nd = (sp.check && nd) || st->steps_since_build >= sp.every;
                 if (!nd && sp.policy == 0) {
                     const float rx = ph.x + pl.x, ry = ph.y + pl.y, rz = ph.z + pl.z;
-                    nd = rx < 0.f || rx >= sp.Lh[0] || ry < 0.f || ry >= sp.Lh[1] || rz < 0.f || rz >= sp.Lh[2];
+                    nd = (sp.per[0] && (rx < 0.f || rx >= sp.Lh[0])) || (sp.per[1] && (ry < 0.f || ry >= sp.Lh[1])) ||
+                     (sp.per[2] && (rz < 0.f || rz >= sp.Lh[2]));
                 }
                 need = nd;
             }
@@ -135,17 +136,18 @@ __global__ void __launch_bounds__(BLK) k_initial(Dev d) {
                 const double4 b = d.lbp[i];
                 double dx = x.x - b.x, dy = x.y - b.y, dz = x.z - b.z;
                 const double hbx = sp.L[0] * 0.5, hby = sp.L[1] * 0.5, hbz = sp.L[2] * 0.5;
-                if (dx > hbx) dx -= sp.L[0]; else if (dx < -hbx) dx += sp.L[0];
-                if (dy > hby) dy -= sp.L[1]; else if (dy < -hby) dy += sp.L[1];
-                if (dz > hbz) dz -= sp.L[2]; else if (dz < -hbz) dz += sp.L[2];
+                if (sp.per[0]) { if (dx > hbx) dx -= sp.L[0]; else if (dx < -hbx) dx += sp.L[0]; }
+                if (sp.per[1]) { if (dy > hby) dy -= sp.L[1]; else if (dy < -hby) dy += sp.L[1]; }
+                if (sp.per[2]) { if (dz > hbz) dz -= sp.L[2]; else if (dz < -hbz) dz += sp.L[2]; }
                 disp = dx * dx + dy * dy + dz * dz > sp.disp_thr_sq;
             }
             if (sp.every == 0) need = disp;
             else if (sp.check) need = (st->steps_since_build >= sp.every) || disp;
             else need = st->steps_since_build >= sp.every;
             if (!need && sp.policy == 0)
-                need = (x.x < sp.lo[0] || x.x >= sp.hi[0] || x.y < sp.lo[1] || x.y >= sp.hi[1] ||
-                        x.z < sp.lo[2] || x.z >= sp.hi[2]);
+                need = (sp.per[0] && (x.x < sp.lo[0] || x.x >= sp.hi[0])) ||
+                       (sp.per[1] && (x.y < sp.lo[1] || x.y >= sp.hi[1])) ||
+                       (sp.per[2] && (x.z < sp.lo[2] || x.z >= sp.hi[2]));
         }
     }
     if (__any_sync(0xffffffffu, need) && (threadIdx.x & 31) == 0) atomicOr(&st->rebuild, 1);
@@ -245,9 +247,14 @@ __device__ __forceinline__ void cells_block(const Dev& d, int s, int lb) {
     if (vload(&st->rebuild)) {
         int4 im = d.img[i];
         const double hx = sp.lo[0] + sp.L[0], hy = sp.lo[1] + sp.L[1], hz = sp.lo[2] + sp.L[2];
-        if (x.x < sp.lo[0]) { x.x += sp.L[0]; im.x -= 1; } else if (x.x >= hx) { x.x -= sp.L[0]; im.x += 1; }
-        if (x.y < sp.lo[1]) { x.y += sp.L[1]; im.y -= 1; } else if (x.y >= hy) { x.y -= sp.L[1]; im.y += 1; }
-        if (x.z < sp.lo[2]) { x.z += sp.L[2]; im.z -= 1; } else if (x.z >= hz) { x.z -= sp.L[2]; im.z += 1; }
+        // wrap on periodic axes only; on a fixed axis a particle outside the box
+        // (which pbc's slow path, domain.rs:434-452, removes) is an error
+        if ((!sp.per[0] && (x.x < sp.lo[0] || x.x >= sp.hi[0])) || (!sp.per[1] && (x.y < sp.lo[1] || x.y >= sp.hi[1])) ||
+            (!sp.per[2] && (x.z < sp.lo[2] || x.z >= sp.hi[2])))
+            atomicOr(&d.ss[s].status, ST_LOST);
+        if (sp.per[0]) { if (x.x < sp.lo[0]) { x.x += sp.L[0]; im.x -= 1; } else if (x.x >= hx) { x.x -= sp.L[0]; im.x += 1; } }
+        if (sp.per[1]) { if (x.y < sp.lo[1]) { x.y += sp.L[1]; im.y -= 1; } else if (x.y >= hy) { x.y -= sp.L[1]; im.y += 1; } }
+        if (sp.per[2]) { if (x.z < sp.lo[2]) { x.z += sp.L[2]; im.z -= 1; } else if (x.z >= hz) { x.z -= sp.L[2]; im.z += 1; } }
         d.pos[i] = x;
         d.img[i] = im;
     }
@@ -637,14 +644,17 @@ __device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
         for (int ox = -sp.win[0]; ox <= sp.win[0]; ox++) {
             int qx = qx0 + ox, sx = 0;
             if (qx < 0) { qx += sp.nc[0]; sx = -1; } else if (qx >= sp.nc[0]) { qx -= sp.nc[0]; sx = 1; }
+            if (sx && !sp.per[0]) continue;  // fixed axis: no periodic image
             if (qx < 0 || qx >= sp.nc[0]) continue;
             for (int oy = -sp.win[1]; oy <= sp.win[1]; oy++) {
                 int qy = qy0 + oy, sy = 0;
                 if (qy < 0) { qy += sp.nc[1]; sy = -1; } else if (qy >= sp.nc[1]) { qy -= sp.nc[1]; sy = 1; }
+                if (sy && !sp.per[1]) continue;  // fixed axis: no periodic image
                 if (qy < 0 || qy >= sp.nc[1]) continue;
                 for (int oz = -sp.win[2]; oz <= sp.win[2]; oz++) {
                     int qz = qz0 + oz, sz = 0;
                     if (qz < 0) { qz += sp.nc[2]; sz = -1; } else if (qz >= sp.nc[2]) { qz -= sp.nc[2]; sz = 1; }
+                    if (sz && !sp.per[2]) continue;  // fixed axis: no periodic image
                     if (qz < 0 || qz >= sp.nc[2]) continue;
                     const bool shifted = (sx | sy | sz) != 0;
                     const uint32_t sc = (uint32_t)((sx + 1) * 9 + (sy + 1) * 3 + (sz + 1));
@@ -1422,6 +1432,115 @@ __global__ void k_loop_ctl(Dev d, long long* counter, unsigned long long handle)
 
 int launch_loop_ctl(const Dev& d, long long* counter, unsigned long long handle, cudaStream_t st) {
     k_loop_ctl<<<1, 32, 0, st>>>(d, counter, handle);
+    return 1;
+}
+
+// Plane walls (wall_contact_force, crates/dem_wall/src/lib.rs:848-990), added
+// after the pair forces: sphere-wall Hertz with R* = r and m* = m, viscous
+// damping, JKR / DMT / SJKR adhesion, no tangential force, and the constant
+// twisting torque; the reference's fp64 arithmetic (this file: no fma).
+// wall_contact_force for plane walls (dem_wall/src/lib.rs:848-985).  A wall
+// with a constant velocity has moved by velocity * dt once per step before the
+// force (wall_move, lib.rs:766-790): moves = steps done + 1 inside a step,
+// steps done for a force evaluation outside one.
+__global__ void __launch_bounds__(BLK) k_walls(Dev d, int integrating) {
+    const int gb = d.blk_run[blockIdx.x];
+    const int s = d.blk_sys[gb];
+    const SysParams& sp = d.sp[s];
+    if (sp.nwall == 0 || sp.kind != 0 || !sys_active(d.ss + s)) return;
+    const int li = (gb - sp.b0) * BLK + threadIdx.x;
+    if (li >= sp.n) return;
+    const long long i = (long long)sp.p0 + li;
+    const double PI = 3.141592653589793;
+    const double SQRT_5_3 = 0.9128709291752768;
+    const double4 x = d.pos[i];
+    const double4 v = d.vel[i];
+    const double4 w = d.omg[i];
+    const double radius = x.w;
+    const int mi = (int)d.type[i];
+    double4 f = d.frc[i], tq = d.trq[i];
+    bool touched = false;
+    const double moves = (double)(d.ss[s].step + integrating);
+    for (int k = 0; k < sp.nwall; k++) {
+        const WallP& W = sp.walls[k];
+        const double px = W.p[0] + moves * (W.vel[0] * sp.dt), py = W.p[1] + moves * (W.vel[1] * sp.dt),
+                     pz = W.p[2] + moves * (W.vel[2] * sp.dt);
+        if (!(x.x >= W.lo[0] && x.x <= W.hi[0] && x.y >= W.lo[1] && x.y <= W.hi[1] && x.z >= W.lo[2] &&
+              x.z <= W.hi[2]))
+            continue;
+        const double dx = x.x - px, dy = x.y - py, dz = x.z - pz;
+        const double distance = dx * W.nrm[0] + dy * W.nrm[1] + dz * W.nrm[2];
+        if (distance <= 0.0) continue;
+        const double r_eff = radius;
+        const double e_eff = mtab(d, sp, T_EEFF, mi, W.mat);
+        const double surface_energy = mtab(d, sp, T_SURFACE, mi, W.mat);
+        const bool use_dmt = sp.adhesion_model == 1;
+        const double delta_pulloff = (surface_energy > 0.0 && !use_dmt)
+                                         ? cbrt(PI * PI * surface_energy * surface_energy * r_eff /
+                                                (4.0 * e_eff * e_eff))
+                                         : 0.0;
+        const double delta = fmin(radius - distance, 0.5 * radius);
+        if (delta <= 0.0 && surface_energy <= 0.0) continue;
+        if (delta < -delta_pulloff) continue;
+        const bool jkr_adhesion_only = surface_energy > 0.0 && !use_dmt && delta <= 0.0;
+        double s_n = 0.0, k_n = 0.0;
+        if (delta > 0.0) {
+            const double sdr = sqrt(delta * r_eff);
+            s_n = 2.0 * e_eff * sdr;
+            k_n = 4.0 / 3.0 * e_eff * sdr;
+        }
+        const double m_r = d.mass[i];
+        const double vx = v.x - W.vel[0], vy = v.y - W.vel[1], vz = v.z - W.vel[2];
+        const double v_n = vx * W.nrm[0] + vy * W.nrm[1] + vz * W.nrm[2];
+        const double beta = mtab(d, sp, T_BETA, mi, W.mat);
+        const double cohesion_energy = mtab(d, sp, T_COHESION, mi, W.mat);
+        double f_net;
+        if (surface_energy > 0.0 && use_dmt) {
+            const double f_dmt = 2.0 * PI * surface_energy * r_eff;
+            const double f_diss = 2.0 * beta * SQRT_5_3 * sqrt(s_n * m_r) * v_n;
+            f_net = k_n * delta - f_diss - f_dmt;
+        } else if (surface_energy > 0.0) {
+            const double f_adhesion = 1.5 * PI * surface_energy * r_eff;
+            if (jkr_adhesion_only) {
+                f_net = -f_adhesion;
+            } else {
+                const double f_diss = 2.0 * beta * SQRT_5_3 * sqrt(s_n * m_r) * v_n;
+                f_net = k_n * delta - f_diss - f_adhesion;
+            }
+        } else if (cohesion_energy > 0.0) {
+            const double f_diss = 2.0 * beta * SQRT_5_3 * sqrt(s_n * m_r) * v_n;
+            const double f_cohesion = cohesion_energy * PI * delta * r_eff;
+            f_net = k_n * delta - f_diss - f_cohesion;
+        } else {
+            const double f_diss = 2.0 * beta * SQRT_5_3 * sqrt(s_n * m_r) * v_n;
+            f_net = fmax(k_n * delta - f_diss, 0.0);
+        }
+        f.x += f_net * W.nrm[0];
+        f.y += f_net * W.nrm[1];
+        f.z += f_net * W.nrm[2];
+        if (delta > 0.0) {
+            const double mu_tw = mtab(d, sp, T_TWIST_FRICTION, mi, W.mat);
+            if (mu_tw > 0.0) {
+                const double twist = w.x * W.nrm[0] + w.y * W.nrm[1] + w.z * W.nrm[2];
+                if (fabs(twist) > 1e-30) {
+                    const double tau = mu_tw * fabs(f_net) * r_eff;
+                    const double sign_tw = twist > 0.0 ? -1.0 : 1.0;
+                    tq.x += sign_tw * tau * W.nrm[0];
+                    tq.y += sign_tw * tau * W.nrm[1];
+                    tq.z += sign_tw * tau * W.nrm[2];
+                }
+            }
+        }
+        touched = true;
+    }
+    if (touched) {
+        d.frc[i] = f;
+        d.trq[i] = tq;
+    }
+}
+
+int launch_walls(const Dev& d, int integrating, cudaStream_t st) {
+    k_walls<<<d.nrun, BLK, 0, st>>>(d, integrating);
     return 1;
 }
 

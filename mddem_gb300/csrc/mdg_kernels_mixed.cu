@@ -553,7 +553,8 @@ __global__ void __launch_bounds__(BLK) k_initial_mixed(Dev d, int nh_only, const
             if (sp.every > 0) nd = (sp.check && nd) || st->steps_since_build >= sp.every;
             if (!nd && sp.policy == 0) {
                 const float rx = ph.x + pl.x, ry = ph.y + pl.y, rz = ph.z + pl.z;
-                nd = rx < 0.f || rx >= sp.Lh[0] || ry < 0.f || ry >= sp.Lh[1] || rz < 0.f || rz >= sp.Lh[2];
+                nd = (sp.per[0] && (rx < 0.f || rx >= sp.Lh[0])) || (sp.per[1] && (ry < 0.f || ry >= sp.Lh[1])) ||
+                     (sp.per[2] && (rz < 0.f || rz >= sp.Lh[2]));
             }
             need = nd;
         }
@@ -623,7 +624,9 @@ __device__ __forceinline__ void dem_wl_block(const Dev& d, int s, int lb) {
     const int li = lb * BLK + threadIdx.x;
     const bool in = li < sp.n;
     const long long i = (long long)sp.p0 + li;
-    const bool has = in && d.nnum[i] > 0;
+    // with walls every particle is visited each step (the wall kernel adds to
+    // the force the pair kernel writes)
+    const bool has = in && (d.nnum[i] > 0 || sp.nwall > 0);
     if (in && !has) {
         d.frc[i] = make_double4(0.0, 0.0, 0.0, 0.0);
         d.trq[i] = make_double4(0.0, 0.0, 0.0, 0.0);
@@ -796,7 +799,8 @@ __global__ void __launch_bounds__(BLK) k_step_mixed(Dev d, const long long* loop
             if (sp.every > 0) nd = (sp.check && nd) || ssb >= sp.every;
             if (!nd && sp.policy == 0) {
                 const float rx = ph.x + pl.x, ry = ph.y + pl.y, rz = ph.z + pl.z;
-                nd = rx < 0.f || rx >= sp.Lh[0] || ry < 0.f || ry >= sp.Lh[1] || rz < 0.f || rz >= sp.Lh[2];
+                nd = (sp.per[0] && (rx < 0.f || rx >= sp.Lh[0])) || (sp.per[1] && (ry < 0.f || ry >= sp.Lh[1])) ||
+                     (sp.per[2] && (rz < 0.f || rz >= sp.Lh[2]));
             }
             need = nd;
         }

@@ -5,7 +5,7 @@ CorePlugins + GranularDefaultPlugins or LJDefaultPlugins): the TOML sections
 the hot path reads (``config.from_toml``), the initial state from ``[lattice]``
 (FCC, crates/md_lattice/src/lib.rs:232-471) or ``[[particles.insert]]``
 (random insertion, crates/dem_atom/src/insert.rs:417-614: region = domain
-inset by the radius, rejection at 1.1 (r_i + r_j), per-component Gaussian
+inset by the radius or a block region, rejection at 1.1 (r_i + r_j), per-component Gaussian
 velocities of std ``velocity`` plus ``velocity_x/y/z``; or ``source = "file"``
 CSV, insert.rs:652-776), the timestep (``[run] dt``, else 0.15 Rayleigh time
 of the smallest sphere, insert.rs:1392-1431, or 0.005 for a lattice), then
@@ -55,11 +55,14 @@ def _insert(doc, cfg, seed):
             rmin, rmax = float(rad["min"]), float(rad["max"])
         else:
             rmin = rmax = float(rad)
-        lo = cfg.box_lo
-        hi = cfg.box_hi
-        if b.get("region"):
-            raise RunError("insertion regions other than the domain are not supported")
-        pos, r = capi.rsa_spheres(n, lo, hi, rmin, rmax, sep_factor=1.1, inset=True, seed=seed + k)
+        lo, hi, inset = cfg.box_lo, cfg.box_hi, True
+        reg = b.get("region")
+        if reg:
+            # Region::Block: centres uniform inside [min, max], no inset (insert.rs:522-543)
+            if reg.get("type") != "block":
+                raise RunError(f"insertion region {reg.get('type')!r}: only block regions are supported")
+            lo, hi, inset = tuple(map(float, reg["min"])), tuple(map(float, reg["max"])), False
+        pos, r = capi.rsa_spheres(n, lo, hi, rmin, rmax, sep_factor=1.1, inset=inset, seed=seed + k)
         rng = np.random.default_rng(seed + 7919 * (k + 1))
         v = float(b.get("velocity", 0.0))
         vel = rng.normal(0.0, v, size=(n, 3)) if v > 0.0 else np.zeros((n, 3))

@@ -164,6 +164,8 @@ struct Sim {
     double pe = 0;
     long step_count = 0, nbuilds = 0, overlap_total = 0;
     int error = 0;
+    bool periodic[3] = {true, true, true};  // Domain::periodic_flags
+    std::vector<orc_wall> walls;            // plane walls, unit normals
 
     size_t len() const { return pos.size(); }
 
@@ -175,7 +177,17 @@ struct Sim {
             lo[d] = c->lo[d];
             hi[d] = c->hi[d];
             size[d] = hi[d] - lo[d];
+            periodic[d] = !c->fixed[d];
         }
+        walls.clear();
+        for (int w = 0; dem && w < c->n_walls; w++) {
+            orc_wall q = c->walls[w];
+            // WallPlane normalisation, dem_wall/src/lib.rs:1259-1262
+            double mag = std::sqrt(q.normal[0] * q.normal[0] + q.normal[1] * q.normal[1] + q.normal[2] * q.normal[2]);
+            for (int d = 0; d < 3; d++) q.normal[d] /= mag;
+            walls.push_back(q);
+        }
+        cfg.walls = nullptr;
         dt = c->dt;
         skin_fraction = c->skin_fraction;
         bin_min_size = c->bin_size;
@@ -446,9 +458,9 @@ struct Sim {
             double dx = pos[i][0] - last_build_pos[i][0];
             double dy = pos[i][1] - last_build_pos[i][1];
             double dz = pos[i][2] - last_build_pos[i][2];
-            if (dx > hbx) dx -= bx; else if (dx < -hbx) dx += bx;
-            if (dy > hby) dy -= by; else if (dy < -hby) dy += by;
-            if (dz > hbz) dz -= bz; else if (dz < -hbz) dz += bz;
+            if (periodic[0]) { if (dx > hbx) dx -= bx; else if (dx < -hbx) dx += bx; }
+            if (periodic[1]) { if (dy > hby) dy -= by; else if (dy < -hby) dy += by; }
+            if (periodic[2]) { if (dz > hbz) dz -= bz; else if (dz < -hbz) dz += bz; }
             if (dx * dx + dy * dy + dz * dz > thr) return true;
         }
         return false;
@@ -467,7 +479,7 @@ struct Sim {
         if (!need) {
             for (int i = 0; i < nlocal && !need; i++)
                 for (int d = 0; d < 3; d++)
-                    if (pos[i][d] < lo[d] || pos[i][d] >= hi[d]) { need = true; break; }
+                    if (periodic[d] && (pos[i][d] < lo[d] || pos[i][d] >= hi[d])) { need = true; break; }
         }
         if (need) state = FullRebuild;
         else steps_since_build += 1;
@@ -479,12 +491,18 @@ struct Sim {
         if (dem) for (auto& t : torque) t = {0, 0, 0};
     }
 
-    // pbc + wrap_periodic, crates/mddem_core/src/domain.rs:396-459 (fully periodic fast path)
+    // pbc + wrap_periodic, crates/mddem_core/src/domain.rs:396-459.  On a
+    // fixed axis the reference removes a particle outside [lo, hi); the
+    // oracle, like the GPU path, reports it as an error (12) instead.
     void pbc() {
         for (int i = 0; i < nlocal; i++)
             for (int d = 0; d < 3; d++) {
                 double p = pos[i][d];
                 double high = lo[d] + size[d];
+                if (!periodic[d]) {
+                    if (p < lo[d] || p >= hi[d]) error = 12;
+                    continue;
+                }
                 if (p < lo[d]) { p += size[d]; image[i][d] -= 1; }
                 else if (p >= high) { p -= size[d]; image[i][d] += 1; }
                 pos[i][d] = p;
@@ -533,6 +551,9 @@ struct Sim {
         int scan_end = nlocal;
         for (int dim = 0; dim < 3; dim++) {
             int dim_scan_end = scan_end;
+            // a fixed axis has no neighbor in either direction on one rank
+            // (comm_setup, comm.rs:226-250): no ghosts, no swaps
+            if (!periodic[dim]) continue;
             for (int sw = 0; sw < 2; sw++) {
                 double periodic_offset = (sw == 0) ? 1.0 : -1.0;
                 Swap s;
@@ -987,6 +1008,62 @@ struct Sim {
         }
     }
 
+    // wall_contact_force (plane walls), crates/dem_wall/src/lib.rs:848-985:
+    // Hertz normal force against a half-space of infinite radius and mass,
+    // damping, JKR / DMT / SJKR adhesion, twisting friction torque.
+    void wall_force() {
+        bool use_dmt = cfg.adhesion_model == 1;
+        for (const orc_wall& W : walls) {
+            int wm = W.material;
+            for (int i = 0; i < nlocal; i++) {
+                const V3& p = pos[i];
+                if (!(p[0] >= W.bound_lo[0] && p[0] <= W.bound_hi[0] && p[1] >= W.bound_lo[1] &&
+                      p[1] <= W.bound_hi[1] && p[2] >= W.bound_lo[2] && p[2] <= W.bound_hi[2]))
+                    continue;
+                double distance = (p[0] - W.point[0]) * W.normal[0] + (p[1] - W.point[1]) * W.normal[1] +
+                                  (p[2] - W.point[2]) * W.normal[2];
+                if (distance <= 0.0) continue;
+                double r = radius[i];
+                int mi = (int)type[i];
+                double e_eff = mt.at(mt.e_eff, mi, wm);
+                double gam = mt.at(mt.surface, mi, wm);
+                double pull = (gam > 0.0 && !use_dmt) ? std::cbrt(kPi * kPi * gam * gam * r / (4.0 * e_eff * e_eff)) : 0.0;
+                double delta = std::fmin(r - distance, 0.5 * r);
+                if (delta <= 0.0 && gam <= 0.0) continue;
+                if (delta < -pull) continue;
+                bool adhesion_only = gam > 0.0 && !use_dmt && delta <= 0.0;
+                double s_n = 0.0, k_n = 0.0;
+                if (delta > 0.0) {
+                    double sdr = std::sqrt(delta * r);
+                    s_n = 2.0 * e_eff * sdr;
+                    k_n = 4.0 / 3.0 * e_eff * sdr;
+                }
+                double v_n = (vel[i][0] - W.velocity[0]) * W.normal[0] + (vel[i][1] - W.velocity[1]) * W.normal[1] +
+                             (vel[i][2] - W.velocity[2]) * W.normal[2];
+                double beta = mt.at(mt.beta, mi, wm);
+                double coh = mt.at(mt.cohesion, mi, wm);
+                double f_diss = 2.0 * beta * SQRT_5_3 * std::sqrt(s_n * mass[i]) * v_n;
+                double fn;
+                if (gam > 0.0 && use_dmt) fn = k_n * delta - f_diss - 2.0 * kPi * gam * r;
+                else if (gam > 0.0) fn = adhesion_only ? -(1.5 * kPi * gam * r) : k_n * delta - f_diss - 1.5 * kPi * gam * r;
+                else if (coh > 0.0) fn = k_n * delta - f_diss - coh * kPi * delta * r;
+                else fn = std::fmax(k_n * delta - f_diss, 0.0);
+                for (int d = 0; d < 3; d++) force[i][d] += fn * W.normal[d];
+                if (delta > 0.0) {
+                    double mu = mt.at(mt.twisting_friction, mi, wm);
+                    if (mu > 0.0) {
+                        double tw = omega[i][0] * W.normal[0] + omega[i][1] * W.normal[1] + omega[i][2] * W.normal[2];
+                        if (std::fabs(tw) > 1e-30) {
+                            double tau = mu * std::fabs(fn) * r;
+                            double sg = tw > 0.0 ? -1.0 : 1.0;
+                            for (int d = 0; d < 3; d++) torque[i][d] += sg * tau * W.normal[d];
+                        }
+                    }
+                }
+            }
+        }
+    }
+
     void compute_forces() {
         if (virial) for (double& v : vir) v = 0.0;  // zero_virial_stress
         if (dem) contact_force();
@@ -995,6 +1072,9 @@ struct Sim {
 
     // One timestep in the compiled schedule order (schedule.dot:45-153).
     void step() {
+        // wall_move, crates/dem_wall/src/lib.rs:766-790 (PreInitialIntegration)
+        for (orc_wall& W : walls)
+            for (int d = 0; d < 3; d++) W.point[d] += W.velocity[d] * dt;
         if (nh) nh_pre_initial();
         else {
             initial_integration();
@@ -1015,6 +1095,7 @@ struct Sim {
         }
         compute_forces();
         reverse_send_force();
+        if (!walls.empty()) wall_force();
         if (nh) nh_post_final();
         else {
             final_integration();
@@ -1033,6 +1114,7 @@ struct Sim {
         bin_neighbor_list();
         compute_forces();
         reverse_send_force();
+        if (!walls.empty()) wall_force();
     }
 
     // print_granular_temperature, crates/dem_granular/src/granular_temp.rs:44-134

@@ -30,9 +30,17 @@ typedef struct orc_material {
     double kn, kt, rolling_stiffness, rolling_damping, twisting_stiffness, twisting_damping;
 } orc_material;
 
+/* One plane wall ([[wall]], dem_wall/src/lib.rs:160-260): a point, a normal
+ * (normalised here, lib.rs:1259), the bounding region, a constant velocity and
+ * a material index. */
+typedef struct orc_wall {
+    double point[3], normal[3], bound_lo[3], bound_hi[3], velocity[3];
+    int material;
+} orc_wall;
+
 typedef struct orc_config {
     int kind;                 /* 0 = DEM granular, 1 = LJ */
-    double lo[3], hi[3];      /* [domain], fully periodic */
+    double lo[3], hi[3];      /* [domain] */
     double dt;                /* [run] dt */
     double skin_fraction;     /* [neighbor] */
     double bin_size;
@@ -47,6 +55,9 @@ typedef struct orc_config {
     int nose_hoover;          /* 1 = NoseHooverPlugin present */
     double nh_temperature, nh_coupling;
     int virial;               /* VirialStress active each step */
+    int fixed[3];             /* boundary_x/y/z = "fixed" (0 = periodic) */
+    int n_walls;              /* plane walls (DEM) */
+    const orc_wall* walls;
 } orc_config;
 
 enum {

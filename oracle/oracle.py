@@ -37,6 +37,11 @@ class OrcMaterial(C.Structure):
         "twisting_stiffness", "twisting_damping")]
 
 
+class OrcWall(C.Structure):
+    _fields_ = [("point", C.c_double * 3), ("normal", C.c_double * 3), ("bound_lo", C.c_double * 3),
+                ("bound_hi", C.c_double * 3), ("velocity", C.c_double * 3), ("material", C.c_int)]
+
+
 class OrcConfig(C.Structure):
     _fields_ = [
         ("kind", C.c_int), ("lo", C.c_double * 3), ("hi", C.c_double * 3), ("dt", C.c_double),
@@ -48,6 +53,7 @@ class OrcConfig(C.Structure):
         ("lj_epsilon", C.c_double), ("lj_sigma", C.c_double), ("lj_cutoff", C.c_double),
         ("nose_hoover", C.c_int), ("nh_temperature", C.c_double), ("nh_coupling", C.c_double),
         ("virial", C.c_int),
+        ("fixed", C.c_int * 3), ("n_walls", C.c_int), ("walls", C.POINTER(OrcWall)),
     ]
 
 
@@ -115,6 +121,15 @@ class Oracle:
         c.nose_hoover = int(cfg.nose_hoover)
         c.nh_temperature, c.nh_coupling = float(cfg.nh_temperature), float(cfg.nh_coupling)
         c.virial = int(cfg.virial)
+        c.fixed[:] = [int(x) for x in getattr(cfg, "fixed", (0, 0, 0))]
+        wl = list(getattr(cfg, "walls", ()))
+        walls = (OrcWall * max(1, len(wl)))()
+        for k, w in enumerate(wl):
+            for f in ("point", "normal", "bound_lo", "bound_hi", "velocity"):
+                getattr(walls[k], f)[:] = [float(x) for x in getattr(w, f)]
+            walls[k].material = int(w.material)
+        c.n_walls = len(wl) if cfg.kind == "dem" else 0
+        c.walls = C.cast(walls, C.POINTER(OrcWall))
         self._mats = mats
         self.h = self.lib.orc_create(C.byref(c))
         self.kind = cfg.kind

@@ -144,7 +144,8 @@ def test_toml_unknown_field_rejected():
     with pytest.raises(ConfigError):
         from_toml(REF_DEM_TOML.replace("bin_size = 0.005", "bin_size = 0.005\nbogus = 1"))
     with pytest.raises(ConfigError):
-        from_toml(REF_DEM_TOML.replace('boundary_x = "periodic"', 'boundary_x = "fixed"'))
+        from_toml(REF_DEM_TOML.replace('boundary_x = "periodic"', 'boundary_x = "shrink_wrap"'))
+    assert from_toml(REF_DEM_TOML.replace('boundary_x = "periodic"', 'boundary_x = "fixed"')).fixed == (1, 0, 0)
 
 
 def test_rayleigh_dt_matches_reference_formula():
