@@ -317,6 +317,9 @@ int setup_grid(const mdg_config& c, const double* cutr, size_t n, SysParams& p) 
     }
     if (ncell > (1LL << 30)) return MDG_ERR_CONFIG;
     p.ncell = (int)ncell;
+    // under about 6 particles per bin a warp per bin leaves most lanes idle:
+    // build the list with a thread per particle instead (same rows)
+    p.build_tpp = (double)n < 6.0 * (double)p.nc[0] * (double)p.nc[1] * (double)p.nc[2] ? 1 : 0;
     p.max_cutoff = max_cutoff;
     p.stencil_cut_sq = max_cutoff * max_cutoff;
     // stencil membership of every offset (compute_bin_grid's distance test,
@@ -346,6 +349,11 @@ int setup_grid(const mdg_config& c, const double* cutr, size_t n, SysParams& p) 
     for (int d = 0; d < 3; d++) {
         p.Lh[d] = (float)p.L[d];
         p.Ll[d] = (float)(p.L[d] - (double)p.Lh[d]);
+        p.uinv[d] = std::ldexp(1.0, 32) / p.L[d];
+        p.uscale[d] = (float)std::ldexp(p.L[d], -32);
+        // mixed LJ: the wrapped fixed-point difference is the separation only
+        // below L / 2, on fixed axes too
+        if (c.kind == MDG_KIND_LJ && c.precision == MDG_MIXED && !(p.L[d] > 2.0 * max_cutoff)) return MDG_ERR_CONFIG;
     }
     const double per_atom_skin = (sf - 1.0) * min_skin;
     p.disp_thr_sq = per_atom_skin * per_atom_skin;
@@ -417,10 +425,14 @@ int ensure_layout(mdg_ctx* c, int fresh = -1) {
     if (realloc_cells) {
         c->free_ptr(c->d.cnt);
         c->free_ptr(c->d.cstart);
+        c->free_ptr(c->d.csum);
+        c->free_ptr(c->d.cbase);
         c->free_ptr(c->d_cblk_sys);
         c->free_ptr(c->d_cblk_run);
         c->d.cnt = c->alloc<int>(cells, err);
         c->d.cstart = c->alloc<int>(cells, err);
+        c->d.csum = c->alloc<int>(cells / BLK, err);
+        c->d.cbase = c->alloc<int>(cells / BLK, err);
         c->d_cblk_sys = c->alloc<int>(cells / BLK, err);
         c->d_cblk_run = c->alloc<int>(cells / BLK, err);
         if (err) return err;
@@ -504,7 +516,7 @@ void advance_budgets(mdg_ctx* c, int64_t n) {
 int launch_rb(mdg_ctx* c, const Dev& d, cudaStream_t st) {
     return launch_rebuild(d, st) + (c->has_mixed ? launch_rebuild_tail_mixed(d, c->has_dem, st) : 0);
 }
-int rb_kernels(const mdg_ctx* c) { return 8 + (c->has_mixed && c->has_dem ? 1 : 0); }
+int rb_kernels(const mdg_ctx* c) { return 9 + (c->has_mixed && c->has_dem ? 1 : 0); }
 int launch_fin(mdg_ctx* c, const Dev& d, cudaStream_t st, int integrate) {
     return c->has_mixed ? launch_final_mixed(d, st, integrate) : launch_final(d, st, integrate);
 }
@@ -859,7 +871,11 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     d.s_type = c->alloc<uint32_t>(P, err);
     d.s_img = c->alloc<int4>(P, err);
     d.pos2 = c->alloc<float4>(2 * P, err);
-    if (c->has_mixed) d.lbp2 = c->alloc<float4>(2 * P, err);
+    if (c->has_mixed) {
+        d.lbp2 = c->alloc<float4>(2 * P, err);
+        d.posu = c->alloc<uint4>(P, err);
+        d.lbpu = c->alloc<uint4>(P, err);
+    }
     if (c->has_dem) {
         d.omg = c->alloc<double4>(P, err);
         d.trq = c->alloc<double4>(P, err);

@@ -68,6 +68,7 @@ struct SysParams {
     int ext[3];          // extended grid (interior + 2*layers)
     int sl[3];           // ghost layers per side
     int win[3];          // enumeration half-width in interior cells
+    int build_tpp;       // list build: thread per particle (few per bin) or warp per bin
     double lo[3], hi[3], L[3];
     double bin[3], inv_bin[3], origin[3];
     double max_cutoff, stencil_cut_sq;
@@ -77,6 +78,10 @@ struct SysParams {
     float ucut2f;        // fp32 copy of uniform_cutoff_sq
     float sf2f;          // fp32 copy of sf2
     float Lh[3], Ll[3];  // two-float split of the box lengths
+    // fixed-point geometry of mixed LJ systems: u = (x - lo) 2^32 / L mod 2^32,
+    // so an int32 difference is the minimum-image separation in units of L / 2^32
+    double uinv[3];      // 2^32 / L
+    float uscale[3];     // L / 2^32
     double skin_fraction, sf2;
     int uniform;         // all cutoff radii equal
     double uniform_cutoff_sq;
@@ -168,6 +173,10 @@ struct Dev {
     // radius), pos2[2i+1] = (x_lo, y_lo, z_lo, 0).  lbp2: same at the last build.
     float4* pos2;
     float4* lbp2;
+    // mixed LJ systems: 32-bit fixed-point positions (x, y, z, 0) written by the
+    // integrator every step and read by the pair kernel; lbpu: same at the last build
+    uint4* posu;
+    uint4* lbpu;
     // per-particle virial (6 x P) when any system accumulates it
     double* vir;
     // reductions
@@ -175,6 +184,8 @@ struct Dev {
     const int* blk_sys;   // particle block -> system
     const int* cblk_sys;  // cell block -> system (-1 past the systems' cells)
     const int* cblk0;     // first cell block of each system
+    int* csum;            // particles per cell block (k_cells -> k_scan, cleared there)
+    int* cbase;           // first particle of each cell block (k_scan -> k_cellscan)
     int ncblocks;         // allocated cell blocks
     // Run maps: the particle / cell blocks of the systems that advance in this
     // launch (uploaded, step budget not exhausted).  The step kernels' grids
@@ -243,6 +254,65 @@ __device__ __forceinline__ void two_float_add(float& hi, float& lo, float t) {
     const float h2 = s + l;
     lo = l - (h2 - s);
     hi = h2;
+}
+
+// 32-bit fixed-point position of a mixed LJ particle: round((x - lo) 2^32 / L)
+// modulo 2^32 per axis.  Differences wrap like the periodic box, so
+// (int)(u_j - u_i) * L / 2^32 is the minimum-image separation whenever it is
+// below L / 2 (the list cutoff is), with ~L 2^-33 quantisation.
+__device__ __forceinline__ uint4 fixed_pos(const SysParams& sp, const double4& x) {
+    return make_uint4((unsigned int)__double2ll_rn((x.x - sp.lo[0]) * sp.uinv[0]),
+                      (unsigned int)__double2ll_rn((x.y - sp.lo[1]) * sp.uinv[1]),
+                      (unsigned int)__double2ll_rn((x.z - sp.lo[2]) * sp.uinv[2]), 0u);
+}
+
+__device__ __forceinline__ float3 fixed_sep(const SysParams& sp, const uint4& uj, const uint4& ui) {
+    return make_float3((float)(int)(uj.x - ui.x) * sp.uscale[0], (float)(int)(uj.y - ui.y) * sp.uscale[1],
+                       (float)(int)(uj.z - ui.z) * sp.uscale[2]);
+}
+
+// Geometry copy of a mixed-precision particle after its drift (tx, ty, tz)
+// to the fp64 position x, and its rebuild request (decide_rebuild's per-atom
+// tests, neighbor.rs:564-674) when test is set: displacement since the last
+// build in fp32 against a threshold 1e-5 on the safe side, every / check,
+// and (reference policy) leaving the box on a periodic axis.  LJ systems keep
+// the fixed-point copy (box exit tested on the fp64 position, as the
+// reference does); DEM systems the two-float copy.
+__device__ __forceinline__ bool mixed_drift(const Dev& d, const SysParams& sp, long long i, const double4& x,
+                                            double tx, double ty, double tz, bool test, int ssb) {
+    if (sp.kind == 1) {
+        const uint4 u = fixed_pos(sp, x);
+        d.posu[i] = u;
+        if (!test) return false;
+        const float3 m = fixed_sep(sp, u, d.lbpu[i]);
+        bool nd = m.x * m.x + m.y * m.y + m.z * m.z > sp.disp_thr2f;
+        if (sp.every > 0) nd = (sp.check && nd) || ssb >= sp.every;
+        if (!nd && sp.policy == 0)
+            nd = (sp.per[0] && (x.x < sp.lo[0] || x.x >= sp.hi[0])) || (sp.per[1] && (x.y < sp.lo[1] || x.y >= sp.hi[1])) ||
+                 (sp.per[2] && (x.z < sp.lo[2] || x.z >= sp.hi[2]));
+        return nd;
+    }
+    // advance the two-float copy by the same drift in fp32 (exact two-sum,
+    // renormalised); it is re-derived from the fp64 position at every build
+    float4 ph = d.pos2[2 * i], pl = d.pos2[2 * i + 1];
+    two_float_add(ph.x, pl.x, (float)tx);
+    two_float_add(ph.y, pl.y, (float)ty);
+    two_float_add(ph.z, pl.z, (float)tz);
+    d.pos2[2 * i] = ph;
+    d.pos2[2 * i + 1] = pl;
+    if (!test) return false;
+    const float4 bh = d.lbp2[2 * i], bl = d.lbp2[2 * i + 1];
+    const float dx = (ph.x - bh.x) + (pl.x - bl.x);
+    const float dy = (ph.y - bh.y) + (pl.y - bl.y);
+    const float dz = (ph.z - bh.z) + (pl.z - bl.z);
+    bool nd = dx * dx + dy * dy + dz * dz > sp.disp_thr2f;
+    if (sp.every > 0) nd = (sp.check && nd) || ssb >= sp.every;
+    if (!nd && sp.policy == 0) {
+        const float rx = ph.x + pl.x, ry = ph.y + pl.y, rz = ph.z + pl.z;
+        nd = (sp.per[0] && (rx < 0.f || rx >= sp.Lh[0])) || (sp.per[1] && (ry < 0.f || ry >= sp.Lh[1])) ||
+             (sp.per[2] && (rz < 0.f || rz >= sp.Lh[2]));
+    }
+    return nd;
 }
 
 // ---- kernel launchers (mdg_kernels_fp64.cu / mdg_kernels_mixed.cu) ----------

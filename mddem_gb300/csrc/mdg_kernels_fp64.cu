@@ -80,31 +80,7 @@ __global__ void __launch_bounds__(BLK) k_initial(Dev d) {
         x.z += tz;
         d.vel[i] = v;
         d.pos[i] = x;
-        if (sp.precision == 1) {
-            // advance the two-float copy by the same drift in fp32 (exact two-sum,
-            // renormalised); it is re-derived from the fp64 position at every build
-            float4 ph = d.pos2[2 * i], pl = d.pos2[2 * i + 1];
-            two_float_add(ph.x, pl.x, (float)tx);
-            two_float_add(ph.y, pl.y, (float)ty);
-            two_float_add(ph.z, pl.z, (float)tz);
-            d.pos2[2 * i] = ph;
-            d.pos2[2 * i + 1] = pl;
-            if (!already) {
-                // rebuild decision in fp32 on the two-float copy, erring early
-                const float4 bh = d.lbp2[2 * i], bl = d.lbp2[2 * i + 1];
-                const float dx = (ph.x - bh.x) + (pl.x - bl.x);
-                const float dy = (ph.y - bh.y) + (pl.y - bl.y);
-                const float dz = (ph.z - bh.z) + (pl.z - bl.z);
-                bool nd = dx * dx + dy * dy + dz * dz > sp.disp_thr2f;
-                if (sp.every > 0) nd = (sp.check && nd) || st->steps_since_build >= sp.every;
-                if (!nd && sp.policy == 0) {
-                    const float rx = ph.x + pl.x, ry = ph.y + pl.y, rz = ph.z + pl.z;
-                    nd = (sp.per[0] && (rx < 0.f || rx >= sp.Lh[0])) || (sp.per[1] && (ry < 0.f || ry >= sp.Lh[1])) ||
-                     (sp.per[2] && (rz < 0.f || rz >= sp.Lh[2]));
-                }
-                need = nd;
-            }
-        }
+        if (sp.precision == 1) need = mixed_drift(d, sp, i, x, tx, ty, tz, !already, st->steps_since_build);
         if (sp.kind == 0) {
             double4 w = d.omg[i];
             if (w.w != 0.0) {
@@ -239,9 +215,10 @@ __global__ void __launch_bounds__(1024) k_rb_plan(Dev d) {
 __device__ __forceinline__ void cells_block(const Dev& d, int s, int lb) {
     const SysParams& sp = d.sp[s];
     const SysState* st = d.ss + s;
-    if (!do_sort(st)) return;
+    if (!do_sort(st)) return;  // uniform over the block
     const int li = lb * BLK + threadIdx.x;
-    if (li >= sp.n) return;
+    int key = -1;  // global cell block of the particle's cell
+    if (li < sp.n) {
     const long long i = (long long)sp.p0 + li;
     double4 x = d.pos[i];
     if (vload(&st->rebuild)) {
@@ -264,55 +241,70 @@ __device__ __forceinline__ void cells_block(const Dev& d, int s, int lb) {
     const int flat = (cx * sp.ext[1] + cy) * sp.ext[2] + cz;
     d.cell[i] = flat;
     atomicAdd(&d.cnt[sp.c0 + flat], 1);
+    key = d.cblk0[s] + flat / BLK;
+    }
+    // particle counts per 128-cell block, aggregated over the warp (particles
+    // are in bin order after the first sort, so a warp mostly shares one block)
+    const unsigned int grp = __match_any_sync(0xffffffffu, key);
+    if (key >= 0 && (int)(threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&d.csum[key], __popc(grp));
 }
 __global__ void __launch_bounds__(BLK) k_cells(Dev d) RB_FOR_PARTICLE_BLOCKS(cells_block)
 
-// exclusive scan of one system's cell counts -> absolute starts (+ sentinel);
-// counts are reset for use as scatter cursors.  One block per listed system.
+// Cell starts in two levels.  k_scan: per listed system (one block), the
+// exclusive scan of its 128-cell block counts (k_cells' csum) -> block bases
+// (absolute particle offsets); csum is cleared for the next rebuild.
+// k_cellscan: per cell block, the scan of its 128 counts + the block base ->
+// cstart (with the sentinel cstart[ncell] = p0 + n); counts are reset for use
+// as scatter cursors.
 __device__ void scan_system(const Dev& d, int s) {
     const SysParams& sp = d.sp[s];
     if (!do_sort(d.ss + s)) return;
     __shared__ int wsum[32];
-    __shared__ int carry;
     const int t = threadIdx.x;
-    if (t == 0) carry = sp.p0;
-    __syncthreads();
-    for (int base = 0; base < sp.ncell; base += 1024) {
-        const int c = base + t;
-        const int v = c < sp.ncell ? d.cnt[sp.c0 + c] : 0;
-        int x = v;
-        for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(0xffffffffu, x, o);
-            if ((t & 31) >= o) x += y;
+    const int cb0 = d.cblk0[s];
+    int carry = sp.p0;
+    for (int base = 0; base < sp.ncb; base += 1024) {
+        const int b = base + t;
+        const int v = b < sp.ncb ? d.csum[cb0 + b] : 0;
+        int tot;
+        const int ex = block_scan1024(v, wsum, tot);
+        if (b < sp.ncb) {
+            d.cbase[cb0 + b] = carry + ex;
+            d.csum[cb0 + b] = 0;
         }
-        if ((t & 31) == 31) wsum[t >> 5] = x;
-        __syncthreads();
-        if (t < 32) {
-            int w = wsum[t];
-            for (int o = 1; o < 32; o <<= 1) {
-                int y = __shfl_up_sync(0xffffffffu, w, o);
-                if (t >= o) w += y;
-            }
-            wsum[t] = w;
-        }
-        __syncthreads();
-        const int incl = x + ((t >> 5) ? wsum[(t >> 5) - 1] : 0);
-        const int c0v = carry;
-        if (c < sp.ncell) {
-            d.cstart[sp.c0 + c] = c0v + incl - v;
-            d.cnt[sp.c0 + c] = 0;
-        }
-        __syncthreads();
-        if (t == 1023) carry = c0v + incl;
-        __syncthreads();
+        carry += tot;
     }
-    if (t == 0) d.cstart[sp.c0 + sp.ncell] = carry;
-    __syncthreads();
 }
 __global__ void __launch_bounds__(1024) k_scan(Dev d) {
     const int rbn = *d.rb_n;
     for (int k = blockIdx.x; k < rbn; k += gridDim.x) scan_system(d, d.rb_sys[k]);
 }
+
+__device__ __forceinline__ void cellscan_block(const Dev& d, int s, int lcb, int) {
+    const SysParams& sp = d.sp[s];
+    if (!do_sort(d.ss + s)) return;  // uniform over the block
+    __shared__ int wsum[BLK / 32];
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int c = lcb * BLK + t;
+    const int v = c < sp.ncell ? d.cnt[sp.c0 + c] : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    int off = d.cbase[d.cblk0[s] + lcb];
+    for (int q = 0; q < w; q++) off += wsum[q];
+    if (c < sp.ncell) {
+        d.cstart[sp.c0 + c] = off + x - v;
+        d.cnt[sp.c0 + c] = 0;
+    } else if (c == sp.ncell) {
+        d.cstart[sp.c0 + c] = off + x - v;  // sentinel: p0 + n
+    }
+    __syncthreads();
+}
+__global__ void __launch_bounds__(BLK) k_cellscan(Dev d) RB_FOR_CELL_BLOCKS(cellscan_block, 1)
 
 __device__ __forceinline__ void scatter_block(const Dev& d, int s, int lb) {
     const SysParams& sp = d.sp[s];
@@ -330,31 +322,70 @@ __global__ void __launch_bounds__(BLK) k_scatter(Dev d) RB_FOR_PARTICLE_BLOCKS(s
 // made stable (documented deviation from sort_unstable_by_key,
 // neighbor.rs:740).  Also detects a non-identity permutation, which turns a
 // periodic sort into a rebuild (neighbor.rs:784-793).
-__device__ __forceinline__ void cellsort_block(const Dev& d, int s, int lcb, int) {
+// One warp per cell: the cell's keys (old indices, distinct) sit in registers,
+// CS_K per lane; each key's rank is the count of smaller keys, gathered by
+// warp shuffles; the keys are then written at their ranks.  Cells of more
+// than 32 * CS_K particles fall back to an insertion sort on lane 0.
+constexpr int CS_WARPS = BLK / 32;
+constexpr int CS_SUBS = BLK / CS_WARPS;  // blocks per 128-cell block
+constexpr int CS_K = 4;
+__device__ __forceinline__ void cellsort_cells(const Dev& d, int s, int lcb, int sub) {
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
     if (!do_sort(st)) return;
-    const int c = lcb * BLK + threadIdx.x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c = lcb * BLK + sub * CS_WARPS + warp;
     if (c >= sp.ncell) return;
     const int start = d.cstart[sp.c0 + c];
     const int m = d.cnt[sp.c0 + c];
     int* p = d.perm + start;
-    for (int a = 1; a < m; a++) {
-        const int key = p[a];
-        int b = a - 1;
-        while (b >= 0 && p[b] > key) {
-            p[b + 1] = p[b];
-            b--;
-        }
-        p[b + 1] = key;
-    }
     bool ident = true;
-    for (int a = 0; a < m; a++)
-        if (p[a] != start + a) ident = false;
-    d.cnt[sp.c0 + c] = 0;
-    if (!ident) atomicOr(&st->nonid, 1);
+    if (m <= 32 * CS_K) {
+        int key[CS_K], rank[CS_K];
+#pragma unroll
+        for (int k = 0; k < CS_K; k++) {
+            const int a = lane + 32 * k;
+            key[k] = a < m ? p[a] : 0x7fffffff;
+            rank[k] = 0;
+        }
+#pragma unroll
+        for (int kk = 0; kk < CS_K; kk++) {
+            if (32 * kk >= m) break;  // uniform over the warp
+            for (int t = 0; t < 32; t++) {
+                const int other = __shfl_sync(0xffffffffu, key[kk], t);
+#pragma unroll
+                for (int k = 0; k < CS_K; k++) rank[k] += other < key[k] ? 1 : 0;
+            }
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < CS_K; k++) {
+            const int a = lane + 32 * k;
+            if (a < m) {
+                p[rank[k]] = key[k];
+                if (key[k] != start + rank[k]) ident = false;
+            }
+        }
+        ident = __all_sync(0xffffffffu, ident);
+    } else if (lane == 0) {
+        for (int a = 1; a < m; a++) {
+            const int key = p[a];
+            int b = a - 1;
+            while (b >= 0 && p[b] > key) {
+                p[b + 1] = p[b];
+                b--;
+            }
+            p[b + 1] = key;
+        }
+        for (int a = 0; a < m; a++)
+            if (p[a] != start + a) ident = false;
+    }
+    if (lane == 0) {
+        d.cnt[sp.c0 + c] = 0;
+        if (!ident) atomicOr(&st->nonid, 1);
+    }
 }
-__global__ void __launch_bounds__(BLK) k_cellsort(Dev d) RB_FOR_CELL_BLOCKS(cellsort_block, 1)
+__global__ void __launch_bounds__(BLK) k_cellsort(Dev d) RB_FOR_CELL_BLOCKS(cellsort_cells, CS_SUBS)
 
 // Atom::apply_permutation + AtomDataRegistry::apply_permutation_all +
 // ContactHistoryStore::apply_permutation (atom.rs:383-394, 197-202,
@@ -437,6 +468,11 @@ __device__ __forceinline__ void copyback_block(const Dev& d, int s, int lb) {
     if (sp.precision == 1) {
         d.lbp2[2 * k] = ph;
         d.lbp2[2 * k + 1] = pl;
+        if (sp.kind == 1) {
+            const uint4 u = fixed_pos(sp, x);
+            d.posu[k] = u;
+            d.lbpu[k] = u;
+        }
     }
     // ext cell in the new order, with a flag when a bin coordinate lies within
     // 1e-9 of a bin edge (the list build then recomputes image cells in fp64)
@@ -608,6 +644,112 @@ __device__ __noinline__ int near_pair(const Dev& d, const SysParams& sp, long lo
 
 constexpr int BUILD_SUBS = BLK / BUILD_WARPS;  // blocks per 128-bin cell block
 
+// Thread per particle, for systems with few particles per bin (dilute
+// granular gases), where a warp per bin would leave most lanes idle: the same
+// window walk, candidates in the same order, the same screen, owner rule and
+// precise path as the warp-per-bin build, so both give identical rows.
+// Unit u covers particles [u BLK, u BLK + BLK) of system s.
+__device__ void build_particles(const Dev& d, int s, int u) {
+    const SysParams& sp = d.sp[s];
+    SysState* st = d.ss + s;
+    const int li = u * BLK + threadIdx.x;
+    if (li >= sp.n) return;  // no warp-synchronous code below
+    const long long i = (long long)sp.p0 + li;
+    d.lbp[i] = d.pos[i];
+    const float4 hi = d.pos2[2 * i], lo = d.pos2[2 * i + 1];
+    const int cr = d.cell[i];
+    const bool edge_i = cr < 0;
+    const int c = cr & 0x7fffffff;
+    const int ez = c % sp.ext[2];
+    const int ey = (c / sp.ext[2]) % sp.ext[1];
+    const int ex = c / (sp.ext[2] * sp.ext[1]);
+    const int qx0 = min(max(ex - sp.sl[0], 0), sp.nc[0] - 1);
+    const int qy0 = min(max(ey - sp.sl[1], 0), sp.nc[1] - 1);
+    const int qz0 = min(max(ez - sp.sl[2], 0), sp.nc[2] - 1);
+    const float brel = sp.band_rel;
+    const long long base = sp.lst0 + li;
+    int count = 0;
+    for (int ox = -sp.win[0]; ox <= sp.win[0]; ox++) {
+        int qx = qx0 + ox, sx = 0;
+        if (qx < 0) { qx += sp.nc[0]; sx = -1; } else if (qx >= sp.nc[0]) { qx -= sp.nc[0]; sx = 1; }
+        if (sx && !sp.per[0]) continue;  // fixed axis: no periodic image
+        if (qx < 0 || qx >= sp.nc[0]) continue;
+        for (int oy = -sp.win[1]; oy <= sp.win[1]; oy++) {
+            int qy = qy0 + oy, sy = 0;
+            if (qy < 0) { qy += sp.nc[1]; sy = -1; } else if (qy >= sp.nc[1]) { qy -= sp.nc[1]; sy = 1; }
+            if (sy && !sp.per[1]) continue;
+            if (qy < 0 || qy >= sp.nc[1]) continue;
+            for (int oz = -sp.win[2]; oz <= sp.win[2]; oz++) {
+                int qz = qz0 + oz, sz = 0;
+                if (qz < 0) { qz += sp.nc[2]; sz = -1; } else if (qz >= sp.nc[2]) { qz -= sp.nc[2]; sz = 1; }
+                if (sz && !sp.per[2]) continue;
+                if (qz < 0 || qz >= sp.nc[2]) continue;
+                const bool shifted = (sx | sy | sz) != 0;
+                const uint32_t sc = (uint32_t)((sx + 1) * 9 + (sy + 1) * 3 + (sz + 1));
+                const float hsx = hi.x - (float)sx * sp.Lh[0];
+                const float hsy = hi.y - (float)sy * sp.Lh[1];
+                const float hsz = hi.z - (float)sz * sp.Lh[2];
+                const int axa = (qx == 0) ? -1 : 0, axb = (qx == sp.nc[0] - 1) ? 1 : 0;
+                const int aya = (qy == 0) ? -1 : 0, ayb = (qy == sp.nc[1] - 1) ? 1 : 0;
+                const int aza = (qz == 0) ? -1 : 0, azb = (qz == sp.nc[2] - 1) ? 1 : 0;
+                for (int ax = axa; ax <= axb; ax++)
+                    for (int ay = aya; ay <= ayb; ay++)
+                        for (int az = aza; az <= azb; az++) {
+                            const int Ex = qx + sp.sl[0] + ax, Ey = qy + sp.sl[1] + ay, Ez = qz + sp.sl[2] + az;
+                            const int flatE = (Ex * sp.ext[1] + Ey) * sp.ext[2] + Ez;
+                            const int m0 = d.cstart[sp.c0 + flatE], m1 = d.cstart[sp.c0 + flatE + 1];
+                            if (m0 == m1) continue;
+                            const TileRule tr = tile_rule(sp, ex, ey, ez, Ex, Ey, Ez, sx, sy, sz);
+                            if (!tr.own && !tr.oth && !tr.same && !shifted) continue;
+                            for (int jj = m0; jj < m1; jj++) {
+                                const long long j = jj;
+                                if (!shifted && j == i) continue;
+                                const float4 hj = d.pos2[2 * j];
+                                const float px = hj.x - hsx, py = hj.y - hsy, pz = hj.z - hsz;
+                                const float r2h = px * px + py * py + pz * pz;
+                                float c2h;
+                                if (sp.uniform) {
+                                    c2h = sp.ucut2f;
+                                } else {
+                                    const float ssum = hi.w + hj.w;
+                                    c2h = ssum * ssum * sp.sf2f;
+                                }
+                                if (!(r2h <= c2h * (1.f + brel))) continue;
+                                const bool near = r2h > c2h * (1.f - brel);
+                                const bool edge = shifted && (edge_i || d.cell[j] < 0);
+                                int bits;
+                                if (!near && !edge) {
+                                    bits = ((tr.own || (tr.same && (sp.newton ? j > i : true))) ? 1 : 0) |
+                                           ((tr.oth || (tr.same && sp.newton && i > j)) ? 2 : 0);
+                                } else {
+                                    bits = near_pair(d, sp, i, j, hi, lo, hj, d.pos2[2 * j + 1], sx, sy, sz, edge, ex,
+                                                     ey, ez, Ex, Ey, Ez, tr);
+                                }
+                                const uint32_t jl = (uint32_t)(j - sp.p0);
+                                if (bits & 1) {
+                                    if (count < sp.ncap)
+                                        d.nlist[base + (long long)count * sp.npad] = jl | ((sc + 27u) << IDX_BITS);
+                                    count++;
+                                }
+                                if (bits & 2) {
+                                    if (count < sp.ncap) d.nlist[base + (long long)count * sp.npad] = jl | (sc << IDX_BITS);
+                                    count++;
+                                }
+                            }
+                        }
+            }
+        }
+    }
+    if (count > sp.ncap) {
+        atomicOr(&st->status, ST_NBR_OVF);
+        atomicMax(&st->max_nbr, count);
+        count = sp.ncap;
+    } else {
+        atomicMax(&st->max_nbr, count);
+    }
+    d.nnum[i] = count;
+}
+
 // One warp per bin: bin `sub * BUILD_WARPS + warp` of cell block `lcb` of
 // system s.  Warp-synchronous only (no block barrier), so warps may leave early.
 __device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
@@ -617,6 +759,10 @@ __device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
     if (!do_rebuild(st)) return;
+    if (sp.build_tpp) {  // uniform over the block
+        build_particles(d, s, lcb * BUILD_SUBS + sub);
+        return;
+    }
     const int c = lcb * BLK + sub * BUILD_WARPS + warp;
     if (c >= sp.ncell) return;
     const int a0 = d.cstart[sp.c0 + c], a1 = d.cstart[sp.c0 + c + 1];
@@ -641,102 +787,143 @@ __device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
         }
         const long long base = sp.lst0 + (i - sp.p0);
         int count = 0;
-        for (int ox = -sp.win[0]; ox <= sp.win[0]; ox++) {
-            int qx = qx0 + ox, sx = 0;
-            if (qx < 0) { qx += sp.nc[0]; sx = -1; } else if (qx >= sp.nc[0]) { qx -= sp.nc[0]; sx = 1; }
-            if (sx && !sp.per[0]) continue;  // fixed axis: no periodic image
-            if (qx < 0 || qx >= sp.nc[0]) continue;
-            for (int oy = -sp.win[1]; oy <= sp.win[1]; oy++) {
-                int qy = qy0 + oy, sy = 0;
-                if (qy < 0) { qy += sp.nc[1]; sy = -1; } else if (qy >= sp.nc[1]) { qy -= sp.nc[1]; sy = 1; }
-                if (sy && !sp.per[1]) continue;  // fixed axis: no periodic image
-                if (qy < 0 || qy >= sp.nc[1]) continue;
-                for (int oz = -sp.win[2]; oz <= sp.win[2]; oz++) {
-                    int qz = qz0 + oz, sz = 0;
+        // the window's cells in the reference's stencil order (ox, oy, oz
+        // ascending), 32 at a time: lane k describes entry e0 + k -- validity,
+        // periodic shift, boundary flags, its interior cell's ext index and
+        // particle range, and the tile rule -- so the warp walks the window
+        // with shuffles instead of dependent loads per cell
+        const int wy = 2 * sp.win[1] + 1, wz = 2 * sp.win[2] + 1;
+        const int nent = (2 * sp.win[0] + 1) * wy * wz;
+        for (int e0 = 0; e0 < nent; e0 += 32) {
+            int eq = 0, eE = 0, em0 = 0, em1 = 0;
+            {
+                const int e = e0 + lane;
+                if (e < nent) {
+                    int qx = qx0 + e / (wy * wz) - sp.win[0], sx = 0;
+                    int qy = qy0 + (e / wz) % wy - sp.win[1], sy = 0;
+                    int qz = qz0 + e % wz - sp.win[2], sz = 0;
+                    if (qx < 0) { qx += sp.nc[0]; sx = -1; } else if (qx >= sp.nc[0]) { qx -= sp.nc[0]; sx = 1; }
+                    if (qy < 0) { qy += sp.nc[1]; sy = -1; } else if (qy >= sp.nc[1]) { qy -= sp.nc[1]; sy = 1; }
                     if (qz < 0) { qz += sp.nc[2]; sz = -1; } else if (qz >= sp.nc[2]) { qz -= sp.nc[2]; sz = 1; }
-                    if (sz && !sp.per[2]) continue;  // fixed axis: no periodic image
-                    if (qz < 0 || qz >= sp.nc[2]) continue;
-                    const bool shifted = (sx | sy | sz) != 0;
-                    const uint32_t sc = (uint32_t)((sx + 1) * 9 + (sy + 1) * 3 + (sz + 1));
-                    // centre position moved by -s L: the candidate's own hi part
-                    // then gives the prefilter separation directly
-                    const float hsx = hi.x - (float)sx * sp.Lh[0];
-                    const float hsy = hi.y - (float)sy * sp.Lh[1];
-                    const float hsz = hi.z - (float)sz * sp.Lh[2];
-                    const int axa = (qx == 0) ? -1 : 0, axb = (qx == sp.nc[0] - 1) ? 1 : 0;
-                    const int aya = (qy == 0) ? -1 : 0, ayb = (qy == sp.nc[1] - 1) ? 1 : 0;
-                    const int aza = (qz == 0) ? -1 : 0, azb = (qz == sp.nc[2] - 1) ? 1 : 0;
-                    for (int ax = axa; ax <= axb; ax++)
-                        for (int ay = aya; ay <= ayb; ay++)
-                            for (int az = aza; az <= azb; az++) {
-                                const int Ex = qx + sp.sl[0] + ax, Ey = qy + sp.sl[1] + ay, Ez = qz + sp.sl[2] + az;
+                    // fixed axes have no periodic image
+                    const bool ok = !(sx && !sp.per[0]) && !(sy && !sp.per[1]) && !(sz && !sp.per[2]) && qx >= 0 &&
+                                    qx < sp.nc[0] && qy >= 0 && qy < sp.nc[1] && qz >= 0 && qz < sp.nc[2];
+                    if (ok) {
+                        const int Ex = qx + sp.sl[0], Ey = qy + sp.sl[1], Ez = qz + sp.sl[2];
+                        const int flatE = (Ex * sp.ext[1] + Ey) * sp.ext[2] + Ez;
+                        em0 = d.cstart[sp.c0 + flatE];
+                        em1 = d.cstart[sp.c0 + flatE + 1];
+                        const TileRule tr = tile_rule(sp, ex, ey, ez, Ex, Ey, Ez, sx, sy, sz);
+                        eE = flatE;
+                        eq = 1 | ((sx + 1) << 1) | ((sy + 1) << 3) | ((sz + 1) << 5) | (qx == 0 ? 1 << 7 : 0) |
+                             (qx == sp.nc[0] - 1 ? 1 << 8 : 0) | (qy == 0 ? 1 << 9 : 0) |
+                             (qy == sp.nc[1] - 1 ? 1 << 10 : 0) | (qz == 0 ? 1 << 11 : 0) |
+                             (qz == sp.nc[2] - 1 ? 1 << 12 : 0) | (tr.own ? 1 << 13 : 0) | (tr.oth ? 1 << 14 : 0) |
+                             (tr.same ? 1 << 15 : 0);
+                    }
+                }
+            }
+            const int ne = min(32, nent - e0);
+            for (int k = 0; k < ne; k++) {
+                const int q = __shfl_sync(0xffffffffu, eq, k);
+                const int qE = __shfl_sync(0xffffffffu, eE, k);
+                const int qm0 = __shfl_sync(0xffffffffu, em0, k);
+                const int qm1 = __shfl_sync(0xffffffffu, em1, k);
+                if (!(q & 1)) continue;  // uniform over the warp
+                const int sx = ((q >> 1) & 3) - 1, sy = ((q >> 3) & 3) - 1, sz = ((q >> 5) & 3) - 1;
+                const int Ez0 = qE % sp.ext[2], Ey0 = (qE / sp.ext[2]) % sp.ext[1], Ex0 = qE / (sp.ext[2] * sp.ext[1]);
+                const bool shifted = (sx | sy | sz) != 0;
+                const uint32_t sc = (uint32_t)((sx + 1) * 9 + (sy + 1) * 3 + (sz + 1));
+                // centre position moved by -s L: the candidate's own hi part
+                // then gives the prefilter separation directly
+                const float hsx = hi.x - (float)sx * sp.Lh[0];
+                const float hsy = hi.y - (float)sy * sp.Lh[1];
+                const float hsz = hi.z - (float)sz * sp.Lh[2];
+                // an interior cell on the box face also visits the adjacent
+                // ghost-layer cells (particles binned there by rounding)
+                const int axa = (q >> 7) & 1 ? -1 : 0, axb = (q >> 8) & 1 ? 1 : 0;
+                const int aya = (q >> 9) & 1 ? -1 : 0, ayb = (q >> 10) & 1 ? 1 : 0;
+                const int aza = (q >> 11) & 1 ? -1 : 0, azb = (q >> 12) & 1 ? 1 : 0;
+                for (int ax = axa; ax <= axb; ax++)
+                    for (int ay = aya; ay <= ayb; ay++)
+                        for (int az = aza; az <= azb; az++) {
+                            const int Ex = Ex0 + ax, Ey = Ey0 + ay, Ez = Ez0 + az;
+                            int m0, m1;
+                            TileRule tr;
+                            if ((ax | ay | az) == 0) {
+                                m0 = qm0;
+                                m1 = qm1;
+                                tr = TileRule{((q >> 13) & 1) != 0, ((q >> 14) & 1) != 0, ((q >> 15) & 1) != 0};
+                            } else {
                                 const int flatE = (Ex * sp.ext[1] + Ey) * sp.ext[2] + Ez;
-                                const int m0 = d.cstart[sp.c0 + flatE], m1 = d.cstart[sp.c0 + flatE + 1];
+                                m0 = d.cstart[sp.c0 + flatE];
+                                m1 = d.cstart[sp.c0 + flatE + 1];
                                 if (m0 == m1) continue;
-                                const TileRule tr = tile_rule(sp, ex, ey, ez, Ex, Ey, Ez, sx, sy, sz);
-                                // nothing in this bin pair can enter the list unless a
-                                // bin-edge particle needs its image bin recomputed
-                                const bool maybe_edge = shifted;
-                                if (!tr.own && !tr.oth && !tr.same && !maybe_edge) continue;
-                                for (int t0 = m0; t0 < m1; t0 += 32) {
-                                    const int nt = min(32, m1 - t0);
-                                    __syncwarp();
-                                    if (lane < nt) {
-                                        tile_h[warp][lane] = d.pos2[2 * (long long)(t0 + lane)];
-                                        tile_l[warp][lane] = d.pos2[2 * (long long)(t0 + lane) + 1];
-                                        tile_e[warp][lane] = d.cell[t0 + lane] < 0;
+                                tr = tile_rule(sp, ex, ey, ez, Ex, Ey, Ez, sx, sy, sz);
+                            }
+                            if (m0 == m1) continue;
+                            // nothing in this bin pair can enter the list unless a
+                            // bin-edge particle needs its image bin recomputed
+                            const bool maybe_edge = shifted;
+                            if (!tr.own && !tr.oth && !tr.same && !maybe_edge) continue;
+                            for (int t0 = m0; t0 < m1; t0 += 32) {
+                                const int nt = min(32, m1 - t0);
+                                __syncwarp();
+                                if (lane < nt) {
+                                    tile_h[warp][lane] = d.pos2[2 * (long long)(t0 + lane)];
+                                    tile_l[warp][lane] = d.pos2[2 * (long long)(t0 + lane) + 1];
+                                    tile_e[warp][lane] = d.cell[t0 + lane] < 0;
+                                }
+                                __syncwarp();
+                                if (!act) continue;
+                                // pass 1: hi-part fp32 screen of the whole tile into two bit
+                                // masks: clearly inside the cutoff / near it (precise path)
+                                unsigned int mask = 0u, near = 0u;
+        #pragma unroll 4
+                                for (int t = 0; t < nt; t++) {
+                                    const float4 hj = tile_h[warp][t];
+                                    const float px = hj.x - hsx, py = hj.y - hsy, pz = hj.z - hsz;
+                                    const float r2h = px * px + py * py + pz * pz;
+                                    float c2h;
+                                    if (sp.uniform) {
+                                        c2h = sp.ucut2f;
+                                    } else {
+                                        const float ssum = hi.w + hj.w;
+                                        c2h = ssum * ssum * sp.sf2f;
                                     }
-                                    __syncwarp();
-                                    if (!act) continue;
-                                    // pass 1: hi-part fp32 screen of the whole tile into two bit
-                                    // masks: clearly inside the cutoff / near it (precise path)
-                                    unsigned int mask = 0u, near = 0u;
-#pragma unroll 4
-                                    for (int t = 0; t < nt; t++) {
-                                        const float4 hj = tile_h[warp][t];
-                                        const float px = hj.x - hsx, py = hj.y - hsy, pz = hj.z - hsz;
-                                        const float r2h = px * px + py * py + pz * pz;
-                                        float c2h;
-                                        if (sp.uniform) {
-                                            c2h = sp.ucut2f;
-                                        } else {
-                                            const float ssum = hi.w + hj.w;
-                                            c2h = ssum * ssum * sp.sf2f;
-                                        }
-                                        mask |= (r2h <= c2h * (1.f + brel) ? 1u : 0u) << t;
-                                        near |= (r2h > c2h * (1.f - brel) ? 1u : 0u) << t;
+                                    mask |= (r2h <= c2h * (1.f + brel) ? 1u : 0u) << t;
+                                    near |= (r2h > c2h * (1.f - brel) ? 1u : 0u) << t;
+                                }
+                                if (!shifted && i >= t0 && i < t0 + nt) mask &= ~(1u << (int)(i - t0));
+                                // pass 2: survivors only
+                                while (mask) {
+                                    const int t = __ffs(mask) - 1;
+                                    mask &= mask - 1u;
+                                    const long long j = t0 + t;
+                                    const bool edge = shifted && (edge_i || tile_e[warp][t] != 0);
+                                    int bits;
+                                    if (!((near >> t) & 1u) && !edge) {
+                                        // clearly inside: owner decision only
+                                        bits = ((tr.own || (tr.same && (sp.newton ? j > i : true))) ? 1 : 0) |
+                                               ((tr.oth || (tr.same && sp.newton && i > j)) ? 2 : 0);
+                                    } else {
+                                        bits = near_pair(d, sp, i, j, hi, lo, tile_h[warp][t], tile_l[warp][t], sx, sy,
+                                                         sz, edge, ex, ey, ez, Ex, Ey, Ez, tr);
                                     }
-                                    if (!shifted && i >= t0 && i < t0 + nt) mask &= ~(1u << (int)(i - t0));
-                                    // pass 2: survivors only
-                                    while (mask) {
-                                        const int t = __ffs(mask) - 1;
-                                        mask &= mask - 1u;
-                                        const long long j = t0 + t;
-                                        const bool edge = shifted && (edge_i || tile_e[warp][t] != 0);
-                                        int bits;
-                                        if (!((near >> t) & 1u) && !edge) {
-                                            // clearly inside: owner decision only
-                                            bits = ((tr.own || (tr.same && (sp.newton ? j > i : true))) ? 1 : 0) |
-                                                   ((tr.oth || (tr.same && sp.newton && i > j)) ? 2 : 0);
-                                        } else {
-                                            bits = near_pair(d, sp, i, j, hi, lo, tile_h[warp][t], tile_l[warp][t], sx, sy,
-                                                             sz, edge, ex, ey, ez, Ex, Ey, Ez, tr);
-                                        }
-                                        const uint32_t jl = (uint32_t)(j - sp.p0);
-                                        if (bits & 1) {
-                                            if (count < sp.ncap)
-                                                d.nlist[base + (long long)count * sp.npad] = jl | ((sc + 27u) << IDX_BITS);
-                                            count++;
-                                        }
-                                        if (bits & 2) {
-                                            if (count < sp.ncap)
-                                                d.nlist[base + (long long)count * sp.npad] = jl | (sc << IDX_BITS);
-                                            count++;
-                                        }
+                                    const uint32_t jl = (uint32_t)(j - sp.p0);
+                                    if (bits & 1) {
+                                        if (count < sp.ncap)
+                                            d.nlist[base + (long long)count * sp.npad] = jl | ((sc + 27u) << IDX_BITS);
+                                        count++;
+                                    }
+                                    if (bits & 2) {
+                                        if (count < sp.ncap)
+                                            d.nlist[base + (long long)count * sp.npad] = jl | (sc << IDX_BITS);
+                                        count++;
                                     }
                                 }
                             }
-                }
+                        }
             }
         }
         if (act) {
@@ -1387,18 +1574,20 @@ int launch_initial(const Dev& d, cudaStream_t st) {
 int launch_rebuild(const Dev& d, cudaStream_t st) {
     constexpr int CAP = 152 * 16;
     const int gp = d.nrun < CAP ? d.nrun : CAP;
-    const int gc = d.ncrun < CAP ? d.ncrun : CAP;
     const int gb = d.ncrun * BUILD_SUBS < 2 * CAP ? d.ncrun * BUILD_SUBS : 2 * CAP;
     const int gs = d.nrun_sys < 304 ? d.nrun_sys : 304;
+    const int gc = d.ncrun < CAP ? d.ncrun : CAP;
+    const int gs_ = d.ncrun * CS_SUBS < 2 * CAP ? d.ncrun * CS_SUBS : 2 * CAP;
     k_rb_plan<<<1, 1024, 0, st>>>(d);
     k_cells<<<gp, BLK, 0, st>>>(d);
     k_scan<<<gs, 1024, 0, st>>>(d);
+    k_cellscan<<<gc, BLK, 0, st>>>(d);
     k_scatter<<<gp, BLK, 0, st>>>(d);
-    k_cellsort<<<gc, BLK, 0, st>>>(d);
+    k_cellsort<<<gs_, BLK, 0, st>>>(d);
     k_gather<<<gp, BLK, 0, st>>>(d);
     k_copyback<<<gp, BLK, 0, st>>>(d);
     k_build<<<gb, BUILD_WARPS * 32, 0, st>>>(d);
-    return 8;
+    return 9;
 }
 
 int launch_force_fp64(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st) {

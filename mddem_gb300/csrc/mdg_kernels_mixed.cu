@@ -24,7 +24,12 @@ struct Kahan {
 };
 
 // LJ 12-6 in FP32 with compensated per-particle sums (same list, same owner
-// frames as the FP64 kernel).
+// frames as the FP64 kernel).  Geometry from the 32-bit fixed-point copy: one
+// 16-byte gather per list entry, and the wrapped integer difference is the
+// minimum-image separation, so the entry's image code is not needed.  The
+// separation carries the fixed-point quantisation (L 2^-33) plus one fp32
+// rounding (2^-24 relative) and the fp32 scale (2^-24 relative, the same for
+// every pair).
 // Minimum resident blocks per SM asked of ptxas for k_lj_mixed (a compile-time
 // tuning knob; 8 caps it at 64 registers).
 #ifndef MDG_LJ_MINB
@@ -43,20 +48,18 @@ __global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
     const long long i = (long long)sp.p0 + li;
     Kahan kx, ky, kz;
     if (act) {
-        const float4 hi = d.pos2[2 * i];
-        const float4 lo = d.pos2[2 * i + 1];
+        const uint4 ui = d.posu[i];
         const int nn = d.nnum[i];
         const long long base = sp.lst0 + li;
         const float lj1 = sp.lj1f, lj2 = sp.lj2f;
         const float cut2 = sp.lj_cut2f;
-        const float Lh0 = sp.Lh[0], Lh1 = sp.Lh[1], Lh2 = sp.Lh[2];
-        const float Ll0 = sp.Ll[0], Ll1 = sp.Ll[1], Ll2 = sp.Ll[2];
+        const float s0 = sp.uscale[0], s1 = sp.uscale[1], s2 = sp.uscale[2];
         // U entries in flight per lane: list loads first, then the gathers, then
         // the arithmetic, so each lane keeps U independent load chains open
         constexpr int U = 4;
         for (int k0 = lane; k0 < nn; k0 += U * TPP) {
             uint32_t e[U];
-            float4 hj[U], lj[U];
+            uint4 uj[U];
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int k = k0 + u * TPP;
@@ -65,27 +68,16 @@ __global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const long long j = sp.p0 + (e[u] != 0xffffffffu ? (e[u] & IDX_MASK) : 0u);
-                hj[u] = __ldg(d.pos2 + 2 * j);
-                lj[u] = __ldg(d.pos2 + 2 * j + 1);
+                uj[u] = __ldg(d.posu + j);
             }
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 if (e[u] == 0xffffffffu) continue;
-                const uint32_t code = e[u] >> IDX_BITS;
-                const int sc = (int)(code >= 27u ? code - 27u : code);
-                // d_i = x_j(+s) - x_i for owner and partner entries alike: the
-                // force on i is -fpair d_i either way
-                float dx, dy, dz;
-                if (sc == 13) {  // no periodic image (most entries)
-                    dx = (hj[u].x - hi.x) + (lj[u].x - lo.x);
-                    dy = (hj[u].y - hi.y) + (lj[u].y - lo.y);
-                    dz = (hj[u].z - hi.z) + (lj[u].z - lo.z);
-                } else {
-                    const int sx = sc / 9 - 1, sy = (sc / 3) % 3 - 1, sz = sc % 3 - 1;
-                    dx = two_float_sep(hj[u].x, lj[u].x, hi.x, lo.x, sx, Lh0, Ll0);
-                    dy = two_float_sep(hj[u].y, lj[u].y, hi.y, lo.y, sy, Lh1, Ll1);
-                    dz = two_float_sep(hj[u].z, lj[u].z, hi.z, lo.z, sz, Lh2, Ll2);
-                }
+                // d_i = x_j(+image) - x_i for owner and partner entries alike:
+                // the force on i is -fpair d_i either way
+                const float dx = (float)(int)(uj[u].x - ui.x) * s0;
+                const float dy = (float)(int)(uj[u].y - ui.y) * s1;
+                const float dz = (float)(int)(uj[u].z - ui.z) * s2;
                 const float r2 = dx * dx + dy * dy + dz * dz;
                 if (r2 >= cut2) continue;
                 const float r2inv = __frcp_rn(r2);
@@ -538,26 +530,7 @@ __global__ void __launch_bounds__(BLK) k_initial_mixed(Dev d, int nh_only, const
         x.z += tz;
         d.vel[i] = v;
         d.pos[i] = x;
-        float4 ph = d.pos2[2 * i], pl = d.pos2[2 * i + 1];
-        two_float_add(ph.x, pl.x, (float)tx);
-        two_float_add(ph.y, pl.y, (float)ty);
-        two_float_add(ph.z, pl.z, (float)tz);
-        d.pos2[2 * i] = ph;
-        d.pos2[2 * i + 1] = pl;
-        if (!already) {
-            const float4 bh = d.lbp2[2 * i], bl = d.lbp2[2 * i + 1];
-            const float dx = (ph.x - bh.x) + (pl.x - bl.x);
-            const float dy = (ph.y - bh.y) + (pl.y - bl.y);
-            const float dz = (ph.z - bh.z) + (pl.z - bl.z);
-            bool nd = dx * dx + dy * dy + dz * dz > sp.disp_thr2f;
-            if (sp.every > 0) nd = (sp.check && nd) || st->steps_since_build >= sp.every;
-            if (!nd && sp.policy == 0) {
-                const float rx = ph.x + pl.x, ry = ph.y + pl.y, rz = ph.z + pl.z;
-                nd = (sp.per[0] && (rx < 0.f || rx >= sp.Lh[0])) || (sp.per[1] && (ry < 0.f || ry >= sp.Lh[1])) ||
-                     (sp.per[2] && (rz < 0.f || rz >= sp.Lh[2]));
-            }
-            need = nd;
-        }
+        need = mixed_drift(d, sp, i, x, tx, ty, tz, !already, st->steps_since_build);
         if (sp.kind == 0) {
             double4 w = d.omg[i];
             if (w.w != 0.0) {
@@ -785,24 +758,7 @@ __global__ void __launch_bounds__(BLK) k_step_mixed(Dev d, const long long* loop
             x.y += ty;
             x.z += tz;
             d.pos[i] = x;
-            float4 ph = d.pos2[2 * i], pl = d.pos2[2 * i + 1];
-            two_float_add(ph.x, pl.x, (float)tx);
-            two_float_add(ph.y, pl.y, (float)ty);
-            two_float_add(ph.z, pl.z, (float)tz);
-            d.pos2[2 * i] = ph;
-            d.pos2[2 * i + 1] = pl;
-            const float4 bh = d.lbp2[2 * i], bl = d.lbp2[2 * i + 1];
-            const float dx = (ph.x - bh.x) + (pl.x - bl.x);
-            const float dy = (ph.y - bh.y) + (pl.y - bl.y);
-            const float dz = (ph.z - bh.z) + (pl.z - bl.z);
-            bool nd = dx * dx + dy * dy + dz * dz > sp.disp_thr2f;
-            if (sp.every > 0) nd = (sp.check && nd) || ssb >= sp.every;
-            if (!nd && sp.policy == 0) {
-                const float rx = ph.x + pl.x, ry = ph.y + pl.y, rz = ph.z + pl.z;
-                nd = (sp.per[0] && (rx < 0.f || rx >= sp.Lh[0])) || (sp.per[1] && (ry < 0.f || ry >= sp.Lh[1])) ||
-                     (sp.per[2] && (rz < 0.f || rz >= sp.Lh[2]));
-            }
-            need = nd;
+            need = mixed_drift(d, sp, i, x, tx, ty, tz, true, ssb);
         }
         d.vel[i] = v;
         if (sp.kind == 0) {

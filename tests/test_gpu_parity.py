@@ -320,3 +320,28 @@ def test_fused_multistep_equals_unfused(gpu_lib):
     for ta, tb in zip(out[0][3], out[1][3]):
         assert ta["step"] == tb["step"] and ta["nbuilds"] == tb["nbuilds"] and ta["p_xi"] == tb["p_xi"]
     assert out[0][3][1]["step"] == 23
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_dilute_gas_list_parity(gpu_lib, precision):
+    """A dilute gas (about 2 spheres per bin, list built with a thread per
+    particle) gives the oracle's pair set and forces, at the first build and
+    after 600 steps with rebuilds."""
+    from mddem_gb300 import workloads as w
+
+    cfg, st = w.gas(4000, phi=0.08, seed=5, precision=precision, policy="reference")
+    cfg = cfg.replace(dt=1e-6)
+    ctx = _ctx(cfg, st)
+    o = _oracle(cfg.replace(precision="fp64"), st)
+    ctx.force_only()
+    o.force_only()
+    assert pair_set(ctx.pairs()) == pair_set(o.pairs())
+    ctx.step(600)
+    o.step(600)
+    assert ctx.thermo()["nbuilds"] >= 3
+    if precision == "fp64":
+        assert ctx.thermo()["nbuilds"] == o.thermo()["nbuilds"]
+        assert pair_set(ctx.pairs()) == pair_set(o.pairs())
+        gpos, = by_tag(ctx.download(), "pos")
+        rpos, = by_tag(o.state(), "pos")
+        assert np.max(np.abs(gpos - rpos)) <= 1e-12 * cfg.box[0]
