@@ -317,9 +317,14 @@ int setup_grid(const mdg_config& c, const double* cutr, size_t n, SysParams& p) 
     }
     if (ncell > (1LL << 30)) return MDG_ERR_CONFIG;
     p.ncell = (int)ncell;
-    // under about 6 particles per bin a warp per bin leaves most lanes idle:
-    // build the list with a thread per particle instead (same rows)
-    p.build_tpp = (double)n < 6.0 * (double)p.nc[0] * (double)p.nc[1] * (double)p.nc[2] ? 1 : 0;
+    // list build mode (all give the same rows): under about 6 particles per bin
+    // a thread per particle; a warp per bin when there are enough bins to fill
+    // the GPU (and no more bins than particles, as bins take particle slots);
+    // else a warp per particle
+    const double nbins = (double)p.nc[0] * (double)p.nc[1] * (double)p.nc[2];
+    if ((double)n < 6.0 * nbins) p.build_mode = 2;
+    else if (nbins >= 2048.0 && (size_t)p.ncell <= n) p.build_mode = 0;
+    else p.build_mode = 1;
     p.max_cutoff = max_cutoff;
     p.stencil_cut_sq = max_cutoff * max_cutoff;
     // stencil membership of every offset (compute_bin_grid's distance test,

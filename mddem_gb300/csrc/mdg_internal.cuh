@@ -68,7 +68,7 @@ struct SysParams {
     int ext[3];          // extended grid (interior + 2*layers)
     int sl[3];           // ghost layers per side
     int win[3];          // enumeration half-width in interior cells
-    int build_tpp;       // list build: thread per particle (few per bin) or warp per bin
+    int build_mode;      // list build: 0 warp per bin, 1 warp per particle, 2 thread per particle
     double lo[3], hi[3], L[3];
     double bin[3], inv_bin[3], origin[3];
     double max_cutoff, stencil_cut_sq;
@@ -496,6 +496,16 @@ __device__ __forceinline__ int rb_find(const int* off, int n, int v) {
         for (int v_ = blockIdx.x; v_ < tot_; v_ += gridDim.x) {       \
             const int k_ = rb_find(d.rb_poff, rbn_, v_);              \
             BODY(d, d.rb_sys[k_], v_ - d.rb_poff[k_]);                \
+        }                                                             \
+    }
+#define RB_FOR_PARTICLE_SUBS(BODY, SUB)                               \
+    {                                                                 \
+        const int rbn_ = *d.rb_n;                                     \
+        const int tot_ = d.rb_poff[rbn_] * (SUB);                     \
+        for (int v_ = blockIdx.x; v_ < tot_; v_ += gridDim.x) {       \
+            const int pv_ = v_ % d.rb_poff[rbn_];                     \
+            const int k_ = rb_find(d.rb_poff, rbn_, pv_);             \
+            BODY(d, d.rb_sys[k_], pv_ - d.rb_poff[k_], v_ / d.rb_poff[rbn_]); \
         }                                                             \
     }
 #define RB_FOR_CELL_BLOCKS(BODY, SUB)                                 \

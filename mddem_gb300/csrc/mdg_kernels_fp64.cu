@@ -568,19 +568,22 @@ __device__ __forceinline__ TileRule tile_rule(const SysParams& sp, int ex, int e
     return r;
 }
 
-// Neighbour list build, one warp per (ext) bin: the lanes are the bin's
-// particles (32 at a time); every neighbouring bin of the interior-cell window
-// (with its periodic image shift) is staged into shared memory 32 particles at
-// a time.  Each candidate is screened by a 10-instruction fp32 test on the hi
-// parts (conservative radius); survivors get the two-float separation, and
-// the reference's own fp64 cutoff test (fma form) only within 1e-5 of the
-// cutoff.  The reference's owner rule is applied twice: `own` (i holds the
-// pair in the reference's half list) and `oth` (the partner holds it); both go
-// into i's full row, so forces are summed per particle without atomics while
-// pair arithmetic stays in the owner's frame.  Owner decisions are per tile
-// (they depend only on the two bins) except for same-bin order and for
-// particles within 1e-9 of a bin edge, whose image bins are recomputed in
-// fp64.  Also saves last_build_pos (neighbor.rs:545-561).
+// Neighbour list build.  Each particle walks the interior-cell window of its
+// bin (with periodic image shifts) in the reference's stencil order; every
+// candidate is screened by an fp32 test on the hi parts (conservative
+// radius); survivors get the two-float separation, and the reference's own
+// fp64 cutoff test (fma form) only within 1e-5 of the cutoff.  The
+// reference's owner rule is applied twice: `own` (i holds the pair in the
+// reference's half list) and `oth` (the partner holds it); both go into i's
+// full row, so forces are summed per particle without atomics while pair
+// arithmetic stays in the owner's frame.  Owner decisions depend only on the
+// two bins (the tile rule) except for same-bin order and for particles within
+// 1e-9 of a bin edge, whose image bins are recomputed in fp64.  Three modes
+// give identical rows: a warp per bin (lanes over the bin's particles, for
+// systems with enough bins to fill the GPU), a warp per particle (lanes over
+// candidates, rows written in order by ballot, for small dense systems) and a
+// thread per particle (dilute systems).  Also saves last_build_pos
+// (neighbor.rs:545-561).
 constexpr int BUILD_WARPS = 4;
 
 // The survivors of the fp32 screen that lie near the cutoff, or that involve
@@ -644,16 +647,11 @@ __device__ __noinline__ int near_pair(const Dev& d, const SysParams& sp, long lo
 
 constexpr int BUILD_SUBS = BLK / BUILD_WARPS;  // blocks per 128-bin cell block
 
-// Thread per particle, for systems with few particles per bin (dilute
-// granular gases), where a warp per bin would leave most lanes idle: the same
-// window walk, candidates in the same order, the same screen, owner rule and
-// precise path as the warp-per-bin build, so both give identical rows.
-// Unit u covers particles [u BLK, u BLK + BLK) of system s.
-__device__ void build_particles(const Dev& d, int s, int u) {
+// Row of particle li of system s by one thread (dilute systems, and the
+// rare particles whose window has particles in ghost-layer bins).
+__device__ void build_one(const Dev& d, int s, int li) {
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
-    const int li = u * BLK + threadIdx.x;
-    if (li >= sp.n) return;  // no warp-synchronous code below
     const long long i = (long long)sp.p0 + li;
     d.lbp[i] = d.pos[i];
     const float4 hi = d.pos2[2 * i], lo = d.pos2[2 * i + 1];
@@ -752,6 +750,8 @@ __device__ void build_particles(const Dev& d, int s, int u) {
 
 // One warp per bin: bin `sub * BUILD_WARPS + warp` of cell block `lcb` of
 // system s.  Warp-synchronous only (no block barrier), so warps may leave early.
+// One warp per bin (large dense systems): bin `sub * BUILD_WARPS + warp` of
+// block `lcb` of system s; the lanes are the bin's particles, 32 at a time.  Warp-synchronous only (no block barrier), so warps may leave early.
 __device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
     __shared__ float4 tile_h[BUILD_WARPS][32], tile_l[BUILD_WARPS][32];
     __shared__ int tile_e[BUILD_WARPS][32];
@@ -759,10 +759,6 @@ __device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
     if (!do_rebuild(st)) return;
-    if (sp.build_tpp) {  // uniform over the block
-        build_particles(d, s, lcb * BUILD_SUBS + sub);
-        return;
-    }
     const int c = lcb * BLK + sub * BUILD_WARPS + warp;
     if (c >= sp.ncell) return;
     const int a0 = d.cstart[sp.c0 + c], a1 = d.cstart[sp.c0 + c + 1];
@@ -939,6 +935,205 @@ __device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
     }
 }
 
+// Row of particle li of system s by one warp: lane k describes window entry
+// e0 + k (its main bin's particle range, shift and tile rule); the entries'
+// candidates are laid end to end and screened 32 at a time, one per lane;
+// hits are written in candidate order at ballot offsets.  A window with
+// particles in a ghost-layer bin (rounding at the box face) falls back to
+// build_one on lane 0.
+__device__ void build_warp(const Dev& d, int s, int li) {
+    __shared__ int s_pre[BUILD_WARPS][33], s_m0[BUILD_WARPS][32], s_q[BUILD_WARPS][32], s_E[BUILD_WARPS][32];
+    const SysParams& sp = d.sp[s];
+    SysState* st = d.ss + s;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long i = (long long)sp.p0 + li;
+    const int cr = d.cell[i];
+    const bool edge_i = cr < 0;
+    const int c = cr & 0x7fffffff;
+    const int ez = c % sp.ext[2];
+    const int ey = (c / sp.ext[2]) % sp.ext[1];
+    const int ex = c / (sp.ext[2] * sp.ext[1]);
+    const int qx0 = min(max(ex - sp.sl[0], 0), sp.nc[0] - 1);
+    const int qy0 = min(max(ey - sp.sl[1], 0), sp.nc[1] - 1);
+    const int qz0 = min(max(ez - sp.sl[2], 0), sp.nc[2] - 1);
+    const int wy = 2 * sp.win[1] + 1, wz = 2 * sp.win[2] + 1;
+    const int nent = (2 * sp.win[0] + 1) * wy * wz;
+    // first pass: any particle in a ghost-layer bin next to a face cell?
+    bool ghost = false;
+    for (int e = lane; e < nent; e += 32) {
+        int qx = qx0 + e / (wy * wz) - sp.win[0];
+        int qy = qy0 + (e / wz) % wy - sp.win[1];
+        int qz = qz0 + e % wz - sp.win[2];
+        if (qx < 0) qx += sp.nc[0]; else if (qx >= sp.nc[0]) qx -= sp.nc[0];
+        if (qy < 0) qy += sp.nc[1]; else if (qy >= sp.nc[1]) qy -= sp.nc[1];
+        if (qz < 0) qz += sp.nc[2]; else if (qz >= sp.nc[2]) qz -= sp.nc[2];
+        if (qx < 0 || qx >= sp.nc[0] || qy < 0 || qy >= sp.nc[1] || qz < 0 || qz >= sp.nc[2]) continue;
+        const int axa = (qx == 0) ? -1 : 0, axb = (qx == sp.nc[0] - 1) ? 1 : 0;
+        const int aya = (qy == 0) ? -1 : 0, ayb = (qy == sp.nc[1] - 1) ? 1 : 0;
+        const int aza = (qz == 0) ? -1 : 0, azb = (qz == sp.nc[2] - 1) ? 1 : 0;
+        for (int ax = axa; ax <= axb; ax++)
+            for (int ay = aya; ay <= ayb; ay++)
+                for (int az = aza; az <= azb; az++) {
+                    if ((ax | ay | az) == 0) continue;
+                    const int Ex = qx + sp.sl[0] + ax, Ey = qy + sp.sl[1] + ay, Ez = qz + sp.sl[2] + az;
+                    const int flatE = (Ex * sp.ext[1] + Ey) * sp.ext[2] + Ez;
+                    if (d.cstart[sp.c0 + flatE] != d.cstart[sp.c0 + flatE + 1]) ghost = true;
+                }
+    }
+    if (__any_sync(0xffffffffu, ghost)) {
+        if (lane == 0) build_one(d, s, li);
+        return;
+    }
+    if (lane == 0) d.lbp[i] = d.pos[i];
+    const float4 hi = d.pos2[2 * i], lo = d.pos2[2 * i + 1];
+    const float brel = sp.band_rel;
+    const long long base = sp.lst0 + li;
+    int count = 0;  // uniform over the warp
+    for (int e0 = 0; e0 < nent; e0 += 32) {
+        int nseg = 0, eq = 0, eE = 0, em0 = 0;
+        {
+            const int e = e0 + lane;
+            if (e < nent) {
+                int qx = qx0 + e / (wy * wz) - sp.win[0], sx = 0;
+                int qy = qy0 + (e / wz) % wy - sp.win[1], sy = 0;
+                int qz = qz0 + e % wz - sp.win[2], sz = 0;
+                if (qx < 0) { qx += sp.nc[0]; sx = -1; } else if (qx >= sp.nc[0]) { qx -= sp.nc[0]; sx = 1; }
+                if (qy < 0) { qy += sp.nc[1]; sy = -1; } else if (qy >= sp.nc[1]) { qy -= sp.nc[1]; sy = 1; }
+                if (qz < 0) { qz += sp.nc[2]; sz = -1; } else if (qz >= sp.nc[2]) { qz -= sp.nc[2]; sz = 1; }
+                // fixed axes have no periodic image
+                const bool ok = !(sx && !sp.per[0]) && !(sy && !sp.per[1]) && !(sz && !sp.per[2]) && qx >= 0 &&
+                                qx < sp.nc[0] && qy >= 0 && qy < sp.nc[1] && qz >= 0 && qz < sp.nc[2];
+                if (ok) {
+                    const int Ex = qx + sp.sl[0], Ey = qy + sp.sl[1], Ez = qz + sp.sl[2];
+                    const int flatE = (Ex * sp.ext[1] + Ey) * sp.ext[2] + Ez;
+                    const TileRule tr = tile_rule(sp, ex, ey, ez, Ex, Ey, Ez, sx, sy, sz);
+                    const bool shifted = (sx | sy | sz) != 0;
+                    // nothing in this bin pair can enter the list unless a
+                    // bin-edge particle needs its image bin recomputed
+                    if (tr.own || tr.oth || tr.same || shifted) {
+                        em0 = d.cstart[sp.c0 + flatE];
+                        nseg = d.cstart[sp.c0 + flatE + 1] - em0;
+                    }
+                    eE = flatE;
+                    eq = ((sx + 1) << 1) | ((sy + 1) << 3) | ((sz + 1) << 5) | (tr.own ? 1 << 13 : 0) |
+                         (tr.oth ? 1 << 14 : 0) | (tr.same ? 1 << 15 : 0);
+                }
+            }
+        }
+        // entries' candidates laid end to end: exclusive offsets
+        int incl = nseg;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        __syncwarp();
+        s_pre[warp][lane] = incl - nseg;
+        s_m0[warp][lane] = em0;
+        s_q[warp][lane] = eq;
+        s_E[warp][lane] = eE;
+        if (lane == 0) s_pre[warp][32] = total;
+        __syncwarp();
+        for (int p0 = 0; p0 < total; p0 += 32) {
+            const int p = p0 + lane;
+            int bits = 0, sc = 0;
+            long long j = 0;
+            if (p < total) {
+                // the entry holding candidate p: last k with s_pre[k] <= p
+                // (entries without candidates share the next one's offset)
+                int k = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (k + step < 32 && s_pre[warp][k + step] <= p) k += step;
+                const int q = s_q[warp][k];
+                j = s_m0[warp][k] + (p - s_pre[warp][k]);
+                const int sx = ((q >> 1) & 3) - 1, sy = ((q >> 3) & 3) - 1, sz = ((q >> 5) & 3) - 1;
+                const bool shifted = (sx | sy | sz) != 0;
+                sc = (sx + 1) * 9 + (sy + 1) * 3 + (sz + 1);
+                if (shifted || j != i) {
+                    const float4 hj = d.pos2[2 * j];
+                    const float px = hj.x - (hi.x - (float)sx * sp.Lh[0]);
+                    const float py = hj.y - (hi.y - (float)sy * sp.Lh[1]);
+                    const float pz = hj.z - (hi.z - (float)sz * sp.Lh[2]);
+                    const float r2h = px * px + py * py + pz * pz;
+                    float c2h;
+                    if (sp.uniform) {
+                        c2h = sp.ucut2f;
+                    } else {
+                        const float ssum = hi.w + hj.w;
+                        c2h = ssum * ssum * sp.sf2f;
+                    }
+                    if (r2h <= c2h * (1.f + brel)) {
+                        const TileRule tr{((q >> 13) & 1) != 0, ((q >> 14) & 1) != 0, ((q >> 15) & 1) != 0};
+                        const bool near = r2h > c2h * (1.f - brel);
+                        const bool edge = shifted && (edge_i || d.cell[j] < 0);
+                        if (!near && !edge) {
+                            bits = ((tr.own || (tr.same && (sp.newton ? j > i : true))) ? 1 : 0) |
+                                   ((tr.oth || (tr.same && sp.newton && i > j)) ? 2 : 0);
+                        } else {
+                            const int fE = s_E[warp][k];
+                            const int Ez = fE % sp.ext[2], Ey = (fE / sp.ext[2]) % sp.ext[1],
+                                      Ex = fE / (sp.ext[2] * sp.ext[1]);
+                            bits = near_pair(d, sp, i, j, hi, lo, hj, d.pos2[2 * j + 1], sx, sy, sz, edge, ex, ey, ez,
+                                             Ex, Ey, Ez, tr);
+                        }
+                    }
+                }
+            }
+            // row entries in candidate order: owner entry first, then partner entry
+            const int nb = __popc(bits);
+            int off = nb;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, off, o);
+                if (lane >= o) off += y;
+            }
+            const int tot = __shfl_sync(0xffffffffu, off, 31);
+            int slot = count + off - nb;
+            const uint32_t jl = (uint32_t)(j - sp.p0);
+            if (bits & 1) {
+                if (slot < sp.ncap) d.nlist[base + (long long)slot * sp.npad] = jl | ((uint32_t)(sc + 27) << IDX_BITS);
+                slot++;
+            }
+            if (bits & 2) {
+                if (slot < sp.ncap) d.nlist[base + (long long)slot * sp.npad] = jl | ((uint32_t)sc << IDX_BITS);
+            }
+            count += tot;
+        }
+        __syncwarp();
+    }
+    if (lane == 0) {
+        if (count > sp.ncap) {
+            atomicOr(&st->status, ST_NBR_OVF);
+            atomicMax(&st->max_nbr, count);
+            count = sp.ncap;
+        } else {
+            atomicMax(&st->max_nbr, count);
+        }
+        d.nnum[i] = count;
+    }
+}
+
+// Work unit (particle block pb, sub-unit sub) of system s, by the system's
+// build mode: 2 (dilute) the block's particles with a thread each (sub-unit
+// 0); 0 (many dense bins) a bin per warp, bins numbered like particle slots;
+// 1 (few dense bins) a particle per warp, BUILD_WARPS per sub-unit.
+__device__ void build_unit(const Dev& d, int s, int pb, int sub) {
+    const SysParams& sp = d.sp[s];
+    if (!do_rebuild(d.ss + s)) return;  // uniform over the block
+    if (sp.build_mode == 2) {
+        if (sub != 0) return;
+        const int li = pb * BLK + (int)threadIdx.x;
+        if (li < sp.n) build_one(d, s, li);
+        return;
+    }
+    if (sp.build_mode == 0) {
+        build_cells(d, s, pb, sub);  // the system has no more bins than particle slots
+        return;
+    }
+    const int li = pb * BLK + sub * BUILD_WARPS + (int)(threadIdx.x >> 5);
+    if (li < sp.n) build_warp(d, s, li);  // uniform over the warp
+}
+
 // Minimum resident blocks per SM asked of ptxas for k_build: 5 caps it at
 // 96 registers (from 125) with ~100 B of spills and runs 22 % faster on GB300
 // (LJ 256k) than no cap; a compile-time tuning knob.
@@ -946,7 +1141,7 @@ __device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
 #define MDG_BUILD_MINB 5
 #endif
 __global__ void __launch_bounds__(BUILD_WARPS * 32, MDG_BUILD_MINB) k_build(Dev d)
-    RB_FOR_CELL_BLOCKS(build_cells, BUILD_SUBS)
+    RB_FOR_PARTICLE_SUBS(build_unit, BUILD_SUBS)
 
 // ----------------------------------------------------------------------------
 // LJ 12-6 force (lj_force, md_lj/src/lib.rs:488-633) over the full list.
@@ -1574,7 +1769,7 @@ int launch_initial(const Dev& d, cudaStream_t st) {
 int launch_rebuild(const Dev& d, cudaStream_t st) {
     constexpr int CAP = 152 * 16;
     const int gp = d.nrun < CAP ? d.nrun : CAP;
-    const int gb = d.ncrun * BUILD_SUBS < 2 * CAP ? d.ncrun * BUILD_SUBS : 2 * CAP;
+    const int gb = d.nrun * BUILD_SUBS < 2 * CAP ? d.nrun * BUILD_SUBS : 2 * CAP;
     const int gs = d.nrun_sys < 304 ? d.nrun_sys : 304;
     const int gc = d.ncrun < CAP ? d.ncrun : CAP;
     const int gs_ = d.ncrun * CS_SUBS < 2 * CAP ? d.ncrun * CS_SUBS : 2 * CAP;
