@@ -382,7 +382,9 @@ __device__ __forceinline__ void cellsort_cells(const Dev& d, int s, int lcb, int
     }
     if (lane == 0) {
         d.cnt[sp.c0 + c] = 0;
-        if (!ident) atomicOr(&st->nonid, 1);
+        // one flag per system: read before the atomic, so that a first sort
+        // (every cell permuted) does not queue an atomic per cell on one word
+        if (!ident && !vload(&st->nonid)) atomicOr(&st->nonid, 1);
     }
 }
 __global__ void __launch_bounds__(BLK) k_cellsort(Dev d) RB_FOR_CELL_BLOCKS(cellsort_cells, CS_SUBS)
@@ -742,7 +744,7 @@ __device__ void build_one(const Dev& d, int s, int li) {
         atomicOr(&st->status, ST_NBR_OVF);
         atomicMax(&st->max_nbr, count);
         count = sp.ncap;
-    } else {
+    } else if (count > vload(&st->max_nbr)) {  // skip the atomic on one word when it cannot raise it
         atomicMax(&st->max_nbr, count);
     }
     d.nnum[i] = count;
@@ -927,7 +929,7 @@ __device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
                 atomicOr(&st->status, ST_NBR_OVF);
                 atomicMax(&st->max_nbr, count);
                 count = sp.ncap;
-            } else {
+            } else if (count > vload(&st->max_nbr)) {  // skip the atomic on one word when it cannot raise it
                 atomicMax(&st->max_nbr, count);
             }
             d.nnum[i] = count;
@@ -1106,7 +1108,7 @@ __device__ void build_warp(const Dev& d, int s, int li) {
             atomicOr(&st->status, ST_NBR_OVF);
             atomicMax(&st->max_nbr, count);
             count = sp.ncap;
-        } else {
+        } else if (count > vload(&st->max_nbr)) {  // skip the atomic on one word when it cannot raise it
             atomicMax(&st->max_nbr, count);
         }
         d.nnum[i] = count;
