@@ -421,19 +421,21 @@ def plain_job_by_job(trace, made):
 
 # Compulsory DRAM bytes per particle of the per-particle kernels (each array
 # touched once per launch; neighbours' rows assumed L2-resident), by kind and
-# precision.  k_initial: v, f, x (+ two-float x, build-time x for the mixed
-# rebuild test; fp64: build-time x) (+ DEM: omega, torque, quaternion) read,
-# v, x (+ two-float x) (+ omega, quaternion) written.  k_final: f, v, m, x
-# (+ omega, torque) read, v (+ omega) written.
-INIT_BYTES = {("dem", "mixed"): 416, ("dem", "fp64"): 352, ("lj", "mixed"): 256, ("lj", "fp64"): 192}
+# precision.  k_initial: v, f, x (+ mixed geometry copy and its build-time
+# value for the rebuild test: DEM two-float 2 x 32, LJ fixed-point 2 x 16;
+# fp64: build-time x) (+ DEM: omega, torque, quaternion) read, v, x (+ the
+# geometry copy) (+ omega, quaternion) written.  k_final: f, v, m, x (+ omega,
+# torque) read, v (+ omega) written.
+INIT_BYTES = {("dem", "mixed"): 416, ("dem", "fp64"): 352, ("lj", "mixed"): 192, ("lj", "fp64"): 192}
 FINAL_BYTES = {"dem": 232, "lj": 136}
 
 
-def force_bytes(kind, nfull, contacts):
-    """k_lj_* / k_dem_*: row length 4 + entries 4 each + own geometry 32 +
-    force 32 written; DEM adds v and omega 64, torque 32, and per contact the
-    partner tag and 7 spring values read and written (2 x 60)."""
-    b = 4 + 4 * nfull + 32 + 32
+def force_bytes(kind, nfull, contacts, prec="fp64"):
+    """k_lj_* / k_dem_*: row length 4 + entries 4 each + own geometry (32; the
+    mixed LJ kernel's fixed-point position 16) + force 32 written; DEM adds v
+    and omega 64, torque 32, and per contact the partner tag and 7 spring
+    values read and written (2 x 60)."""
+    b = 4 + 4 * nfull + (16 if (kind, prec) == ("lj", "mixed") else 32) + 32
     if kind == "dem":
         b += 64 + 32 + 4 + 120 * contacts
     return b
@@ -474,7 +476,7 @@ def serve_roofline(a, trace, made, mix):
     }
     for k, p in per.items():
         name = ("k_dem_" if k == "dem" else "k_lj_") + prec
-        cands[name] = (p["force"], p["n"] * force_bytes(k, p["nfull"], p["contacts"]))
+        cands[name] = (p["force"], p["n"] * force_bytes(k, p["nfull"], p["contacts"], prec))
     name = max(cands, key=lambda q: cands[q][0])
     ms, nbytes = cands[name]
     peak, src = peak_hbm()
@@ -655,7 +657,7 @@ def bench_ensemble(a, world, rank, local, dist):
         contacts = sum(len(ctx.history(q)[0]) for q in range(len(sts))) / n
         nfull = sum(2.0 * len(ctx.pairs(q)) for q in range(len(sts))) / n
         cands = {"k_initial": (float(t[:, 1].mean()), n * INIT_BYTES[("dem", a.precision)]),
-                 "k_dem_" + a.precision: (float(t[:, 3].mean()), n * force_bytes("dem", nfull, contacts)),
+                 "k_dem_" + a.precision: (float(t[:, 3].mean()), n * force_bytes("dem", nfull, contacts, a.precision)),
                  "k_final": (float(t[:, 4].mean()), n * FINAL_BYTES["dem"])}
         name = max(cands, key=lambda q: cands[q][0])
         kms, nbytes = cands[name]
@@ -794,7 +796,7 @@ def main():
     suffix = "mixed" if a.precision == "mixed" else "fp64"
     # the dominant per-particle kernel of the step: force, initial or final
     # integration (phases timed by CUDA events; rebuild steps averaged in)
-    cands = {("k_dem_" if kind == "dem" else "k_lj_") + suffix: (force_ms, force_bytes(kind, nfull_avg, contacts)),
+    cands = {("k_dem_" if kind == "dem" else "k_lj_") + suffix: (force_ms, force_bytes(kind, nfull_avg, contacts, a.precision)),
              ("k_initial_mixed" if a.precision == "mixed" else "k_initial"):
                  (float(t[:, 1].mean()), INIT_BYTES[(kind, a.precision)]),
              ("k_final_mixed" if a.precision == "mixed" else "k_final"):
