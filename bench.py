@@ -314,6 +314,20 @@ SERVE_HBM_BUDGET = 12 << 30  # admission budget of resident jobs' device bytes
 PLAIN_SAMPLE_STEPS = 200
 
 
+def reduce_over_ranks(dist, ms, work):
+    """Job-wide figures of a replicas-only run: the slowest rank's time and the
+    work of all ranks (a max and a sum over the ranks; no other exchange)."""
+    if dist is None:
+        return float(ms), float(work)
+    import torch
+
+    t = torch.tensor([ms], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    w = torch.tensor([work], dtype=torch.float64)
+    dist.all_reduce(w, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(w.item())
+
+
 def serve_trace(a):
     from mddem_gb300 import workloads as w
 
@@ -550,14 +564,7 @@ def bench_serve(a, world, rank, local, dist):
         win, infos, run = replay(a, srv, trace, made, clk)
     ps = win["s1"]["particle_steps"] - win["s0"]["particle_steps"]
     ms = win["ms"]
-    if dist:
-        import torch
-
-        tt = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        tp = torch.tensor([ps], dtype=torch.float64)
-        dist.all_reduce(tp, op=dist.ReduceOp.SUM)
-        ms, ps = float(tt.item()), float(tp.item())
+    ms, ps = reduce_over_ranks(dist, ms, ps)
     lat = np.array([infos[k]["end_s"] - infos[k]["submit_s"] for k in sorted(infos)])
     failed = [k for k in infos if infos[k]["status"] != 0]
     total_ps = float(sum(j.n * j.steps for j in trace))
@@ -633,12 +640,9 @@ def bench_ensemble(a, world, rank, local, dist):
         c1 = clk.mark()
     ms = e0.elapsed_time(e1)
     l1 = ctx.launches()
-    if dist:
-        tt = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    ms, work = reduce_over_ranks(dist, ms, float(n * a.steps))
     line = {
-        "metric": "particle-steps/s", "value": world * n * a.steps / (ms / 1e3), "unit": "particle-steps/s",
+        "metric": "particle-steps/s", "value": work / (ms / 1e3), "unit": "particle-steps/s",
         "n_gpus": world, "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if a.precision == "mixed" else "f64", "data": "synthetic",
@@ -778,14 +782,8 @@ def main():
         dist.barrier()
     with ClockSampler(local) as clk:
         t, kernels, rebuilt = ctx.timed_steps(a.steps, L2_FLUSH)
-    total_ms = float(t[:, 0].sum())
-    if dist:
-        import torch
-
-        tt = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
-    value = world * n * a.steps / (total_ms / 1e3)
+    total_ms, work = reduce_over_ranks(dist, float(t[:, 0].sum()), float(n * a.steps))
+    value = work / (total_ms / 1e3)
     th = ctx.thermo()
     nfull = th["max_neighbors"]
     pairs = len(ctx.pairs())
