@@ -254,6 +254,10 @@ void apply_physics(mdg_ctx* c, int s, const mdg_config& k, std::vector<double>& 
         c->cfg[s].materials = c->mats[s].data();
         material_tables(k.materials, k.n_materials, tabs);
         p.nmat = k.n_materials;
+        // no JKR pull-off range: a pair interacts only when the spheres touch
+        bool pull = false;
+        for (int m = 0; m < k.n_materials; m++) pull = pull || k.materials[m].surface_energy > 0.0;
+        p.touch_only = (k.contact_model == 1 || k.adhesion_model == 1 || !pull) ? 1 : 0;
     } else {
         // LJPairCoeffs::from_params (crates/md_lj/src/lib.rs:230-239)
         const double s2 = k.lj_sigma * k.lj_sigma;

@@ -52,6 +52,7 @@ struct SysParams {
     int kind;            // 0 DEM, 1 LJ
     int precision;       // 0 fp64, 1 mixed
     int contact_model, adhesion_model, rolling_model, twisting_model;
+    int touch_only;      // DEM without a JKR pull-off range (no pair acts beyond r_i + r_j)
     int p0, n, npad;     // particle segment
     int b0, nb;          // first particle block; blocks holding the n particles
     int ncb;             // cell blocks of the system's cell segment

@@ -434,17 +434,30 @@ __global__ void __launch_bounds__(BLK, MDG_DEM_MINB) k_dem_mixed(Dev d) {
         const int sc = (int)(own ? code - 27u : code);
         const int sx = sc / 9 - 1, sy = (sc / 3) % 3 - 1, sz = sc % 3 - 1;
         const float4 hj = d.pos2[2 * j], lj4 = d.pos2[2 * j + 1];
+        float dh[3], dl[3];
+        if (own) {
+            sep_df(hj.x, lj4.x, hi.x, lo.x, sx, sp.Lh[0], sp.Ll[0], dh[0], dl[0]);
+            sep_df(hj.y, lj4.y, hi.y, lo.y, sy, sp.Lh[1], sp.Ll[1], dh[1], dl[1]);
+            sep_df(hj.z, lj4.z, hi.z, lo.z, sz, sp.Lh[2], sp.Ll[2], dh[2], dl[2]);
+        } else {
+            // owner frame: owner j, partner i's image -s
+            sep_df(hi.x, lo.x, hj.x, lj4.x, -sx, sp.Lh[0], sp.Ll[0], dh[0], dl[0]);
+            sep_df(hi.y, lo.y, hj.y, lj4.y, -sy, sp.Lh[1], sp.Ll[1], dh[1], dl[1]);
+            sep_df(hi.z, lo.z, hj.z, lj4.z, -sz, sp.Lh[2], sp.Ll[2], dh[2], dl[2]);
+        }
+        if (sp.touch_only) {
+            // spheres clearly apart (2e-5 margin over the hi parts' ~1e-7
+            // error): the pair has no force, skip its state and history loads
+            const float rs = hi.w + hj.w;
+            if (dh[0] * dh[0] + dh[1] * dh[1] + dh[2] * dh[2] > rs * rs * 1.00002f) continue;
+        }
         const double4 vj = d.vel[j];
         const double4 wj = d.omg[j];
         const int tj_ = (int)d.type[j];
         const uint32_t tag_j = d.tag[j];
         double stored[7] = {0, 0, 0, 0, 0, 0, 0};
-        float dh[3], dl[3];
         if (own) {
             hist_find_m(d, sp, hcur, i, li, tag_j, stored);
-            sep_df(hj.x, lj4.x, hi.x, lo.x, sx, sp.Lh[0], sp.Ll[0], dh[0], dl[0]);
-            sep_df(hj.y, lj4.y, hi.y, lo.y, sy, sp.Lh[1], sp.Ll[1], dh[1], dl[1]);
-            sep_df(hj.z, lj4.z, hi.z, lo.z, sz, sp.Lh[2], sp.Ll[2], dh[2], dl[2]);
             hm_pair_mixed(d, sp, dh, dl, hi.w, lo.w, hj.w, lj4.w, vi, vj, wi, wj, ti_, tj_, tag_i, tag_j, stored, o);
             if (!o.hit) continue;
             F.add(-o.fn[0], -o.fn[1], -o.fn[2]);
@@ -459,11 +472,7 @@ __global__ void __launch_bounds__(BLK, MDG_DEM_MINB) k_dem_mixed(Dev d) {
             }
             nh++;
         } else {
-            // owner frame: owner j, partner i's image -s
             hist_find_m(d, sp, hcur, j, lj, tag_i, stored);
-            sep_df(hi.x, lo.x, hj.x, lj4.x, -sx, sp.Lh[0], sp.Ll[0], dh[0], dl[0]);
-            sep_df(hi.y, lo.y, hj.y, lj4.y, -sy, sp.Lh[1], sp.Ll[1], dh[1], dl[1]);
-            sep_df(hi.z, lo.z, hj.z, lj4.z, -sz, sp.Lh[2], sp.Ll[2], dh[2], dl[2]);
             hm_pair_mixed(d, sp, dh, dl, hj.w, lj4.w, hi.w, lo.w, vj, vi, wj, wi, tj_, ti_, tag_j, tag_i, stored, o);
             if (!o.hit) continue;
             F.add(o.fn[0], o.fn[1], o.fn[2]);
