@@ -362,12 +362,15 @@ class Server:
 
     def context(self):
         """The server's batch context as a non-owning Context (diagnostics:
-        timed steps, thermo, pairs of a resident slot)."""
+        timed steps, thermo, pairs or the state of a resident slot; particle
+        counts are those of the jobs resident at this call)."""
         ctx = C.c_void_p()
         _check(self.lib.mdg_server_context(self.h, C.byref(ctx)), "mdg_server_context")
         c = Context.__new__(Context)
         c.lib, c.h, c.nsys, c.owner = self.lib, ctx, self.nslots, False
         c.configs, c._keep, c.n = list(self.slot_configs), [], [0] * self.nslots
+        for r in self.resident():
+            c.n[r["slot"]] = int(r["n"])
         return c
 
     def launches(self):
