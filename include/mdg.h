@@ -100,9 +100,10 @@ typedef struct mdg_material {
 /* Plane wall ([[wall]] type = "plane", crates/dem_wall/src/lib.rs:171-347):
  * the plane through `point` with outward `normal` (normalised on use); active
  * for particles inside [bound_lo, bound_hi] (use +-HUGE_VAL for unbounded);
- * `velocity` a constant wall velocity; `material` an index into the config's
- * materials.  Sphere-wall Hertz normal force with damping and adhesion and a
- * twisting torque (wall_contact_force, lib.rs:848-990). */
+ * `velocity` a constant wall velocity (the plane moves by velocity * dt before
+ * every step's force, wall_move, lib.rs:766-790); `material` an index into the
+ * config's materials.  Sphere-wall Hertz normal force with damping and
+ * adhesion and a twisting torque (wall_contact_force, lib.rs:848-990). */
 typedef struct mdg_wall {
     double point[3], normal[3];
     double bound_lo[3], bound_hi[3];
@@ -143,7 +144,8 @@ typedef struct mdg_config {
     double lv_temperature, lv_damping;
     uint64_t lv_seed;
     /* [domain] boundary_x/y/z = "fixed": no periodic images along that axis
-     * (0 = periodic, the default); particles must stay inside the box there. */
+     * (0 = periodic, the default); a particle found outside the box there at a
+     * rebuild makes the step return MDG_ERR_LOST (the reference removes it). */
     int fixed[3];
     /* [[wall]] plane walls (DEM), at most MDG_MAX_WALLS */
     int n_walls;
