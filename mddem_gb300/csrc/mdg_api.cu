@@ -107,7 +107,7 @@ int validate_config(const mdg_config& c) {
         const double mag = sqrt(q.normal[0] * q.normal[0] + q.normal[1] * q.normal[1] + q.normal[2] * q.normal[2]);
         if (!(mag > 1e-15) || q.material < 0 || q.material >= c.n_materials) return MDG_ERR_CONFIG;
     }
-    if (c.precision == MDG_MIXED && c.virial) return MDG_ERR_CONFIG;
+    if (c.precision == MDG_MIXED && c.virial && c.kind == MDG_KIND_DEM) return MDG_ERR_CONFIG;
     const int t = c.threads_per_particle;
     if (!(t == 0 || t == 1 || t == 2 || t == 4 || t == 8)) return MDG_ERR_CONFIG;
     if (c.neighbor_capacity < 0 || c.history_capacity < 0) return MDG_ERR_CONFIG;
@@ -919,7 +919,7 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     d.ss = c->alloc<SysState>(nsys, err);
     c->d_mat = c->alloc<double>(std::max<size_t>(mat_all.size(), 1), err);
     c->d_matf = c->alloc<float>(std::max<size_t>(mat_all.size(), 1), err);
-    c->d_thermo = c->alloc<double>((size_t)nsys * 16, err);
+    c->d_thermo = c->alloc<double>((size_t)nsys * THERMO_W, err);
     d.grid_ctr = c->alloc<unsigned int>(1, err);
     d.stat_ctr = c->alloc<unsigned long long>(4, err);
     c->d_loop = c->alloc<long long>(2, err);
@@ -1468,9 +1468,9 @@ int mdg_thermo(mdg_ctx* c, int sys, mdg_thermo_t* out) {
     c->launches += launch_thermo(c->d, c->d_thermo, c->stream);
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_err(e);
-    double t[16];
+    double t[THERMO_W];
     SysState ss;
-    cudaMemcpy(t, c->d_thermo + (size_t)sys * 16, sizeof(t), cudaMemcpyDeviceToHost);
+    cudaMemcpy(t, c->d_thermo + (size_t)sys * THERMO_W, sizeof(t), cudaMemcpyDeviceToHost);
     cudaMemcpy(&ss, c->d.ss + sys, sizeof(SysState), cudaMemcpyDeviceToHost);
     const SysParams& p = c->sp[sys];
     const double ndof = 3.0 * (double)p.n - 3.0;
@@ -1480,7 +1480,8 @@ int mdg_thermo(mdg_ctx* c, int sys, mdg_thermo_t* out) {
     out->p_xi = ss.p_xi_post;
     out->granular_temp = t[4];
     out->momentum = t[5];
-    for (int k = 0; k < 6; k++) out->virial[k] = ss.vir[k];
+    // mixed systems: the virial of the last force evaluation, summed here
+    for (int k = 0; k < 6; k++) out->virial[k] = (p.precision == MDG_MIXED && p.virial) ? t[16 + k] : ss.vir[k];
     out->step = ss.step;
     out->nbuilds = ss.nbuilds;
     out->n = p.n;

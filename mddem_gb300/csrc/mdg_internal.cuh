@@ -24,6 +24,7 @@ constexpr int BLK = 128;               // particles per block (segment padding u
 constexpr int IDX_BITS = 26;
 constexpr uint32_t IDX_MASK = (1u << IDX_BITS) - 1u;
 constexpr int NTAB = 14;               // material pair tables
+constexpr int THERMO_W = 24;           // doubles per system in the thermo record
 
 // device status bits (sticky per system)
 enum : int {

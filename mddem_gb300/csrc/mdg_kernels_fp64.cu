@@ -1690,7 +1690,7 @@ __global__ void __launch_bounds__(BLK) k_thermo1(Dev d, double* out16) {
     }
     double out[7];
     if (system_reduce<7>(d, s, gb, vals, out) && threadIdx.x == 0) {
-        double* o = out16 + (size_t)s * 16;
+        double* o = out16 + (size_t)s * THERMO_W;
         o[0] = 0.5 * out[4];
         o[1] = out[5];
         o[5] = sqrt(out[1] * out[1] + out[2] * out[2] + out[3] * out[3]);
@@ -1702,24 +1702,38 @@ __global__ void __launch_bounds__(BLK) k_thermo1(Dev d, double* out16) {
     }
 }
 
-// thermo pass 2: sum m |v - vbar|^2 -> granular temperature
+// thermo pass 2: sum m |v - vbar|^2 -> granular temperature; for mixed
+// systems with a virial, also the sum of the per-particle virials the force
+// kernel wrote (the plain path reduces them every step in k_final)
 __global__ void __launch_bounds__(BLK) k_thermo2(Dev d, double* out16) {
     const int gb = blockIdx.x;
     const int s = d.blk_sys[gb];
     const SysParams& sp = d.sp[s];
     if (gb - sp.b0 >= sp.nb) return;  // past the particles: not in the reduction
     const int li = (gb - sp.b0) * BLK + threadIdx.x;
-    const double* o = out16 + (size_t)s * 16;
-    double vals[1] = {0.0};
+    double* o = out16 + (size_t)s * THERMO_W;
+    const bool vir = sp.precision == 1 && sp.virial;
+    double vals[7] = {0, 0, 0, 0, 0, 0, 0};
     if (li < sp.n) {
         const long long i = (long long)sp.p0 + li;
         const double4 v = d.vel[i];
         const double m = d.mass[i];
         const double dx = v.x - o[9], dy = v.y - o[10], dz = v.z - o[11];
         vals[0] = m * (dx * dx) + m * (dy * dy) + m * (dz * dz);
+        if (vir)
+            for (int q = 0; q < 6; q++) vals[1 + q] = d.vir[q * d.P + i];
     }
-    double out[1];
-    if (system_reduce<1>(d, s, gb, vals, out) && threadIdx.x == 0) out16[(size_t)s * 16 + 4] = out[0] / (3.0 * o[8]);
+    double out[7];
+    if (vir) {
+        if (system_reduce<7>(d, s, gb, vals, out) && threadIdx.x == 0) {
+            o[4] = out[0] / (3.0 * o[8]);
+            for (int q = 0; q < 6; q++) o[16 + q] = out[1 + q];
+        }
+    } else {
+        const double v1[1] = {vals[0]};
+        double o1[1];
+        if (system_reduce<1>(d, s, gb, v1, o1) && threadIdx.x == 0) o[4] = o1[0] / (3.0 * o[8]);
+    }
 }
 
 // LJ potential energy per particle (owner entries of the full row; the sum

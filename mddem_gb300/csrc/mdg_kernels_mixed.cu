@@ -35,7 +35,11 @@ struct Kahan {
 #ifndef MDG_LJ_MINB
 #define MDG_LJ_MINB 8
 #endif
-template <int TPP>
+// VIR: systems with `virial` also write their per-particle virial (the
+// owner-entry sum of d_a f_b, VirialStress::add_pair, virial.rs:61-68; fp32
+// per lane, summed in fp64 at the thermo query); a separate instantiation so
+// the common path keeps its registers.
+template <int TPP, bool VIR>
 __global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
     const int pb = d.blk_run[blockIdx.x / TPP];
     const int sub = blockIdx.x % TPP;
@@ -47,6 +51,8 @@ __global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
     const bool act = li < sp.n;
     const long long i = (long long)sp.p0 + li;
     Kahan kx, ky, kz;
+    const bool vir = VIR && sp.virial;
+    float w0 = 0.f, w1 = 0.f, w2 = 0.f, w3 = 0.f, w4 = 0.f, w5 = 0.f;
     if (act) {
         const uint4 ui = d.posu[i];
         const int nn = d.nnum[i];
@@ -86,6 +92,15 @@ __global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
                 kx.add(-fpair * dx);
                 ky.add(-fpair * dy);
                 kz.add(-fpair * dz);
+                if (VIR && vir && (e[u] >> IDX_BITS) >= 27u) {  // owner entry: the reference's half-list pair
+                    const float px = -fpair * dx, py = -fpair * dy, pz = -fpair * dz;
+                    w0 += dx * px;
+                    w1 += dy * py;
+                    w2 += dz * pz;
+                    w3 += dx * py;
+                    w4 += dx * pz;
+                    w5 += dy * pz;
+                }
             }
         }
     }
@@ -104,7 +119,29 @@ __global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
             kz.c += cz_;
         }
     }
-    if (act && lane == 0) d.frc[i] = make_double4(kx.value(), ky.value(), kz.value(), 0.0);
+    if (VIR && vir && TPP > 1) {
+#pragma unroll
+        for (int o = TPP / 2; o > 0; o >>= 1) {
+            w0 += __shfl_down_sync(0xffffffffu, w0, o, TPP);
+            w1 += __shfl_down_sync(0xffffffffu, w1, o, TPP);
+            w2 += __shfl_down_sync(0xffffffffu, w2, o, TPP);
+            w3 += __shfl_down_sync(0xffffffffu, w3, o, TPP);
+            w4 += __shfl_down_sync(0xffffffffu, w4, o, TPP);
+            w5 += __shfl_down_sync(0xffffffffu, w5, o, TPP);
+        }
+    }
+    if (act && lane == 0) {
+        d.frc[i] = make_double4(kx.value(), ky.value(), kz.value(), 0.0);
+        if (VIR && vir) {
+            const double half = sp.newton ? 1.0 : 0.5;
+            d.vir[0 * d.P + i] = (double)w0 * half;
+            d.vir[1 * d.P + i] = (double)w1 * half;
+            d.vir[2 * d.P + i] = (double)w2 * half;
+            d.vir[3 * d.P + i] = (double)w3 * half;
+            d.vir[4 * d.P + i] = (double)w4 * half;
+            d.vir[5 * d.P + i] = (double)w5 * half;
+        }
+    }
 }
 
 // ----------------------------------------------------------------------------
@@ -871,11 +908,20 @@ int launch_force_mixed(const Dev& d, int has_lj, int has_dem, int tpp, cudaStrea
         n++;
     }
     if (has_lj) {
-        switch (tpp) {
-            case 2: k_lj_mixed<2><<<d.nrun * 2, BLK, 0, st>>>(d); break;
-            case 4: k_lj_mixed<4><<<d.nrun * 4, BLK, 0, st>>>(d); break;
-            case 8: k_lj_mixed<8><<<d.nrun * 8, BLK, 0, st>>>(d); break;
-            default: k_lj_mixed<1><<<d.nrun, BLK, 0, st>>>(d); break;
+        if (d.vir) {  // some system asks for its virial
+            switch (tpp) {
+                case 2: k_lj_mixed<2, true><<<d.nrun * 2, BLK, 0, st>>>(d); break;
+                case 4: k_lj_mixed<4, true><<<d.nrun * 4, BLK, 0, st>>>(d); break;
+                case 8: k_lj_mixed<8, true><<<d.nrun * 8, BLK, 0, st>>>(d); break;
+                default: k_lj_mixed<1, true><<<d.nrun, BLK, 0, st>>>(d); break;
+            }
+        } else {
+            switch (tpp) {
+                case 2: k_lj_mixed<2, false><<<d.nrun * 2, BLK, 0, st>>>(d); break;
+                case 4: k_lj_mixed<4, false><<<d.nrun * 4, BLK, 0, st>>>(d); break;
+                case 8: k_lj_mixed<8, false><<<d.nrun * 8, BLK, 0, st>>>(d); break;
+                default: k_lj_mixed<1, false><<<d.nrun, BLK, 0, st>>>(d); break;
+            }
         }
         n++;
     }

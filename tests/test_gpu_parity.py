@@ -345,3 +345,35 @@ def test_dilute_gas_list_parity(gpu_lib, precision):
         gpos, = by_tag(ctx.download(), "pos")
         rpos, = by_tag(o.state(), "pos")
         assert np.max(np.abs(gpos - rpos)) <= 1e-12 * cfg.box[0]
+
+
+@pytest.mark.parametrize("newton", [True, False])
+def test_mixed_lj_virial(gpu_lib, newton):
+    """Precision form with a virial: the mixed LJ kernel's per-particle
+    virials (fp32 per lane, summed in fp64) give the plain path's virial and
+    pressure to 2e-6 of the virial's largest component on an off-lattice
+    melt; after 30 steps (trajectories differ by the force error) to 1e-4."""
+    from mddem_gb300 import config, inputs
+
+    st = inputs.lj_fcc(6, 10.06, 0.85, 0.85, seed=12)
+    rng = np.random.default_rng(4)
+    st["pos"] = st["pos"] + rng.normal(scale=0.05, size=st["pos"].shape)
+    base = config.lj_fluid_config(virial=True, newton=newton)
+    a = _ctx(base, st)
+    b = _ctx(base.replace(precision="mixed"), st)
+    for step in (0, 30):
+        if step:
+            a.step(step)
+            b.step(step)
+        else:
+            a.force_only()
+            b.force_only()
+        tol = 1e-4 if step else 2e-6
+        ta, tb = a.thermo(), b.thermo()
+        wa, wb = np.array(ta["virial"]), np.array(tb["virial"])
+        assert np.max(np.abs(wa)) > 0
+        assert np.max(np.abs(wb - wa)) <= tol * np.max(np.abs(wa))
+        # virial pressure terms -tr(W) / 3V (+ the same tail correction)
+        pa = ta["pressure"] - 864 / 10.06 ** 3 * ta["temp"]
+        pb = tb["pressure"] - 864 / 10.06 ** 3 * tb["temp"]
+        assert abs(pb - pa) <= tol * np.max(np.abs(wa)) / 10.06 ** 3
