@@ -219,29 +219,29 @@ __device__ __forceinline__ void cells_block(const Dev& d, int s, int lb) {
     const int li = lb * BLK + threadIdx.x;
     int key = -1;  // global cell block of the particle's cell
     if (li < sp.n) {
-    const long long i = (long long)sp.p0 + li;
-    double4 x = d.pos[i];
-    if (vload(&st->rebuild)) {
-        int4 im = d.img[i];
-        const double hx = sp.lo[0] + sp.L[0], hy = sp.lo[1] + sp.L[1], hz = sp.lo[2] + sp.L[2];
-        // wrap on periodic axes only; on a fixed axis a particle outside the box
-        // (which pbc's slow path, domain.rs:434-452, removes) is an error
-        if ((!sp.per[0] && (x.x < sp.lo[0] || x.x >= sp.hi[0])) || (!sp.per[1] && (x.y < sp.lo[1] || x.y >= sp.hi[1])) ||
-            (!sp.per[2] && (x.z < sp.lo[2] || x.z >= sp.hi[2])))
-            atomicOr(&d.ss[s].status, ST_LOST);
-        if (sp.per[0]) { if (x.x < sp.lo[0]) { x.x += sp.L[0]; im.x -= 1; } else if (x.x >= hx) { x.x -= sp.L[0]; im.x += 1; } }
-        if (sp.per[1]) { if (x.y < sp.lo[1]) { x.y += sp.L[1]; im.y -= 1; } else if (x.y >= hy) { x.y -= sp.L[1]; im.y += 1; } }
-        if (sp.per[2]) { if (x.z < sp.lo[2]) { x.z += sp.L[2]; im.z -= 1; } else if (x.z >= hz) { x.z -= sp.L[2]; im.z += 1; } }
-        d.pos[i] = x;
-        d.img[i] = im;
-    }
-    const int cx = ext_cell_1d(x.x, sp.origin[0], sp.inv_bin[0], sp.ext[0]);
-    const int cy = ext_cell_1d(x.y, sp.origin[1], sp.inv_bin[1], sp.ext[1]);
-    const int cz = ext_cell_1d(x.z, sp.origin[2], sp.inv_bin[2], sp.ext[2]);
-    const int flat = (cx * sp.ext[1] + cy) * sp.ext[2] + cz;
-    d.cell[i] = flat;
-    atomicAdd(&d.cnt[sp.c0 + flat], 1);
-    key = d.cblk0[s] + flat / BLK;
+        const long long i = (long long)sp.p0 + li;
+        double4 x = d.pos[i];
+        if (vload(&st->rebuild)) {
+            int4 im = d.img[i];
+            const double hx = sp.lo[0] + sp.L[0], hy = sp.lo[1] + sp.L[1], hz = sp.lo[2] + sp.L[2];
+            // wrap on periodic axes only; on a fixed axis a particle outside the box
+            // (which pbc's slow path, domain.rs:434-452, removes) is an error
+            if ((!sp.per[0] && (x.x < sp.lo[0] || x.x >= sp.hi[0])) || (!sp.per[1] && (x.y < sp.lo[1] || x.y >= sp.hi[1])) ||
+                (!sp.per[2] && (x.z < sp.lo[2] || x.z >= sp.hi[2])))
+                atomicOr(&d.ss[s].status, ST_LOST);
+            if (sp.per[0]) { if (x.x < sp.lo[0]) { x.x += sp.L[0]; im.x -= 1; } else if (x.x >= hx) { x.x -= sp.L[0]; im.x += 1; } }
+            if (sp.per[1]) { if (x.y < sp.lo[1]) { x.y += sp.L[1]; im.y -= 1; } else if (x.y >= hy) { x.y -= sp.L[1]; im.y += 1; } }
+            if (sp.per[2]) { if (x.z < sp.lo[2]) { x.z += sp.L[2]; im.z -= 1; } else if (x.z >= hz) { x.z -= sp.L[2]; im.z += 1; } }
+            d.pos[i] = x;
+            d.img[i] = im;
+        }
+        const int cx = ext_cell_1d(x.x, sp.origin[0], sp.inv_bin[0], sp.ext[0]);
+        const int cy = ext_cell_1d(x.y, sp.origin[1], sp.inv_bin[1], sp.ext[1]);
+        const int cz = ext_cell_1d(x.z, sp.origin[2], sp.inv_bin[2], sp.ext[2]);
+        const int flat = (cx * sp.ext[1] + cy) * sp.ext[2] + cz;
+        d.cell[i] = flat;
+        atomicAdd(&d.cnt[sp.c0 + flat], 1);
+        key = d.cblk0[s] + flat / BLK;
     }
     // particle counts per 128-cell block, aggregated over the warp (particles
     // are in bin order after the first sort, so a warp mostly shares one block)
