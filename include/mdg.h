@@ -96,7 +96,6 @@ typedef struct mdg_material {
     double kn, kt, rolling_stiffness, rolling_damping, twisting_stiffness, twisting_damping;
 } mdg_material;
 
-/* One simulation (a "system"): the TOML sections the plugins read. */
 /* Plane wall ([[wall]] type = "plane", crates/dem_wall/src/lib.rs:171-347):
  * the plane through `point` with outward `normal` (normalised on use); active
  * for particles inside [bound_lo, bound_hi] (use +-HUGE_VAL for unbounded);
@@ -112,6 +111,7 @@ typedef struct mdg_wall {
 } mdg_wall;
 #define MDG_MAX_WALLS 6
 
+/* One simulation (a "system"): the TOML sections the plugins read. */
 typedef struct mdg_config {
     int kind;                    /* MDG_KIND_* */
     int precision;               /* MDG_FP64 or MDG_MIXED ([gpu] precision) */

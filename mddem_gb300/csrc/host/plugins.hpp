@@ -1,0 +1,25 @@
+// plugins.hpp -- helpers shared by the plugin sources.
+#pragma once
+#include <set>
+#include <string>
+#include <vector>
+
+#include "app.hpp"
+
+namespace mdg_host {
+
+// The TOML table `name` (the first stage when it is an array of tables), or
+// nullptr when absent.
+const toml::Table* section(const App& app, const std::string& name);
+// deny_unknown_fields: ConfigError naming the unknown keys.
+void check_keys(const std::string& sec, const toml::Table& t, const std::set<std::string>& allowed);
+double num(const toml::Table* t, const std::string& key, double dflt);
+long long integer(const toml::Table* t, const std::string& key, long long dflt);
+bool boolean(const toml::Table* t, const std::string& key, bool dflt);
+std::string text(const toml::Table* t, const std::string& key, const std::string& dflt);
+std::vector<const toml::Table*> table_array(const toml::Table& t, const std::string& key);
+
+// The device context and the upload (PostSetup, after the state plugins).
+void add_device_context(App& app);
+
+}  // namespace mdg_host

@@ -1,0 +1,248 @@
+"""The C++ host above the C ABI (mddem_gb300/csrc/host: TOML reader, App and
+plugins, `mdg_run`) on CPU: `mdg_run --check` resolves the reference's TOML
+sections into the same device configuration as the Python binding
+(config.from_toml + capi.to_c_config) and the same initial state as the
+Python runner's setup (positions from the seeded insertion / FCC lattice), and
+a configuration error exits with status 1 and a message, like the
+reference."""
+import json
+import math
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+GAS = """
+[domain]
+x_high = 0.025
+y_high = 0.025
+z_high = 0.025
+
+[neighbor]
+skin_fraction = 1.1
+bin_size = 0.005
+
+[run]
+dt = 2.934e-7
+steps = 500
+thermo = 100
+
+[dem]
+contact_model = "hertz"
+rolling_model = "sds"
+
+[[dem.materials]]
+name = "glass"
+youngs_mod = 8.7e9
+poisson_ratio = 0.3
+restitution = 0.95
+friction = 0.4
+rolling_friction = 0.02
+
+[[dem.materials]]
+name = "steel"
+youngs_mod = 2.0e11
+poisson_ratio = 0.3
+restitution = 0.8
+friction = 0.3
+
+[[particles.insert]]
+material = "glass"
+count = 300
+radius = 0.001
+density = 2500.0
+velocity = 0.3
+
+[[particles.insert]]
+material = "steel"
+count = 100
+radius = { distribution = "uniform", min = 0.0008, max = 0.0012 }
+density = 7800.0
+
+[gpu]
+precision = "mixed"
+rebuild_policy = "displacement"
+history_capacity = 16
+"""
+
+REBOUND = """
+[domain]
+x_low = -0.01
+x_high = 0.01
+y_low = -0.01
+y_high = 0.01
+z_low = 0.0
+z_high = 0.1
+boundary_x = "fixed"
+boundary_y = "fixed"
+boundary_z = "fixed"
+
+[neighbor]
+skin_fraction = 1.1
+bin_size = 0.015
+every = 1
+
+[[dem.materials]]
+name = "glass"
+youngs_mod = 70.0e9
+poisson_ratio = 0.22
+restitution = 0.9
+friction = 0.0
+
+[[particles.insert]]
+material = "glass"
+count = 1
+radius = 0.005
+density = 2500.0
+velocity_z = -1.0
+region = { type = "block", min = [-0.001, -0.001, 0.007], max = [0.001, 0.001, 0.008] }
+
+[[wall]]
+point_z = 0.0
+normal_z = 1.0
+material = "glass"
+
+[[wall]]
+point_z = 0.1
+normal_z = -1.0
+bound_x_low = -0.005
+velocity = [0.0, 0.0, -0.5]
+material = "glass"
+
+[run]
+steps = 20000
+"""
+
+LJ = """
+[domain]
+x_high = 10.06
+y_high = 10.06
+z_high = 10.06
+
+[neighbor]
+skin_fraction = 1.12
+bin_size = 1.0
+
+[lj]
+epsilon = 1.0
+sigma = 1.0
+cutoff = 2.5
+
+[lattice]
+density = 0.85
+temperature = 1.1
+
+[thermostat]
+temperature = 0.85
+coupling = 1.0
+
+[gpu]
+precision = "mixed"
+virial = true
+"""
+
+LANGEVIN = LJ.replace("""[thermostat]
+temperature = 0.85
+coupling = 1.0
+""", """[langevin]
+temperature = 1.2
+damping = 0.5
+seed = 99
+""")
+
+
+@pytest.fixture(scope="module")
+def runner():
+    from mddem_gb300 import build
+
+    build.build()
+    return os.path.join(ROOT, "mddem_gb300", "_lib", "mdg_run")
+
+
+def _run(runner, tmp_path, text, *args):
+    p = tmp_path / "config.toml"
+    p.write_text(text)
+    return subprocess.run([runner, str(p), *args], capture_output=True, text=True, timeout=120)
+
+
+def _num(x):
+    return {"inf": math.inf, "-inf": -math.inf}.get(x, x) if isinstance(x, str) else x
+
+
+@pytest.mark.parametrize("text", [GAS, REBOUND, LJ, LANGEVIN], ids=["gas", "rebound", "lj", "langevin"])
+def test_check_matches_python_binding(runner, tmp_path, text):
+    from mddem_gb300 import capi, run
+
+    r = _run(runner, tmp_path, text, "--check")
+    assert r.returncode == 0, r.stderr
+    got = json.loads(r.stdout)
+    cfg, st, s = run.setup(text, seed=0)
+    cc, _keep = capi.to_c_config(cfg)
+    for f in ("kind", "precision", "every", "check", "sort_every", "newton", "n_materials", "contact_model",
+              "adhesion_model", "rolling_model", "twisting_model", "nose_hoover", "virial", "rebuild_policy",
+              "threads_per_particle", "neighbor_capacity", "history_capacity", "langevin", "lv_seed"):
+        assert got[f] == getattr(cc, f), f
+    for f in ("dt", "skin_fraction", "bin_size", "lj_epsilon", "lj_sigma", "lj_cutoff", "nh_temperature",
+              "nh_coupling", "lv_temperature", "lv_damping"):
+        assert got[f] == getattr(cc, f), f
+    assert got["box_lo"] == list(cc.box_lo) and got["box_hi"] == list(cc.box_hi)
+    assert got["fixed"] == list(cc.fixed)
+    for k in range(cc.n_materials):
+        want = [getattr(cc.materials[k], f) for f, _ in capi.Material._fields_]
+        assert got["materials"][k] == want
+    assert len(got["walls"]) == cc.n_walls
+    for k, w in enumerate(got["walls"]):
+        for f in ("point", "normal", "bound_lo", "bound_hi", "velocity"):
+            assert [_num(x) for x in w[f]] == list(getattr(cc.walls[k], f)), f
+        assert w["material"] == cc.walls[k].material
+    assert got["steps"] == s["steps"] and got["thermo"] == s["thermo"]
+    # the initial state: same particles at the same places (velocities come
+    # from each host's own seeded generator)
+    assert got["n"] == len(st["tag"])
+    assert np.allclose(got["pos_sum"], np.sum(st["pos"], axis=0), rtol=1e-12, atol=0)
+    assert got["mass_sum"] == pytest.approx(float(np.sum(st["mass"])), rel=1e-12)
+    if "radius" in st:
+        assert got["radius_sum"] == pytest.approx(float(np.sum(st["radius"])), rel=1e-12)
+
+
+@pytest.mark.parametrize("edit,msg", [
+    (("bin_size = 0.005", "bin_size = 0.005\nbogus = 1"), "unknown field"),
+    (("[gpu]", "[gpu]\nwarp = 2"), "unknown field"),
+    (('rolling_model = "sds"', 'rolling_model = "spring"'), "rolling_model"),
+    (('name = "steel"', 'name = "brass"'), "not in [[dem.materials]]"),
+    (("count = 300", "count = 300\nrate = 1.0"), "rate-based"),
+    (("[domain]", '[domain]\nboundary_y = "shrink_wrap"'), "boundary_y"),
+])
+def test_config_errors_exit_1(runner, tmp_path, edit, msg):
+    r = _run(runner, tmp_path, GAS.replace(*edit), "--check")
+    assert r.returncode == 1
+    assert msg in r.stderr
+
+
+def test_toml_syntax_error_names_the_line(runner, tmp_path):
+    r = _run(runner, tmp_path, GAS.replace("[neighbor]", "[neighbor"), "--check")
+    assert r.returncode == 1 and "line" in r.stderr
+
+
+def test_cli_overrides(runner, tmp_path):
+    r = _run(runner, tmp_path, LJ, "--check", "--steps", "77", "--precision", "fp64")
+    got = json.loads(r.stdout)
+    assert got["steps"] == 77 and got["precision"] == 0
+    assert _run(runner, tmp_path, LJ, "--precision", "half").returncode == 1
+
+
+def test_run_without_a_device_reports_it(runner, tmp_path):
+    from mddem_gb300 import capi
+
+    n = capi.load()
+    import ctypes
+
+    c = ctypes.c_int(0)
+    n.mdg_device_count(ctypes.byref(c))
+    if c.value > 0:
+        pytest.skip("a CUDA device is present")
+    r = _run(runner, tmp_path, LJ)
+    assert r.returncode == 1 and "no CUDA device" in r.stderr

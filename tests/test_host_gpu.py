@@ -1,0 +1,44 @@
+"""The C++ host (`mdg_run`) driving the device: an LJ melt prints its thermo
+lines at the print interval, and a glass sphere dropped on a wall through the
+config's [[wall]], fixed boundaries and block insertion region leaves with
+e^2 of its kinetic energy (restitution 0.9)."""
+import os
+import re
+import subprocess
+
+import pytest
+
+from test_host_cpu import LJ, REBOUND
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _run(tmp_path, text, *args):
+    from mddem_gb300 import build
+
+    build.build()
+    p = tmp_path / "config.toml"
+    p.write_text(text)
+    exe = os.path.join(ROOT, "mddem_gb300", "_lib", "mdg_run")
+    return subprocess.run([exe, str(p), *args], capture_output=True, text=True, timeout=300, cwd=tmp_path)
+
+
+def test_mdg_run_lj(gpu_lib, tmp_path):
+    r = _run(tmp_path, LJ + "\n[run]\nsteps = 100\nthermo = 50\n")
+    assert r.returncode == 0, r.stderr
+    lines = [l for l in r.stdout.splitlines() if not l.startswith("#")]
+    steps = [int(l.split()[0]) for l in lines]
+    assert steps == [0, 50, 100]
+    temps = [float(re.search(r" T (\S+)", l).group(1)) for l in lines]
+    assert all(0.3 < t < 3.0 for t in temps)
+
+
+def test_mdg_run_wall_rebound(gpu_lib, tmp_path):
+    r = _run(tmp_path, REBOUND, "--steps", "6000")
+    assert r.returncode == 0, r.stderr
+    lines = [l for l in r.stdout.splitlines() if not l.startswith("#")]
+    ke = [float(re.search(r" KE (\S+)", l).group(1)) for l in lines]
+    assert int(lines[-1].split()[0]) == 6000
+    assert ke[-1] / ke[0] == pytest.approx(0.9 ** 2, rel=0.04)
