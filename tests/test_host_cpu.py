@@ -246,3 +246,82 @@ def test_run_without_a_device_reports_it(runner, tmp_path):
         pytest.skip("a CUDA device is present")
     r = _run(runner, tmp_path, LJ)
     assert r.returncode == 1 and "no CUDA device" in r.stderr
+
+
+TOML_FORMS = """
+# comments, literal and escaped strings, dotted keys, inline tables and
+# arrays across lines, integers with separators, exponents
+dem.contact_model = "hooke"
+
+[domain]
+x_low = -0.01   # trailing comment
+x_high = +0.01
+y_low = -1e-2
+y_high = 1E-2
+z_low = 0
+z_high = 0.1
+boundary_x = 'fixed'
+"boundary_y" = "fixed"
+boundary_z = "f\\u0069xed"
+
+[neighbor]
+skin_fraction = 1.1
+bin_size = 0.015
+every = 1_0
+sort_every = 1_000
+
+[[dem.materials]]
+name = 'gl"ass'
+youngs_mod = 70_000_000_000.0
+poisson_ratio = 0.22
+restitution = 0.9
+friction = 0.0
+kn = 2e5
+kt = 5e4
+
+[[particles.insert]]
+material = 'gl"ass'
+count = 3
+radius = 0.002
+density = 2500
+region = { type = "block", min = [-0.005, -0.005, 0.01], max = [
+    0.005,
+    0.005,  # still the same array
+    0.02,
+] }
+
+[[wall]]
+normal_z = 1
+velocity = [ 0.0, 0.0,
+             0.25 ]
+material = 'gl"ass'
+"""
+
+
+def test_toml_forms_read_like_tomllib(runner, tmp_path):
+    from mddem_gb300 import capi, run
+
+    r = _run(runner, tmp_path, TOML_FORMS, "--check")
+    assert r.returncode == 0, r.stderr
+    got = json.loads(r.stdout)
+    cfg, st, s = run.setup(TOML_FORMS, seed=0)
+    cc, _keep = capi.to_c_config(cfg)
+    assert got["box_lo"] == list(cc.box_lo) and got["box_hi"] == list(cc.box_hi)
+    assert got["fixed"] == [1, 1, 1] == list(cc.fixed)
+    assert got["every"] == 10 and got["sort_every"] == 1000
+    assert got["contact_model"] == 1 == cc.contact_model
+    assert got["materials"][0] == [getattr(cc.materials[0], f) for f, _ in capi.Material._fields_]
+    assert [_num(x) for x in got["walls"][0]["velocity"]] == [0.0, 0.0, 0.25]
+    assert got["n"] == 3 and np.allclose(got["pos_sum"], np.sum(st["pos"], axis=0), rtol=1e-12, atol=0)
+
+
+@pytest.mark.parametrize("bad", [
+    "[domain]\nx_low = 1\nx_low = 2\n",          # duplicate key
+    "[domain]\nx_low = \"open\n",                 # unterminated string
+    "[domain]\nx_low = [1, 2\n",                  # unterminated array
+    "[domain]\nx_low = 1 2\n",                    # junk after a value
+    "[domain]\nx_low = \"\\q\"\n",                # bad escape
+])
+def test_toml_errors(runner, tmp_path, bad):
+    r = _run(runner, tmp_path, bad + "[lj]\n[lattice]\n", "--check")
+    assert r.returncode == 1 and "line" in r.stderr
