@@ -25,7 +25,7 @@ LIB = os.path.join(OUT_DIR, "libmddem_gb300.so")
 HOST_DIR = os.path.join(CSRC, "host")
 RUNNER = os.path.join(OUT_DIR, "mdg_run")
 # the C++ host above the ABI (App, plugins, TOML reader) and its CLI
-HOST_SOURCES = ["toml.cpp", "app.cpp", "plugins.cpp", "mdg_run.cpp"]
+HOST_SOURCES = ["toml.cpp", "app.cpp", "plugins.cpp", "restart.cpp", "mdg_run.cpp"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math",

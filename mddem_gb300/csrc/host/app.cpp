@@ -284,6 +284,7 @@ struct GpuPlugin : Plugin {
         a.cfg.walls = a.walls.empty() ? nullptr : a.walls.data();
         a.cfg.n_walls = (int)a.walls.size();
         if (a.opts.check) {
+            if (!a.opts.write_restart.empty()) write_initial_restart(a, a.opts.write_restart);
             std::printf("%s\n", config_json(a).c_str());
             return;
         }
@@ -320,6 +321,7 @@ void add_core_plugins(App& app) {
     app.add_plugin(std::make_unique<RunPlugin>());
     app.add_plugin(std::make_unique<PrintPlugin>());
     app.add_plugin(std::make_unique<GpuPlugin>());
+    add_restart_plugin(app);
 }
 
 void add_device_context(App& app) { app.add_setup_system(Schedule::PostSetup, GpuPlugin::create); }

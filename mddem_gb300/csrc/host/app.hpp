@@ -37,7 +37,7 @@ struct ConfigError : std::runtime_error {
 struct HostState {
     bool dem = true;
     std::vector<uint32_t> tag, type;
-    std::vector<double> pos, vel, mass, cutoff_radius, radius, inv_inertia, omega, quat;
+    std::vector<double> pos, vel, mass, cutoff_radius, radius, density, inv_inertia, omega, quat;
     size_t size() const { return tag.size(); }
 };
 
@@ -47,6 +47,7 @@ struct Options {
     uint64_t seed = 0;
     std::string precision;      // "fp64" | "mixed" | "" (config)
     bool check = false;         // resolve and print the configuration, no device
+    std::string write_restart;  // with check: write the initial state as a restart file here
 };
 
 class App;

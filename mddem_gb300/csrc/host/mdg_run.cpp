@@ -1,13 +1,15 @@
 // mdg_run -- run a reference TOML config on the GB300 path from C++:
 //
 //   mdg_run config.toml [--steps N] [--seed S] [--precision fp64|mixed] [--check]
+//                       [--write-restart PATH]
 //
 // The reference's examples compose `CorePlugins` with `GranularDefaultPlugins`
 // or `LJDefaultPlugins` (examples/*/main.rs); this does the same from the
 // config: [lj] or [lattice] selects the LJ group, otherwise the granular
 // group, plus WallPlugin for [[wall]] and LangevinPlugin for [langevin].
 // --check resolves the configuration and the initial state and prints them
-// as JSON without touching a device.  A configuration error prints its
+// as JSON without touching a device (--write-restart also writes that initial
+// state as a restart file).  A configuration error prints its
 // message and exits with status 1, like the reference.
 #include <cstdio>
 #include <cstdlib>
@@ -21,7 +23,9 @@
 using namespace mdg_host;
 
 static int usage() {
-    std::fprintf(stderr, "usage: mdg_run config.toml [--steps N] [--seed S] [--precision fp64|mixed] [--check]\n");
+    std::fprintf(stderr,
+                 "usage: mdg_run config.toml [--steps N] [--seed S] [--precision fp64|mixed] [--check] "
+                 "[--write-restart PATH]\n");
     return 1;
 }
 
@@ -41,6 +45,7 @@ int main(int argc, char** argv) {
         else if (a == "--seed") app.opts.seed = std::strtoull(next("--seed"), nullptr, 10);
         else if (a == "--precision") app.opts.precision = next("--precision");
         else if (a == "--check") app.opts.check = true;
+        else if (a == "--write-restart") app.opts.write_restart = next("--write-restart");
         else if (a == "-h" || a == "--help") return usage();
         else if (!a.empty() && a[0] == '-') return usage();
         else path = a;

@@ -9,6 +9,7 @@
 #include <sstream>
 
 #include "plugins.hpp"
+#include "restart.hpp"
 
 namespace mdg_host {
 namespace {
@@ -91,6 +92,7 @@ void push_sphere(HostState& h, const double* x, const double* v, double r, doubl
     h.mass.push_back(m);
     h.cutoff_radius.push_back(r);
     h.radius.push_back(r);
+    h.density.push_back(density);
     h.inv_inertia.push_back(sphere_inv_inertia(m, r));
     h.omega.insert(h.omega.end(), {0.0, 0.0, 0.0});
     h.quat.insert(h.quat.end(), {1.0, 0.0, 0.0, 0.0});
@@ -454,6 +456,91 @@ struct MeasurePlugin : Plugin {
     }
 };
 
+// RestartPlugin: [restart] interval, format (PrintPlugin's restart output,
+// crates/mddem_print/src/lib.rs:1050-1066): restart_{step}_rank0.bin in the
+// output directory every `interval` steps, bincode only.
+struct RestartPlugin : Plugin {
+    std::string name() const override { return "RestartPlugin"; }
+    void build(App& app) override {
+        auto every = std::make_shared<long long>(0);
+        app.add_setup_system(Schedule::Setup, [every](App& a) {
+            const toml::Table* r = section(a, "restart");
+            if (!r) return;
+            *every = integer(r, "interval", 0);
+            if (text(r, "format", "bincode") != "bincode")
+                throw ConfigError("restart format: the C++ host writes bincode (the Python runner also writes json)");
+            if (*every > 0) a.intervals.push_back(*every);
+        });
+        app.add_update_system(Schedule::LastOutput, [every](App& a) {
+            if (*every <= 0 || a.step == 0 || a.step % *every != 0) return;
+            const size_t n = a.state.size();
+            HostState d;
+            d.dem = a.state.dem;
+            d.tag.resize(n);
+            d.type.resize(n);
+            d.pos.resize(3 * n);
+            d.vel.resize(3 * n);
+            d.mass.resize(n);
+            d.cutoff_radius.resize(n);
+            std::vector<double> force(3 * n), torque(3 * n), density;
+            std::vector<int32_t> image(3 * n);
+            mdg_state_view v{};
+            v.n = n;
+            v.tag = d.tag.data();
+            v.type = d.type.data();
+            v.pos = d.pos.data();
+            v.vel = d.vel.data();
+            v.force = force.data();
+            v.mass = d.mass.data();
+            v.cutoff_radius = d.cutoff_radius.data();
+            v.image = image.data();
+            if (d.dem) {
+                d.radius.resize(n);
+                d.inv_inertia.resize(n);
+                d.omega.resize(3 * n);
+                d.quat.resize(4 * n);
+                v.radius = d.radius.data();
+                v.inv_inertia = d.inv_inertia.data();
+                v.omega = d.omega.data();
+                v.torque = torque.data();
+                v.quat = d.quat.data();
+            }
+            int st = mdg_download_state(a.ctx, 0, &v);
+            if (st != MDG_OK) throw ConfigError(std::string("mdg_download_state: ") + mdg_status_string(st));
+            std::vector<uint32_t> keys;
+            std::vector<double> vals;
+            RestartInput in;
+            in.state = &d;
+            in.force = &force;
+            in.step = (uint64_t)a.step;
+            in.dt = a.cfg.dt;
+            if (d.dem) {
+                in.torque = &torque;
+                // densities by tag (tags are the insertion order)
+                density.resize(n);
+                for (size_t i = 0; i < n; i++) density[i] = a.state.density[d.tag[i]];
+                in.density = &density;
+                size_t nh = 0;
+                st = mdg_get_history(a.ctx, 0, nullptr, nullptr, 0, &nh);
+                if (st != MDG_OK) throw ConfigError(std::string("mdg_get_history: ") + mdg_status_string(st));
+                keys.resize(2 * nh);
+                vals.resize(7 * nh);
+                if (nh) st = mdg_get_history(a.ctx, 0, keys.data(), vals.data(), nh, &nh);
+                if (st != MDG_OK) throw ConfigError(std::string("mdg_get_history: ") + mdg_status_string(st));
+                keys.resize(2 * nh);
+                vals.resize(7 * nh);
+                in.hist_keys = &keys;
+                in.hist_vals = &vals;
+            }
+            std::filesystem::create_directories(a.out_dir);
+            const std::string path = a.out_dir + "/" + restart_filename((uint64_t)a.step);
+            std::ofstream f(path, std::ios::binary);
+            f << restart_bincode(in);
+            if (!f) throw ConfigError("cannot write " + path);
+        });
+    }
+};
+
 void json_num(std::ostringstream& o, double x) {
     if (std::isinf(x)) {
         o << (x > 0 ? "\"inf\"" : "\"-inf\"");
@@ -499,6 +586,17 @@ void add_lj_plugins(App& app) {
 }
 
 void add_wall_plugin(App& app) { app.add_plugin(std::make_unique<WallPlugin>()); }
+void add_restart_plugin(App& app) { app.add_plugin(std::make_unique<RestartPlugin>()); }
+
+void write_initial_restart(const App& a, const std::string& path) {
+    RestartInput in;
+    in.state = &a.state;
+    in.density = a.state.dem ? &a.state.density : nullptr;
+    in.dt = a.cfg.dt;
+    std::ofstream f(path, std::ios::binary);
+    f << restart_bincode(in);
+    if (!f) throw ConfigError("cannot write " + path);
+}
 void add_langevin_plugin(App& app) { app.add_plugin(std::make_unique<LangevinPlugin>()); }
 
 std::string config_json(const App& a) {

@@ -21,5 +21,9 @@ std::vector<const toml::Table*> table_array(const toml::Table& t, const std::str
 
 // The device context and the upload (PostSetup, after the state plugins).
 void add_device_context(App& app);
+// [restart] files (registered by the core group).
+void add_restart_plugin(App& app);
+// The initial state (after the state plugins) as a step-0 restart file.
+void write_initial_restart(const App& a, const std::string& path);
 
 }  // namespace mdg_host

@@ -325,3 +325,28 @@ def test_toml_forms_read_like_tomllib(runner, tmp_path):
 def test_toml_errors(runner, tmp_path, bad):
     r = _run(runner, tmp_path, bad + "[lj]\n[lattice]\n", "--check")
     assert r.returncode == 1 and "line" in r.stderr
+
+
+@pytest.mark.parametrize("text", [GAS, LJ], ids=["gas", "lj"])
+def test_restart_file_from_the_cpp_host(runner, tmp_path, text):
+    """`mdg_run --check --write-restart` writes the initial state in the
+    reference's bincode RestartData: the Python reader gets back the Python
+    runner's particles, and the Python writer re-encodes it to the same bytes."""
+    from mddem_gb300 import restart, run
+
+    path = tmp_path / "restart_0_rank0.bin"
+    r = _run(runner, tmp_path, text, "--check", "--write-restart", str(path))
+    assert r.returncode == 0, r.stderr
+    st, hist, step, dt = restart.read_restart(path)
+    cfg, ref, _ = run.setup(text, seed=0)
+    assert step == 0 and dt == cfg.dt
+    assert np.array_equal(st["tag"], ref["tag"]) and np.array_equal(st["type"], ref["type"])
+    assert np.array_equal(st["pos"], ref["pos"])
+    assert np.array_equal(st["mass"], ref["mass"]) and np.array_equal(st["cutoff_radius"], ref["cutoff_radius"])
+    if cfg.kind == "dem":
+        assert np.array_equal(st["radius"], ref["radius"]) and np.array_equal(st["density"], ref["density"])
+        assert np.array_equal(st["inv_inertia"], ref["inv_inertia"])
+        assert hist is not None and len(hist[0]) == 0
+    again = tmp_path / "again.bin"
+    restart.write_restart(again, st, hist, step=step, dt=dt)
+    assert again.read_bytes() == path.read_bytes()

@@ -1,7 +1,7 @@
 """The C++ host (`mdg_run`) driving the device: an LJ melt prints its thermo
 lines at the print interval, and a glass sphere dropped on a wall through the
 config's [[wall]], fixed boundaries and block insertion region leaves with
-e^2 of its kinetic energy (restitution 0.9)."""
+e^2 of its kinetic energy (restitution 0.9); its [restart] files read back."""
 import os
 import re
 import subprocess
@@ -36,9 +36,16 @@ def test_mdg_run_lj(gpu_lib, tmp_path):
 
 
 def test_mdg_run_wall_rebound(gpu_lib, tmp_path):
-    r = _run(tmp_path, REBOUND, "--steps", "6000")
+    from mddem_gb300 import restart
+
+    r = _run(tmp_path, REBOUND + "\n[restart]\ninterval = 3000\n", "--steps", "6000")
     assert r.returncode == 0, r.stderr
     lines = [l for l in r.stdout.splitlines() if not l.startswith("#")]
     ke = [float(re.search(r" KE (\S+)", l).group(1)) for l in lines]
     assert int(lines[-1].split()[0]) == 6000
     assert ke[-1] / ke[0] == pytest.approx(0.9 ** 2, rel=0.04)
+    # restart files of the running system, read by the Python reader
+    st, hist, step, dt = restart.read_restart(tmp_path / "output" / "restart_6000_rank0.bin")
+    assert step == 6000 and len(st["tag"]) == 1 and hist is not None
+    assert st["vel"][0, 2] == pytest.approx(0.9, rel=0.04)
+    assert (tmp_path / "output" / "restart_3000_rank0.bin").exists()
