@@ -647,7 +647,7 @@ __device__ __noinline__ int near_pair(const Dev& d, const SysParams& sp, long lo
     return (own ? 1 : 0) | (oth ? 2 : 0);
 }
 
-constexpr int BUILD_SUBS = BLK / BUILD_WARPS;  // blocks per 128-bin cell block
+constexpr int BUILD_SUBS = BLK / BUILD_WARPS;  // work units per 128-particle block (BUILD_WARPS warps each)
 
 // Row of particle li of system s by one thread (dilute systems, and the
 // rare particles whose window has particles in ghost-layer bins).
@@ -753,7 +753,8 @@ __device__ void build_one(const Dev& d, int s, int li) {
 // One warp per bin: bin `sub * BUILD_WARPS + warp` of cell block `lcb` of
 // system s.  Warp-synchronous only (no block barrier), so warps may leave early.
 // One warp per bin (large dense systems): bin `sub * BUILD_WARPS + warp` of
-// block `lcb` of system s; the lanes are the bin's particles, 32 at a time.  Warp-synchronous only (no block barrier), so warps may leave early.
+// block `lcb` of system s; the lanes are the bin's particles, 32 at a time.
+// Warp-synchronous only (no block barrier), so warps may leave early.
 __device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
     __shared__ float4 tile_h[BUILD_WARPS][32], tile_l[BUILD_WARPS][32];
     __shared__ int tile_e[BUILD_WARPS][32];
