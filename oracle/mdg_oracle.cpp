@@ -1064,6 +1064,35 @@ struct Sim {
         }
     }
 
+    // Counter-based N(0,1): SplitMix64 finaliser over (seed, step, tag, draw),
+    // 53-bit uniforms, Box-Muller cosine branch with the reference's
+    // max(u1, 1e-300) clamp (normal_sample, md_thermostat/src/lib.rs:565-581).
+    static uint64_t lv_mix(uint64_t z) {
+        z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+        z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+        return z ^ (z >> 31);
+    }
+    static double lv_uniform(uint64_t seed, long step, uint32_t tag, int draw) {
+        const uint64_t h = lv_mix(seed + lv_mix((uint64_t)step * 0x9e3779b97f4a7c15ull +
+                                                lv_mix(((uint64_t)tag << 3) + (uint64_t)draw)));
+        return (double)(h >> 11) * 0x1.0p-53;
+    }
+    static double lv_normal(uint64_t seed, long step, uint32_t tag, int k) {
+        const double u1 = lv_uniform(seed, step, tag, 2 * k), u2 = lv_uniform(seed, step, tag, 2 * k + 1);
+        return std::sqrt(-2.0 * std::log(std::fmax(u1, 1e-300))) * std::cos(6.283185307179586 * u2);
+    }
+    // langevin_force, md_thermostat/src/lib.rs:529-563 (PostForce)
+    void langevin_force() {
+        const double gamma = cfg.lv_damping, kt = cfg.lv_temperature;
+        if (gamma == 0.0) return;
+        for (int i = 0; i < nlocal; i++) {
+            const double drag = gamma * mass[i];
+            const double rc = std::sqrt(2.0 * drag * kt / dt);
+            for (int d = 0; d < 3; d++) force[i][d] -= drag * vel[i][d];
+            for (int d = 0; d < 3; d++) force[i][d] += rc * lv_normal(cfg.lv_seed, step_count, tag[i], d);
+        }
+    }
+
     void compute_forces() {
         if (virial) for (double& v : vir) v = 0.0;  // zero_virial_stress
         if (dem) contact_force();
@@ -1096,6 +1125,7 @@ struct Sim {
         compute_forces();
         reverse_send_force();
         if (!walls.empty()) wall_force();
+        if (cfg.langevin) langevin_force();
         if (nh) nh_post_final();
         else {
             final_integration();

@@ -58,6 +58,12 @@ typedef struct orc_config {
     int fixed[3];             /* boundary_x/y/z = "fixed" (0 = periodic) */
     int n_walls;              /* plane walls (DEM) */
     const orc_wall* walls;
+    /* [langevin] (md_thermostat/src/lib.rs:529-581); the N(0,1) draws come
+     * from the counter-based stream the device uses, keyed by (seed, step,
+     * tag, component), instead of the reference's ChaCha8 stream */
+    int langevin;
+    double lv_temperature, lv_damping;
+    uint64_t lv_seed;
 } orc_config;
 
 enum {

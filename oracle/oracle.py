@@ -54,6 +54,8 @@ class OrcConfig(C.Structure):
         ("nose_hoover", C.c_int), ("nh_temperature", C.c_double), ("nh_coupling", C.c_double),
         ("virial", C.c_int),
         ("fixed", C.c_int * 3), ("n_walls", C.c_int), ("walls", C.POINTER(OrcWall)),
+        ("langevin", C.c_int), ("lv_temperature", C.c_double), ("lv_damping", C.c_double),
+        ("lv_seed", C.c_uint64),
     ]
 
 
@@ -130,6 +132,10 @@ class Oracle:
             walls[k].material = int(w.material)
         c.n_walls = len(wl) if cfg.kind == "dem" else 0
         c.walls = C.cast(walls, C.POINTER(OrcWall))
+        c.langevin = int(getattr(cfg, "langevin", False))
+        c.lv_temperature = float(getattr(cfg, "lv_temperature", 0.85))
+        c.lv_damping = float(getattr(cfg, "lv_damping", 1.0))
+        c.lv_seed = int(getattr(cfg, "lv_seed", 12345))
         self._mats = mats
         self.h = self.lib.orc_create(C.byref(c))
         self.kind = cfg.kind
