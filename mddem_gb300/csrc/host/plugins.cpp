@@ -1,5 +1,6 @@
 // plugins.cpp -- the granular and LJ plugin groups, walls, Langevin,
 // measurements, and the JSON summary of a resolved configuration.
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <filesystem>
