@@ -419,3 +419,75 @@ def test_runner_rebound_config(gpu_lib, tmp_path):
     v = ctx.download()["vel"][0]
     assert v[2] == pytest.approx(COR * V0, rel=0.03)
     assert "1000 steps" in out.getvalue()
+
+
+def _one_sphere_force(z, w=(0.0, 0.0, 0.0), v=(0.0, 0.0, 0.0), **mat):
+    """Oracle force and torque on one 5 mm sphere at height z above the floor
+    wall (one force evaluation)."""
+    from mddem_gb300 import config, inputs
+    from oracle.oracle import Oracle
+
+    cfg = rebound_config()
+    m = config.Material(name="glass", youngs_mod=E, poisson_ratio=NU, restitution=COR, friction=0.0, **mat)
+    cfg = cfg.replace(materials=[m])
+    st = inputs._dem_state(np.array([[0.0, 0.0, z]]), np.array([v]), np.array([R]), RHO)
+    st["omega"] = np.array([w], dtype=float)
+    o = Oracle(cfg)
+    o.load(st)
+    o.force_only()
+    s = o.state()
+    return s["force"][0], s["torque"][0]
+
+
+def test_oracle_wall_hertz_force_closed_form():
+    """Elastic part at rest: 4/3 E* sqrt(R delta) delta along the normal, with
+    E* of the same material on both sides (wall_contact_force, lib.rs:905-944)."""
+    delta = 1e-5
+    f, t = _one_sphere_force(R - delta)
+    e_star = E / (2.0 * (1.0 - NU * NU))
+    assert f[2] == pytest.approx(4.0 / 3.0 * e_star * math.sqrt(R * delta) * delta, rel=1e-12)
+    assert f[0] == 0.0 and f[1] == 0.0 and np.all(t == 0.0)
+    f_far, _ = _one_sphere_force(R + 1e-6)  # out of contact, no adhesion: nothing
+    assert np.all(f_far == 0.0)
+
+
+def test_oracle_wall_twisting_torque_opposes_spin():
+    """A sphere pressed on the floor and spinning about the normal feels
+    -sign(omega_n) mu_tw |F_n| R about the normal (lib.rs:947-962)."""
+    delta, mu_tw = 1e-5, 0.05
+    for wz in (30.0, -30.0):
+        f, t = _one_sphere_force(R - delta, w=(0.0, 0.0, wz), twisting_friction=mu_tw)
+        assert t[2] == pytest.approx(-math.copysign(1.0, wz) * mu_tw * abs(f[2]) * R, rel=1e-12)
+        assert t[0] == 0.0 and t[1] == 0.0
+
+
+def test_oracle_wall_jkr_adhesion_only_range():
+    """JKR: inside the pull-off distance but not touching, the wall pulls with
+    1.5 pi gamma R (lib.rs:929-934); beyond it, nothing."""
+    gamma = 0.05
+    e_star = E / (2.0 * (1.0 - NU * NU))
+    pull = (math.pi ** 2 * gamma ** 2 * R / (4.0 * e_star ** 2)) ** (1.0 / 3.0)
+    f, _ = _one_sphere_force(R + 0.5 * pull, surface_energy=gamma)
+    assert f[2] == pytest.approx(-1.5 * math.pi * gamma * R, rel=1e-12)
+    f2, _ = _one_sphere_force(R + 2.0 * pull, surface_energy=gamma)
+    assert np.all(f2 == 0.0)
+
+
+def test_oracle_elastic_rebound_keeps_the_energy():
+    """e = 1 (no damping): the sphere leaves with its impact speed, to the
+    Verlet error of ~46 contact steps."""
+    from mddem_gb300 import config
+    from oracle.oracle import Oracle
+
+    cfg = rebound_config()
+    cfg = cfg.replace(materials=[config.Material(name="glass", youngs_mod=E, poisson_ratio=NU, restitution=1.0,
+                                                 friction=0.0)])
+    o = Oracle(cfg)
+    o.load(rebound_state())
+
+    def read():
+        s = o.state()
+        return s["pos"][0, 2], s["vel"][0, 2]
+
+    cor, _, _ = track_rebound(lambda: o.step(1), read)
+    assert cor == pytest.approx(1.0, abs=2e-3)
