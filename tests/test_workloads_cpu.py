@@ -1,0 +1,48 @@
+"""The benchmark's synthetic workloads on CPU: the served stream is a fixed,
+seeded trace with the job mix the served-stream config describes (half
+cooling gases of 100-200000 spheres, a quarter two-sphere rebounds, a quarter
+LJ melts of 500-100000 atoms, 1000-50000 steps), every job fits a slot class,
+and job states are reproducible."""
+import numpy as np
+
+
+def test_serve_trace_is_seeded_and_has_the_stated_mix():
+    from mddem_gb300 import workloads as w
+
+    a = w.serve_trace(njobs=128, rate=2.0, seed=2024)
+    b = w.serve_trace(njobs=128, rate=2.0, seed=2024)
+    assert [(j.kind, j.n, j.steps, j.arrival) for j in a] == [(j.kind, j.n, j.steps, j.arrival) for j in b]
+    kinds = [j.kind for j in a]
+    assert (kinds.count("gas"), kinds.count("rebound"), kinds.count("lj")) == (56, 40, 32)
+    assert all(1000 <= j.steps <= 50000 for j in a)
+    assert all(100 <= j.n <= 200000 for j in a if j.kind == "gas")
+    assert all(j.n == 2 for j in a if j.kind == "rebound")
+    assert all(500 <= j.n <= 4 * 29 ** 3 for j in a if j.kind == "lj")
+    arr = [j.arrival for j in a]
+    assert arr == sorted(arr) and arr[0] == 0.0
+
+
+def test_every_job_fits_a_slot_class():
+    from mddem_gb300 import workloads as w
+
+    dem_cap = max(c for c, _ in w.SERVE_DEM_SLOTS)
+    lj_cap = max(c for c, _ in w.SERVE_LJ_SLOTS)
+    for j in w.serve_trace(njobs=128, rate=2.0, seed=2024):
+        assert j.n <= (lj_cap if j.kind == "lj" else dem_cap)
+    cfgs, caps = w.serve_slots("mixed")
+    assert len(cfgs) == len(caps) == sum(c for _, c in w.SERVE_DEM_SLOTS) + sum(c for _, c in w.SERVE_LJ_SLOTS)
+    assert all(c.precision == "mixed" for c in cfgs)
+
+
+def test_job_states_are_reproducible():
+    from mddem_gb300 import workloads as w
+
+    trace = w.serve_trace(njobs=12, rate=2.0, seed=5)
+    for j in trace:
+        if j.n > 5000:
+            continue
+        c1, s1 = j.make("mixed", "displacement")
+        c2, s2 = j.make("mixed", "displacement")
+        assert len(s1["tag"]) == j.n
+        assert np.array_equal(s1["pos"], s2["pos"]) and np.array_equal(s1["vel"], s2["vel"])
+        assert c1 == c2
