@@ -350,3 +350,54 @@ def test_restart_file_from_the_cpp_host(runner, tmp_path, text):
     again = tmp_path / "again.bin"
     restart.write_restart(again, st, hist, step=step, dt=dt)
     assert again.read_bytes() == path.read_bytes()
+
+
+@pytest.fixture(scope="module")
+def fake_runner(runner, tmp_path_factory):
+    """mdg_run next to a CPU stand-in of the library (tests/fake_mdg.cpp): the
+    host's run path without a GPU."""
+    import shutil
+
+    d = tmp_path_factory.mktemp("fake")
+    src = os.path.join(ROOT, "tests", "fake_mdg.cpp")
+    subprocess.run(["g++", "-O1", "-std=c++17", "-shared", "-fPIC", "-I", os.path.join(ROOT, "include"), src, "-o",
+                    str(d / "libmddem_gb300.so")], check=True)
+    shutil.copy(runner, d / "mdg_run")
+    return str(d / "mdg_run")
+
+
+def test_run_path_with_outputs_and_restarts(fake_runner, tmp_path):
+    from mddem_gb300 import restart
+
+    text = GAS.replace("steps = 500\nthermo = 100", "steps = 300\nthermo = 100") + "\n[restart]\ninterval = 100\n"
+    p = tmp_path / "config.toml"
+    p.write_text(text)
+    r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    lines = [l for l in r.stdout.splitlines() if not l.startswith("#")]
+    assert [int(l.split()[0]) for l in lines] == [0, 100, 200, 300]
+    # one launch per output interval, not per step
+    assert r.stderr.count("fake: step 100") == 3 and "fake: upload n=400" in r.stderr
+    a = restart.read_restart(tmp_path / "output" / "restart_100_rank0.bin")
+    b = restart.read_restart(tmp_path / "output" / "restart_200_rank0.bin")
+    assert a[2] == 100 and b[2] == 200 and len(a[0]["tag"]) == 400
+    assert np.allclose(b[0]["pos"] - a[0]["pos"], a[0]["vel"] * 2.934e-7 * 100, rtol=1e-9, atol=1e-15)
+    assert np.array_equal(a[0]["density"][:300], np.full(300, 2500.0))
+    assert np.array_equal(a[0]["density"][300:], np.full(100, 7800.0))
+    keys, vals = a[1]
+    assert keys.tolist() == [[0, 1]] and np.allclose(vals, [[0.5 * (q + 1) for q in range(7)]])
+
+
+def test_run_path_lj_measurements(fake_runner, tmp_path):
+    text = LJ + "\n[run]\nsteps = 200\nthermo = 100\n\n[measure]\nrdf_interval = 50\nmsd_interval = 50\nrdf_bins = 30\n"
+    p = tmp_path / "config.toml"
+    p.write_text(text)
+    r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    lines = [l for l in r.stdout.splitlines() if not l.startswith("#")]
+    assert [int(l.split()[0]) for l in lines] == [0, 100, 200]
+    assert r.stderr.count("fake: step 50") == 4  # measurement marks every 50 steps
+    rdf = np.loadtxt(tmp_path / "output" / "rdf.txt")
+    assert rdf.shape == (30, 2)
+    msd = np.loadtxt(tmp_path / "output" / "msd.txt")
+    assert msd[:, 0].tolist() == [50, 100, 150, 200] and msd[:, 1].tolist() == [50, 100, 150, 200]
