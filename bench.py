@@ -48,6 +48,15 @@ def workload(name):
     if name == "lj864":
         cfg = config.lj_fluid_config(box=10.06)
         return "LJ fluid 864 atoms FCC rho=0.85 T=0.85 NH rc=2.5", cfg, lambda: inputs.lj_fcc(6, 10.06, 0.85, 0.85, seed=2024)
+    if name == "lj500":
+        cfg = config.lj_fluid_config(box=8.252)
+        return ("LJ fluid 500 atoms FCC rho=0.89 T=1.0 NH rc=2.5 (few bins: warp-per-particle list build)", cfg,
+                lambda: inputs.lj_fcc(5, 8.252, 500 / 8.252 ** 3, 1.0, seed=3))
+    if name == "lj88k":
+        L = (87808 / 0.884) ** (1.0 / 3.0)
+        cfg = config.lj_fluid_config(box=L)
+        return ("LJ fluid 87808 atoms FCC rho=0.884 T=1.0 NH rc=2.5 (warp-per-bin list build)", cfg,
+                lambda: inputs.lj_fcc(28, L, 87808 / L ** 3, 1.0, seed=3))
     if name == "dem500":
         cfg = config.granular_gas_config()
         return "DEM granular gas 500 glass spheres r=1mm box 0.025", cfg, lambda: inputs.dem_granular_gas(500, seed=0)
@@ -57,6 +66,10 @@ def workload(name):
         cfg = config.granular_gas_config(box=w.gas_box(200000, 0.15), dt=w.DT_GAS)
         return ("DEM granular gas 200000 glass spheres r=1mm solid fraction 0.15", cfg,
                 lambda: w.gas(200000, phi=0.15, seed=2024)[1])
+    if name == "gas138k":
+        cfg = config.granular_gas_config(box=w.gas_box(138195, 0.05), dt=w.DT_GAS)
+        return ("DEM granular gas 138195 glass spheres r=1mm solid fraction 0.05 (thread-per-particle list build)",
+                cfg, lambda: w.gas(138195, phi=0.05, seed=3)[1])
     if name == "poly1m":
         cfg = w.polydisperse_config()
         return ("DEM polydisperse gas 1000000 glass spheres r~U[0.8,1.2]mm solid fraction 0.30 Maxwellian", cfg,
