@@ -4,7 +4,8 @@
  * TEST INFRASTRUCTURE ONLY. The oracle is a plain C++17 restatement of
  * MDDEM's single-rank CPU path for the particle hot path (periodic ghosts,
  * bin sort, half neighbor list, Hertz-Mindlin / Hooke contact with history,
- * LJ 12-6, velocity Verlet, rotational Verlet, Nose-Hoover).  It is used by
+ * LJ 12-6, velocity Verlet, rotational Verlet, Nose-Hoover, plane walls and
+ * fixed boundaries, Langevin).  It is used by
  * tests/, by __graft_entry__.smoke() and by bench.py's CPU baseline leg as the
  * checker, never as the product path.
  *
@@ -12,7 +13,8 @@
  * cannot be built here, so the oracle is pinned against the known-answer tests
  * held in the reference's own unit tests (analytic Hertz force, Verlet exact
  * values, rotational kick, beta(e) formula, bin list vs brute force), restated
- * in tests/test_oracle_kat.py and tests/golden/.
+ * in tests/test_kat.py and tests/golden/; walls by the reference's sphere-wall
+ * rebound benchmark bounds (tests/test_walls.py).
  */
 #ifndef MDG_ORACLE_H
 #define MDG_ORACLE_H
