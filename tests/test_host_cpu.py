@@ -401,3 +401,12 @@ def test_run_path_lj_measurements(fake_runner, tmp_path):
     assert rdf.shape == (30, 2)
     msd = np.loadtxt(tmp_path / "output" / "msd.txt")
     assert msd[:, 0].tolist() == [50, 100, 150, 200] and msd[:, 1].tolist() == [50, 100, 150, 200]
+
+
+def test_crlf_config_reads_the_same(runner, tmp_path):
+    a = _run(runner, tmp_path, GAS, "--check")
+    p = tmp_path / "crlf.toml"
+    p.write_bytes(GAS.replace("\n", "\r\n").encode())
+    b = subprocess.run([runner, str(p), "--check"], capture_output=True, text=True, timeout=60)
+    assert a.returncode == 0 and b.returncode == 0, b.stderr
+    assert json.loads(a.stdout) == json.loads(b.stdout)
