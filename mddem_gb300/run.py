@@ -11,7 +11,10 @@ CSV, insert.rs:652-776), the timestep (``[run] dt``, else 0.15 Rayleigh time
 of the smallest sphere, insert.rs:1392-1431, or 0.005 for a lattice), then
 ``[run] steps`` steps with a thermo line every ``[run] thermo`` steps,
 ``[measure]`` RDF / MSD sampling (md_measure) written at the end, and
-``[restart]`` files in the reference's format every ``interval`` steps.
+``[restart]`` files in the reference's format every ``interval`` steps in
+``<output dir>/restart`` (restart_base_dir, crates/mddem_print/src/lib.rs:
+528-534); ``read = true`` resumes from the latest file there (read_restart,
+lib.rs:1143-1260): state, forces, contact history and the step count.
 The state lives on the GPU throughout; the host only sees thermo values and
 the states it writes.
 """
@@ -118,6 +121,24 @@ def setup(text, seed=0, precision=None):
     return cfg, st, settings
 
 
+def latest_restart(directory, fmt="bincode", rank=0):
+    """The restart file with the highest step for `rank` and `fmt` in
+    `directory`, or None (read_restart's scan, lib.rs:1163-1185)."""
+    ext = "json" if fmt == "json" else "bin"
+    suffix = f"_rank{rank}.{ext}"
+    best = None
+    try:
+        names = os.listdir(directory)
+    except OSError:
+        return None
+    for name in names:
+        if name.startswith("restart_") and name.endswith(suffix):
+            mid = name[len("restart_"):len(name) - len(suffix)]
+            if mid.isdigit() and (best is None or int(mid) > best[0]):
+                best = (int(mid), name)
+    return os.path.join(directory, best[1]) if best else None
+
+
 def thermo_line(step, t, kind):
     if kind == "lj":
         return (f"{step:10d} T {t['temp']:.6f} KE {t['ke']:.6e} PE {t['pe']:.6e} E {t['ke'] + t['pe']:.6e} "
@@ -129,41 +150,51 @@ def thermo_line(step, t, kind):
 def run(text, seed=0, precision=None, steps=None, out=sys.stdout):
     cfg, st, s = setup(text, seed, precision)
     nsteps = s["steps"] if steps is None else steps
+    rs = s["restart"]
+    rst_dir = os.path.join(s["output"], "restart")
+    base = 0
+    src = latest_restart(rst_dir, rs.get("format", "bincode")) if rs and rs.get("read") else None
+    if src:
+        st, hist, base, _ = restart.read_restart(src)
+        print(f"# Restart: reading from {src}", file=out)
     n = len(st["tag"])
     ctx = capi.Context(cfg, n)
     ctx.upload(st)
+    if src and hist is not None and len(hist[0]):
+        ctx.set_history(*hist)
     meas = s["measure"]
     rdf_every = int(meas.get("rdf_interval", 0)) if cfg.kind == "lj" and meas else 0
     msd_every = int(meas.get("msd_interval", 0)) if cfg.kind == "lj" and meas else 0
     nbins, rmax = int(meas.get("rdf_bins", 200)), float(meas.get("rdf_cutoff", 3.0))
-    rs = s["restart"]
     rst_every = int(rs.get("interval", 0)) if rs else 0
     fmt = rs.get("format", "bincode") if rs else "bincode"
     if rst_every or rdf_every or msd_every:
         os.makedirs(s["output"], exist_ok=True)
+    if rst_every:
+        os.makedirs(rst_dir, exist_ok=True)
     g_sum, g_n, msd = None, 0, []
     if msd_every:
         ctx.msd_reset()
     marks = sorted({k for every in (s["thermo"], rdf_every, msd_every, rst_every) if every
                     for k in range(every, nsteps + 1, every)} | {nsteps})
     print(f"# {cfg.kind} N={n} dt={cfg.dt:.6e} steps={nsteps} precision={cfg.precision}", file=out)
-    print(thermo_line(0, ctx.thermo(), cfg.kind), file=out)
+    print(thermo_line(base, ctx.thermo(), cfg.kind), file=out)
     done, t0 = 0, time.perf_counter()
     for k in marks:
         ctx.step(k - done)  # one graph launch for all the steps up to the next mark
         done = k
         if s["thermo"] and k % s["thermo"] == 0 or k == nsteps:
-            print(thermo_line(k, ctx.thermo(), cfg.kind), file=out)
+            print(thermo_line(base + k, ctx.thermo(), cfg.kind), file=out)
         if rdf_every and k % rdf_every == 0:
             r, g, _ = ctx.rdf(r_max=rmax, nbins=nbins)
             g_sum = g if g_sum is None else g_sum + g
             g_n += 1
         if msd_every and k % msd_every == 0:
-            msd.append((k, ctx.msd()))
+            msd.append((base + k, ctx.msd()))
         if rst_every and k % rst_every == 0:
-            p = os.path.join(s["output"], restart.restart_filename(k, 0, fmt))
+            p = os.path.join(rst_dir, restart.restart_filename(base + k, 0, fmt))
             hist = ctx.history() if cfg.kind == "dem" else None
-            restart.write_restart(p, ctx.download(), hist, step=k, dt=cfg.dt, fmt=fmt)
+            restart.write_restart(p, ctx.download(), hist, step=base + k, dt=cfg.dt, fmt=fmt)
     el = time.perf_counter() - t0
     print(f"# {nsteps} steps in {el:.3f} s: {n * nsteps / max(el, 1e-9):.4e} particle-steps/s", file=out)
     if g_n:

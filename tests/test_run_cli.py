@@ -128,6 +128,27 @@ def test_runner_runs_both_kinds(gpu_lib, tmp_path):
     out = io.StringIO()
     dem = DEM + f'\n[output]\ndir = "{tmp_path / "dem"}"\n'
     run.run(dem, out=out, precision="mixed")
-    st, hist, step, dt = restart.read_restart(tmp_path / "dem" / "restart_400_rank0.bin")
+    # the reference's restart directory: <output dir>/restart
+    st, hist, step, dt = restart.read_restart(tmp_path / "dem" / "restart" / "restart_400_rank0.bin")
     assert step == 400 and len(st["tag"]) == 500
-    assert (tmp_path / "dem" / "restart_200_rank0.bin").exists()
+    assert (tmp_path / "dem" / "restart" / "restart_200_rank0.bin").exists()
+    # [restart] read = true resumes from the latest file and numbers on from it
+    out = io.StringIO()
+    run.run(dem.replace('format = "bincode"', 'format = "bincode"\nread = true'), out=out, precision="mixed")
+    lines = [x for x in out.getvalue().splitlines() if not x.startswith("#")]
+    assert [int(x.split()[0]) for x in lines] == [400, 600, 800]
+    assert "Restart: reading from" in out.getvalue()
+    st2, _, step2, _ = restart.read_restart(tmp_path / "dem" / "restart" / "restart_800_rank0.bin")
+    assert step2 == 800 and len(st2["tag"]) == 500
+
+
+def test_latest_restart_picks_the_highest_step(tmp_path):
+    from mddem_gb300 import run
+
+    for name in ("restart_200_rank0.bin", "restart_1000_rank0.bin", "restart_900_rank0.bin",
+                 "restart_5000_rank1.bin", "restart_7000_rank0.json", "notes.txt"):
+        (tmp_path / name).write_bytes(b"")
+    assert run.latest_restart(tmp_path).endswith("restart_1000_rank0.bin")
+    assert run.latest_restart(tmp_path, "json").endswith("restart_7000_rank0.json")
+    assert run.latest_restart(tmp_path, rank=1).endswith("restart_5000_rank1.bin")
+    assert run.latest_restart(tmp_path / "missing") is None
