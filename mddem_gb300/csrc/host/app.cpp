@@ -59,9 +59,11 @@ void App::run_set(std::vector<std::pair<Schedule, std::function<void(App&)>>>& s
 int App::start() {
     for (Schedule s : {Schedule::PreSetup, Schedule::Setup, Schedule::PostSetup}) run_set(setup_, s);
     if (opts.check || !ctx) return 0;
-    // Output marks: every update system runs at multiples of the print interval
-    // and at the last step; between marks one mdg_step launch runs the whole
-    // fused schedule (InitialIntegration ... PostFinalIntegration) on the device.
+    // Output marks (steps into this run): every update system runs at multiples
+    // of the print interval and at the last step; between marks one mdg_step
+    // launch runs the whole fused schedule (InitialIntegration ...
+    // PostFinalIntegration) on the device.
+    step = first_step;
     std::set<long long> marks{run_steps};
     std::vector<long long> every = intervals;
     every.push_back(thermo_every);
@@ -69,13 +71,13 @@ int App::start() {
         for (long long k = e; e > 0 && k < run_steps; k += e) marks.insert(k);
     run_set(update_, Schedule::LastOutput);
     for (long long k : marks) {
-        if (k <= step) continue;
-        const int st = mdg_step(ctx, k - step);
+        if (k <= done()) continue;
+        const int st = mdg_step(ctx, k - done());
         if (st != MDG_OK) {
             std::fprintf(stderr, "Error: step %lld: %s\n", step, mdg_status_string(st));
             return 2;
         }
-        step = k;
+        step = first_step + k;
         run_set(update_, Schedule::LastOutput);
     }
     for (auto& f : finish) f(*this);
@@ -237,7 +239,7 @@ struct PrintPlugin : Plugin {
     std::string name() const override { return "PrintPlugin"; }
     void build(App& app) override {
         app.add_update_system(Schedule::LastOutput, [](App& a) {
-            if (!(a.thermo_every > 0 && a.step % a.thermo_every == 0) && a.step != a.run_steps) return;
+            if (!(a.thermo_every > 0 && a.done() % a.thermo_every == 0) && a.done() != a.run_steps) return;
             mdg_thermo_t t{};
             const int st = mdg_thermo(a.ctx, 0, &t);
             if (st != MDG_OK) throw ConfigError(std::string("thermo: ") + mdg_status_string(st));
@@ -279,6 +281,8 @@ struct GpuPlugin : Plugin {
     }
     // registered by add_core_plugins after the group plugins' PostSetup
     static void create(App& a) {
+        Resumed res;
+        if (a.restart_read) res = resume_from_restart(a);
         a.cfg.materials = a.materials.empty() ? nullptr : a.materials.data();
         a.cfg.n_materials = a.dem ? (int)a.materials.size() : 0;
         a.cfg.walls = a.walls.empty() ? nullptr : a.walls.data();
@@ -299,14 +303,20 @@ struct GpuPlugin : Plugin {
         v.vel = h.vel.data();
         v.mass = h.mass.data();
         v.cutoff_radius = h.cutoff_radius.data();
+        v.force = res.force.empty() ? nullptr : res.force.data();
         if (h.dem) {
             v.radius = h.radius.data();
             v.inv_inertia = h.inv_inertia.data();
             v.omega = h.omega.data();
             v.quat = h.quat.data();
+            v.torque = res.torque.empty() ? nullptr : res.torque.data();
         }
         st = mdg_upload_state(a.ctx, 0, &v);
         if (st != MDG_OK) throw ConfigError(std::string("mdg_upload_state: ") + mdg_status_string(st));
+        if (!res.hist_keys.empty()) {
+            st = mdg_set_history(a.ctx, 0, res.hist_keys.size() / 2, res.hist_keys.data(), res.hist_vals.data());
+            if (st != MDG_OK) throw ConfigError(std::string("mdg_set_history: ") + mdg_status_string(st));
+        }
         std::printf("# %s N=%zu dt=%.6e steps=%lld precision=%s\n", a.dem ? "dem" : "lj", h.size(), a.cfg.dt,
                     a.run_steps, a.cfg.precision == MDG_MIXED ? "mixed" : "fp64");
     }

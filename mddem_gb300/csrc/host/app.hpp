@@ -84,7 +84,10 @@ public:
     HostState state;
     long long run_steps = 1000, thermo_every = 100;
     std::vector<long long> intervals;   // other output intervals (measurements)
-    long long step = 0;             // steps done
+    long long step = 0;             // step counter: first_step + the steps done in this run
+    long long first_step = 0;       // the restart's step when [restart] read resumed one
+    bool restart_read = false;      // [restart] read = true
+    long long done() const { return step - first_step; }
     mdg_ctx* ctx = nullptr;
     std::vector<std::string> provided;
     std::string out_dir = "output";

@@ -5,9 +5,11 @@
 #include <cstdio>
 #include <filesystem>
 #include <fstream>
+#include <iterator>
 #include <limits>
 #include <random>
 #include <sstream>
+#include <unordered_map>
 
 #include "plugins.hpp"
 #include "restart.hpp"
@@ -407,11 +409,11 @@ struct MeasurePlugin : Plugin {
             if (c->msd_every > 0) a.intervals.push_back(c->msd_every);
         });
         app.add_update_system(Schedule::LastOutput, [c](App& a) {
-            if (a.step == 0) {
+            if (a.done() == 0) {
                 if (c->msd_every > 0 && mdg_msd_reset(a.ctx, 0) != MDG_OK) throw ConfigError("msd reset failed");
                 return;
             }
-            if (c->rdf_every > 0 && a.step % c->rdf_every == 0) {
+            if (c->rdf_every > 0 && a.done() % c->rdf_every == 0) {
                 std::vector<uint64_t> counts((size_t)c->bins);
                 if (mdg_rdf(a.ctx, 0, c->rmax, c->bins, counts.data()) != MDG_OK) throw ConfigError("rdf failed");
                 // g_k = counts_k V / (N (N - 1) / 2 shell_k) (md_measure/src/lib.rs:420-440)
@@ -427,7 +429,7 @@ struct MeasurePlugin : Plugin {
                 }
                 c->samples++;
             }
-            if (c->msd_every > 0 && a.step % c->msd_every == 0) {
+            if (c->msd_every > 0 && a.done() % c->msd_every == 0) {
                 double v = 0.0;
                 if (mdg_msd(a.ctx, 0, &v) != MDG_OK) throw ConfigError("msd failed");
                 c->msd.emplace_back(a.step, v);
@@ -457,9 +459,13 @@ struct MeasurePlugin : Plugin {
     }
 };
 
-// RestartPlugin: [restart] interval, format (PrintPlugin's restart output,
-// crates/mddem_print/src/lib.rs:1050-1066): restart_{step}_rank0.bin in the
-// output directory every `interval` steps, bincode only.
+std::string restart_dir(const App& a) { return a.out_dir + "/restart"; }
+
+// RestartPlugin: [restart] interval, format, read (RestartConfig and the
+// restart output, crates/mddem_print/src/lib.rs:267-277, 1050-1066):
+// restart_{step}_rank0.bin in <output>/restart (restart_base_dir,
+// lib.rs:528-534) every `interval` steps, bincode only; `read` resumes from
+// the latest of them (resume_from_restart).
 struct RestartPlugin : Plugin {
     std::string name() const override { return "RestartPlugin"; }
     void build(App& app) override {
@@ -467,13 +473,15 @@ struct RestartPlugin : Plugin {
         app.add_setup_system(Schedule::Setup, [every](App& a) {
             const toml::Table* r = section(a, "restart");
             if (!r) return;
+            check_keys("restart", *r, {"interval", "format", "read"});
             *every = integer(r, "interval", 0);
             if (text(r, "format", "bincode") != "bincode")
                 throw ConfigError("restart format: the C++ host writes bincode (the Python runner also writes json)");
+            a.restart_read = boolean(r, "read", false);
             if (*every > 0) a.intervals.push_back(*every);
         });
         app.add_update_system(Schedule::LastOutput, [every](App& a) {
-            if (*every <= 0 || a.step == 0 || a.step % *every != 0) return;
+            if (*every <= 0 || a.done() == 0 || a.done() % *every != 0) return;
             const size_t n = a.state.size();
             HostState d;
             d.dem = a.state.dem;
@@ -517,9 +525,11 @@ struct RestartPlugin : Plugin {
             in.dt = a.cfg.dt;
             if (d.dem) {
                 in.torque = &torque;
-                // densities by tag (tags are the insertion order)
+                // densities by tag (the device keeps no density)
+                std::unordered_map<uint32_t, double> by_tag;
+                for (size_t i = 0; i < n; i++) by_tag[a.state.tag[i]] = a.state.density[i];
                 density.resize(n);
-                for (size_t i = 0; i < n; i++) density[i] = a.state.density[d.tag[i]];
+                for (size_t i = 0; i < n; i++) density[i] = by_tag.at(d.tag[i]);
                 in.density = &density;
                 size_t nh = 0;
                 st = mdg_get_history(a.ctx, 0, nullptr, nullptr, 0, &nh);
@@ -533,8 +543,9 @@ struct RestartPlugin : Plugin {
                 in.hist_keys = &keys;
                 in.hist_vals = &vals;
             }
-            std::filesystem::create_directories(a.out_dir);
-            const std::string path = a.out_dir + "/" + restart_filename((uint64_t)a.step);
+            const std::string dir = restart_dir(a);
+            std::filesystem::create_directories(dir);
+            const std::string path = dir + "/" + restart_filename((uint64_t)a.step);
             std::ofstream f(path, std::ios::binary);
             f << restart_bincode(in);
             if (!f) throw ConfigError("cannot write " + path);
@@ -588,6 +599,31 @@ void add_lj_plugins(App& app) {
 
 void add_wall_plugin(App& app) { app.add_plugin(std::make_unique<WallPlugin>()); }
 void add_restart_plugin(App& app) { app.add_plugin(std::make_unique<RestartPlugin>()); }
+
+Resumed resume_from_restart(App& a) {
+    Resumed out;
+    const std::string dir = restart_dir(a);
+    const std::string path = latest_restart(dir);
+    if (path.empty()) {
+        std::printf("# Restart: no restart files found in %s\n", dir.c_str());
+        return out;
+    }
+    std::printf("# Restart: reading from %s\n", path.c_str());
+    std::ifstream f(path, std::ios::binary);
+    const std::string bytes((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    if (!f.good() && !f.eof()) throw ConfigError("cannot read " + path);
+    RestartRead r = restart_read(bytes);
+    if (r.state.dem != a.dem)
+        throw ConfigError(path + (a.dem ? ": no DemAtom buffer for a granular run" : ": a DEM file for an LJ run"));
+    a.state = std::move(r.state);
+    a.first_step = (long long)r.step;
+    out.force = std::move(r.force);
+    out.torque = std::move(r.torque);
+    out.hist_keys = std::move(r.hist_keys);
+    out.hist_vals = std::move(r.hist_vals);
+    std::printf("# Restart: loaded %zu atoms from step %llu\n", a.state.size(), (unsigned long long)r.step);
+    return out;
+}
 
 void write_initial_restart(const App& a, const std::string& path) {
     RestartInput in;

@@ -26,4 +26,15 @@ void add_restart_plugin(App& app);
 // The initial state (after the state plugins) as a step-0 restart file.
 void write_initial_restart(const App& a, const std::string& path);
 
+// [restart] read = true (read_restart, crates/mddem_print/src/lib.rs:1152-1251):
+// the latest restart_{step}_rank0.bin in <output>/restart replaces the state
+// and sets first_step to its step; the forces, torques and contact history it
+// returns go to the device with the upload.  No file: a note, the state stays.
+struct Resumed {
+    std::vector<double> force, torque;
+    std::vector<uint32_t> hist_keys;
+    std::vector<double> hist_vals;
+};
+Resumed resume_from_restart(App& a);
+
 }  // namespace mdg_host

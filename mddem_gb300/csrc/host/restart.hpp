@@ -32,4 +32,20 @@ std::string restart_bincode(const RestartInput& in);
 // restart_{step}_rank{rank}.bin
 std::string restart_filename(uint64_t step, int rank = 0);
 
+// A restart file read back: the state (DEM when it carries the DemAtom
+// buffer), forces, torques, contact history, step and dt.
+struct RestartRead {
+    HostState state;
+    std::vector<double> force, torque;
+    std::vector<uint32_t> hist_keys;
+    std::vector<double> hist_vals;
+    uint64_t step = 0;
+    double dt = 0.0;
+};
+// Parse bincode RestartData; throws ConfigError on malformed input.
+RestartRead restart_read(const std::string& bytes);
+// The restart file with the highest step for rank 0 in `dir` (bincode), or
+// "" (read_restart's scan, crates/mddem_print/src/lib.rs:1163-1185).
+std::string latest_restart(const std::string& dir);
+
 }  // namespace mdg_host

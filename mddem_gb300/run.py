@@ -111,6 +111,9 @@ def setup(text, seed=0, precision=None):
             dens = np.asarray(st.get("density", np.full(len(st["tag"]), 2500.0)))
             cfg = cfg.replace(dt=config.rayleigh_dt(float(np.min(st["radius"])), float(np.max(dens)),
                                                     m.youngs_mod, m.poisson_ratio))
+    extra = set(doc.get("restart", {})) - {"interval", "format", "read"}
+    if extra:
+        raise RunError(f"[restart]: unknown key(s) {sorted(extra)} (RestartConfig: interval, format, read)")
     settings = {
         "steps": int(run.get("steps", 1000)),
         "thermo": int(run.get("thermo", 100)),

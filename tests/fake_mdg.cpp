@@ -1,8 +1,9 @@
 // fake_mdg.cpp -- test infrastructure: a CPU stand-in for libmddem_gb300.so
 // with the entry points the C++ host calls, so the host's run path (create,
-// upload, steps between outputs, thermo, download, history, restart files)
-// runs without a GPU.  Particles fly freely (x += v dt per step); every call
-// checks its arguments against the uploaded state and logs itself to stderr.
+// upload, steps between outputs, thermo, download, history, restart files,
+// resume) runs without a GPU.  Particles fly freely (x += v dt per step) and
+// keep the force and torque they were uploaded with; every call checks its
+// arguments against the uploaded state and logs itself to stderr.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -16,7 +17,10 @@ struct mdg_ctx {
     bool dem = false, uploaded = false;
     long long step = 0;
     std::vector<uint32_t> tag, type;
-    std::vector<double> pos, vel, mass, cutr, radius, inv_inertia, omega, quat;
+    std::vector<double> pos, vel, force, torque, mass, cutr, radius, inv_inertia, omega, quat;
+    bool history_set = false;
+    std::vector<uint32_t> hkeys;
+    std::vector<double> hvals;
 };
 
 extern "C" {
@@ -47,6 +51,10 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* v) {
     c->type.assign(v->type, v->type + n);
     c->pos.assign(v->pos, v->pos + 3 * n);
     c->vel.assign(v->vel, v->vel + 3 * n);
+    c->force.assign(3 * n, 0.0);
+    if (v->force) c->force.assign(v->force, v->force + 3 * n);
+    c->torque.assign(3 * n, 0.0);
+    if (c->dem && v->torque) c->torque.assign(v->torque, v->torque + 3 * n);
     c->mass.assign(v->mass, v->mass + n);
     c->cutr.assign(v->cutoff_radius, v->cutoff_radius + n);
     if (c->dem) {
@@ -56,7 +64,8 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* v) {
         c->quat.assign(v->quat, v->quat + 4 * n);
     }
     c->uploaded = true;
-    std::fprintf(stderr, "fake: upload n=%zu\n", n);
+    std::fprintf(stderr, "fake: upload n=%zu force=%d torque=%d\n", n, v->force != nullptr,
+                 c->dem && v->torque != nullptr);
     return MDG_OK;
 }
 
@@ -92,7 +101,7 @@ int mdg_download_state(mdg_ctx* c, int sys, mdg_state_view* v) {
     if (v->type) std::memcpy(v->type, c->type.data(), n * sizeof(uint32_t));
     std::memcpy(v->pos, c->pos.data(), 3 * n * sizeof(double));
     std::memcpy(v->vel, c->vel.data(), 3 * n * sizeof(double));
-    if (v->force) std::memset(v->force, 0, 3 * n * sizeof(double));
+    if (v->force) std::memcpy(v->force, c->force.data(), 3 * n * sizeof(double));
     if (v->mass) std::memcpy(v->mass, c->mass.data(), n * sizeof(double));
     if (v->cutoff_radius) std::memcpy(v->cutoff_radius, c->cutr.data(), n * sizeof(double));
     if (v->image) std::memset(v->image, 0, 3 * n * sizeof(int32_t));
@@ -102,14 +111,33 @@ int mdg_download_state(mdg_ctx* c, int sys, mdg_state_view* v) {
         std::memcpy(v->inv_inertia, c->inv_inertia.data(), n * sizeof(double));
         std::memcpy(v->omega, c->omega.data(), 3 * n * sizeof(double));
         std::memcpy(v->quat, c->quat.data(), 4 * n * sizeof(double));
-        if (v->torque) std::memset(v->torque, 0, 3 * n * sizeof(double));
+        if (v->torque) std::memcpy(v->torque, c->torque.data(), 3 * n * sizeof(double));
     }
     return MDG_OK;
 }
 
-// one synthetic contact (tag 0 with tag 1) when the system has two particles
+int mdg_set_history(mdg_ctx* c, int sys, size_t n, const uint32_t* keys, const double* vals) {
+    if (!c || sys != 0 || !c->dem || !c->uploaded || (n && (!keys || !vals))) return MDG_ERR_ARG;
+    c->hkeys.assign(keys, keys + 2 * n);
+    c->hvals.assign(vals, vals + 7 * n);
+    c->history_set = true;
+    std::fprintf(stderr, "fake: set_history n=%zu\n", n);
+    return MDG_OK;
+}
+
+// the history that was set, else one synthetic contact (tag 0 with tag 1)
+// when the system has two particles
 int mdg_get_history(mdg_ctx* c, int sys, uint32_t* keys, double* vals, size_t cap, size_t* n) {
     if (!c || sys != 0 || !n) return MDG_ERR_ARG;
+    if (c->history_set) {
+        const size_t have = c->hkeys.size() / 2;
+        if (cap >= have && have) {
+            std::memcpy(keys, c->hkeys.data(), 2 * have * sizeof(uint32_t));
+            std::memcpy(vals, c->hvals.data(), 7 * have * sizeof(double));
+        }
+        *n = have;
+        return MDG_OK;
+    }
     const size_t have = (c->dem && c->n >= 2) ? 1 : 0;
     if (cap >= have && have) {
         keys[0] = 0;

@@ -377,15 +377,59 @@ def test_run_path_with_outputs_and_restarts(fake_runner, tmp_path):
     lines = [l for l in r.stdout.splitlines() if not l.startswith("#")]
     assert [int(l.split()[0]) for l in lines] == [0, 100, 200, 300]
     # one launch per output interval, not per step
-    assert r.stderr.count("fake: step 100") == 3 and "fake: upload n=400" in r.stderr
-    a = restart.read_restart(tmp_path / "output" / "restart_100_rank0.bin")
-    b = restart.read_restart(tmp_path / "output" / "restart_200_rank0.bin")
+    assert r.stderr.count("fake: step 100") == 3 and "fake: upload n=400 force=0" in r.stderr
+    a = restart.read_restart(tmp_path / "output" / "restart" / "restart_100_rank0.bin")
+    b = restart.read_restart(tmp_path / "output" / "restart" / "restart_200_rank0.bin")
     assert a[2] == 100 and b[2] == 200 and len(a[0]["tag"]) == 400
     assert np.allclose(b[0]["pos"] - a[0]["pos"], a[0]["vel"] * 2.934e-7 * 100, rtol=1e-9, atol=1e-15)
     assert np.array_equal(a[0]["density"][:300], np.full(300, 2500.0))
     assert np.array_equal(a[0]["density"][300:], np.full(100, 7800.0))
     keys, vals = a[1]
     assert keys.tolist() == [[0, 1]] and np.allclose(vals, [[0.5 * (q + 1) for q in range(7)]])
+
+
+def test_run_path_resumes_from_the_latest_restart(fake_runner, tmp_path):
+    """`[restart] read = true` (read_restart, mddem_print/src/lib.rs:1152-1251):
+    the latest file in output/restart replaces the inserted state, the step
+    counter continues from its step, and its forces, torques and contact
+    history go to the device with the upload."""
+    from mddem_gb300 import restart
+
+    text = GAS.replace("steps = 500\nthermo = 100", "steps = 300\nthermo = 100") + "\n[restart]\ninterval = 100\n"
+    p = tmp_path / "config.toml"
+    p.write_text(text)
+    r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    # mark the newest file so the resume can be told from a fresh insertion
+    src = tmp_path / "output" / "restart" / "restart_300_rank0.bin"
+    st, hist, step, dt = restart.read_restart(src)
+    st["force"] = np.arange(st["pos"].size, dtype=float).reshape(-1, 3)
+    st["torque"] = -st["force"]
+    hist = (np.array([[3, 7], [5, 9]], np.uint32), np.arange(14, dtype=float).reshape(2, 7))
+    restart.write_restart(src, st, hist, step=step, dt=dt)
+
+    p.write_text(text.replace("steps = 300", "steps = 200") + "read = true\n")
+    r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert "# Restart: reading from output/restart/restart_300_rank0.bin" in r.stdout
+    lines = [l for l in r.stdout.splitlines() if not l.startswith("#")]
+    assert [int(l.split()[0]) for l in lines] == [300, 400, 500]
+    assert "fake: upload n=400 force=1 torque=1" in r.stderr and "fake: set_history n=2" in r.stderr
+    c = restart.read_restart(tmp_path / "output" / "restart" / "restart_500_rank0.bin")
+    assert c[2] == 500
+    assert np.allclose(c[0]["pos"] - st["pos"], st["vel"] * 2.934e-7 * 200, rtol=1e-9, atol=1e-15)
+    for f in ("tag", "type", "mass", "radius", "density", "force", "torque", "quat"):
+        assert np.array_equal(c[0][f], st[f]), f
+    assert c[1][0].tolist() == [[3, 7], [5, 9]] and np.array_equal(c[1][1], hist[1])
+
+
+def test_resume_without_files_runs_from_the_inserted_state(fake_runner, tmp_path):
+    p = tmp_path / "config.toml"
+    p.write_text(GAS.replace("steps = 500", "steps = 100") + "\n[restart]\nread = true\n")
+    r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert "# Restart: no restart files found in output/restart" in r.stdout
+    assert [int(l.split()[0]) for l in r.stdout.splitlines() if not l.startswith("#")] == [0, 100]
 
 
 def test_run_path_lj_measurements(fake_runner, tmp_path):

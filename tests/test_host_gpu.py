@@ -45,7 +45,7 @@ def test_mdg_run_wall_rebound(gpu_lib, tmp_path):
     assert int(lines[-1].split()[0]) == 6000
     assert ke[-1] / ke[0] == pytest.approx(0.9 ** 2, rel=0.04)
     # restart files of the running system, read by the Python reader
-    st, hist, step, dt = restart.read_restart(tmp_path / "output" / "restart_6000_rank0.bin")
+    st, hist, step, dt = restart.read_restart(tmp_path / "output" / "restart" / "restart_6000_rank0.bin")
     assert step == 6000 and len(st["tag"]) == 1 and hist is not None
     assert st["vel"][0, 2] == pytest.approx(0.9, rel=0.04)
-    assert (tmp_path / "output" / "restart_3000_rank0.bin").exists()
+    assert (tmp_path / "output" / "restart" / "restart_3000_rank0.bin").exists()

@@ -152,3 +152,10 @@ def test_latest_restart_picks_the_highest_step(tmp_path):
     assert run.latest_restart(tmp_path, "json").endswith("restart_7000_rank0.json")
     assert run.latest_restart(tmp_path, rank=1).endswith("restart_5000_rank1.bin")
     assert run.latest_restart(tmp_path / "missing") is None
+
+
+def test_restart_section_rejects_unknown_keys():
+    from mddem_gb300 import run
+
+    with pytest.raises(run.RunError, match="unknown key"):
+        run.setup(DEM.replace("[restart]\n", "[restart]\nevery = 3\n"))
