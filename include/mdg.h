@@ -111,6 +111,12 @@ typedef struct mdg_wall {
 } mdg_wall;
 #define MDG_MAX_WALLS 6
 
+/* One LJ type pair: well depth, length scale and the cutoff in units of
+ * sigma (LJPairCoeffs::from_params, crates/md_lj/src/lib.rs:226-238). */
+typedef struct mdg_lj_pair {
+    double epsilon, sigma, cutoff;
+} mdg_lj_pair;
+
 /* One simulation (a "system"): the TOML sections the plugins read. */
 typedef struct mdg_config {
     int kind;                    /* MDG_KIND_* */
@@ -150,6 +156,13 @@ typedef struct mdg_config {
     /* [[wall]] plane walls (DEM), at most MDG_MAX_WALLS */
     int n_walls;
     const mdg_wall* walls;
+    /* [lj] multi-type mode (build_lj_pair_table, crates/md_lj/src/lib.rs:
+     * 334-384): n_lj_types > 1 gives the n x n pair table `lj_pairs`
+     * (row-major and symmetric, with the mixing rule and the pair_coeffs
+     * overrides applied), and each particle's `type` (< n_lj_types) picks its
+     * row and column; 0 or 1 = the single type of lj_epsilon/sigma/cutoff. */
+    int n_lj_types;
+    const mdg_lj_pair* lj_pairs;
 } mdg_config;
 
 
@@ -157,7 +170,8 @@ typedef struct mdg_config {
 typedef struct mdg_state_view {
     size_t n;
     uint32_t* tag;
-    uint32_t* type;          /* material index (DEM) or LJ type */
+    uint32_t* type;          /* material index (DEM) or LJ type (< n_lj_types in
+                                multi-type mode, else unused) */
     double* pos;             /* n*3 */
     double* vel;             /* n*3 */
     double* force;           /* n*3: initial force on upload (restart), NULL = zero */

@@ -56,6 +56,10 @@ class Wall(C.Structure):
                 ("bound_hi", C.c_double * 3), ("velocity", C.c_double * 3), ("material", C.c_int)]
 
 
+class LJPair(C.Structure):
+    _fields_ = [("epsilon", C.c_double), ("sigma", C.c_double), ("cutoff", C.c_double)]
+
+
 class Config(C.Structure):
     _fields_ = [
         ("kind", C.c_int), ("precision", C.c_int),
@@ -72,6 +76,7 @@ class Config(C.Structure):
         ("history_capacity", C.c_int),
         ("langevin", C.c_int), ("lv_temperature", C.c_double), ("lv_damping", C.c_double), ("lv_seed", C.c_uint64),
         ("fixed", C.c_int * 3), ("n_walls", C.c_int), ("walls", C.POINTER(Wall)),
+        ("n_lj_types", C.c_int), ("lj_pairs", C.POINTER(LJPair)),
     ]
 
 
@@ -245,7 +250,14 @@ def to_c_config(c: SimConfig):
         walls[k].material = int(w.material)
     cc.n_walls = len(c.walls)
     cc.walls = C.cast(walls, C.POINTER(Wall))
-    return cc, (mats, walls)
+    nt = int(c.lj_types) if c.kind == "lj" else 0
+    ljp = (LJPair * max(1, nt * nt))()
+    if nt > 1:
+        for k, (e, s, rc) in enumerate(c.lj_pairs):
+            ljp[k].epsilon, ljp[k].sigma, ljp[k].cutoff = float(e), float(s), float(rc)
+    cc.n_lj_types = nt
+    cc.lj_pairs = C.cast(ljp, C.POINTER(LJPair))
+    return cc, (mats, walls, ljp)
 
 
 def _upload_view(state):

@@ -74,6 +74,10 @@ class SimConfig:
     lj_epsilon: float = 1.0
     lj_sigma: float = 1.0
     lj_cutoff: float = 2.5
+    # [lj] multi-type mode: the number of types (0 = single type) and the
+    # row-major n x n pair table of (epsilon, sigma, cutoff) triples
+    lj_types: int = 0
+    lj_pairs: tuple = ()
     # [thermostat]
     nose_hoover: bool = False
     nh_temperature: float = 0.85
@@ -192,11 +196,31 @@ def from_toml(text: str, kind: str | None = None) -> SimConfig:
     else:
         lj = doc.get("lj", {})
         _check_keys("lj", lj, _SECTIONS["lj"])
-        if lj.get("types") or lj.get("pair_coeffs"):
-            raise ConfigError("multi-type LJ is not supported by the GPU path")
         c.lj_epsilon = float(lj.get("epsilon", 1.0))
         c.lj_sigma = float(lj.get("sigma", 1.0))
         c.lj_cutoff = float(lj.get("cutoff", 2.5))
+        if lj.get("types") is not None:
+            types = []
+            for t in lj["types"]:
+                _check_keys("lj.types", t, {"epsilon", "sigma"})
+                if "epsilon" not in t or "sigma" not in t:
+                    raise ConfigError("[[lj.types]] needs epsilon and sigma")
+                types.append((float(t["epsilon"]), float(t["sigma"])))
+            overrides = []
+            for o in lj.get("pair_coeffs") or ():
+                _check_keys("lj.pair_coeffs", o, {"types", "epsilon", "sigma", "cutoff"})
+                if "types" not in o or "epsilon" not in o or "sigma" not in o or len(o["types"]) != 2:
+                    raise ConfigError("[[lj.pair_coeffs]] needs types = [a, b], epsilon and sigma")
+                overrides.append((int(o["types"][0]), int(o["types"][1]), float(o["epsilon"]), float(o["sigma"]),
+                                  None if o.get("cutoff") is None else float(o["cutoff"])))
+            if not types:
+                raise ConfigError("[lj] types is empty")
+            table = lj_pair_table(types, c.lj_cutoff, lj.get("mixing"), overrides)
+            if len(types) == 1:
+                # one type: lj_force reads the 1 x 1 table
+                c.lj_epsilon, c.lj_sigma, c.lj_cutoff = table[0]
+            else:
+                c.lj_types, c.lj_pairs = len(types), table
         if c.dt == 0.0:
             c.dt = 0.005  # lattice_set_dt (crates/md_lattice/src/lib.rs:461-471)
         th = doc.get("thermostat")
@@ -223,6 +247,31 @@ def from_toml(text: str, kind: str | None = None) -> SimConfig:
         if k in gpu:
             setattr(c, k, gpu[k])
     return c
+
+
+def lj_pair_table(types, cutoff=2.5, mixing=None, overrides=()):
+    """The LJ pair table of build_lj_pair_table (crates/md_lj/src/lib.rs:
+    334-384) as a row-major tuple of (epsilon, sigma, cutoff) for n x n type
+    pairs: `types` is [(epsilon, sigma), ...]; cross pairs mix by
+    sqrt(e_i e_j), sqrt(s_i s_j) ("geometric", the default and any other
+    name) or by (e_i + e_j) / 2, (s_i + s_j) / 2 ("arithmetic"), all at the
+    global `cutoff` (units of sigma); then each override (a, b, epsilon,
+    sigma, cutoff or None for the global one) replaces pair (a, b) and (b, a)
+    in order, as PairCoeffTable::set does."""
+    n = len(types)
+    arith = mixing == "arithmetic"
+    tab = [[None] * n for _ in range(n)]
+    for i in range(n):
+        for j in range(i, n):
+            (ei, si), (ej, sj) = types[i], types[j]
+            eps = (ei + ej) / 2.0 if arith else math.sqrt(ei * ej)
+            sig = (si + sj) / 2.0 if arith else math.sqrt(si * sj)
+            tab[i][j] = tab[j][i] = (float(eps), float(sig), float(cutoff))
+    for a, b, eps, sig, cut in overrides:
+        if not (0 <= a < n and 0 <= b < n):
+            raise ConfigError(f"[[lj.pair_coeffs]] types = [{a}, {b}]: only {n} types")
+        tab[a][b] = tab[b][a] = (float(eps), float(sig), float(cutoff if cut is None else cut))
+    return tuple(x for row in tab for x in row)
 
 
 def rayleigh_dt(radius, density, youngs_mod, poisson_ratio, fraction=0.15):

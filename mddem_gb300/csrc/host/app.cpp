@@ -151,6 +151,18 @@ std::vector<const toml::Table*> table_array(const toml::Table& t, const std::str
     return out;
 }
 
+std::vector<double> numbers(const toml::Table* t, const std::string& key) {
+    std::vector<double> out;
+    const toml::Value* v = t ? toml::find(*t, key) : nullptr;
+    if (!v) return out;
+    if (v->kind != toml::Value::ARRAY) throw ConfigError("'" + key + "' must be an array of numbers");
+    for (const toml::Value& e : *v->a) {
+        if (!e.is_number()) throw ConfigError("'" + key + "' must be an array of numbers");
+        out.push_back(e.number());
+    }
+    return out;
+}
+
 // ---------------------------------------------------------------------------
 // core plugins
 // ---------------------------------------------------------------------------
@@ -287,6 +299,8 @@ struct GpuPlugin : Plugin {
         a.cfg.n_materials = a.dem ? (int)a.materials.size() : 0;
         a.cfg.walls = a.walls.empty() ? nullptr : a.walls.data();
         a.cfg.n_walls = (int)a.walls.size();
+        a.cfg.n_lj_types = a.dem ? 0 : a.lj_types;
+        a.cfg.lj_pairs = a.lj_pairs.empty() ? nullptr : a.lj_pairs.data();
         if (a.opts.check) {
             if (!a.opts.write_restart.empty()) write_initial_restart(a, a.opts.write_restart);
             std::printf("%s\n", config_json(a).c_str());

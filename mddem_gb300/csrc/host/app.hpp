@@ -81,6 +81,8 @@ public:
     std::vector<mdg_material> materials;
     std::vector<std::string> material_names;
     std::vector<mdg_wall> walls;
+    int lj_types = 0;                       // [lj] types: > 1 = multi-type mode
+    std::vector<mdg_lj_pair> lj_pairs;      // its n x n pair table
     HostState state;
     long long run_steps = 1000, thermo_every = 100;
     std::vector<long long> intervals;   // other output intervals (measurements)

@@ -288,8 +288,12 @@ struct LatticePlugin : Plugin {
         app.add_setup_system(Schedule::PostSetup, [](App& a) {
             const toml::Table* lat = section(a, "lattice");
             if (!lat || text(lat, "style", "fcc") != "fcc") throw ConfigError("an LJ config needs [lattice] style = \"fcc\"");
+            check_keys("lattice", *lat,
+                       {"style", "density", "temperature", "mass", "skin", "type_fractions", "type_masses"});
             const double rho = num(lat, "density", 0.85), T = num(lat, "temperature", 0.85);
             const double mass = num(lat, "mass", 1.0), skin = num(lat, "skin", 1.25);
+            std::vector<double> fractions = numbers(lat, "type_fractions"), tmass = numbers(lat, "type_masses");
+            if (fractions.empty()) fractions.push_back(1.0);
             const double L = a.cfg.box_hi[0] - a.cfg.box_lo[0], lo = a.cfg.box_lo[0];
             const int nc = (int)std::floor(L / std::pow(4.0 / rho, 1.0 / 3.0));
             if (nc < 1) throw ConfigError("[lattice] density leaves no FCC cell in the box");
@@ -299,20 +303,35 @@ struct LatticePlugin : Plugin {
             h = HostState{};
             h.dem = false;
             std::mt19937_64 gen(a.opts.seed);
-            std::normal_distribution<double> nd(0.0, std::sqrt(T / mass));
+            std::normal_distribution<double> nd(0.0, std::sqrt(T / mass)), n01(0.0, 1.0);
+            // types by index (fcc_insert, md_lattice/src/lib.rs:291-327): the
+            // first cumulative fraction above (k + 0.5) / n, else the last type
+            const size_t total = (size_t)4 * nc * nc * nc;
             for (int ix = 0; ix < nc; ix++)
                 for (int iy = 0; iy < nc; iy++)
                     for (int iz = 0; iz < nc; iz++)
                         for (int b = 0; b < 4; b++) {
+                            const double f = ((double)h.tag.size() + 0.5) / (double)total;
+                            uint32_t t = (uint32_t)fractions.size() - 1;
+                            for (size_t q = 0; q < fractions.size(); q++)
+                                if (f < fractions[q]) {
+                                    t = (uint32_t)q;
+                                    break;
+                                }
+                            const double m = tmass.empty() ? mass : (t < tmass.size() ? tmass[t] : mass);
+                            if (!(m > 0.0)) throw ConfigError("[lattice] masses must be positive");
                             h.tag.push_back((uint32_t)h.tag.size());
-                            h.type.push_back(0);
+                            h.type.push_back(t);
                             h.pos.push_back(lo + (ix + basis[b][0]) * ax);
                             h.pos.push_back(lo + (iy + basis[b][1]) * ax);
                             h.pos.push_back(lo + (iz + basis[b][2]) * ax);
-                            for (int d = 0; d < 3; d++) h.vel.push_back(nd(gen));
-                            h.mass.push_back(mass);
+                            for (int d = 0; d < 3; d++)
+                                h.vel.push_back(tmass.empty() ? nd(gen) : n01(gen) * std::sqrt(T / m));
+                            h.mass.push_back(m);
                             h.cutoff_radius.push_back(skin);
                         }
+            if (a.lj_types > 1 && (int)fractions.size() > a.lj_types)
+                throw ConfigError("[lattice] type_fractions give more types than [lj] types");
             const size_t n = h.size();
             double vs[3] = {0, 0, 0};
             for (size_t i = 0; i < n; i++)
@@ -321,8 +340,8 @@ struct LatticePlugin : Plugin {
                 for (int d = 0; d < 3; d++) h.vel[3 * i + d] -= vs[d] / (double)n;
             double ke = 0.0;
             for (size_t i = 0; i < n; i++)
-                ke += mass * (h.vel[3 * i] * h.vel[3 * i] + h.vel[3 * i + 1] * h.vel[3 * i + 1] +
-                              h.vel[3 * i + 2] * h.vel[3 * i + 2]);
+                ke += h.mass[i] * (h.vel[3 * i] * h.vel[3 * i] + h.vel[3 * i + 1] * h.vel[3 * i + 1] +
+                                   h.vel[3 * i + 2] * h.vel[3 * i + 2]);
             const double cur = ke / (3.0 * (double)n - 3.0);
             if (cur > 1e-20)
                 for (double& v : h.vel) v *= std::sqrt(T / cur);
@@ -331,21 +350,64 @@ struct LatticePlugin : Plugin {
     }
 };
 
-// LJForcePlugin: [lj] one type (crates/md_lj/src/lib.rs:115-140).
+// LJForcePlugin: [lj] (LJConfig, crates/md_lj/src/lib.rs:115-184) and
+// build_lj_pair_table (lib.rs:334-384): one type from epsilon / sigma, or
+// with [[lj.types]] the n x n table, cross pairs by the mixing rule
+// (arithmetic means for "arithmetic", else geometric) at the global cutoff,
+// then the [[lj.pair_coeffs]] overrides set (a, b) and (b, a) in order.
 struct LJForcePlugin : Plugin {
     std::string name() const override { return "LJForcePlugin"; }
     std::vector<std::string> requires_() const override { return {"neighbor_list"}; }
     void build(App& app) override {
         app.add_setup_system(Schedule::Setup, [](App& a) {
             const toml::Table* lj = section(a, "lj");
-            if (lj) {
-                check_keys("lj", *lj, {"epsilon", "sigma", "cutoff", "mixing", "types", "pair_coeffs"});
-                if (toml::find(*lj, "types") || toml::find(*lj, "pair_coeffs"))
-                    throw ConfigError("multi-type LJ is not supported by the GPU path");
-            }
+            if (lj) check_keys("lj", *lj, {"epsilon", "sigma", "cutoff", "mixing", "types", "pair_coeffs"});
             a.cfg.lj_epsilon = num(lj, "epsilon", 1.0);
             a.cfg.lj_sigma = num(lj, "sigma", 1.0);
             a.cfg.lj_cutoff = num(lj, "cutoff", 2.5);
+            if (!lj || !toml::find(*lj, "types")) return;
+            std::vector<std::pair<double, double>> types;
+            for (const toml::Table* t : table_array(*lj, "types")) {
+                check_keys("lj.types", *t, {"epsilon", "sigma"});
+                if (!toml::find(*t, "epsilon") || !toml::find(*t, "sigma"))
+                    throw ConfigError("[[lj.types]] needs epsilon and sigma");
+                types.emplace_back(num(t, "epsilon", 0.0), num(t, "sigma", 0.0));
+            }
+            if (types.empty()) throw ConfigError("[lj] types is empty");
+            const toml::Value* mix = toml::find(*lj, "mixing");
+            const bool arith = mix && mix->kind == toml::Value::STRING && mix->s == "arithmetic";
+            const size_t n = types.size();
+            const double cut = a.cfg.lj_cutoff;
+            std::vector<mdg_lj_pair> tab(n * n);
+            for (size_t i = 0; i < n; i++)
+                for (size_t j = i; j < n; j++) {
+                    const double ei = types[i].first, si = types[i].second;
+                    const double ej = types[j].first, sj = types[j].second;
+                    const double eps = arith ? (ei + ej) / 2.0 : std::sqrt(ei * ej);
+                    const double sig = arith ? (si + sj) / 2.0 : std::sqrt(si * sj);
+                    tab[i * n + j] = tab[j * n + i] = mdg_lj_pair{eps, sig, cut};
+                }
+            for (const toml::Table* o : table_array(*lj, "pair_coeffs")) {
+                check_keys("lj.pair_coeffs", *o, {"types", "epsilon", "sigma", "cutoff"});
+                const toml::Value* tv = toml::find(*o, "types");
+                if (!tv || tv->kind != toml::Value::ARRAY || tv->array().size() != 2 || !toml::find(*o, "epsilon") ||
+                    !toml::find(*o, "sigma"))
+                    throw ConfigError("[[lj.pair_coeffs]] needs types = [a, b], epsilon and sigma");
+                const long long ta = tv->array()[0].integer(), tb = tv->array()[1].integer();
+                if (ta < 0 || tb < 0 || ta >= (long long)n || tb >= (long long)n)
+                    throw ConfigError("[[lj.pair_coeffs]] types = [" + std::to_string(ta) + ", " + std::to_string(tb) +
+                                      "]: only " + std::to_string(n) + " types");
+                const mdg_lj_pair q{num(o, "epsilon", 0.0), num(o, "sigma", 0.0), num(o, "cutoff", cut)};
+                tab[(size_t)ta * n + (size_t)tb] = tab[(size_t)tb * n + (size_t)ta] = q;
+            }
+            if (n == 1) {  // one type: lj_force reads the 1 x 1 table
+                a.cfg.lj_epsilon = tab[0].epsilon;
+                a.cfg.lj_sigma = tab[0].sigma;
+                a.cfg.lj_cutoff = tab[0].cutoff;
+            } else {
+                a.lj_types = (int)n;
+                a.lj_pairs = tab;
+            }
         });
     }
 };
@@ -676,7 +738,12 @@ std::string config_json(const App& a) {
     o << ", \"lv_damping\": ";
     json_num(o, c.lv_damping);
     o << ", \"lv_seed\": " << c.lv_seed << ", \"fixed\": [" << c.fixed[0] << ", " << c.fixed[1] << ", " << c.fixed[2]
-      << "], \"walls\": [";
+      << "], \"n_lj_types\": " << c.n_lj_types << ", \"lj_pairs\": [";
+    for (int k = 0; c.lj_pairs && k < c.n_lj_types * c.n_lj_types; k++) {
+        if (k) o << ", ";
+        json_vec(o, &c.lj_pairs[k].epsilon, 3);
+    }
+    o << "], \"walls\": [";
     for (int k = 0; k < c.n_walls; k++) {
         const mdg_wall& w = c.walls[k];
         if (k) o << ", ";
@@ -694,7 +761,9 @@ std::string config_json(const App& a) {
     }
     const HostState& h = a.state;
     double ps[3] = {0, 0, 0}, rs = 0.0, ms = 0.0;
+    long long ts = 0;
     for (size_t i = 0; i < h.size(); i++) {
+        ts += h.type[i];
         for (int d = 0; d < 3; d++) ps[d] += h.pos[3 * i + d];
         ms += h.mass[i];
         if (h.dem) rs += h.radius[i];
@@ -706,6 +775,7 @@ std::string config_json(const App& a) {
     json_num(o, rs);
     o << ", \"mass_sum\": ";
     json_num(o, ms);
+    o << ", \"type_sum\": " << ts;
     o << "}";
     return o.str();
 }

@@ -18,6 +18,8 @@ long long integer(const toml::Table* t, const std::string& key, long long dflt);
 bool boolean(const toml::Table* t, const std::string& key, bool dflt);
 std::string text(const toml::Table* t, const std::string& key, const std::string& dflt);
 std::vector<const toml::Table*> table_array(const toml::Table& t, const std::string& key);
+// A number array (absent = empty).
+std::vector<double> numbers(const toml::Table* t, const std::string& key);
 
 // The device context and the upload (PostSetup, after the state plugins).
 void add_device_context(App& app);

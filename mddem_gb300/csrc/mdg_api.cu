@@ -95,7 +95,22 @@ int validate_config(const mdg_config& c) {
             for (int k = 0; k < c.n_materials; k++)
                 if (!(c.materials[k].kn > 0.0)) return MDG_ERR_CONFIG;
         }
+    } else if (c.n_lj_types > 1) {
+        // the pair table replaces the single type; it must be symmetric, as
+        // PairCoeffTable::set makes it (mddem_core/src/pair_coeff.rs:37-41)
+        if (!c.lj_pairs) return MDG_ERR_CONFIG;
+        const int nt = c.n_lj_types;
+        for (int a = 0; a < nt; a++)
+            for (int b = 0; b < nt; b++) {
+                const mdg_lj_pair& q = c.lj_pairs[a * nt + b];
+                const mdg_lj_pair& r = c.lj_pairs[b * nt + a];
+                if (!(q.epsilon >= 0.0) || !(q.sigma > 0.0) || !(q.cutoff > 0.0) || !std::isfinite(q.epsilon) ||
+                    !std::isfinite(q.sigma) || !std::isfinite(q.cutoff))
+                    return MDG_ERR_CONFIG;
+                if (q.epsilon != r.epsilon || q.sigma != r.sigma || q.cutoff != r.cutoff) return MDG_ERR_CONFIG;
+            }
     } else {
+        if (c.n_lj_types < 0) return MDG_ERR_CONFIG;
         if (!(c.lj_epsilon > 0.0) || !(c.lj_sigma > 0.0) || !(c.lj_cutoff > 0.0)) return MDG_ERR_CONFIG;
     }
     if (c.nose_hoover && (!(c.nh_temperature > 0.0) || !(c.nh_coupling > 0.0))) return MDG_ERR_CONFIG;
@@ -123,6 +138,8 @@ struct mdg_ctx {
     int nsys = 0;
     std::vector<mdg_config> cfg;
     std::vector<std::vector<mdg_material>> mats;
+    std::vector<std::vector<mdg_lj_pair>> ljp;  // per system: the LJ pair table (1 x 1 for one type)
+    std::vector<int> ljn;                       // its number of types
     std::vector<SysParams> sp;
     std::vector<size_t> capacity;
     std::vector<int> uploaded;
@@ -259,21 +276,50 @@ void apply_physics(mdg_ctx* c, int s, const mdg_config& k, std::vector<double>& 
         for (int m = 0; m < k.n_materials; m++) pull = pull || k.materials[m].surface_energy > 0.0;
         p.touch_only = (k.contact_model == 1 || k.adhesion_model == 1 || !pull) ? 1 : 0;
     } else {
-        // LJPairCoeffs::from_params (crates/md_lj/src/lib.rs:230-239)
-        const double s2 = k.lj_sigma * k.lj_sigma;
-        const double sigma6 = s2 * s2 * s2;
-        p.lj1 = 48.0 * k.lj_epsilon * sigma6 * sigma6;
-        p.lj2 = 24.0 * k.lj_epsilon * sigma6;
-        p.lj3 = 4.0 * k.lj_epsilon * sigma6 * sigma6;
-        p.lj4 = 4.0 * k.lj_epsilon * sigma6;
-        const double rc = k.lj_cutoff * k.lj_sigma;
-        p.lj_cut2 = rc * rc;
+        // the pair table (build_lj_pair_table, crates/md_lj/src/lib.rs:334-384):
+        // n x n from the config, or 1 x 1 from the single type
+        const int nt = k.n_lj_types > 1 ? k.n_lj_types : 1;
+        if (nt > 1)
+            c->ljp[s].assign(k.lj_pairs, k.lj_pairs + (size_t)nt * nt);
+        else
+            c->ljp[s].assign(1, mdg_lj_pair{k.lj_epsilon, k.lj_sigma, k.lj_cutoff});
+        c->ljn[s] = nt;
+        c->cfg[s].lj_pairs = nt > 1 ? c->ljp[s].data() : nullptr;
+        // LJPairCoeffs::from_params (crates/md_lj/src/lib.rs:230-239), plus
+        // 4 eps sigma^12 and 4 eps sigma^6 for the energy
+        auto coeffs = [](const mdg_lj_pair& q, double* o) {
+            const double s2 = q.sigma * q.sigma;
+            const double sigma6 = s2 * s2 * s2;
+            o[TL_LJ1] = 48.0 * q.epsilon * sigma6 * sigma6;
+            o[TL_LJ2] = 24.0 * q.epsilon * sigma6;
+            o[TL_LJ3] = 4.0 * q.epsilon * sigma6 * sigma6;
+            o[TL_LJ4] = 4.0 * q.epsilon * sigma6;
+            const double rc = q.cutoff * q.sigma;
+            o[TL_CUT2] = rc * rc;
+        };
+        double o[NTAB_LJ];
+        coeffs(c->ljp[s][0], o);
+        p.lj1 = o[TL_LJ1];
+        p.lj2 = o[TL_LJ2];
+        p.lj3 = o[TL_LJ3];
+        p.lj4 = o[TL_LJ4];
+        p.lj_cut2 = o[TL_CUT2];
         p.lj1f = (float)p.lj1;
         p.lj2f = (float)p.lj2;
         p.lj3f = (float)p.lj3;
         p.lj4f = (float)p.lj4;
         p.lj_cut2f = (float)p.lj_cut2;
-        p.nmat = 1;
+        p.nmat = nt;
+        if (nt > 1) {
+            tabs.assign((size_t)NTAB_LJ * nt * nt, 0.0);
+            for (int a = 0; a < nt; a++)
+                for (int b = 0; b < nt; b++) {
+                    coeffs(c->ljp[s][(size_t)a * nt + b], o);
+                    for (int t = 0; t < NTAB_LJ; t++) tabs[((size_t)t * nt + a) * nt + b] = o[t];
+                }
+            if (!c->d.lj_multi) c->drop_graphs();  // the force launch changes instantiation
+            c->d.lj_multi = 1;
+        }
     }
 }
 
@@ -795,6 +841,8 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     c->nsys = nsys;
     c->cfg.assign(cfgs, cfgs + nsys);
     c->mats.resize(nsys);
+    c->ljp.resize(nsys);
+    c->ljn.assign(nsys, 1);
     c->sp.assign(nsys, SysParams{});
     c->capacity.assign(capacity, capacity + nsys);
     c->uploaded.assign(nsys, 0);
@@ -836,8 +884,11 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
             hist_entries += (long long)p.hcap * p.npad;
         } else {
             c->has_lj = true;
-            p.matcap = 0;
-            p.mat0 = 0;
+            // pair-table slots: the config's types, at least 4 (a reconfigured
+            // or served system may bring more types than its first config)
+            p.matcap = std::max(k.n_lj_types, 4);
+            p.mat0 = (long long)mat_all.size();
+            mat_all.resize(mat_all.size() + (size_t)NTAB_LJ * p.matcap * p.matcap, 0.0);
             p.hcap = 0;
         }
         if (k.virial) c->any_virial = true;
@@ -964,6 +1015,7 @@ int mdg_configure_system(mdg_ctx* c, int sys, const mdg_config* cfg) {
     SysParams& p = c->sp[sys];
     if (cfg->kind != p.kind || cfg->precision != p.precision) return MDG_ERR_CONFIG;
     if (cfg->kind == MDG_KIND_DEM && cfg->n_materials > p.matcap) return MDG_ERR_CONFIG;
+    if (cfg->kind == MDG_KIND_LJ && cfg->n_lj_types > p.matcap) return MDG_ERR_CONFIG;
     if (cfg->virial && !c->d.vir) return MDG_ERR_CONFIG;
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_err(e);
@@ -1004,6 +1056,9 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
             if (!std::isfinite(st->pos[3 * i + q]) || !std::isfinite(st->vel[3 * i + q])) return MDG_ERR_NAN;
         if (!(st->mass[i] > 0.0) || !(st->cutoff_radius[i] > 0.0)) return MDG_ERR_ARG;
         if (st->type && k.kind == MDG_KIND_DEM && (int)st->type[i] >= k.n_materials) return MDG_ERR_ARG;
+        // multi-type LJ: the type indexes the pair table
+        if (k.kind == MDG_KIND_LJ && c->ljn[sys] > 1 && (!st->type || st->type[i] >= (uint32_t)c->ljn[sys]))
+            return MDG_ERR_ARG;
     }
     int r = setup_grid(k, st->cutoff_radius, n, p);
     if (r) return r;
@@ -1490,20 +1545,30 @@ int mdg_thermo(mdg_ctx* c, int sys, mdg_thermo_t* out) {
     out->rot_temp = t[6];
     out->e_tail = out->p_tail = 0.0;
     if (p.kind == MDG_KIND_LJ) {
-        // setup_lj_tails (md_lj/src/lib.rs:397-445), one type: rho = N / V,
-        // V = the product of the box sides, rc = sqrt((cutoff sigma)^2)
-        const mdg_config& k = c->cfg[sys];
+        // setup_lj_tails (md_lj/src/lib.rs:397-445): rho = N / V, V = the
+        // product of the box sides; per type pair rc = sqrt((cutoff sigma)^2),
+        // weighted by (1 / ntypes)^2 (an equimolar mixture), in table order
+        const int nt = c->ljn[sys];
         const double n = (double)p.n;
         const double rho = n / (p.L[0] * p.L[1] * p.L[2]);
-        const double cs = k.lj_cutoff * k.lj_sigma;
-        const double rc = std::sqrt(cs * cs);
-        const double sigma3 = (k.lj_sigma * k.lj_sigma) * k.lj_sigma;
-        const double rc3 = (rc * rc) * rc, rc9 = (rc3 * rc3) * rc3;
-        const double sigma9 = (sigma3 * sigma3) * sigma3;
+        const double frac = 1.0 / (double)nt;
+        const double w = frac * frac;
         const double pi = 3.141592653589793;
-        out->e_tail = (8.0 / 3.0) * pi * n * rho * k.lj_epsilon * sigma3 * (sigma9 / (3.0 * rc9) - sigma3 / rc3);
-        out->p_tail =
-            (16.0 / 3.0) * pi * rho * rho * k.lj_epsilon * sigma3 * (2.0 * sigma9 / (3.0 * rc9) - sigma3 / rc3);
+        double e_tail = 0.0, p_tail = 0.0;
+        for (int a = 0; a < nt; a++)
+            for (int b = 0; b < nt; b++) {
+                const mdg_lj_pair& q = c->ljp[sys][(size_t)a * nt + b];
+                const double cs = q.cutoff * q.sigma;
+                const double rc = std::sqrt(cs * cs);
+                const double sigma3 = (q.sigma * q.sigma) * q.sigma;
+                const double rc3 = (rc * rc) * rc, rc9 = (rc3 * rc3) * rc3;
+                const double sigma9 = (sigma3 * sigma3) * sigma3;
+                e_tail += w * (8.0 / 3.0) * pi * n * rho * q.epsilon * sigma3 * (sigma9 / (3.0 * rc9) - sigma3 / rc3);
+                p_tail += w * (16.0 / 3.0) * pi * rho * rho * q.epsilon * sigma3 *
+                          (2.0 * sigma9 / (3.0 * rc9) - sigma3 / rc3);
+            }
+        out->e_tail = e_tail;
+        out->p_tail = p_tail;
     }
     {
         // compute_pressure (md_measure/src/lib.rs:605-652): rho T - tr(W) / (3V) + P_tail

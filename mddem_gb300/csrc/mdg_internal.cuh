@@ -24,6 +24,10 @@ constexpr int BLK = 128;               // particles per block (segment padding u
 constexpr int IDX_BITS = 26;
 constexpr uint32_t IDX_MASK = (1u << IDX_BITS) - 1u;
 constexpr int NTAB = 14;               // material pair tables
+// LJ multi-type pair tables (build_lj_pair_table, md_lj/src/lib.rs:334-384),
+// packed in an LJ system's slot of the material tables with the same layout:
+// entry (tab, a, b) at mat0 + (tab * nmat + a) * nmat + b
+enum { TL_LJ1 = 0, TL_LJ2, TL_LJ3, TL_LJ4, TL_CUT2, NTAB_LJ };
 constexpr int THERMO_W = 24;           // doubles per system in the thermo record
 
 // device status bits (sticky per system)
@@ -219,6 +223,7 @@ struct Dev {
     int nblocks;
     long long P;       // total padded particles
     int hist_any;      // history arrays allocated
+    int lj_multi;      // some LJ system has a multi-type pair table (nmat > 1)
     // graph mode: k_initial's last block sets this IF-node condition to
     // "some system rebuilds (or sorts) this step"; 0 = no conditional
     unsigned long long cond;

@@ -1148,9 +1148,12 @@ __global__ void __launch_bounds__(BUILD_WARPS * 32, MDG_BUILD_MINB) k_build(Dev 
 
 // ----------------------------------------------------------------------------
 // LJ 12-6 force (lj_force, md_lj/src/lib.rs:488-633) over the full list.
-// TPP lanes share one particle's row and combine with warp shuffles.
+// TPP lanes share one particle's row and combine with warp shuffles.  MT:
+// systems with a multi-type pair table look up lj1, lj2 and the squared
+// cutoff by the two particles' types (pair_table.get(ti, tj)); a separate
+// instantiation, so the single-type path keeps its code.
 // ----------------------------------------------------------------------------
-template <int TPP>
+template <int TPP, bool MT>
 __global__ void __launch_bounds__(BLK) k_lj_fp64(Dev d) {
     const int pb = d.blk_run[blockIdx.x / TPP];
     const int sub = blockIdx.x % TPP;
@@ -1167,11 +1170,20 @@ __global__ void __launch_bounds__(BLK) k_lj_fp64(Dev d) {
         const double4 xi = d.pos[i];
         const int nn = d.nnum[i];
         const long long base = sp.lst0 + li;
-        const double lj1 = sp.lj1, lj2 = sp.lj2, cut2 = sp.lj_cut2;
+        double lj1 = sp.lj1, lj2 = sp.lj2, cut2 = sp.lj_cut2;
         const double half = sp.newton ? 1.0 : 0.5;
+        const bool mt = MT && sp.nmat > 1;
+        const long long tq = (long long)sp.nmat * sp.nmat;
+        const long long trow = mt ? sp.mat0 + (long long)d.type[i] * sp.nmat : 0;
         for (int k = lane; k < nn; k += TPP) {
             const uint32_t e = d.nlist[base + (long long)k * sp.npad];
             const long long j = sp.p0 + (e & IDX_MASK);
+            if (MT && mt) {
+                const long long o = trow + d.type[j];
+                lj1 = d.mat[o + TL_LJ1 * tq];
+                lj2 = d.mat[o + TL_LJ2 * tq];
+                cut2 = d.mat[o + TL_CUT2 * tq];
+            }
             const uint32_t code = e >> IDX_BITS;
             const bool own = code >= 27u;
             int sx, sy, sz;
@@ -1752,6 +1764,9 @@ __global__ void __launch_bounds__(BLK) k_lj_pe(Dev d) {
     const double4 xi = d.pos[i];
     const int nn = d.nnum[i];
     const long long base = sp.lst0 + li;
+    const bool mt = sp.nmat > 1;  // multi-type pair table
+    const long long tq = (long long)sp.nmat * sp.nmat;
+    const long long trow = mt ? sp.mat0 + (long long)d.type[i] * sp.nmat : 0;
     double pe = 0.0;
     for (int k = 0; k < nn; k++) {
         const uint32_t e = d.nlist[base + (long long)k * sp.npad];
@@ -1759,15 +1774,23 @@ __global__ void __launch_bounds__(BLK) k_lj_pe(Dev d) {
         if (code < 27u) continue;
         int sx, sy, sz;
         decode_shift((int)(code - 27u), sx, sy, sz);
-        const double4 xj = d.pos[sp.p0 + (e & IDX_MASK)];
+        const long long j = sp.p0 + (e & IDX_MASK);
+        const double4 xj = d.pos[j];
         const double dx = img_coord(xj.x, sx, sp.L[0]) - xi.x;
         const double dy = img_coord(xj.y, sy, sp.L[1]) - xi.y;
         const double dz = img_coord(xj.z, sz, sp.L[2]) - xi.z;
         const double r2 = fma(dx, dx, fma(dy, dy, dz * dz));
-        if (r2 >= sp.lj_cut2) continue;
+        double lj3 = sp.lj3, lj4 = sp.lj4, cut2 = sp.lj_cut2;
+        if (mt) {
+            const long long o = trow + d.type[j];
+            lj3 = d.mat[o + TL_LJ3 * tq];
+            lj4 = d.mat[o + TL_LJ4 * tq];
+            cut2 = d.mat[o + TL_CUT2 * tq];
+        }
+        if (r2 >= cut2) continue;
         const double r2inv = 1.0 / r2;
         const double r6inv = r2inv * r2inv * r2inv;
-        pe += r6inv * (sp.lj3 * r6inv - sp.lj4) * (sp.newton ? 1.0 : 0.5);
+        pe += r6inv * (lj3 * r6inv - lj4) * (sp.newton ? 1.0 : 0.5);
     }
     d.frc[i].w = pe;
 }
@@ -1805,11 +1828,20 @@ int launch_rebuild(const Dev& d, cudaStream_t st) {
 int launch_force_fp64(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st) {
     int n = 0;
     if (has_lj) {
-        switch (tpp) {
-            case 2: k_lj_fp64<2><<<d.nrun * 2, BLK, 0, st>>>(d); break;
-            case 4: k_lj_fp64<4><<<d.nrun * 4, BLK, 0, st>>>(d); break;
-            case 8: k_lj_fp64<8><<<d.nrun * 8, BLK, 0, st>>>(d); break;
-            default: k_lj_fp64<1><<<d.nrun, BLK, 0, st>>>(d); break;
+        if (d.lj_multi) {
+            switch (tpp) {
+                case 2: k_lj_fp64<2, true><<<d.nrun * 2, BLK, 0, st>>>(d); break;
+                case 4: k_lj_fp64<4, true><<<d.nrun * 4, BLK, 0, st>>>(d); break;
+                case 8: k_lj_fp64<8, true><<<d.nrun * 8, BLK, 0, st>>>(d); break;
+                default: k_lj_fp64<1, true><<<d.nrun, BLK, 0, st>>>(d); break;
+            }
+        } else {
+            switch (tpp) {
+                case 2: k_lj_fp64<2, false><<<d.nrun * 2, BLK, 0, st>>>(d); break;
+                case 4: k_lj_fp64<4, false><<<d.nrun * 4, BLK, 0, st>>>(d); break;
+                case 8: k_lj_fp64<8, false><<<d.nrun * 8, BLK, 0, st>>>(d); break;
+                default: k_lj_fp64<1, false><<<d.nrun, BLK, 0, st>>>(d); break;
+            }
         }
         n++;
     }

@@ -38,8 +38,10 @@ struct Kahan {
 // VIR: systems with `virial` also write their per-particle virial (the
 // owner-entry sum of d_a f_b, VirialStress::add_pair, virial.rs:61-68; fp32
 // per lane, summed in fp64 at the thermo query); a separate instantiation so
-// the common path keeps its registers.
-template <int TPP, bool VIR>
+// the common path keeps its registers.  MT: systems with a multi-type pair
+// table gather the partner's type and look up lj1, lj2 and the squared cutoff
+// (pair_table.get(ti, tj), fp32 copies); also its own instantiation.
+template <int TPP, bool VIR, bool MT>
 __global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
     const int pb = d.blk_run[blockIdx.x / TPP];
     const int sub = blockIdx.x % TPP;
@@ -57,8 +59,11 @@ __global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
         const uint4 ui = d.posu[i];
         const int nn = d.nnum[i];
         const long long base = sp.lst0 + li;
-        const float lj1 = sp.lj1f, lj2 = sp.lj2f;
-        const float cut2 = sp.lj_cut2f;
+        const float lj1_ = sp.lj1f, lj2_ = sp.lj2f;
+        const float cut2_ = sp.lj_cut2f;
+        const bool mt = MT && sp.nmat > 1;
+        const long long tq = (long long)sp.nmat * sp.nmat;
+        const long long trow = mt ? sp.mat0 + (long long)d.type[i] * sp.nmat : 0;
         const float s0 = sp.uscale[0], s1 = sp.uscale[1], s2 = sp.uscale[2];
         // U entries in flight per lane: list loads first, then the gathers, then
         // the arithmetic, so each lane keeps U independent load chains open
@@ -66,6 +71,7 @@ __global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
         for (int k0 = lane; k0 < nn; k0 += U * TPP) {
             uint32_t e[U];
             uint4 uj[U];
+            uint32_t tj[U];
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const int k = k0 + u * TPP;
@@ -75,6 +81,7 @@ __global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
             for (int u = 0; u < U; u++) {
                 const long long j = sp.p0 + (e[u] != 0xffffffffu ? (e[u] & IDX_MASK) : 0u);
                 uj[u] = __ldg(d.posu + j);
+                if (MT && mt) tj[u] = __ldg(d.type + j);
             }
 #pragma unroll
             for (int u = 0; u < U; u++) {
@@ -85,6 +92,13 @@ __global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
                 const float dy = (float)(int)(uj[u].y - ui.y) * s1;
                 const float dz = (float)(int)(uj[u].z - ui.z) * s2;
                 const float r2 = dx * dx + dy * dy + dz * dz;
+                float lj1 = lj1_, lj2 = lj2_, cut2 = cut2_;
+                if (MT && mt) {
+                    const long long o = trow + tj[u];
+                    lj1 = __ldg(d.matf + o + TL_LJ1 * tq);
+                    lj2 = __ldg(d.matf + o + TL_LJ2 * tq);
+                    cut2 = __ldg(d.matf + o + TL_CUT2 * tq);
+                }
                 if (r2 >= cut2) continue;
                 const float r2inv = __frcp_rn(r2);
                 const float r6inv = r2inv * r2inv * r2inv;
@@ -901,6 +915,16 @@ int launch_initial_mixed(const Dev& d, cudaStream_t st, int nh_only, const long 
     return 1;
 }
 
+template <bool VIR, bool MT>
+void launch_lj_mixed(const Dev& d, int tpp, cudaStream_t st) {
+    switch (tpp) {
+        case 2: k_lj_mixed<2, VIR, MT><<<d.nrun * 2, BLK, 0, st>>>(d); break;
+        case 4: k_lj_mixed<4, VIR, MT><<<d.nrun * 4, BLK, 0, st>>>(d); break;
+        case 8: k_lj_mixed<8, VIR, MT><<<d.nrun * 8, BLK, 0, st>>>(d); break;
+        default: k_lj_mixed<1, VIR, MT><<<d.nrun, BLK, 0, st>>>(d); break;
+    }
+}
+
 int launch_force_mixed(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st) {
     int n = 0;
     if (has_dem) {
@@ -908,20 +932,15 @@ int launch_force_mixed(const Dev& d, int has_lj, int has_dem, int tpp, cudaStrea
         n++;
     }
     if (has_lj) {
-        if (d.vir) {  // some system asks for its virial
-            switch (tpp) {
-                case 2: k_lj_mixed<2, true><<<d.nrun * 2, BLK, 0, st>>>(d); break;
-                case 4: k_lj_mixed<4, true><<<d.nrun * 4, BLK, 0, st>>>(d); break;
-                case 8: k_lj_mixed<8, true><<<d.nrun * 8, BLK, 0, st>>>(d); break;
-                default: k_lj_mixed<1, true><<<d.nrun, BLK, 0, st>>>(d); break;
-            }
+        if (d.lj_multi) {  // some system has a multi-type pair table
+            if (d.vir)
+                launch_lj_mixed<true, true>(d, tpp, st);
+            else
+                launch_lj_mixed<false, true>(d, tpp, st);
+        } else if (d.vir) {  // some system asks for its virial
+            launch_lj_mixed<true, false>(d, tpp, st);
         } else {
-            switch (tpp) {
-                case 2: k_lj_mixed<2, false><<<d.nrun * 2, BLK, 0, st>>>(d); break;
-                case 4: k_lj_mixed<4, false><<<d.nrun * 4, BLK, 0, st>>>(d); break;
-                case 8: k_lj_mixed<8, false><<<d.nrun * 8, BLK, 0, st>>>(d); break;
-                default: k_lj_mixed<1, false><<<d.nrun, BLK, 0, st>>>(d); break;
-            }
+            launch_lj_mixed<false, false>(d, tpp, st);
         }
         n++;
     }

@@ -93,7 +93,10 @@ struct HostState {
 struct Job {
     int64_t id = 0;
     mdg_config cfg{};
+    // owned copies of the arrays cfg points at (the caller's may be gone by admission)
     std::vector<mdg_material> mats;
+    std::vector<mdg_wall> walls;
+    std::vector<mdg_lj_pair> ljp;
     HostState state;
     int64_t steps = 0;
     int64_t left = 0;  // steps still to run while resident
@@ -175,6 +178,14 @@ int mdg_server_submit(mdg_server* s, const mdg_config* cfg, const mdg_state_view
     if (cfg->kind == MDG_KIND_DEM && cfg->materials && cfg->n_materials > 0) {
         j->mats.assign(cfg->materials, cfg->materials + cfg->n_materials);
         j->cfg.materials = j->mats.data();
+    }
+    if (cfg->walls && cfg->n_walls > 0 && cfg->n_walls <= MDG_MAX_WALLS) {
+        j->walls.assign(cfg->walls, cfg->walls + cfg->n_walls);
+        j->cfg.walls = j->walls.data();
+    }
+    if (cfg->kind == MDG_KIND_LJ && cfg->lj_pairs && cfg->n_lj_types > 1) {
+        j->ljp.assign(cfg->lj_pairs, cfg->lj_pairs + (size_t)cfg->n_lj_types * cfg->n_lj_types);
+        j->cfg.lj_pairs = j->ljp.data();
     }
     j->state.take(*st, cfg->kind == MDG_KIND_DEM);
     j->steps = steps;

@@ -170,13 +170,33 @@ def two_sphere_rebound(radius=1e-3, speed=1.0, gap_frac=0.1, box_factor=12.0, de
     return st
 
 
-def lj_fcc(n_cells=6, box=10.06, density=0.85, temperature=0.85, mass=1.0, skin=1.25, seed=0, lo=0.0):
+def lattice_types(n, type_fractions=None):
+    """Atom types of fcc_insert's deterministic assignment
+    (crates/md_lattice/src/lib.rs:291-327): atom k of n takes the first type
+    whose cumulative fraction exceeds (k + 0.5) / n, else the last type."""
+    fr = list(type_fractions) if type_fractions else [1.0]
+    out = np.empty(n, np.uint32)
+    for k in range(n):
+        f = (k + 0.5) / n
+        t = len(fr) - 1
+        for q, thr in enumerate(fr):
+            if f < thr:
+                t = q
+                break
+        out[k] = t
+    return out
+
+
+def lj_fcc(n_cells=6, box=10.06, density=0.85, temperature=0.85, mass=1.0, skin=1.25, seed=0, lo=0.0,
+           type_fractions=None, type_masses=None):
     """FCC lattice with Gaussian velocities, restating ``fcc_insert``
     (``crates/md_lattice/src/lib.rs:232-454``): lattice constant from
     ``(4/rho)^(1/3)``, unit cells stretched to tile the box, 4-atom basis in
     (ix, iy, iz, basis) order, velocities N(0, sqrt(T/m)) per component, COM
     velocity removed, then rescaled to exactly T with 3N-3 degrees of freedom.
-    ``n_cells`` must equal floor(box / a_ideal)."""
+    ``n_cells`` must equal floor(box / a_ideal).  ``type_fractions``
+    (cumulative) and ``type_masses`` give the multi-type lattice: types by
+    lattice_types, each atom's mass from its type (``mass`` past the list)."""
     a_ideal = (4.0 / density) ** (1.0 / 3.0)
     nx = int(math.floor(box / a_ideal))
     if nx != n_cells:
@@ -189,22 +209,29 @@ def lj_fcc(n_cells=6, box=10.06, density=0.85, temperature=0.85, mass=1.0, skin=
     pos = (cells[:, None, :] + basis[None, :, :]).reshape(-1, 3)
     pos = lo + pos * ax
     n = pos.shape[0]
+    types = lattice_types(n, type_fractions)
+    masses = np.full(n, float(mass))
+    if type_masses:
+        tm = [float(m) for m in type_masses]
+        masses = np.array([tm[t] if t < len(tm) else float(mass) for t in types])
     rng = np.random.default_rng(seed)
-    sigma_v = math.sqrt(temperature / mass)
-    vel = rng.normal(0.0, sigma_v, size=(n, 3))
+    if type_masses:
+        vel = rng.standard_normal(size=(n, 3)) * np.sqrt(temperature / masses)[:, None]
+    else:
+        vel = rng.normal(0.0, math.sqrt(temperature / mass), size=(n, 3))
     vel -= vel.sum(axis=0) / n
     ndof = 3.0 * n - 3.0
-    ke = 0.5 * float(np.sum(mass * np.sum(vel * vel, axis=1)))
+    ke = 0.5 * float(np.sum(masses * np.sum(vel * vel, axis=1)))
     cur = 2.0 * ke / ndof
     if cur > 1e-20:
         vel *= math.sqrt(temperature / cur)
     return {
         "kind": "lj",
         "tag": np.arange(n, dtype=np.uint32),
-        "type": np.zeros(n, np.uint32),
+        "type": types,
         "pos": np.ascontiguousarray(pos),
         "vel": np.ascontiguousarray(vel),
-        "mass": np.full(n, float(mass)),
+        "mass": masses,
         "cutoff_radius": np.full(n, float(skin)),
         "box": float(box),
     }

@@ -102,8 +102,15 @@ def setup(text, seed=0, precision=None):
         L = cfg.box[0]
         rho = float(lat.get("density", 0.85))
         ncell = int(math.floor(L / (4.0 / rho) ** (1.0 / 3.0)))
+        extra = set(lat) - {"style", "density", "temperature", "mass", "skin", "type_fractions", "type_masses"}
+        if extra:
+            raise RunError(f"[lattice]: unknown key(s) {sorted(extra)}")
         st = inputs.lj_fcc(ncell, L, rho, float(lat.get("temperature", 0.85)), mass=float(lat.get("mass", 1.0)),
-                           skin=float(lat.get("skin", 1.25)), seed=seed, lo=cfg.box_lo[0])
+                           skin=float(lat.get("skin", 1.25)), seed=seed, lo=cfg.box_lo[0],
+                           type_fractions=lat.get("type_fractions"), type_masses=lat.get("type_masses"))
+        if cfg.lj_types > 1 and int(st["type"].max()) >= cfg.lj_types:
+            raise RunError(f"[lattice] type_fractions give {int(st['type'].max()) + 1} types, [lj] types has "
+                           f"{cfg.lj_types}")
     else:
         st = _insert(doc, cfg, seed)
         if cfg.dt == 0.0:

@@ -153,8 +153,13 @@ struct Sim {
     bool uniform = false;
     double uniform_cutoff_sq = 0;
 
-    // LJ, crates/md_lj/src/lib.rs:230-239
-    double lj1 = 0, lj2 = 0, lj_cut2 = 0, lj3 = 0, lj4 = 0;
+    // LJ, crates/md_lj/src/lib.rs:230-239: the pair table (1 x 1 for one type)
+    struct LJC {
+        double lj1, lj2, cut2, lj3, lj4;
+        orc_lj_pair p;
+    };
+    std::vector<LJC> ljt;
+    int ljn = 1;
     // Nose-Hoover, crates/md_thermostat/src/lib.rs:128-139
     bool nh = false;
     double p_xi = 0, q_mass = 1, target_temp = 0.85, ndof = 3;
@@ -200,15 +205,24 @@ struct Sim {
             mt = build_pair_tables(mats.data(), c->n_materials);
         }
         if (!dem) {
-            // LJPairCoeffs::from_params, crates/md_lj/src/lib.rs:230-239
-            double s2 = c->lj_sigma * c->lj_sigma;
-            double sigma6 = s2 * s2 * s2;
-            lj1 = 48.0 * c->lj_epsilon * sigma6 * sigma6;
-            lj2 = 24.0 * c->lj_epsilon * sigma6;
-            double rc = c->lj_cutoff * c->lj_sigma;
-            lj_cut2 = rc * rc;
-            lj3 = 4.0 * c->lj_epsilon * sigma6 * sigma6;
-            lj4 = 4.0 * c->lj_epsilon * sigma6;
+            // build_lj_pair_table, crates/md_lj/src/lib.rs:334-384: the config's
+            // n x n table, or the single type's 1 x 1
+            ljn = (c->n_lj_types > 1 && c->lj_pairs) ? c->n_lj_types : 1;
+            std::vector<orc_lj_pair> tab;
+            if (ljn > 1)
+                tab.assign(c->lj_pairs, c->lj_pairs + (size_t)ljn * ljn);
+            else
+                tab.push_back(orc_lj_pair{c->lj_epsilon, c->lj_sigma, c->lj_cutoff});
+            ljt.clear();
+            for (const orc_lj_pair& q : tab) {
+                // LJPairCoeffs::from_params, crates/md_lj/src/lib.rs:230-239
+                double s2 = q.sigma * q.sigma;
+                double sigma6 = s2 * s2 * s2;
+                double rc = q.cutoff * q.sigma;
+                ljt.push_back(LJC{48.0 * q.epsilon * sigma6 * sigma6, 24.0 * q.epsilon * sigma6, rc * rc,
+                                  4.0 * q.epsilon * sigma6 * sigma6, 4.0 * q.epsilon * sigma6, q});
+            }
+            cfg.lj_pairs = nullptr;
         }
         nh = c->nose_hoover != 0;
         virial = c->virial != 0;
@@ -724,20 +738,25 @@ struct Sim {
         nb_off.push_back((uint32_t)nb_idx.size());
     }
 
-    // lj_force, crates/md_lj/src/lib.rs:488-633 (+ PE sum, single type)
+    // lj_force, crates/md_lj/src/lib.rs:488-633 (+ PE sum): pair_table.get(ti, tj)
+    // when the table has several types, else the one entry
     void lj_force() {
         pe = 0.0;
         double vxx = 0, vyy = 0, vzz = 0, vxy = 0, vxz = 0, vyz = 0;
         double vs = newton ? 1.0 : 0.5;
+        const bool multi = ljn > 1;
         for (int i = 0; i < nlocal; i++) {
             V3 pi = pos[i];
             V3 fi = force[i];
+            const uint32_t ti = type[i];
             for (uint32_t k = nb_off[i]; k < nb_off[i + 1]; k++) {
                 int j = (int)nb_idx[k];
                 const V3& pj = pos[j];
                 double dx = pj[0] - pi[0], dy = pj[1] - pi[1], dz = pj[2] - pi[2];
                 double r2 = std::fma(dx, dx, std::fma(dy, dy, dz * dz));
-                if (r2 >= lj_cut2) continue;
+                const LJC& c = multi ? ljt[(size_t)ti * ljn + type[j]] : ljt[0];
+                const double lj1 = c.lj1, lj2 = c.lj2, lj3 = c.lj3, lj4 = c.lj4;
+                if (r2 >= c.cut2) continue;
                 double r2inv = 1.0 / r2;
                 double r6inv = r2inv * r2inv * r2inv;
                 double fpair = r2inv * r6inv * std::fma(lj1, r6inv, -lj2);
@@ -1355,26 +1374,33 @@ int orc_thermo(void* h, double* out) {
 
 long orc_overlap_count(void* h) { return static_cast<Sim*>(h)->overlap_total; }
 
-// setup_lj_tails (md_lj/src/lib.rs:397-445), single type: rho = N / V with
-// V = size_x size_y size_z (domain.rs:153); rc = sqrt((cutoff sigma)^2);
-// powi(3) as (x x) x.
+// setup_lj_tails (md_lj/src/lib.rs:397-445): rho = N / V with V = size_x
+// size_y size_z (domain.rs:153); per type pair, in table order, rc =
+// sqrt((cutoff sigma)^2) and the weight (1 / ntypes)^2 of an equimolar
+// mixture; powi(3) as (x x) x.
 int orc_lj_tails(void* h, double* e_tail, double* p_tail) {
     Sim* s = static_cast<Sim*>(h);
     const double n = (double)s->nlocal;
     const double v = s->size[0] * s->size[1] * s->size[2];
     const double rho = n / v;
-    const double eps = s->cfg.lj_epsilon, sig = s->cfg.lj_sigma;
-    const double cs = s->cfg.lj_cutoff * sig;
-    const double rc = std::sqrt(cs * cs);
-    const double sigma3 = (sig * sig) * sig;
-    const double rc3 = (rc * rc) * rc;
-    const double rc9 = (rc3 * rc3) * rc3;
-    const double sigma6 = sigma3 * sigma3;
-    const double sigma9 = sigma6 * sigma3;
-    const double w = 1.0 * 1.0;
+    const double frac = 1.0 / (double)s->ljn;
     const double PI = 3.141592653589793;
-    *e_tail = 0.0 + w * (8.0 / 3.0) * PI * n * rho * eps * sigma3 * (sigma9 / (3.0 * rc9) - sigma3 / rc3);
-    *p_tail = 0.0 + w * (16.0 / 3.0) * PI * rho * rho * eps * sigma3 * (2.0 * sigma9 / (3.0 * rc9) - sigma3 / rc3);
+    double e = 0.0, p = 0.0;
+    for (const Sim::LJC& c : s->ljt) {
+        const double eps = c.p.epsilon, sig = c.p.sigma;
+        const double cs = c.p.cutoff * sig;
+        const double rc = std::sqrt(cs * cs);
+        const double sigma3 = (sig * sig) * sig;
+        const double rc3 = (rc * rc) * rc;
+        const double rc9 = (rc3 * rc3) * rc3;
+        const double sigma6 = sigma3 * sigma3;
+        const double sigma9 = sigma6 * sigma3;
+        const double w = frac * frac;
+        e += w * (8.0 / 3.0) * PI * n * rho * eps * sigma3 * (sigma9 / (3.0 * rc9) - sigma3 / rc3);
+        p += w * (16.0 / 3.0) * PI * rho * rho * eps * sigma3 * (2.0 * sigma9 / (3.0 * rc9) - sigma3 / rc3);
+    }
+    *e_tail = e;
+    *p_tail = p;
     return 0;
 }
 

@@ -40,6 +40,12 @@ typedef struct orc_wall {
     int material;
 } orc_wall;
 
+/* One LJ type pair: epsilon, sigma, cutoff in units of sigma
+ * (LJPairCoeffs::from_params, md_lj/src/lib.rs:226-238). */
+typedef struct orc_lj_pair {
+    double epsilon, sigma, cutoff;
+} orc_lj_pair;
+
 typedef struct orc_config {
     int kind;                 /* 0 = DEM granular, 1 = LJ */
     double lo[3], hi[3];      /* [domain] */
@@ -66,6 +72,11 @@ typedef struct orc_config {
     int langevin;
     double lv_temperature, lv_damping;
     uint64_t lv_seed;
+    /* [lj] multi-type mode: n_lj_types > 1 gives the n x n pair table
+     * (row-major; build_lj_pair_table, md_lj/src/lib.rs:334-384) and
+     * pair_table.get(type_i, type_j) picks each pair's coefficients */
+    int n_lj_types;
+    const orc_lj_pair* lj_pairs;
 } orc_config;
 
 enum {
@@ -104,7 +115,8 @@ int    orc_set_history(void* h, size_t n, const uint32_t* keys, const double* va
  *          vxx, vyy, vzz, vxy, vxz, vyz, nbuilds, step, ndof, q_mass] */
 int    orc_thermo(void* h, double* out16);
 long   orc_overlap_count(void* h);
-/* LJ long-range tail corrections E_tail, P_tail (single type). */
+/* LJ long-range tail corrections E_tail, P_tail (equimolar weights over the
+ * type pairs, setup_lj_tails). */
 int    orc_lj_tails(void* h, double* e_tail, double* p_tail);
 
 #ifdef __cplusplus

@@ -42,6 +42,10 @@ class OrcWall(C.Structure):
                 ("bound_hi", C.c_double * 3), ("velocity", C.c_double * 3), ("material", C.c_int)]
 
 
+class OrcLJPair(C.Structure):
+    _fields_ = [("epsilon", C.c_double), ("sigma", C.c_double), ("cutoff", C.c_double)]
+
+
 class OrcConfig(C.Structure):
     _fields_ = [
         ("kind", C.c_int), ("lo", C.c_double * 3), ("hi", C.c_double * 3), ("dt", C.c_double),
@@ -55,7 +59,7 @@ class OrcConfig(C.Structure):
         ("virial", C.c_int),
         ("fixed", C.c_int * 3), ("n_walls", C.c_int), ("walls", C.POINTER(OrcWall)),
         ("langevin", C.c_int), ("lv_temperature", C.c_double), ("lv_damping", C.c_double),
-        ("lv_seed", C.c_uint64),
+        ("lv_seed", C.c_uint64), ("n_lj_types", C.c_int), ("lj_pairs", C.POINTER(OrcLJPair)),
     ]
 
 
@@ -136,6 +140,13 @@ class Oracle:
         c.lv_temperature = float(getattr(cfg, "lv_temperature", 0.85))
         c.lv_damping = float(getattr(cfg, "lv_damping", 1.0))
         c.lv_seed = int(getattr(cfg, "lv_seed", 12345))
+        nt = int(getattr(cfg, "lj_types", 0)) if cfg.kind == "lj" else 0
+        ljp = (OrcLJPair * max(1, nt * nt))()
+        if nt > 1:
+            for k, (e, s, rc) in enumerate(cfg.lj_pairs):
+                ljp[k].epsilon, ljp[k].sigma, ljp[k].cutoff = float(e), float(s), float(rc)
+        c.n_lj_types = nt
+        c.lj_pairs = C.cast(ljp, C.POINTER(OrcLJPair))
         self._mats = mats
         self.h = self.lib.orc_create(C.byref(c))
         self.kind = cfg.kind

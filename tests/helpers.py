@@ -15,17 +15,26 @@ def pair_set(pairs):
     return set(map(tuple, np.asarray(pairs).tolist()))
 
 
-def lj_pair_force_scale(pos, box, pairs, rc=2.5, eps=1.0, sigma=1.0):
+def lj_pair_force_scale(pos, box, pairs, rc=2.5, eps=1.0, sigma=1.0, types=None, table=None):
     """Per-tag sum of |f_pair| over the particle's LJ pairs (the normaliser of
-    the per-particle force-error metric).  ``pos`` indexed by tag."""
+    the per-particle force-error metric).  ``pos`` indexed by tag; with
+    ``types`` (by tag) and an n x n ``table`` of (eps, sigma, rc) triples the
+    coefficients of each pair come from its two types."""
     n = pos.shape[0]
     p = np.asarray(pairs, dtype=np.int64)
     d = pos[p[:, 1]] - pos[p[:, 0]]
     L = np.asarray(box)
     d -= L * np.round(d / L)
     r2 = np.einsum("ij,ij->i", d, d)
+    if table is not None:
+        nt = int(round(len(table) ** 0.5))
+        tab = np.asarray(table, dtype=np.float64).reshape(nt * nt, 3)
+        c = tab[np.asarray(types)[p[:, 0]].astype(np.int64) * nt + np.asarray(types)[p[:, 1]]]
+        eps, sigma, rc = c[:, 0], c[:, 1], c[:, 2]
+    else:
+        eps, sigma, rc = np.full(len(p), eps), np.full(len(p), sigma), np.full(len(p), rc)
     m = r2 < (rc * sigma) ** 2
-    r2 = r2[m]
+    r2, eps, sigma = r2[m], eps[m], sigma[m]
     s6 = sigma ** 6
     inv2 = 1.0 / r2
     inv6 = inv2 ** 3

@@ -13,6 +13,8 @@ import subprocess
 import numpy as np
 import pytest
 
+from test_lj_types_cpu import LJ_TYPES_TOML
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 GAS = """
@@ -172,7 +174,8 @@ def _num(x):
     return {"inf": math.inf, "-inf": -math.inf}.get(x, x) if isinstance(x, str) else x
 
 
-@pytest.mark.parametrize("text", [GAS, REBOUND, LJ, LANGEVIN], ids=["gas", "rebound", "lj", "langevin"])
+@pytest.mark.parametrize("text", [GAS, REBOUND, LJ, LANGEVIN, LJ_TYPES_TOML],
+                         ids=["gas", "rebound", "lj", "langevin", "lj_types"])
 def test_check_matches_python_binding(runner, tmp_path, text):
     from mddem_gb300 import capi, run
 
@@ -198,6 +201,10 @@ def test_check_matches_python_binding(runner, tmp_path, text):
         for f in ("point", "normal", "bound_lo", "bound_hi", "velocity"):
             assert [_num(x) for x in w[f]] == list(getattr(cc.walls[k], f)), f
         assert w["material"] == cc.walls[k].material
+    assert got["n_lj_types"] == cc.n_lj_types
+    assert got["lj_pairs"] == [[cc.lj_pairs[k].epsilon, cc.lj_pairs[k].sigma, cc.lj_pairs[k].cutoff]
+                               for k in range(cc.n_lj_types ** 2 if cc.n_lj_types > 1 else 0)]
+    assert got["type_sum"] == int(np.sum(st["type"]))
     assert got["steps"] == s["steps"] and got["thermo"] == s["thermo"]
     # the initial state: same particles at the same places (velocities come
     # from each host's own seeded generator)
@@ -454,3 +461,16 @@ def test_crlf_config_reads_the_same(runner, tmp_path):
     b = subprocess.run([runner, str(p), "--check"], capture_output=True, text=True, timeout=60)
     assert a.returncode == 0 and b.returncode == 0, b.stderr
     assert json.loads(a.stdout) == json.loads(b.stdout)
+
+
+@pytest.mark.parametrize("edit,msg", [
+    (("sigma = 0.88\n", "sigma = 0.88\nradius = 1\n"), "unknown field"),
+    (("epsilon = 0.5\nsigma = 0.88\n", "epsilon = 0.5\n"), "needs epsilon and sigma"),
+    (("types = [0, 1]", "types = [0, 2]"), "only 2 types"),
+    (("type_fractions = [0.5, 1.0]", "type_fractions = [0.3, 0.6, 1.0]"), "more types"),
+    (('style = "fcc"', 'style = "fcc"\nbasis = 2'), "unknown field"),
+])
+def test_lj_types_errors_exit_1(runner, tmp_path, edit, msg):
+    r = _run(runner, tmp_path, LJ_TYPES_TOML.replace(*edit), "--check")
+    assert r.returncode == 1
+    assert msg in r.stderr
