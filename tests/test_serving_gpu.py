@@ -115,3 +115,47 @@ def test_server_rejects_jobs_without_a_slot(gpu_lib):
         srv.submit(config.granular_gas_config(), st, 10)
     assert e.value.status == 4  # MDG_ERR_BUDGET
     srv.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_server_walled_and_typed_jobs(gpu_lib, precision):
+    """Jobs whose configs point at arrays (plane walls on fixed axes, a
+    multi-type LJ pair table) are served from the server's own copies: the
+    caller's arrays are gone by admission.  The walled DEM job and the typed LJ
+    job end bitwise where they end alone; a single-type LJ job sharing the
+    context with the typed one (its force launch then runs the typed
+    instantiation, same arithmetic) within 1e-12 of the box."""
+    import gc
+
+    from test_lj_types_gpu import _state as typed_state
+    from test_lj_types_cpu import two_type_config
+    from test_walls import walled_config, walled_state
+
+    from mddem_gb300 import capi, config, inputs
+
+    jobs = [(walled_config(precision=precision, g_frac=0.05), walled_state(seed=6), 60),
+            (config.lj_fluid_config(precision=precision), inputs.lj_fcc(6, 10.06, 0.85, 0.85, seed=44), 50),
+            (two_type_config(precision=precision), typed_state(seed=8), 70)]
+    slots = [config.granular_gas_config(precision=precision), config.lj_fluid_config(precision=precision),
+             config.lj_fluid_config(precision=precision)]
+    srv = capi.Server(slots, [1000, 1000, 1000], hbm_budget=1 << 30)
+    ids = [srv.submit(c, s, n) for c, s, n in jobs]
+    gc.collect()
+    done = {}
+    for _ in range(1000):
+        active, pending = srv.pump(20)
+        for info in srv.poll():
+            done[info["id"]] = info
+        if active == 0 and pending == 0:
+            break
+    done.update({i["id"]: i for i in srv.poll()})
+    for k, (jid, (cfg, st, steps)) in enumerate(zip(ids, jobs)):
+        assert done[jid]["status"] == 0 and done[jid]["steps"] == steps
+        got, ref = srv.fetch(jid), _alone(cfg, st, steps)
+        if k == 1:
+            (x,) = by_tag(got, "pos")
+            (y,) = by_tag(ref, "pos")
+            assert np.max(np.abs(x - y)) <= 1e-12 * 10.06
+        else:
+            assert _same(got, ref, ("pos", "vel", "omega") if cfg.kind == "dem" else ("pos", "vel")), k
+    srv.close()
