@@ -250,8 +250,11 @@ int  mdg_step(mdg_ctx* ctx, int64_t nsteps);
  * inside one multi-step launch. */
 int  mdg_set_remaining(mdg_ctx* ctx, int sys, int64_t steps);
 int  mdg_get_remaining(mdg_ctx* ctx, int sys, int64_t* steps);
-/* A copy of system sys's current config (its materials pointer refers to the
- * context's own copy, valid until the next mdg_configure_system of sys). */
+/* A copy of system sys's current config (its materials, walls and lj_pairs
+ * pointers refer to the context's own copies, valid until the next
+ * mdg_configure_system of sys; passing it back to mdg_configure_system is
+ * fine).  Every array a config points at is copied by mdg_create /
+ * mdg_batch_create / mdg_configure_system / mdg_server_submit. */
 int  mdg_get_config(mdg_ctx* ctx, int sys, mdg_config* out);
 /* Lanes per particle row of the LJ force kernel (1, 2, 4 or 8), for the whole
  * context; changes the per-particle summation order, not the physics. */

@@ -138,6 +138,7 @@ struct mdg_ctx {
     int nsys = 0;
     std::vector<mdg_config> cfg;
     std::vector<std::vector<mdg_material>> mats;
+    std::vector<std::vector<mdg_wall>> wls;     // per system: its plane walls
     std::vector<std::vector<mdg_lj_pair>> ljp;  // per system: the LJ pair table (1 x 1 for one type)
     std::vector<int> ljn;                       // its number of types
     std::vector<SysParams> sp;
@@ -229,6 +230,25 @@ namespace {
 void apply_physics(mdg_ctx* c, int s, const mdg_config& k, std::vector<double>& tabs) {
     SysParams& p = c->sp[s];
     c->cfg[s] = k;
+    // the context keeps its own copies of the arrays the config points at;
+    // each is built aside and swapped in, so a config read back by
+    // mdg_get_config (pointing at the current copies) stays readable here:
+    // the previous copies live in these locals until the function returns
+    std::vector<mdg_wall> wl;
+    std::vector<mdg_material> ml;
+    std::vector<mdg_lj_pair> lp;
+    if (k.walls && k.n_walls > 0) wl.assign(k.walls, k.walls + k.n_walls);
+    c->wls[s].swap(wl);
+    c->cfg[s].walls = c->wls[s].empty() ? nullptr : c->wls[s].data();
+    if (k.kind == MDG_KIND_DEM && k.materials) ml.assign(k.materials, k.materials + k.n_materials);
+    c->mats[s].swap(ml);
+    if (k.kind == MDG_KIND_DEM) c->cfg[s].materials = c->mats[s].data();
+    if (k.kind == MDG_KIND_LJ && k.n_lj_types > 1 && k.lj_pairs)
+        lp.assign(k.lj_pairs, k.lj_pairs + (size_t)k.n_lj_types * k.n_lj_types);
+    else if (k.kind == MDG_KIND_LJ)
+        lp.assign(1, mdg_lj_pair{k.lj_epsilon, k.lj_sigma, k.lj_cutoff});
+    c->ljp[s].swap(lp);
+    c->cfg[s].lj_pairs = (k.kind == MDG_KIND_LJ && k.n_lj_types > 1) ? c->ljp[s].data() : nullptr;
     p.contact_model = k.contact_model;
     p.adhesion_model = k.adhesion_model;
     p.rolling_model = k.rolling_model;
@@ -248,7 +268,7 @@ void apply_physics(mdg_ctx* c, int s, const mdg_config& k, std::vector<double>& 
     }
     for (int w = 0; w < k.n_walls; w++) {
         // WallPlugin's plane set-up (dem_wall/src/lib.rs:675-685): unit normal
-        const mdg_wall& q = k.walls[w];
+        const mdg_wall& q = c->wls[s][w];
         WallP& o = p.walls[w];
         const double mag = sqrt(q.normal[0] * q.normal[0] + q.normal[1] * q.normal[1] + q.normal[2] * q.normal[2]);
         for (int d = 0; d < 3; d++) {
@@ -267,24 +287,17 @@ void apply_physics(mdg_ctx* c, int s, const mdg_config& k, std::vector<double>& 
     p.tpp = k.threads_per_particle ? k.threads_per_particle : 1;
     tabs.clear();
     if (k.kind == MDG_KIND_DEM) {
-        c->mats[s].assign(k.materials, k.materials + k.n_materials);
-        c->cfg[s].materials = c->mats[s].data();
-        material_tables(k.materials, k.n_materials, tabs);
+        material_tables(c->mats[s].data(), k.n_materials, tabs);
         p.nmat = k.n_materials;
         // no JKR pull-off range: a pair interacts only when the spheres touch
         bool pull = false;
-        for (int m = 0; m < k.n_materials; m++) pull = pull || k.materials[m].surface_energy > 0.0;
+        for (int m = 0; m < k.n_materials; m++) pull = pull || c->mats[s][m].surface_energy > 0.0;
         p.touch_only = (k.contact_model == 1 || k.adhesion_model == 1 || !pull) ? 1 : 0;
     } else {
         // the pair table (build_lj_pair_table, crates/md_lj/src/lib.rs:334-384):
         // n x n from the config, or 1 x 1 from the single type
         const int nt = k.n_lj_types > 1 ? k.n_lj_types : 1;
-        if (nt > 1)
-            c->ljp[s].assign(k.lj_pairs, k.lj_pairs + (size_t)nt * nt);
-        else
-            c->ljp[s].assign(1, mdg_lj_pair{k.lj_epsilon, k.lj_sigma, k.lj_cutoff});
         c->ljn[s] = nt;
-        c->cfg[s].lj_pairs = nt > 1 ? c->ljp[s].data() : nullptr;
         // LJPairCoeffs::from_params (crates/md_lj/src/lib.rs:230-239), plus
         // 4 eps sigma^12 and 4 eps sigma^6 for the energy
         auto coeffs = [](const mdg_lj_pair& q, double* o) {
@@ -842,6 +855,7 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     c->cfg.assign(cfgs, cfgs + nsys);
     c->mats.resize(nsys);
     c->ljp.resize(nsys);
+    c->wls.resize(nsys);
     c->ljn.assign(nsys, 1);
     c->sp.assign(nsys, SysParams{});
     c->capacity.assign(capacity, capacity + nsys);
