@@ -12,7 +12,10 @@ import numpy as np
 import pytest
 
 TYPES = [(1.0, 1.0), (0.5, 0.88)]
-OVERRIDE = [(0, 1, 0.8, 0.94, 2.2)]
+# pair cutoffs (sigma x cutoff) 2.5, 0.94 x 2.4 = 2.256 and 0.88 x 2.5 = 2.2 sit
+# between the FCC shells of the density-0.85 lattice (2.05, 2.37, 2.65), so
+# the fp32 cutoff test of the mixed path meets no pair at its edge
+OVERRIDE = [(0, 1, 0.8, 0.94, 2.4)]
 
 LJ_TYPES_TOML = """
 [domain]
@@ -44,7 +47,7 @@ sigma = 0.88
 types = [0, 1]
 epsilon = 0.8
 sigma = 0.94
-cutoff = 2.2
+cutoff = 2.4
 
 [lattice]
 style = "fcc"
@@ -94,7 +97,7 @@ def test_toml_types_and_pair_coeffs():
     cfg = config.from_toml(LJ_TYPES_TOML)
     assert cfg.lj_types == 2
     assert cfg.lj_pairs == config.lj_pair_table(TYPES, 2.5, "geometric", OVERRIDE)
-    assert cfg.lj_pairs[1] == (0.8, 0.94, 2.2)
+    assert cfg.lj_pairs[1] == (0.8, 0.94, 2.4)
     # one entry in types: the single-type path with the table's (0, 0) pair
     one = LJ_TYPES_TOML.split("[[lj.types]]")[0] + "[[lj.types]]\nepsilon = 0.7\nsigma = 1.1\n\n[lattice]\n"
     c1 = config.from_toml(one)
@@ -153,7 +156,7 @@ def test_runner_setup_builds_the_typed_lattice():
 
 @pytest.mark.parametrize("ti,tj,r,want_zero", [
     (0, 0, 1.12, False), (1, 1, 1.0, False), (0, 1, 1.05, False),
-    (0, 1, 2.1, True),    # beyond the (0, 1) override's cutoff 0.94 * 2.2 = 2.068
+    (0, 1, 2.3, True),    # beyond the (0, 1) override's cutoff 0.94 * 2.4 = 2.256
     (1, 1, 2.1, False),   # inside the (1, 1) cutoff 0.88 * 2.5 = 2.2
     (0, 0, 2.45, False),
 ])
@@ -228,7 +231,7 @@ def test_oracle_force_is_the_gradient_of_its_energy():
             assert num == pytest.approx(f0[k, d], rel=1e-5, abs=1e-6), (k, d)
 
 
-@pytest.mark.parametrize("ti,tj,r", [(0, 0, 1.12), (0, 1, 1.3), (1, 1, 0.95), (0, 1, 2.1)])
+@pytest.mark.parametrize("ti,tj,r", [(0, 0, 1.12), (0, 1, 1.3), (1, 1, 0.95), (0, 1, 2.3), (0, 1, 2.2)])
 def test_oracle_pair_energy_by_type(ti, tj, r):
     from mddem_gb300 import config
     from oracle.oracle import Oracle
