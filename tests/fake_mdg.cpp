@@ -34,8 +34,14 @@ int mdg_create(const mdg_config* cfg, size_t capacity, mdg_ctx** out) {
     c->cap = capacity;
     c->dem = cfg->kind == MDG_KIND_DEM;
     *out = c;
-    std::fprintf(stderr, "fake: create kind=%d capacity=%zu materials=%d walls=%d\n", cfg->kind, capacity,
-                 cfg->n_materials, cfg->n_walls);
+    std::fprintf(stderr, "fake: create kind=%d capacity=%zu materials=%d walls=%d lj_types=%d\n", cfg->kind,
+                 capacity, cfg->n_materials, cfg->n_walls, cfg->n_lj_types);
+    if (cfg->n_lj_types > 1) {
+        if (!cfg->lj_pairs) return MDG_ERR_CONFIG;
+        for (int k = 0; k < cfg->n_lj_types * cfg->n_lj_types; k++)
+            std::fprintf(stderr, "fake: lj_pair %d %.17g %.17g %.17g\n", k, cfg->lj_pairs[k].epsilon,
+                         cfg->lj_pairs[k].sigma, cfg->lj_pairs[k].cutoff);
+    }
     return MDG_OK;
 }
 
@@ -46,6 +52,9 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* v) {
         return MDG_ERR_ARG;
     if (c->dem && (!v->radius || !v->inv_inertia || !v->omega || !v->quat)) return MDG_ERR_ARG;
     const size_t n = v->n;
+    if (c->cfg.n_lj_types > 1)
+        for (size_t i = 0; i < n; i++)
+            if (!v->type || v->type[i] >= (uint32_t)c->cfg.n_lj_types) return MDG_ERR_ARG;
     c->n = n;
     c->tag.assign(v->tag, v->tag + n);
     c->type.assign(v->type, v->type + n);

@@ -474,3 +474,17 @@ def test_lj_types_errors_exit_1(runner, tmp_path, edit, msg):
     r = _run(runner, tmp_path, LJ_TYPES_TOML.replace(*edit), "--check")
     assert r.returncode == 1
     assert msg in r.stderr
+
+
+def test_run_path_passes_the_lj_pair_table(fake_runner, tmp_path):
+    """The C++ host hands the device the [lj] types table it built (the same
+    numbers as config.lj_pair_table) and the lattice's typed particles."""
+    from mddem_gb300 import config
+
+    p = tmp_path / "config.toml"
+    p.write_text(LJ_TYPES_TOML)
+    r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert "lj_types=2" in r.stderr and "fake: upload n=864" in r.stderr
+    got = [tuple(float(x) for x in l.split()[3:]) for l in r.stderr.splitlines() if l.startswith("fake: lj_pair")]
+    assert tuple(got) == config.from_toml(LJ_TYPES_TOML).lj_pairs
