@@ -64,6 +64,36 @@ def test_invalid_config_rejected_before_device(lib):
     assert e.value.status == 1
 
 
+def test_lj_pair_table_validated_before_device(lib):
+    """mdg_create checks the multi-type table before it looks for a device: an
+    asymmetric table, a non-positive sigma or cutoff, or a missing table is
+    MDG_ERR_CONFIG (1); a valid one gets as far as the device check."""
+    from mddem_gb300 import capi, config
+
+    n = ctypes.c_int(-1)
+    if lib.mdg_device_count(ctypes.byref(n)) == 0 and n.value > 0:
+        pytest.skip("a CUDA device is present")
+    good = config.lj_pair_table([(1.0, 1.0), (0.5, 0.88)], 2.5)
+    base = config.lj_fluid_config().replace(lj_types=2, lj_pairs=good)
+    with pytest.raises(capi.MdgError) as e:
+        capi.Context(base, 10)
+    assert e.value.status == 11  # valid: MDG_ERR_NODEVICE here
+    asym = list(good)
+    asym[1] = (0.7, 0.94, 2.5)
+    bad_sigma = list(good)
+    bad_sigma[3] = (0.5, 0.0, 2.5)
+    bad_cut = list(good)
+    bad_cut[0] = (1.0, 1.0, -1.0)
+    for table in (tuple(asym), tuple(bad_sigma), tuple(bad_cut)):
+        with pytest.raises(capi.MdgError) as e:
+            capi.Context(base.replace(lj_pairs=table), 10)
+        assert e.value.status == 1
+    cc, keep = capi.to_c_config(base)
+    cc.lj_pairs = ctypes.cast(None, ctypes.POINTER(capi.LJPair))
+    h = ctypes.c_void_p()
+    assert lib.mdg_create(ctypes.byref(cc), 10, ctypes.byref(h)) == 1
+
+
 REF_DEM_TOML = """
 [domain]
 x_low = 0.0
