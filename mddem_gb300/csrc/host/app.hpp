@@ -89,6 +89,7 @@ public:
     long long step = 0;             // step counter: first_step + the steps done in this run
     long long first_step = 0;       // the restart's step when [restart] read resumed one
     bool restart_read = false;      // [restart] read = true
+    bool restart_json = false;      // [restart] format = "json" (else bincode)
     long long done() const { return step - first_step; }
     mdg_ctx* ctx = nullptr;
     std::vector<std::string> provided;

@@ -525,9 +525,9 @@ std::string restart_dir(const App& a) { return a.out_dir + "/restart"; }
 
 // RestartPlugin: [restart] interval, format, read (RestartConfig and the
 // restart output, crates/mddem_print/src/lib.rs:267-277, 1050-1066):
-// restart_{step}_rank0.bin in <output>/restart (restart_base_dir,
-// lib.rs:528-534) every `interval` steps, bincode only; `read` resumes from
-// the latest of them (resume_from_restart).
+// restart_{step}_rank0.bin (bincode) or .json in <output>/restart
+// (restart_base_dir, lib.rs:528-534) every `interval` steps; `read` resumes
+// from the latest of them in the configured format (resume_from_restart).
 struct RestartPlugin : Plugin {
     std::string name() const override { return "RestartPlugin"; }
     void build(App& app) override {
@@ -537,8 +537,8 @@ struct RestartPlugin : Plugin {
             if (!r) return;
             check_keys("restart", *r, {"interval", "format", "read"});
             *every = integer(r, "interval", 0);
-            if (text(r, "format", "bincode") != "bincode")
-                throw ConfigError("restart format: the C++ host writes bincode (the Python runner also writes json)");
+            // write_restart_inner (lib.rs:1050-1070): "json", anything else bincode
+            a.restart_json = text(r, "format", "bincode") == "json";
             a.restart_read = boolean(r, "read", false);
             if (*every > 0) a.intervals.push_back(*every);
         });
@@ -607,9 +607,9 @@ struct RestartPlugin : Plugin {
             }
             const std::string dir = restart_dir(a);
             std::filesystem::create_directories(dir);
-            const std::string path = dir + "/" + restart_filename((uint64_t)a.step);
+            const std::string path = dir + "/" + restart_filename((uint64_t)a.step, 0, a.restart_json);
             std::ofstream f(path, std::ios::binary);
-            f << restart_bincode(in);
+            f << (a.restart_json ? restart_json(in) : restart_bincode(in));
             if (!f) throw ConfigError("cannot write " + path);
         });
     }
@@ -665,7 +665,7 @@ void add_restart_plugin(App& app) { app.add_plugin(std::make_unique<RestartPlugi
 Resumed resume_from_restart(App& a) {
     Resumed out;
     const std::string dir = restart_dir(a);
-    const std::string path = latest_restart(dir);
+    const std::string path = latest_restart(dir, a.restart_json);
     if (path.empty()) {
         std::printf("# Restart: no restart files found in %s\n", dir.c_str());
         return out;
@@ -674,7 +674,7 @@ Resumed resume_from_restart(App& a) {
     std::ifstream f(path, std::ios::binary);
     const std::string bytes((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
     if (!f.good() && !f.eof()) throw ConfigError("cannot read " + path);
-    RestartRead r = restart_read(bytes);
+    RestartRead r = a.restart_json ? restart_read_json(bytes) : restart_read(bytes);
     if (r.state.dem != a.dem)
         throw ConfigError(path + (a.dem ? ": no DemAtom buffer for a granular run" : ": a DEM file for an LJ run"));
     a.state = std::move(r.state);
@@ -692,8 +692,9 @@ void write_initial_restart(const App& a, const std::string& path) {
     in.state = &a.state;
     in.density = a.state.dem ? &a.state.density : nullptr;
     in.dt = a.cfg.dt;
+    const bool json = path.size() >= 5 && path.compare(path.size() - 5, 5, ".json") == 0;
     std::ofstream f(path, std::ios::binary);
-    f << restart_bincode(in);
+    f << (json ? restart_json(in) : restart_bincode(in));
     if (!f) throw ConfigError("cannot write " + path);
 }
 void add_langevin_plugin(App& app) { app.add_plugin(std::make_unique<LangevinPlugin>()); }

@@ -25,11 +25,13 @@ std::vector<double> numbers(const toml::Table* t, const std::string& key);
 void add_device_context(App& app);
 // [restart] files (registered by the core group).
 void add_restart_plugin(App& app);
-// The initial state (after the state plugins) as a step-0 restart file.
+// The initial state (after the state plugins) as a step-0 restart file
+// (JSON when the path ends in .json, else bincode).
 void write_initial_restart(const App& a, const std::string& path);
 
 // [restart] read = true (read_restart, crates/mddem_print/src/lib.rs:1152-1251):
-// the latest restart_{step}_rank0.bin in <output>/restart replaces the state
+// the latest restart_{step}_rank0 file of the configured format in
+// <output>/restart replaces the state
 // and sets first_step to its step; the forces, torques and contact history it
 // returns go to the device with the upload.  No file: a note, the state stays.
 struct Resumed {

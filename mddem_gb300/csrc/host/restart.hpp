@@ -1,5 +1,6 @@
 // restart.hpp -- the reference's restart file (RestartData,
-// crates/mddem_print/src/lib.rs:297-376) in bincode 1.3 form (little-endian,
+// crates/mddem_print/src/lib.rs:297-376) as JSON (serde_json of the struct,
+// lib.rs:1062) or in bincode 1.3 form (little-endian,
 // fixed-width integers, u64 length before every sequence): natoms, total_cycle,
 // dt, tag, atom_type, pos/vel/force x y z, mass, cutoff_radius, the per-atom
 // extension buffers (DemAtom: 17 doubles per atom in declaration order,
@@ -29,8 +30,9 @@ struct RestartInput {
 
 // The file's bytes; throws ConfigError on inconsistent sizes.
 std::string restart_bincode(const RestartInput& in);
-// restart_{step}_rank{rank}.bin
-std::string restart_filename(uint64_t step, int rank = 0);
+std::string restart_json(const RestartInput& in);
+// restart_{step}_rank{rank}.bin (.json)
+std::string restart_filename(uint64_t step, int rank = 0, bool json = false);
 
 // A restart file read back: the state (DEM when it carries the DemAtom
 // buffer), forces, torques, contact history, step and dt.
@@ -42,10 +44,11 @@ struct RestartRead {
     uint64_t step = 0;
     double dt = 0.0;
 };
-// Parse bincode RestartData; throws ConfigError on malformed input.
+// Parse bincode / JSON RestartData; throws ConfigError on malformed input.
 RestartRead restart_read(const std::string& bytes);
-// The restart file with the highest step for rank 0 in `dir` (bincode), or
-// "" (read_restart's scan, crates/mddem_print/src/lib.rs:1163-1185).
-std::string latest_restart(const std::string& dir);
+RestartRead restart_read_json(const std::string& text);
+// The restart file with the highest step for rank 0 and the format in `dir`,
+// or "" (read_restart's scan, crates/mddem_print/src/lib.rs:1163-1185).
+std::string latest_restart(const std::string& dir, bool json = false);
 
 }  // namespace mdg_host

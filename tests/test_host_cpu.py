@@ -357,6 +357,15 @@ def test_restart_file_from_the_cpp_host(runner, tmp_path, text):
     again = tmp_path / "again.bin"
     restart.write_restart(again, st, hist, step=step, dt=dt)
     assert again.read_bytes() == path.read_bytes()
+    # the JSON form of the same state reads back to the same values
+    jpath = tmp_path / "restart_0_rank0.json"
+    r = _run(runner, tmp_path, text, "--check", "--write-restart", str(jpath))
+    assert r.returncode == 0, r.stderr
+    js, jh, jstep, jdt = restart.read_restart(jpath)
+    assert (jstep, jdt) == (step, dt)
+    for k in st:
+        assert np.array_equal(js[k], st[k]), k
+    assert (jh is None) == (hist is None)
 
 
 @pytest.fixture(scope="module")
@@ -488,3 +497,32 @@ def test_run_path_passes_the_lj_pair_table(fake_runner, tmp_path):
     assert "lj_types=2" in r.stderr and "fake: upload n=864" in r.stderr
     got = [tuple(float(x) for x in l.split()[3:]) for l in r.stderr.splitlines() if l.startswith("fake: lj_pair")]
     assert tuple(got) == config.from_toml(LJ_TYPES_TOML).lj_pairs
+
+
+def test_run_path_json_restarts_and_resume(fake_runner, tmp_path):
+    """[restart] format = "json": the C++ host writes restart_{step}_rank0.json
+    (serde_json's field set), and read = true resumes from the latest of them,
+    contact history included."""
+    from mddem_gb300 import restart
+
+    text = GAS.replace("steps = 500\nthermo = 100", "steps = 200\nthermo = 100") + \
+        '\n[restart]\ninterval = 100\nformat = "json"\n'
+    p = tmp_path / "config.toml"
+    p.write_text(text)
+    r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    d = tmp_path / "output" / "restart"
+    assert sorted(x.name for x in d.iterdir()) == ["restart_100_rank0.json", "restart_200_rank0.json"]
+    st, hist, step, _ = restart.read_restart(d / "restart_200_rank0.json")
+    assert step == 200 and len(st["tag"]) == 400 and hist[0].tolist() == [[0, 1]]
+    # the Python writer's JSON (json.dumps spacing and number forms) reads the same
+    restart.write_restart(d / "restart_200_rank0.json", st, hist, step=step, dt=2.934e-7, fmt="json")
+    p.write_text(text + "read = true\n")
+    r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    assert "reading from output/restart/restart_200_rank0.json" in r.stdout
+    assert [int(l.split()[0]) for l in r.stdout.splitlines() if not l.startswith("#")] == [200, 300, 400]
+    assert "fake: set_history n=1" in r.stderr
+    st4, _, step4, _ = restart.read_restart(d / "restart_400_rank0.json")
+    assert step4 == 400
+    assert np.allclose(st4["pos"] - st["pos"], st["vel"] * 2.934e-7 * 200, rtol=1e-9, atol=1e-15)
