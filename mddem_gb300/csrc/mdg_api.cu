@@ -242,7 +242,8 @@ void apply_physics(mdg_ctx* c, int s, const mdg_config& k, std::vector<double>& 
     c->cfg[s].walls = c->wls[s].empty() ? nullptr : c->wls[s].data();
     if (k.kind == MDG_KIND_DEM && k.materials) ml.assign(k.materials, k.materials + k.n_materials);
     c->mats[s].swap(ml);
-    if (k.kind == MDG_KIND_DEM) c->cfg[s].materials = c->mats[s].data();
+    c->cfg[s].materials = k.kind == MDG_KIND_DEM ? c->mats[s].data() : nullptr;
+    if (k.kind != MDG_KIND_DEM) c->cfg[s].n_materials = 0;
     if (k.kind == MDG_KIND_LJ && k.n_lj_types > 1 && k.lj_pairs)
         lp.assign(k.lj_pairs, k.lj_pairs + (size_t)k.n_lj_types * k.n_lj_types);
     else if (k.kind == MDG_KIND_LJ)
