@@ -526,3 +526,20 @@ def test_run_path_json_restarts_and_resume(fake_runner, tmp_path):
     st4, _, step4, _ = restart.read_restart(d / "restart_400_rank0.json")
     assert step4 == 400
     assert np.allclose(st4["pos"] - st["pos"], st["vel"] * 2.934e-7 * 200, rtol=1e-9, atol=1e-15)
+
+
+@pytest.mark.parametrize("fmt", ["bincode", "json"])
+def test_resume_from_a_damaged_file_is_an_error(fake_runner, tmp_path, fmt):
+    """A truncated restart file stops the run with a message (exit 1), as the
+    reference's read_restart does on a deserialisation error."""
+    text = GAS.replace("steps = 500\nthermo = 100", "steps = 100\nthermo = 100") + \
+        f'\n[restart]\ninterval = 100\nformat = "{fmt}"\n'
+    p = tmp_path / "config.toml"
+    p.write_text(text)
+    r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    f = tmp_path / "output" / "restart" / ("restart_100_rank0." + ("json" if fmt == "json" else "bin"))
+    f.write_bytes(f.read_bytes()[:-7])
+    p.write_text(text + "read = true\n")
+    r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 1 and "restart" in r.stderr, (r.returncode, r.stderr)
