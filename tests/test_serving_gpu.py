@@ -124,7 +124,8 @@ def test_server_walled_and_typed_jobs(gpu_lib, precision):
     caller's arrays are gone by admission.  The walled DEM job and the typed LJ
     job end bitwise where they end alone; a single-type LJ job sharing the
     context with the typed one (its force launch then runs the typed
-    instantiation, same arithmetic) within 1e-12 of the box."""
+    instantiation, same arithmetic) within 1e-12 of the box in fp64 and 1e-6
+    in mixed precision (room for one fp32 rounding apart)."""
     import gc
 
     from test_lj_types_gpu import _state as typed_state
@@ -155,7 +156,7 @@ def test_server_walled_and_typed_jobs(gpu_lib, precision):
         if k == 1:
             (x,) = by_tag(got, "pos")
             (y,) = by_tag(ref, "pos")
-            assert np.max(np.abs(x - y)) <= 1e-12 * 10.06
+            assert np.max(np.abs(x - y)) <= (1e-12 if precision == "fp64" else 1e-6) * 10.06
         else:
             assert _same(got, ref, ("pos", "vel", "omega") if cfg.kind == "dem" else ("pos", "vel")), k
     srv.close()
