@@ -142,7 +142,13 @@ RestartRead from_fields(Fields&& f) {
         size_t pos = 0;
         for (size_t i = 0; i < n; i++) {
             if (pos >= hb.size()) throw ConfigError("restart: contact-history buffer too short");
-            const size_t cnt = (size_t)hb[pos++];
+            // the count is stored as a double: it must be a whole number >= 0
+            // whose entries (8 doubles each) fit in what is left of the buffer
+            const double craw = hb[pos++];
+            const size_t left = (hb.size() - pos) / 8;
+            if (!std::isfinite(craw) || craw < 0.0 || craw != std::floor(craw) || craw > (double)left)
+                throw ConfigError("restart: contact-history count is not a whole number within the buffer");
+            const size_t cnt = (size_t)craw;
             for (size_t c = 0; c < cnt; c++) {
                 if (pos + 8 > hb.size()) throw ConfigError("restart: contact-history buffer too short");
                 out.hist_keys.push_back(h.tag[i]);

@@ -204,8 +204,15 @@ def fields_to_state(f):
             h = np.asarray(bufs[1])
             keys, vals, pos = [], [], 0
             for t in f["tag"].tolist():
-                cnt = int(h[pos])
+                if pos >= len(h):
+                    raise ValueError("restart: contact-history buffer too short")
+                craw = float(h[pos])
                 pos += 1
+                # a whole number >= 0 whose entries (8 doubles each) fit in the buffer
+                if not (math.isfinite(craw) and craw >= 0 and craw == math.floor(craw)
+                        and craw <= (len(h) - pos) // 8):
+                    raise ValueError("restart: contact-history count is not a whole number within the buffer")
+                cnt = int(craw)
                 for _ in range(cnt):
                     keys.append((t, int(h[pos])))
                     vals.append(h[pos + 1:pos + 8])

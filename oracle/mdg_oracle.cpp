@@ -1298,6 +1298,12 @@ int orc_get_tags(void* h, uint32_t* out) {
     return 0;
 }
 
+int orc_get_types(void* h, uint32_t* out) {
+    Sim* s = static_cast<Sim*>(h);
+    for (int i = 0; i < s->nlocal; i++) out[i] = s->type[i];
+    return 0;
+}
+
 int orc_get_image(void* h, int32_t* out) {
     Sim* s = static_cast<Sim*>(h);
     for (int i = 0; i < s->nlocal; i++) for (int d = 0; d < 3; d++) out[3 * i + d] = s->image[i][d];

@@ -104,6 +104,8 @@ size_t orc_nlocal(void* h);
 /* Copy a per-local-atom field out (3 or 4 doubles per atom). */
 int    orc_get_field(void* h, int field, double* out);
 int    orc_get_tags(void* h, uint32_t* out);
+/* Per-local-atom type index (material for DEM, LJ type for LJ). */
+int    orc_get_types(void* h, uint32_t* out);
 int    orc_get_image(void* h, int32_t* out);
 /* Half-list pairs as (owner tag, partner tag); returns count, fills up to cap. */
 size_t orc_get_pairs(void* h, uint32_t* out, size_t cap);

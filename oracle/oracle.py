@@ -84,6 +84,7 @@ def _load():
         lib.orc_nlocal.restype = C.c_size_t
         lib.orc_get_field.argtypes = [C.c_void_p, C.c_int, P(C.c_double)]
         lib.orc_get_tags.argtypes = [C.c_void_p, P(C.c_uint32)]
+        lib.orc_get_types.argtypes = [C.c_void_p, P(C.c_uint32)]
         lib.orc_get_image.argtypes = [C.c_void_p, P(C.c_int32)]
         lib.orc_get_pairs.argtypes = [C.c_void_p, P(C.c_uint32), C.c_size_t]
         lib.orc_get_pairs.restype = C.c_size_t
@@ -205,10 +206,12 @@ class Oracle:
         n = self.n
         tags = np.zeros(n, np.uint32)
         self.lib.orc_get_tags(self.h, tags.ctypes.data_as(C.POINTER(C.c_uint32)))
+        types = np.zeros(n, np.uint32)
+        self.lib.orc_get_types(self.h, types.ctypes.data_as(C.POINTER(C.c_uint32)))
         img = np.zeros((n, 3), np.int32)
         self.lib.orc_get_image(self.h, img.ctypes.data_as(C.POINTER(C.c_int32)))
-        st = {"tag": tags, "pos": self.field(F_POS), "vel": self.field(F_VEL), "force": self.field(F_FORCE),
-              "image": img, "mass": self.field(F_MASS, 1)}
+        st = {"tag": tags, "type": types, "pos": self.field(F_POS), "vel": self.field(F_VEL),
+              "force": self.field(F_FORCE), "image": img, "mass": self.field(F_MASS, 1)}
         if self.kind == "dem":
             st.update(omega=self.field(F_OMEGA), torque=self.field(F_TORQUE), quat=self.field(F_QUAT, 4),
                       radius=self.field(F_RADIUS, 1))

@@ -543,3 +543,28 @@ def test_resume_from_a_damaged_file_is_an_error(fake_runner, tmp_path, fmt):
     p.write_text(text + "read = true\n")
     r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
     assert r.returncode == 1 and "restart" in r.stderr, (r.returncode, r.stderr)
+
+
+@pytest.mark.parametrize("count", [-1.0, 2.5, float("nan"), 1e30])
+def test_resume_with_a_damaged_history_count_is_an_error(fake_runner, tmp_path, count):
+    """A contact-history count that is negative, fractional, NaN or larger
+    than the buffer stops the resume with a message (exit 1) in the C++ host
+    and a ValueError in the Python reader, instead of a conversion of the
+    stored double to a count."""
+    from mddem_gb300 import restart
+
+    text = GAS.replace("steps = 500\nthermo = 100", "steps = 100\nthermo = 100") + "\n[restart]\ninterval = 100\n"
+    p = tmp_path / "config.toml"
+    p.write_text(text)
+    r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 0, r.stderr
+    f = tmp_path / "output" / "restart" / "restart_100_rank0.bin"
+    st, hist, step, dt = restart.read_restart(f)
+    fields = restart.restart_fields(st, hist, step, dt)
+    fields["atom_data_buffers"][1][0] = count
+    f.write_bytes(restart._bincode(fields))
+    with pytest.raises(ValueError, match="contact-history"):
+        restart.read_restart(f)
+    p.write_text(text + "read = true\n")
+    r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 1 and "contact-history" in r.stderr, (r.returncode, r.stderr)
