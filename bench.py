@@ -468,53 +468,106 @@ def force_bytes(kind, nfull, contacts, prec="fp64"):
     return b
 
 
-def serve_roofline(a, trace, made, mix):
-    """Per-kernel device times of the resident mix at the middle of the timed
-    window, re-created from the jobs' initial states in a batch context per
-    kind (eager launches, L2 flushed before each step, CUDA events on the
-    library's stream); the dominant kernel's algorithmic bytes / time."""
-    from mddem_gb300 import capi
-
+def serve_mix(srv, trace, sid):
+    """Particles, mean full-list row length and stored contacts per particle
+    of the jobs resident now, by kind."""
+    ctx = srv.context()
     per = {}
-    for kind in ("dem", "lj"):
-        ks = [k for k in mix if (trace[k].kind == "lj") == (kind == "lj")]
-        if not ks:
-            continue
-        cfgs = [made[k][0] for k in ks]
-        sts = [made[k][1] for k in ks]
-        ctx = capi.Context(cfgs, [len(s["tag"]) for s in sts])
-        for q, st in enumerate(sts):
-            ctx.upload(st, q)
-        ctx.set_graph_mode(0)
-        ctx.timed_steps(3, L2_FLUSH)
-        t, _, _ = ctx.timed_steps(5, L2_FLUSH)
-        n = sum(len(s["tag"]) for s in sts)
-        nfull = sum(2.0 * len(ctx.pairs(q)) for q in range(len(sts))) / n
-        contacts = sum(len(ctx.history(q)[0]) for q in range(len(sts))) / n if kind == "dem" else 0.0
-        ctx.close()
-        per[kind] = dict(n=n, init=float(t[:, 1].mean()), force=float(t[:, 3].mean()),
-                         final=float(t[:, 4].mean()), nfull=nfull, contacts=contacts)
+    for r in srv.resident():
+        kind = "lj" if trace[sid[r["id"]]].kind == "lj" else "dem"
+        p = per.setdefault(kind, dict(n=0, pairs=0, contacts=0, jobs=0))
+        p["n"] += int(r["n"])
+        p["jobs"] += 1
+        p["pairs"] += len(ctx.pairs(r["slot"]))
+        if kind == "dem":
+            p["contacts"] += len(ctx.history(r["slot"])[0])
+    return {k: dict(particles=p["n"], jobs=p["jobs"], avg_full_neighbors=2.0 * p["pairs"] / max(1, p["n"]),
+                    contacts_per_particle=p["contacts"] / max(1, p["n"])) for k, p in per.items()}
+
+
+def serve_phases(a, trace, made, at_tick, pumps=2):
+    """Where the served step's time goes: the same stream replayed with
+    ordinary pumps up to `at_tick` (the middle of the timed window), then
+    `pumps` pumps whose timesteps run on the server's own context as
+    single-step graphs with CUDA events between the phases (initial
+    integration, rebuild pipeline, force, final integration), on the mix of
+    jobs resident there.  Admission and retirement run as in a pump
+    (mdg_server_pump with 0 steps before and after)."""
+    import numpy as np
+    from mddem_gb300 import capi, workloads as w
+
+    cfgs, caps = w.serve_slots(a.precision, a.policy)
+    srv = capi.Server(cfgs, caps, SERVE_HBM_BUDGET)
+    order = sorted(range(len(trace)), key=lambda k: trace[k].arrival)
+    nxt, tick, sid = 0, 0, {}
+    rows, mix = [], None
+    while tick < at_tick + pumps:
+        while nxt < len(order) and trace[order[nxt]].arrival <= tick:
+            k = order[nxt]
+            sid[srv.submit(*made[k], trace[k].steps)] = k
+            nxt += 1
+        if tick < at_tick:
+            active, pending = srv.pump(SERVE_PUMP)
+        else:
+            srv.pump(0)
+            if mix is None:
+                mix = serve_mix(srv, trace, sid)
+            t, kern, rb = srv.context().timed_steps(SERVE_PUMP)
+            rows.append((t, kern, rb))
+            active, pending = srv.pump(0)
+        for info in srv.poll():
+            srv.fetch(info["id"])
+        tick += 1
+        if nxt == len(order) and active == 0 and pending == 0:
+            break
+    srv.close()
+    if not rows:
+        return None, None
+    t = np.concatenate([r[0] for r in rows])
+    kern = np.concatenate([r[1] for r in rows])
+    rb = np.concatenate([r[2] for r in rows])
+    names = ("initial", "rebuild", "force", "final")
+    ph = {q: float(t[:, 1 + i].mean()) for i, q in enumerate(names)}
+    return {"at_pump": at_tick, "timesteps": int(len(t)), "step_ms": float(t[:, 0].mean()), "phases_ms": ph,
+            "rebuild_steps_frac": float(rb.mean()), "kernels_per_step": float(kern.mean())}, mix
+
+
+def serve_roofline(a, phases, mix, served_rate):
+    """Roofline of the served step from its phase split: each phase's
+    algorithmic bytes (per-particle figures of the mix's kinds, see INIT_BYTES,
+    FINAL_BYTES, force_bytes) over its CUDA-event time; the dominant phase is
+    reported, plus the whole step's bytes per particle-step times the
+    window's served rate."""
     prec = a.precision
-    cands = {
-        "k_initial": (sum(p["init"] for p in per.values()),
-                      sum(p["n"] * INIT_BYTES[(k, prec)] for k, p in per.items())),
-        "k_final": (sum(p["final"] for p in per.values()),
-                    sum(p["n"] * FINAL_BYTES[k] for k, p in per.items())),
-    }
-    for k, p in per.items():
-        name = ("k_dem_" if k == "dem" else "k_lj_") + prec
-        cands[name] = (p["force"], p["n"] * force_bytes(k, p["nfull"], p["contacts"], prec))
+    init_b = sum(m["particles"] * INIT_BYTES[(k, prec)] for k, m in mix.items())
+    fin_b = sum(m["particles"] * FINAL_BYTES[k] for k, m in mix.items())
+    force_b = sum(m["particles"] * force_bytes(k, m["avg_full_neighbors"], m["contacts_per_particle"], prec)
+                  for k, m in mix.items())
+    ph = phases["phases_ms"]
+    cands = {"initial": (ph["initial"], init_b), "force": (ph["force"], force_b), "final": (ph["final"], fin_b),
+             "rebuild": (ph["rebuild"], None)}
     name = max(cands, key=lambda q: cands[q][0])
     ms, nbytes = cands[name]
     peak, src = peak_hbm()
-    achieved = nbytes / (ms / 1e3) / 1e9
-    traffic = ncu_traffic(name + "/serve")
-    return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": src, "traffic": traffic,
-            "algorithmic_bytes_per_launch": nbytes, "launch_ms": ms,
-            "kernels_ms": {q: v[0] for q, v in cands.items()},
-            "mix": {k: {"particles": p["n"], "avg_full_neighbors": p["nfull"], "contacts_per_particle": p["contacts"]}
-                    for k, p in per.items()}}
+    kernel = {"initial": f"k_initial_{prec}", "final": f"k_final_{prec}", "rebuild": "rebuild pipeline",
+              "force": "k_dem_" + prec + " + k_lj_" + prec}[name]
+    step_b = init_b + fin_b + force_b
+    bpps = step_b / sum(m["particles"] for m in mix.values())
+    out = {"bound": "hbm", "kernel": kernel, "phase": name, "share": ms / phases["step_ms"],
+           "achieved": nbytes / (ms / 1e3) / 1e9 if nbytes else None, "peak": peak, "unit": "GB/s",
+           "peak_source": src, "traffic": ncu_traffic(name + "/serve"), "algorithmic_bytes_per_launch": nbytes,
+           "launch_ms": ms,
+           "phases": {q: {"ms": v[0], "share": v[0] / phases["step_ms"],
+                          "algorithmic_bytes": v[1],
+                          "frac": (v[1] / (v[0] / 1e3) / 1e9 / peak) if v[1] else None}
+                      for q, v in cands.items()},
+           "whole_step": {"bytes_per_particle_step": bpps, "served_particle_steps_per_s": served_rate,
+                          "achieved": bpps * served_rate / 1e9, "frac": bpps * served_rate / 1e9 / peak,
+                          "note": "the mix's algorithmic bytes per particle-step (integrators + force) x the "
+                                  "window's served rate, over the measured copy peak"},
+           "attribution": phases, "mix": mix}
+    out["frac"] = out["achieved"] / peak if out["achieved"] else None
+    return out
 
 
 def _oracle_job(cfg, st, steps_cap, budget):
@@ -603,7 +656,9 @@ def bench_serve(a, world, rank, local, dist):
     }
     srv.close()
     if rank == 0:
-        line["roofline"] = serve_roofline(a, trace, made, win.get("mix", []))
+        phases, mix = serve_phases(a, trace, made, win["warm"] + max(1, win["pumps"] // 2))
+        if phases:
+            line["roofline"] = serve_roofline(a, phases, mix, line["value"] / world)
         if not a.no_plain:
             line["plain_fp64_job_by_job"] = plain_job_by_job(trace, made)
             line["served_vs_plain"] = line["value"] / world / line["plain_fp64_job_by_job"]["value"]

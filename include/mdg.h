@@ -260,6 +260,13 @@ int  mdg_get_config(mdg_ctx* ctx, int sys, mdg_config* out);
  * context; changes the per-particle summation order, not the physics. */
 int  mdg_set_threads_per_particle(mdg_ctx* ctx, int tpp);
 int  mdg_get_threads_per_particle(const mdg_ctx* ctx);
+/* Work split of the neighbour-list build (bin_neighbor_list,
+ * crates/mddem_core/src/neighbor.rs:810-1080) for every system of the
+ * context: 0 = a warp per bin, 1 = a warp per particle, 2 = a thread per
+ * particle, -1 = chosen per system from its particles per bin and bin count
+ * (the default).  Every mode writes the same rows; the mode applies to the
+ * systems uploaded so far and to later uploads. */
+int  mdg_set_build_mode(mdg_ctx* ctx, int mode);
 
 /* ---- autotuner -----------------------------------------------------------------
  * Picks, by timing short trial runs on the context's own systems, the LJ
@@ -347,7 +354,9 @@ int  mdg_timed_steps(mdg_ctx* ctx, int64_t nsteps, size_t l2_flush_bytes, mdg_st
  * static device array inside the library (about 256 KB, held on every GPU that
  * loads the library until exit), which limits n to 1,048,576 particles
  * (larger n returns MDG_ERR_ARG).  The first call on a device looks up that
- * array's device address, so make the first call before any stream capture.
+ * array's device address, so make the first call before any stream capture;
+ * the address is kept for the life of the device's primary context, so do
+ * not call this again after a cudaDeviceReset in the same process.
  * All calls share the array: calls that overlap on the GPU race.  Work is
  * queued on `stream` (NULL = default stream); the call does not synchronise. */
 int  mdg_granular_temp_noalloc(const double* vel, const double* mass, size_t n, double* out3, void* stream);

@@ -34,7 +34,7 @@ EXPORTS = [
     "mdg_server_submit", "mdg_server_pump", "mdg_server_poll", "mdg_server_fetch", "mdg_server_context",
     "mdg_rsa_spheres", "mdg_get_progress", "mdg_get_stream", "mdg_server_stats",
     "mdg_server_resident", "mdg_get_config", "mdg_set_threads_per_particle", "mdg_get_threads_per_particle",
-    "mdg_autotune", "mdg_rdf", "mdg_msd_reset", "mdg_msd",
+    "mdg_set_build_mode", "mdg_autotune", "mdg_rdf", "mdg_msd_reset", "mdg_msd",
 ]
 
 
@@ -182,6 +182,7 @@ def load(path: str = LIB_PATH):
     lib.mdg_msd.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
     lib.mdg_set_threads_per_particle.argtypes = [C.c_void_p, C.c_int]
     lib.mdg_get_threads_per_particle.argtypes = [C.c_void_p]
+    lib.mdg_set_build_mode.argtypes = [C.c_void_p, C.c_int]
     lib.mdg_autotune.argtypes = [C.c_void_p, C.POINTER(TuneOpts), C.POINTER(TuneResult)]
     lib.mdg_server_resident.argtypes = [C.c_void_p, C.POINTER(JobInfo), C.c_int, C.POINTER(C.c_int)]
     lib.mdg_server_stats.argtypes = [C.c_void_p, C.POINTER(ServerStats)]
@@ -593,6 +594,11 @@ class Context:
         if tpp is not None:
             _check(self.lib.mdg_set_threads_per_particle(self.h, int(tpp)), "mdg_set_threads_per_particle")
         return int(self.lib.mdg_get_threads_per_particle(self.h))
+
+    def build_mode(self, mode):
+        """List-build work split of every system: 0 warp per bin, 1 warp per
+        particle, 2 thread per particle, -1 automatic (same rows in all)."""
+        _check(self.lib.mdg_set_build_mode(self.h, int(mode)), "mdg_set_build_mode")
 
     def stream(self):
         """The context's CUDA stream handle (as an int), for events and

@@ -157,6 +157,7 @@ struct mdg_ctx {
     Dev d{};
     bool has_lj = false, has_dem = false, has_mixed = false, any_virial = false;
     int tpp_lj = 1;
+    int build_mode = -1;  // list-build mode of every system; -1 = chosen per system
     long long cells_alloc = 0, lst_alloc = 0;
     int* d_blk_sys = nullptr;
     int* d_cblk_sys = nullptr;
@@ -346,6 +347,17 @@ int cuda_err(cudaError_t e) {
 
 // neighbor_setup + compute_bin_grid (crates/mddem_core/src/neighbor.rs:480-541,
 // 290-371) for one rank, from the uploaded cutoff radii.
+// List build mode (all give the same rows): under about 6 particles per bin
+// a thread per particle; a warp per bin when there are enough bins to fill
+// the GPU (and no more bins than particles, as bins take particle slots);
+// else a warp per particle.
+int auto_build_mode(const SysParams& p, size_t n) {
+    const double nbins = (double)p.nc[0] * (double)p.nc[1] * (double)p.nc[2];
+    if ((double)n < 6.0 * nbins) return 2;
+    if (nbins >= 2048.0 && (size_t)p.ncell <= n) return 0;
+    return 1;
+}
+
 int setup_grid(const mdg_config& c, const double* cutr, size_t n, SysParams& p) {
     double max_skin = 0.0, min_skin = std::numeric_limits<double>::max();
     for (size_t i = 0; i < n; i++) {
@@ -381,14 +393,7 @@ int setup_grid(const mdg_config& c, const double* cutr, size_t n, SysParams& p) 
     }
     if (ncell > (1LL << 30)) return MDG_ERR_CONFIG;
     p.ncell = (int)ncell;
-    // list build mode (all give the same rows): under about 6 particles per bin
-    // a thread per particle; a warp per bin when there are enough bins to fill
-    // the GPU (and no more bins than particles, as bins take particle slots);
-    // else a warp per particle
-    const double nbins = (double)p.nc[0] * (double)p.nc[1] * (double)p.nc[2];
-    if ((double)n < 6.0 * nbins) p.build_mode = 2;
-    else if (nbins >= 2048.0 && (size_t)p.ncell <= n) p.build_mode = 0;
-    else p.build_mode = 1;
+    p.build_mode = auto_build_mode(p, n);
     p.max_cutoff = max_cutoff;
     p.stencil_cut_sq = max_cutoff * max_cutoff;
     // stencil membership of every offset (compute_bin_grid's distance test,
@@ -1077,6 +1082,7 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
     }
     int r = setup_grid(k, st->cutoff_radius, n, p);
     if (r) return r;
+    if (c->build_mode >= 0) p.build_mode = c->build_mode;
     p.n = (int)n;
     p.nb = (int)((n + BLK - 1) / BLK);
     c->maps_dirty = true;
@@ -1398,6 +1404,22 @@ int mdg_set_threads_per_particle(mdg_ctx* c, int tpp) {
 }
 
 int mdg_get_threads_per_particle(const mdg_ctx* c) { return c ? c->tpp_lj : 0; }
+
+int mdg_set_build_mode(mdg_ctx* c, int mode) {
+    if (!c || mode < -1 || mode > 2) return MDG_ERR_ARG;
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(e);
+    c->build_mode = mode;
+    // systems uploaded so far take the mode now; -1 restores the automatic choice
+    for (int s = 0; s < c->nsys; s++) {
+        if (!c->uploaded[s]) continue;
+        SysParams& p = c->sp[s];
+        p.build_mode = mode >= 0 ? mode : auto_build_mode(p, (size_t)p.n);
+        e = cudaMemcpy(c->d_sp + s, &p, sizeof(SysParams), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_err(e);
+    }
+    return MDG_OK;
+}
 
 int mdg_rdf(mdg_ctx* c, int sys, double r_max, int nbins, uint64_t* counts) {
     if (!c || !counts || sys < 0 || sys >= c->nsys || nbins < 1 || nbins > rdf_max_bins() || !(r_max > 0.0))

@@ -155,7 +155,11 @@ extern "C" int mdg_granular_temp_noalloc(const double* vel, const double* mass, 
     double* scr = nullptr;
     {
         // once per device, with that device current: the device address of the
-        // static scratch array (its host-side name is only a stand-in)
+        // static scratch array (its host-side name is only a stand-in).  The
+        // cached address belongs to the device's primary context; it assumes
+        // that context lives as long as the process.  A caller that resets
+        // the device (cudaDeviceReset) must not call this entry point again
+        // in the same process.
         std::lock_guard<std::mutex> lock(g_na_mutex);
         if (!g_na_scratch[dev]) {
             void* p = nullptr;

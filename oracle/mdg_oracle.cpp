@@ -133,6 +133,12 @@ struct Sim {
     std::vector<V3> omega, ang_mom, torque;
     // ContactHistoryStore, crates/dem_granular/src/tangential.rs:54-75
     std::vector<std::vector<Contact>> contacts;
+    // Checker only (no counterpart in the reference): per atom the sums of the
+    // pair force magnitudes |f_pair| and pair torque magnitudes |tau_pair| of
+    // the last force evaluation, folded onto owners like the reverse
+    // communication; the normaliser of the per-particle force-error metric
+    // max(|F|, sum_pairs |f_pair|).
+    std::vector<double> fscale, tscale;
     int nlocal = 0, nghost = 0;
 
     std::vector<Swap> swaps;
@@ -595,6 +601,10 @@ struct Sim {
             for (int k = 0; k < it->recv_count; k++) {
                 int g = it->recv_start + k;
                 int o = origin_index[g];
+                if ((int)fscale.size() > g) {
+                    fscale[o] += fscale[g];
+                    tscale[o] += tscale[g];
+                }
                 force[o][0] += force[g][0];
                 force[o][1] += force[g][1];
                 force[o][2] += force[g][2];
@@ -760,6 +770,8 @@ struct Sim {
                 double r2inv = 1.0 / r2;
                 double r6inv = r2inv * r2inv * r2inv;
                 double fpair = r2inv * r6inv * std::fma(lj1, r6inv, -lj2);
+                add_scale(i, fpair * dx, fpair * dy, fpair * dz, fscale);
+                add_scale(j, fpair * dx, fpair * dy, fpair * dz, fscale);
                 pe += r6inv * (lj3 * r6inv - lj4) * (newton ? 1.0 : 0.5);
                 if (virial) {
                     double fx = -fpair * dx, fy = -fpair * dy, fz = -fpair * dz;
@@ -908,6 +920,8 @@ struct Sim {
                 force[i][0] -= fnx; force[i][1] -= fny; force[i][2] -= fnz;
                 if (newton) { force[j][0] += fnx; force[j][1] += fny; force[j][2] += fnz; }
                 if (jkr_adhesion_only) {
+                    add_scale(i, fnx, fny, fnz, fscale);
+                    add_scale(j, fnx, fny, fnz, fscale);
                     if (virial) add_virial(dx, dy, dz, -fnx * vs, -fny * vs, -fnz * vs);
                     continue;
                 }
@@ -944,6 +958,10 @@ struct Sim {
                 if (newton) { force[j][0] -= ftx; force[j][1] -= fty; force[j][2] -= ftz; }
                 torque[i][0] += tix; torque[i][1] += tiy; torque[i][2] += tiz;
                 if (newton) { torque[j][0] += tjx; torque[j][1] += tjy; torque[j][2] += tjz; }
+                add_scale(i, ftx - fnx, fty - fny, ftz - fnz, fscale);
+                add_scale(j, ftx - fnx, fty - fny, ftz - fnz, fscale);
+                add_scale(i, tix, tiy, tiz, tscale);
+                add_scale(j, tjx, tjy, tjz, tscale);
                 double orx = oix - ojx, ory = oiy - ojy, orz = oiz - ojz;
                 double odn = orx * nx + ory * ny + orz * nz;
                 double rollx = orx - odn * nx, rolly = ory - odn * ny, rollz = orz - odn * nz;
@@ -973,12 +991,16 @@ struct Sim {
                         }
                         torque[i][0] += trx; torque[i][1] += try_; torque[i][2] += trz;
                         if (newton) { torque[j][0] -= trx; torque[j][1] -= try_; torque[j][2] -= trz; }
+                        add_scale(i, trx, try_, trz, tscale);
+                        add_scale(j, trx, try_, trz, tscale);
                     } else if (roll_mag > 1e-30) {
                         double tau_mag = mu_r * std::fabs(f_n_mag) * r_eff;
                         double inv_roll = tau_mag / roll_mag;
                         double trx = -inv_roll * rollx, try_ = -inv_roll * rolly, trz = -inv_roll * rollz;
                         torque[i][0] += trx; torque[i][1] += try_; torque[i][2] += trz;
                         if (newton) { torque[j][0] -= trx; torque[j][1] -= try_; torque[j][2] -= trz; }
+                        add_scale(i, trx, try_, trz, tscale);
+                        add_scale(j, trx, try_, trz, tscale);
                     }
                 }
                 if (mu_tw > 0.0) {
@@ -996,12 +1018,16 @@ struct Sim {
                         double ttx = tau_tw * nx, tty = tau_tw * ny, ttz = tau_tw * nz;
                         torque[i][0] += ttx; torque[i][1] += tty; torque[i][2] += ttz;
                         if (newton) { torque[j][0] -= ttx; torque[j][1] -= tty; torque[j][2] -= ttz; }
+                        add_scale(i, ttx, tty, ttz, tscale);
+                        add_scale(j, ttx, tty, ttz, tscale);
                     } else if (std::fabs(twist_vel) > 1e-30) {
                         double tau = mu_tw * std::fabs(f_n_mag) * r_eff;
                         double sg = twist_vel > 0.0 ? -1.0 : 1.0;
                         double ttx = sg * tau * nx, tty = sg * tau * ny, ttz = sg * tau * nz;
                         torque[i][0] += ttx; torque[i][1] += tty; torque[i][2] += ttz;
                         if (newton) { torque[j][0] -= ttx; torque[j][1] -= tty; torque[j][2] -= ttz; }
+                        add_scale(i, ttx, tty, ttz, tscale);
+                        add_scale(j, ttx, tty, ttz, tscale);
                     }
                 }
                 if (virial) {
@@ -1068,6 +1094,7 @@ struct Sim {
                 else if (coh > 0.0) fn = k_n * delta - f_diss - coh * kPi * delta * r;
                 else fn = std::fmax(k_n * delta - f_diss, 0.0);
                 for (int d = 0; d < 3; d++) force[i][d] += fn * W.normal[d];
+                if (i < (int)fscale.size()) fscale[i] += std::fabs(fn);
                 if (delta > 0.0) {
                     double mu = mt.at(mt.twisting_friction, mi, wm);
                     if (mu > 0.0) {
@@ -1076,6 +1103,7 @@ struct Sim {
                             double tau = mu * std::fabs(fn) * r;
                             double sg = tw > 0.0 ? -1.0 : 1.0;
                             for (int d = 0; d < 3; d++) torque[i][d] += sg * tau * W.normal[d];
+                            if (i < (int)tscale.size()) tscale[i] += std::fabs(tau);
                         }
                     }
                 }
@@ -1112,7 +1140,13 @@ struct Sim {
         }
     }
 
+    void add_scale(int a, double fx, double fy, double fz, std::vector<double>& sc) {
+        sc[a] += std::sqrt(fx * fx + fy * fy + fz * fz);
+    }
+
     void compute_forces() {
+        fscale.assign(len(), 0.0);
+        tscale.assign(len(), 0.0);
         if (virial) for (double& v : vir) v = 0.0;  // zero_virial_stress
         if (dem) contact_force();
         else lj_force();
@@ -1295,6 +1329,16 @@ int orc_get_field(void* h, int field, double* out) {
 int orc_get_tags(void* h, uint32_t* out) {
     Sim* s = static_cast<Sim*>(h);
     for (int i = 0; i < s->nlocal; i++) out[i] = s->tag[i];
+    return 0;
+}
+
+int orc_get_scale(void* h, double* fs, double* ts) {
+    Sim* s = static_cast<Sim*>(h);
+    for (int i = 0; i < s->nlocal; i++) {
+        const bool have = i < (int)s->fscale.size();
+        if (fs) fs[i] = have ? s->fscale[i] : 0.0;
+        if (ts) ts[i] = have ? s->tscale[i] : 0.0;
+    }
     return 0;
 }
 

@@ -104,6 +104,10 @@ size_t orc_nlocal(void* h);
 /* Copy a per-local-atom field out (3 or 4 doubles per atom). */
 int    orc_get_field(void* h, int field, double* out);
 int    orc_get_tags(void* h, uint32_t* out);
+/* Per local atom: sum over its pairs of |f_pair| and of |tau_pair| at the
+ * last force evaluation (either array may be NULL); the normaliser of the
+ * per-particle force and torque error metric. */
+int    orc_get_scale(void* h, double* fs, double* ts);
 /* Per-local-atom type index (material for DEM, LJ type for LJ). */
 int    orc_get_types(void* h, uint32_t* out);
 int    orc_get_image(void* h, int32_t* out);

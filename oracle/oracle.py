@@ -85,6 +85,7 @@ def _load():
         lib.orc_get_field.argtypes = [C.c_void_p, C.c_int, P(C.c_double)]
         lib.orc_get_tags.argtypes = [C.c_void_p, P(C.c_uint32)]
         lib.orc_get_types.argtypes = [C.c_void_p, P(C.c_uint32)]
+        lib.orc_get_scale.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
         lib.orc_get_image.argtypes = [C.c_void_p, P(C.c_int32)]
         lib.orc_get_pairs.argtypes = [C.c_void_p, P(C.c_uint32), C.c_size_t]
         lib.orc_get_pairs.restype = C.c_size_t
@@ -216,6 +217,14 @@ class Oracle:
             st.update(omega=self.field(F_OMEGA), torque=self.field(F_TORQUE), quat=self.field(F_QUAT, 4),
                       radius=self.field(F_RADIUS, 1))
         return st
+
+    def pair_scale(self):
+        """Per local atom (storage order, like state()): the sums over its
+        pairs of |f_pair| and |tau_pair| at the last force evaluation."""
+        fs, ts = np.zeros(self.n), np.zeros(self.n)
+        self.lib.orc_get_scale(self.h, fs.ctypes.data_as(C.POINTER(C.c_double)),
+                               ts.ctypes.data_as(C.POINTER(C.c_double)))
+        return fs, ts
 
     def pairs(self):
         n = self.lib.orc_get_pairs(self.h, None, 0)

@@ -107,9 +107,10 @@ def _check_dem_force_parity(cfg, st, hist=True):
     r = o.state()
     assert pair_set(ctx.pairs()) == pair_set(o.pairs())
     gf, gt = by_tag(g, "force", "torque")
-    rf, rt = by_tag(r, "force", "torque")
-    fs = np.max(np.abs(rf)) * 1e-3
-    ts = np.max(np.abs(rt)) * 1e-3 if np.max(np.abs(rt)) > 0 else 1e-300
+    # per particle: |F_gpu - F_ref|_inf / max(|F_ref|_inf, sum_pairs |f_pair|)
+    # (and the same with torques), the sums from the oracle's pair loop
+    r["fscale"], r["tscale"] = o.pair_scale()
+    rf, rt, fs, ts = by_tag(r, "force", "torque", "fscale", "tscale")
     assert rel_err(gf, rf, fs) <= 1e-12
     assert rel_err(gt, rt, ts) <= 1e-12
     gk, gv = ctx.history()

@@ -8,10 +8,10 @@ fluid with per-type masses, a geometric cross pair replaced by a
     within 1e-10 of the box length, tail corrections equal to 1e-14;
   * mixed: forces within 1e-5 of the fp64 path (the precision form's bound);
   * a single-type system batched with a multi-type one keeps its own
-    coefficients: after 20 steps its positions are within 1e-12 of the box
-    (fp64) of it run alone, or within 1e-6 (mixed, where one fp32 rounding
-    apart in a force grows to ~1e-8 in 20 steps), should the typed kernel
-    instantiation round differently;
+    coefficients: its force launch then runs the typed kernel instantiation,
+    whose table entries hold the same coefficients, so after 20 steps its
+    positions equal those of it run alone bit for bit (both precisions;
+    measured on GB300);
   * a particle type outside the table is refused at upload.
 """
 import numpy as np
@@ -113,7 +113,7 @@ def test_single_type_system_batched_with_a_typed_one(gpu_lib, precision):
     b.step(20)
     (x,) = by_tag(b.download(0), "pos")
     (y,) = by_tag(alone.download(), "pos")
-    assert np.max(np.abs(x - y)) <= (1e-12 if precision == "fp64" else 1e-6) * 10.06
+    assert np.array_equal(x, y)
     o = _oracle(c2, s2)
     o.step(20)
     (gx,) = by_tag(b.download(1), "pos")

@@ -325,9 +325,11 @@ def test_gpu_walled_force_parity(gpu_lib, variant):
     assert pair_set(ctx.pairs()) == pair_set(o.pairs())
     g, r = ctx.download(), o.state()
     gf, gt = by_tag(g, "force", "torque")
-    rf, rt = by_tag(r, "force", "torque")
-    assert rel_err(gf, rf, np.max(np.abs(rf)) * 1e-3) <= 1e-12
-    assert rel_err(gt, rt, max(np.max(np.abs(rt)) * 1e-3, 1e-300)) <= 1e-12
+    # per particle against max(|F_ref|, sum of its pair and wall force magnitudes)
+    r["fscale"], r["tscale"] = o.pair_scale()
+    rf, rt, fs, ts = by_tag(r, "force", "torque", "fscale", "tscale")
+    assert rel_err(gf, rf, fs) <= 1e-12
+    assert rel_err(gt, rt, ts) <= 1e-12
     # mixed: 1e-5 per particle against the fp64 path
     m = _ctx(cfg.replace(precision="mixed"), st)
     m.force_only()
