@@ -122,7 +122,6 @@ int validate_config(const mdg_config& c) {
         const double mag = sqrt(q.normal[0] * q.normal[0] + q.normal[1] * q.normal[1] + q.normal[2] * q.normal[2]);
         if (!(mag > 1e-15) || q.material < 0 || q.material >= c.n_materials) return MDG_ERR_CONFIG;
     }
-    if (c.precision == MDG_MIXED && c.virial && c.kind == MDG_KIND_DEM) return MDG_ERR_CONFIG;
     const int t = c.threads_per_particle;
     if (!(t == 0 || t == 1 || t == 2 || t == 4 || t == 8)) return MDG_ERR_CONFIG;
     if (c.neighbor_capacity < 0 || c.history_capacity < 0) return MDG_ERR_CONFIG;
@@ -984,6 +983,8 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     if (c->has_mixed && c->has_dem) {
         d.dem_wl = c->alloc<int>(P, err);
         d.dem_wl_n = c->alloc<int>(nsys, err);
+        d.dem_cl = c->alloc<int>(P, err);
+        d.dem_cl_n = c->alloc<int>(2, err);
     }
     c->d_cblk0 = c->alloc<int>(nsys, err);
     c->d_sp = c->alloc<SysParams>(nsys, err);
@@ -1334,7 +1335,8 @@ int mdg_step(mdg_ctx* c, int64_t nsteps) {
     advance_budgets(c, nsteps);
     // kernels that ran: per step initial + force + final (+ loop control),
     // plus the rebuild kernels on the steps whose rebuild branch opened
-    const long long nforce = (c->has_lj ? 1 : 0) + (c->has_dem ? 1 : 0) + (c->has_walls ? 1 : 0);
+    // (the mixed DEM force is two kernels: screen and contact)
+    const long long nforce = (c->has_lj ? 1 : 0) + (c->has_dem ? (c->has_mixed ? 2 : 1) : 0) + (c->has_walls ? 1 : 0);
     long long base = 2 + nforce + (c->graph_mode ? 1 : 0);
     if (c->graph_mode && c->has_mixed) {
         // fused step kernel (+ thermostatted initial) per iteration, the

@@ -215,6 +215,12 @@ struct Dev {
     // each rebuild; the force kernel visits only these.
     int* dem_wl;
     int* dem_wl_n;
+    // Mixed DEM contexts: the particles (absolute indices, all systems) whose
+    // rows hold a touching pair this step, appended by the screening pass and
+    // consumed by the contact pass; dem_cl_n = {count, blocks done}, cleared
+    // by the contact pass's last block.
+    int* dem_cl;
+    int* dem_cl_n;
     const SysParams* sp;
     SysState* ss;
     const double* mat;

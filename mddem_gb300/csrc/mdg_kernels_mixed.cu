@@ -245,7 +245,10 @@ __device__ void hm_pair_mixed(const Dev& d, const SysParams& sp, const float (&d
         float t, te;
         two_sum(Sh, p, t, te);
         Sh = t;
-        Sl += te + e + 2.f * dh[k] * dl[k];
+        // (dh + dl)^2 = dh^2 + dl (2 dh + dl): the dl^2 term matters in
+        // large boxes, where dl (the lo parts of coordinates near L) reaches
+        // ~1e-8 L and (r1 + r2)^2 - d^2 of a grazing contact is small
+        Sl += te + e + dl[k] * (2.f * dh[k] + dl[k]);
     }
     // r1 + r2 in double-float
     float sh, se;
@@ -446,25 +449,90 @@ __device__ __forceinline__ bool hist_find_m(const Dev& d, const SysParams& sp, i
     return false;
 }
 
-// Minimum resident blocks per SM asked of ptxas for k_dem_mixed: 4 caps it at
-// 128 registers (from 162) with ~130 B of spills and runs 16 % faster on GB300
-// (256-replica gas ensemble) than no cap; a compile-time tuning knob.
-#ifndef MDG_DEM_MINB
-#define MDG_DEM_MINB 4
-#endif
-__global__ void __launch_bounds__(BLK, MDG_DEM_MINB) k_dem_mixed(Dev d) {
+// Mixed DEM force, in two passes.
+//
+// Screen (k_dem_screen): one thread per particle of a system's worklist (the
+// particles with listed partners).  With a touch-only contact law a listed
+// pair acts only while the spheres overlap, so each partner is tested on the
+// two-float separation (dh + dl, ~1e-7 of the distance) against r_i + r_j
+// with a 2e-5 margin on the squares.  A particle with no touching partner
+// gets its zero force, torque, virial and contact count written here; the
+// others are appended to one list for the whole context (warp-aggregated; the
+// order does not matter, each particle's force comes from its own row).
+// Systems with a pull-off range (JKR) send every worklist particle on.  The
+// screen needs few registers, so it runs at full occupancy with many
+// partner gathers in flight, where the contact law's registers would not.
+//
+// Contact (k_dem_contact): a fixed grid walks the list and evaluates the
+// contact law on every listed pair of each particle's row, owner frames on
+// both sides, Kahan sums; its last block clears the list for the next step.
+
+// True when some listed partner of particle i (row li of its system) may
+// overlap it.
+__device__ __forceinline__ bool dem_touching(const Dev& d, const SysParams& sp, long long i, int li) {
+    const int nn = d.nnum[i];
+    const float4 hi = d.pos2[2 * i], lo = d.pos2[2 * i + 1];
+    const long long base = sp.lst0 + li;
+    for (int k = 0; k < nn; k++) {
+        const uint32_t e = d.nlist[base + (long long)k * sp.npad];
+        const long long j = sp.p0 + (int)(e & IDX_MASK);
+        const uint32_t code = e >> IDX_BITS;
+        const int sc = (int)(code >= 27u ? code - 27u : code);
+        const float4 hj = d.pos2[2 * j], lj4 = d.pos2[2 * j + 1];
+        // |(x_j + s L) - x_i|: the same distance in either owner frame
+        float dh, dl;
+        sep_df(hj.x, lj4.x, hi.x, lo.x, sc / 9 - 1, sp.Lh[0], sp.Ll[0], dh, dl);
+        const float x = dh + dl;
+        sep_df(hj.y, lj4.y, hi.y, lo.y, (sc / 3) % 3 - 1, sp.Lh[1], sp.Ll[1], dh, dl);
+        const float y = dh + dl;
+        sep_df(hj.z, lj4.z, hi.z, lo.z, sc % 3 - 1, sp.Lh[2], sp.Ll[2], dh, dl);
+        const float z = dh + dl;
+        const float rs = hi.w + hj.w;
+        if (x * x + y * y + z * z <= rs * rs * 1.00002f) return true;
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(BLK) k_dem_screen(Dev d) {
     const int gb = d.blk_run[blockIdx.x];
     const int s = d.blk_sys[gb];
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
-    if (sp.kind != 0 || !sys_active(st)) return;
-    const int hcur = st->hcur;
-    // the system's worklist: particles with listed partners (the others keep
-    // the zero force, torque and history written at the build)
+    if (sp.kind != 0 || !sys_active(st)) return;  // uniform over the block
     const int k = (gb - sp.b0) * BLK + threadIdx.x;
-    if (k >= d.dem_wl_n[s]) return;
-    const int li = d.dem_wl[sp.p0 + k];
-    const long long i = (long long)sp.p0 + li;
+    bool contact = false;
+    long long i = 0;
+    if (k < d.dem_wl_n[s]) {
+        const int li = d.dem_wl[sp.p0 + k];
+        i = (long long)sp.p0 + li;
+        contact = !sp.touch_only || dem_touching(d, sp, i, li);
+        if (!contact) {
+            d.frc[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+            d.trq[i] = make_double4(0.0, 0.0, 0.0, 0.0);
+            d.hcnt[st->hcur ^ 1][i] = 0;
+            if (sp.virial)
+                for (int q = 0; q < 6; q++) d.vir[q * d.P + i] = 0.0;
+        }
+    }
+    const unsigned int m = __ballot_sync(0xffffffffu, contact);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(d.dem_cl_n, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (contact) d.dem_cl[base + __popc(m & ((1u << lane) - 1u))] = (int)i;
+}
+
+// The contact law over the row of particle i of system s: force, torque,
+// the next history buffer, the large-overlap count and (VIR) the owner-side
+// virial sum of d_a f_b (hertz_mindlin_contact_force's add_pair,
+// contact.rs:559-569; fp32 pair terms summed in fp64).
+template <bool VIR>
+__device__ __forceinline__ void dem_contact_particle(const Dev& d, int s, long long i) {
+    const SysParams& sp = d.sp[s];
+    SysState* st = d.ss + s;
+    const int li = (int)(i - sp.p0);
+    const int hcur = st->hcur;
     const int hn = hcur ^ 1;
     const int nn = d.nnum[i];
     const float4 hi = d.pos2[2 * i], lo = d.pos2[2 * i + 1];
@@ -473,7 +541,10 @@ __global__ void __launch_bounds__(BLK, MDG_DEM_MINB) k_dem_mixed(Dev d) {
     const int ti_ = (int)d.type[i];
     const uint32_t tag_i = d.tag[i];
     const long long base = sp.lst0 + li;
+    const bool vir = VIR && sp.virial;
+    const float vs = sp.newton ? 1.f : 0.5f;
     Kahan3 F, T;
+    double V[6] = {0, 0, 0, 0, 0, 0};
     int nh = 0, nover = 0;
     PairMixed o;
     for (int k = 0; k < nn; k++) {
@@ -497,10 +568,10 @@ __global__ void __launch_bounds__(BLK, MDG_DEM_MINB) k_dem_mixed(Dev d) {
             sep_df(hi.z, lo.z, hj.z, lj4.z, -sz, sp.Lh[2], sp.Ll[2], dh[2], dl[2]);
         }
         if (sp.touch_only) {
-            // spheres clearly apart (2e-5 margin over the hi parts' ~1e-7
-            // error): the pair has no force, skip its state and history loads
+            // spheres clearly apart: no force, skip the partner's state and history
             const float rs = hi.w + hj.w;
-            if (dh[0] * dh[0] + dh[1] * dh[1] + dh[2] * dh[2] > rs * rs * 1.00002f) continue;
+            const float x = dh[0] + dl[0], y = dh[1] + dl[1], z = dh[2] + dl[2];
+            if (x * x + y * y + z * z > rs * rs * 1.00002f) continue;
         }
         const double4 vj = d.vel[j];
         const double4 wj = d.omg[j];
@@ -513,6 +584,15 @@ __global__ void __launch_bounds__(BLK, MDG_DEM_MINB) k_dem_mixed(Dev d) {
             if (!o.hit) continue;
             F.add(-o.fn[0], -o.fn[1], -o.fn[2]);
             if (o.overlap) nover++;
+            if (vir) {
+                // owner frame: separation owner -> partner, the owner's pair force
+                const float fx = (-o.fn[0] + (o.tang ? o.ft[0] : 0.f)) * vs;
+                const float fy = (-o.fn[1] + (o.tang ? o.ft[1] : 0.f)) * vs;
+                const float fz = (-o.fn[2] + (o.tang ? o.ft[2] : 0.f)) * vs;
+                const float x = dh[0] + dl[0], y = dh[1] + dl[1], z = dh[2] + dl[2];
+                V[0] += (double)(x * fx); V[1] += (double)(y * fy); V[2] += (double)(z * fz);
+                V[3] += (double)(x * fy); V[4] += (double)(x * fz); V[5] += (double)(y * fz);
+            }
             if (!o.tang) continue;
             F.add(o.ft[0], o.ft[1], o.ft[2]);
             T.add(o.ti[0] + o.tr[0] + o.tw[0], o.ti[1] + o.tr[1] + o.tw[1], o.ti[2] + o.tr[2] + o.tw[2]);
@@ -540,6 +620,32 @@ __global__ void __launch_bounds__(BLK, MDG_DEM_MINB) k_dem_mixed(Dev d) {
     if (nover) atomicAdd(&st->overlap, nover);
     d.frc[i] = make_double4(F.x.value(), F.y.value(), F.z.value(), 0.0);
     d.trq[i] = make_double4(T.x.value(), T.y.value(), T.z.value(), 0.0);
+    if (vir)
+        for (int q = 0; q < 6; q++) d.vir[q * d.P + i] = V[q];
+}
+
+// Minimum resident blocks per SM asked of ptxas for k_dem_contact (a
+// compile-time tuning knob: 4 caps it at 128 registers).
+#ifndef MDG_DEM_MINB
+#define MDG_DEM_MINB 4
+#endif
+constexpr int DEM_CONTACT_GRID = 152 * MDG_DEM_MINB;
+
+template <bool VIR>
+__global__ void __launch_bounds__(BLK, MDG_DEM_MINB) k_dem_contact(Dev d) {
+    const int n = *((const volatile int*)d.dem_cl_n);
+    for (int k = blockIdx.x * BLK + threadIdx.x; k < n; k += gridDim.x * BLK) {
+        const long long i = d.dem_cl[k];
+        dem_contact_particle<VIR>(d, d.blk_sys[i / BLK], i);
+    }
+    // every block has read the count: the last one to finish clears the list
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd((unsigned int*)d.dem_cl_n + 1, 1u) == gridDim.x - 1) {
+            d.dem_cl_n[0] = 0;
+            d.dem_cl_n[1] = 0;
+        }
+    }
 }
 
 // Initial integration of the mixed path: the same update as k_initial (NH
@@ -665,6 +771,8 @@ __device__ __forceinline__ void dem_wl_block(const Dev& d, int s, int lb) {
         d.trq[i] = make_double4(0.0, 0.0, 0.0, 0.0);
         d.hcnt[0][i] = 0;
         d.hcnt[1][i] = 0;
+        if (sp.virial)
+            for (int q = 0; q < 6; q++) d.vir[q * d.P + i] = 0.0;
     }
     const unsigned int m = __ballot_sync(0xffffffffu, has);
     if (!m) return;
@@ -928,8 +1036,12 @@ void launch_lj_mixed(const Dev& d, int tpp, cudaStream_t st) {
 int launch_force_mixed(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st) {
     int n = 0;
     if (has_dem) {
-        k_dem_mixed<<<d.nrun, BLK, 0, st>>>(d);
-        n++;
+        k_dem_screen<<<d.nrun, BLK, 0, st>>>(d);
+        if (d.vir)
+            k_dem_contact<true><<<DEM_CONTACT_GRID, BLK, 0, st>>>(d);
+        else
+            k_dem_contact<false><<<DEM_CONTACT_GRID, BLK, 0, st>>>(d);
+        n += 2;
     }
     if (has_lj) {
         if (d.lj_multi) {  // some system has a multi-type pair table

@@ -378,3 +378,57 @@ def test_mixed_lj_virial(gpu_lib, newton):
         pa = ta["pressure"] - 864 / 10.06 ** 3 * ta["temp"]
         pb = tb["pressure"] - 864 / 10.06 ** 3 * tb["temp"]
         assert abs(pb - pa) <= tol * np.max(np.abs(wa)) / 10.06 ** 3
+
+
+def test_mixed_dem_virial(gpu_lib):
+    """Precision form, DEM with a virial (contact.rs:559-569): the mixed
+    contact pass's owner-side sums of d_a f_b (fp32 pair terms, fp64 sums)
+    give the plain path's virial to 1e-5 of its largest component after one
+    force evaluation with seeded springs, and to 1e-4 after 30 steps."""
+    st = _dem_state(seed=27)
+    c64 = _dem_cfg(virial=True)
+    o = _oracle(c64, st)
+    o.force_only()
+    keys, vals = o.history()
+    vals = np.random.default_rng(28).normal(scale=1e-6, size=vals.shape)
+    a, b = _ctx(c64, st), _ctx(c64.replace(precision="mixed"), st)
+    a.set_history(keys, vals)
+    b.set_history(keys, vals)
+    a.force_only()
+    b.force_only()
+    wa, wb = np.array(a.thermo()["virial"]), np.array(b.thermo()["virial"])
+    assert np.max(np.abs(wa)) > 0
+    assert np.max(np.abs(wb - wa)) <= 1e-5 * np.max(np.abs(wa))
+    a2, b2 = _ctx(c64, st), _ctx(c64.replace(precision="mixed"), st)
+    a2.step(30)
+    b2.step(30)
+    wa, wb = np.array(a2.thermo()["virial"]), np.array(b2.thermo()["virial"])
+    assert np.max(np.abs(wb - wa)) <= 1e-4 * np.max(np.abs(wa))
+
+
+def test_mixed_dem_grazing_contacts_in_a_large_box(gpu_lib):
+    """Pairs overlapping by 1e-8 m (5e-6 of the radius sum) scattered through
+    a 0.25 m box, where the lo parts of the two-float positions reach ~1e-8 m:
+    the mixed path screens on the full two-float separation and keeps the
+    dl^2 term of the squared distance, so every pair acts, with the fp64
+    path's force to 1e-5."""
+    from mddem_gb300 import config, inputs
+
+    rng = np.random.default_rng(30)
+    L, r, npair = 0.25, 1e-3, 200
+    a = rng.uniform(0.01, L - 0.01, size=(npair, 3))
+    u = rng.normal(size=(npair, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    b = a + u * (2 * r - 1e-8)
+    pos = np.empty((2 * npair, 3))
+    pos[0::2], pos[1::2] = a, b
+    st = inputs._dem_state(pos, np.zeros((2 * npair, 3)), np.full(2 * npair, r), 2500.0)
+    cfg = config.granular_gas_config(box=L, dt=1e-7)
+    c64, cmx = _ctx(cfg, st), _ctx(cfg.replace(precision="mixed"), st)
+    c64.force_only()
+    cmx.force_only()
+    (f64,) = by_tag(c64.download(), "force")
+    (fmx,) = by_tag(cmx.download(), "force")
+    mag = np.linalg.norm(f64, axis=1)
+    assert np.all(mag > 0)
+    assert rel_err(fmx, f64, mag) <= 1e-5
