@@ -151,6 +151,7 @@ struct mdg_ctx {
     bool maps_dirty = true;
     std::vector<int> cblk0_host, cseg_blocks;  // cell segment of each system
     int* d_blk_run = nullptr;
+    int* d_blk_run_kind[2] = {nullptr, nullptr};
     int* d_cblk_run = nullptr;
     int* d_run_sys = nullptr;
     Dev d{};
@@ -553,10 +554,13 @@ int update_run_maps(mdg_ctx* c) {
     for (int s = 0; s < c->nsys; s++)
         if (c->uploaded[s] && c->rem_host[s] != 0) run.push_back(s);
     if (!c->maps_dirty && run == c->run_sys) return (int)run.size();
-    std::vector<int> pb, cb;
+    std::vector<int> pb, cb, pk[2];
     for (int s : run) {
         const SysParams& p = c->sp[s];
-        for (int b = 0; b < p.nb; b++) pb.push_back(p.b0 + b);
+        for (int b = 0; b < p.nb; b++) {
+            pb.push_back(p.b0 + b);
+            pk[p.kind == 1 ? 1 : 0].push_back(p.b0 + b);
+        }
         for (int b = 0; b < c->cseg_blocks[s]; b++) cb.push_back(c->cblk0_host[s] + b);
     }
     if (!pb.empty() &&
@@ -564,6 +568,13 @@ int update_run_maps(mdg_ctx* c) {
          cudaMemcpy(c->d_cblk_run, cb.data(), cb.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
          cudaMemcpy(c->d_run_sys, run.data(), run.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess))
         return -MDG_ERR_CUDA;
+    for (int q = 0; q < 2; q++) {
+        if (!pk[q].empty() && cudaMemcpy(c->d_blk_run_kind[q], pk[q].data(), pk[q].size() * sizeof(int),
+                                         cudaMemcpyHostToDevice) != cudaSuccess)
+            return -MDG_ERR_CUDA;
+        c->d.blk_run_kind[q] = c->d_blk_run_kind[q];
+        c->d.nrun_kind[q] = (int)pk[q].size();
+    }
     c->drop_graphs();  // grid sizes follow the maps
     c->d.blk_run = c->d_blk_run;
     c->d.cblk_run = c->d_cblk_run;
@@ -975,6 +986,7 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     d.blkpart = c->alloc<double>((size_t)nblocks * 8, err);
     c->d_blk_sys = c->alloc<int>(nblocks, err);
     c->d_blk_run = c->alloc<int>(nblocks, err);
+    for (int q = 0; q < 2; q++) c->d_blk_run_kind[q] = c->alloc<int>(nblocks, err);
     c->d_run_sys = c->alloc<int>(nsys, err);
     d.rb_sys = c->alloc<int>(nsys + 1, err);
     d.rb_poff = c->alloc<int>(nsys + 1, err);
@@ -1335,8 +1347,10 @@ int mdg_step(mdg_ctx* c, int64_t nsteps) {
     advance_budgets(c, nsteps);
     // kernels that ran: per step initial + force + final (+ loop control),
     // plus the rebuild kernels on the steps whose rebuild branch opened
-    // (the mixed DEM force is two kernels: screen and contact)
-    const long long nforce = (c->has_lj ? 1 : 0) + (c->has_dem ? (c->has_mixed ? 2 : 1) : 0) + (c->has_walls ? 1 : 0);
+    // (the mixed DEM force is two kernels: screen and contact; each kind's
+    // force kernels launch only while some system of that kind runs)
+    const long long nforce = (c->d.nrun_kind[1] ? 1 : 0) + (c->d.nrun_kind[0] ? (c->has_mixed ? 2 : 1) : 0) +
+                             (c->has_walls ? 1 : 0);
     long long base = 2 + nforce + (c->graph_mode ? 1 : 0);
     if (c->graph_mode && c->has_mixed) {
         // fused step kernel (+ thermostatted initial) per iteration, the

@@ -202,6 +202,10 @@ struct Dev {
     int ncrun;
     const int* run_sys;   // the running systems, ascending
     int nrun_sys;
+    // the run map's blocks split by particle kind (ascending): the force
+    // kernels of one kind launch over its blocks only
+    const int* blk_run_kind[2];  // [0] DEM, [1] LJ
+    int nrun_kind[2];
     // Rebuild work list, written on the device by k_rb_plan when a step
     // rebuilds: the systems that sort or rebuild, with prefix offsets of their
     // particle blocks and cell blocks (rb_poff / rb_coff have rb_n + 1 entries).
@@ -284,6 +288,36 @@ __device__ __forceinline__ float3 fixed_sep(const SysParams& sp, const uint4& uj
                        (float)(int)(uj.z - ui.z) * sp.uscale[2]);
 }
 
+// Conversions between double and float by integer operations.  On GB300 the
+// hardware conversions run on the FP64 pipe at the rate of a DFMA (measured
+// ~0.6 T/s, against ~36 T/s for FFMA), so the mixed integrators convert with
+// these instead.  dbl_to_flt rounds to nearest (ties away from zero), so
+// its errors carry no bias that a long run could accumulate (|x| < 2^-126
+// gives a signed zero, |x| >= 2^128 infinity); flt_to_dbl is exact for normal
+// floats (subnormals give zero).  Finite inputs.
+__device__ __forceinline__ float dbl_to_flt(double x) {
+    // half of the 29 dropped mantissa bits; a carry moves into the exponent
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x) + (1ull << 28);
+    const unsigned int hi = (unsigned int)(b >> 32);
+    const unsigned int sign = hi & 0x80000000u;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 896;  // rebias 1023 -> 127
+    if (e <= 0) return __uint_as_float(sign);
+    if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
+    return __uint_as_float(sign | ((unsigned int)e << 23) | ((unsigned int)(b >> 29) & 0x7fffffu));
+}
+__device__ __forceinline__ double flt_to_dbl(float f) {
+    const unsigned int b = __float_as_uint(f);
+    const unsigned int e = (b >> 23) & 0xffu;
+    const unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
+    if (e == 0) return __longlong_as_double((long long)sign);
+    return __longlong_as_double(
+        (long long)(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+// x != 0 for a double, by its bits (no FP64 compare)
+__device__ __forceinline__ bool dbl_nonzero(double x) {
+    return ((unsigned long long)__double_as_longlong(x) << 1) != 0ull;
+}
+
 // Geometry copy of a mixed-precision particle after its drift (tx, ty, tz)
 // to the fp64 position x, and its rebuild request (decide_rebuild's per-atom
 // tests, neighbor.rs:564-674) when test is set: displacement since the last
@@ -292,7 +326,7 @@ __device__ __forceinline__ float3 fixed_sep(const SysParams& sp, const uint4& uj
 // the fixed-point copy (box exit tested on the fp64 position, as the
 // reference does); DEM systems the two-float copy.
 __device__ __forceinline__ bool mixed_drift(const Dev& d, const SysParams& sp, long long i, const double4& x,
-                                            double tx, double ty, double tz, bool test, int ssb) {
+                                            float tx, float ty, float tz, bool test, int ssb) {
     if (sp.kind == 1) {
         const uint4 u = fixed_pos(sp, x);
         d.posu[i] = u;
@@ -308,9 +342,9 @@ __device__ __forceinline__ bool mixed_drift(const Dev& d, const SysParams& sp, l
     // advance the two-float copy by the same drift in fp32 (exact two-sum,
     // renormalised); it is re-derived from the fp64 position at every build
     float4 ph = d.pos2[2 * i], pl = d.pos2[2 * i + 1];
-    two_float_add(ph.x, pl.x, (float)tx);
-    two_float_add(ph.y, pl.y, (float)ty);
-    two_float_add(ph.z, pl.z, (float)tz);
+    two_float_add(ph.x, pl.x, tx);
+    two_float_add(ph.y, pl.y, ty);
+    two_float_add(ph.z, pl.z, tz);
     d.pos2[2 * i] = ph;
     d.pos2[2 * i + 1] = pl;
     if (!test) return false;
@@ -326,6 +360,15 @@ __device__ __forceinline__ bool mixed_drift(const Dev& d, const SysParams& sp, l
              (sp.per[2] && (rz < 0.f || rz >= sp.Lh[2]));
     }
     return nd;
+}
+
+// The device view restricted to the running blocks of one particle kind
+// (kind 0 DEM, 1 LJ): for kernels that only act on that kind.
+__host__ __forceinline__ Dev kind_view(const Dev& d, int kind) {
+    Dev k = d;
+    k.blk_run = d.blk_run_kind[kind];
+    k.nrun = d.nrun_kind[kind];
+    return k;
 }
 
 // ---- kernel launchers (mdg_kernels_fp64.cu / mdg_kernels_mixed.cu) ----------

@@ -80,7 +80,8 @@ __global__ void __launch_bounds__(BLK) k_initial(Dev d) {
         x.z += tz;
         d.vel[i] = v;
         d.pos[i] = x;
-        if (sp.precision == 1) need = mixed_drift(d, sp, i, x, tx, ty, tz, !already, st->steps_since_build);
+        if (sp.precision == 1)
+            need = mixed_drift(d, sp, i, x, (float)tx, (float)ty, (float)tz, !already, st->steps_since_build);
         if (sp.kind == 0) {
             double4 w = d.omg[i];
             if (w.w != 0.0) {
@@ -1825,9 +1826,12 @@ int launch_rebuild(const Dev& d, cudaStream_t st) {
     return 9;
 }
 
-int launch_force_fp64(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st) {
+int launch_force_fp64(const Dev& dall, int has_lj, int has_dem, int tpp, cudaStream_t st) {
     int n = 0;
+    has_dem = has_dem && dall.nrun_kind[0] > 0;
+    has_lj = has_lj && dall.nrun_kind[1] > 0;
     if (has_lj) {
+        const Dev d = kind_view(dall, 1);
         if (d.lj_multi) {
             switch (tpp) {
                 case 2: k_lj_fp64<2, true><<<d.nrun * 2, BLK, 0, st>>>(d); break;
@@ -1846,6 +1850,7 @@ int launch_force_fp64(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream
         n++;
     }
     if (has_dem) {
+        const Dev d = kind_view(dall, 0);
         k_dem_fp64<<<d.nrun, BLK, 0, st>>>(d);
         n++;
     }

@@ -648,14 +648,63 @@ __global__ void __launch_bounds__(BLK, MDG_DEM_MINB) k_dem_contact(Dev d) {
     }
 }
 
+// Per-particle pieces of the mixed integrators, shared by the separate
+// initial / final kernels and the fused step kernel (so both give the same
+// bits).  FP64 arithmetic is kept to the Verlet kicks and the drift (FMA
+// form), the spin kicks and the quaternion sum; conversions go through
+// dbl_to_flt / flt_to_dbl (integer operations), and the rotation increment is
+// fp32.  A DEM particle-step costs 22 FP64-pipe operations.
+
+// dt as an unevaluated fp32 sum hi + lo (one FP64 subtraction)
+__device__ __forceinline__ float2 dt_split(double dt) {
+    const float h = dbl_to_flt(dt);
+    return make_float2(h, dbl_to_flt(dt - flt_to_dbl(h)));
+}
+
+// drift x += v dt (FMA) and the fp32 displacement for the geometry copy of
+// the particle, v (rounded to fp32) times the two-float dt: unbiased, ~1e-7
+// relative
+__device__ __forceinline__ void drift_mixed(double4& x, const double4& v, double dt, float2 dts, float& tx, float& ty,
+                                            float& tz) {
+    x.x = fma(v.x, dt, x.x);
+    x.y = fma(v.y, dt, x.y);
+    x.z = fma(v.z, dt, x.z);
+    const float vx = dbl_to_flt(v.x), vy = dbl_to_flt(v.y), vz = dbl_to_flt(v.z);
+    tx = fmaf(vx, dts.x, vx * dts.y);
+    ty = fmaf(vy, dts.x, vy * dts.y);
+    tz = fmaf(vz, dts.x, vz * dts.y);
+}
+
+// initial_rotation's quaternion update (rotational.rs:59-84): q' = dq * q
+// with dq = (cos(angle/2), sin(angle/2) w / |w|), angle = |w| dt.  The
+// increment q' - q = (c1, a) * q, c1 = cos(angle/2) - 1 = -2 sin^2(angle/4)
+// (full relative precision for small angles), is formed in fp32 from an
+// fp32 copy of q and added to the fp64 q: its error is ~1e-7 of the
+// increment, about 1e-7 x angle/2 per step.
+__device__ __forceinline__ void rotate_mixed(const Dev& d, long long i, const double4& w, float dtf) {
+    const float wx = dbl_to_flt(w.x), wy = dbl_to_flt(w.y), wz = dbl_to_flt(w.z);
+    const float om = sqrtf(wx * wx + wy * wy + wz * wz);
+    const float angle = om * dtf;
+    if (!(angle > 1e-14f)) return;
+    const float half = 0.5f * angle;
+    const float sq = sinf(0.5f * half);
+    const float c1 = -2.f * sq * sq;
+    const float k = sinf(half) / om;
+    const float a1 = wx * k, a2 = wy * k, a3 = wz * k;
+    const double4 q = d.quat[i];
+    const float qw = dbl_to_flt(q.x), qx = dbl_to_flt(q.y), qy = dbl_to_flt(q.z), qz = dbl_to_flt(q.w);
+    const float rw = c1 * qw - (a1 * qx + a2 * qy + a3 * qz);
+    const float rx = c1 * qx + (a1 * qw + a2 * qz - a3 * qy);
+    const float ry = c1 * qy + (a2 * qw + a3 * qx - a1 * qz);
+    const float rz = c1 * qz + (a3 * qw + a1 * qy - a2 * qx);
+    d.quat[i] = make_double4(q.x + flt_to_dbl(rw), q.y + flt_to_dbl(rx), q.z + flt_to_dbl(ry), q.w + flt_to_dbl(rz));
+}
+
 // Initial integration of the mixed path: the same update as k_initial (NH
 // scale, half kick, drift, two-float drift copy, fp32 rebuild test, half
-// spin kick, quaternion update) with FP64 kept for x, v, omega and q, FMA
-// contraction, and the rotation increment of initial_rotation
-// (rotational.rs:59-84) formed in FP32: |omega|, sin and cos of the half angle
-// are fp32, cos as 1 - 2 sin^2(angle/4) so its tiny deviation from 1 keeps
-// full relative precision, and the Hamilton product dq * q runs in FP64.  Per
-// step this perturbs q by about 1e-7 x angle/2 (angle = |omega| dt).
+// spin kick, quaternion update) with FP64 state for x, v, omega and q, FMA
+// contraction, and the rotation of initial_rotation (rotational.rs:59-84)
+// by rotate_mixed.
 //
 // nh_only: only thermostatted systems (the multi-step graph's fused kernel
 // below does the others), and nothing on the first iteration of a launch
@@ -690,38 +739,22 @@ __global__ void __launch_bounds__(BLK) k_initial_mixed(Dev d, int nh_only, const
         v.x = fma(h, f.x, v.x);
         v.y = fma(h, f.y, v.y);
         v.z = fma(h, f.z, v.z);
-        const double tx = v.x * dt, ty = v.y * dt, tz = v.z * dt;
-        x.x += tx;
-        x.y += ty;
-        x.z += tz;
+        const float2 dts = dt_split(dt);
+        const float dtf = dts.x;
+        float tx, ty, tz;
+        drift_mixed(x, v, dt, dts, tx, ty, tz);
         d.vel[i] = v;
         d.pos[i] = x;
         need = mixed_drift(d, sp, i, x, tx, ty, tz, !already, st->steps_since_build);
         if (sp.kind == 0) {
             double4 w = d.omg[i];
-            if (w.w != 0.0) {
+            if (dbl_nonzero(w.w)) {
                 const double4 tq = d.trq[i];
                 const double hw = 0.5 * dt * w.w;
                 w.x = fma(hw, tq.x, w.x);
                 w.y = fma(hw, tq.y, w.y);
                 w.z = fma(hw, tq.z, w.z);
-                const float wx = (float)w.x, wy = (float)w.y, wz = (float)w.z;
-                const float om = sqrtf(wx * wx + wy * wy + wz * wz);
-                const float angle = om * (float)dt;
-                if (angle > 1e-14f) {
-                    const float half = 0.5f * angle;
-                    const float sq = sinf(0.5f * half);
-                    const double c1 = (double)(-2.f * sq * sq);  // cos(half) - 1
-                    const float k = sinf(half) / om;
-                    const double a1 = (double)(wx * k), a2 = (double)(wy * k), a3 = (double)(wz * k);
-                    const double4 q = d.quat[i];
-                    double4 r;  // (1 + c1, a) * q, Hamilton product (rotational.rs:34-41)
-                    r.x = fma(c1, q.x, q.x) - (a1 * q.y + a2 * q.z + a3 * q.w);
-                    r.y = fma(c1, q.y, q.y) + (a1 * q.x + a2 * q.w - a3 * q.z);
-                    r.z = fma(c1, q.z, q.z) + (a2 * q.x + a3 * q.y - a1 * q.w);
-                    r.w = fma(c1, q.w, q.w) + (a3 * q.x + a1 * q.z - a2 * q.y);
-                    d.quat[i] = r;
-                }
+                rotate_mixed(d, i, w, dtf);
                 d.omg[i] = w;
             }
         }
@@ -827,7 +860,7 @@ __global__ void __launch_bounds__(BLK) k_final_mixed(Dev d, int integrate) {
         if (sp.nh) ke2 = d.mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z);
         if (sp.kind == 0 && integrate) {
             double4 w = d.omg[i];
-            if (w.w != 0.0) {
+            if (dbl_nonzero(w.w)) {
                 const double4 tq = d.trq[i];
                 const double hw = 0.5 * dt * w.w;
                 w.x = fma(hw, tq.x, w.x);
@@ -879,6 +912,8 @@ __global__ void __launch_bounds__(BLK) k_step_mixed(Dev d, const long long* loop
     const int li = (gb - sp.b0) * BLK + threadIdx.x;
     const long long i = (long long)sp.p0 + li;
     const double dt = sp.dt;
+    const float2 dts = dt_split(dt);
+    const float dtf = dts.x;
     const bool first = loop[0] == loop[1];
     // read before this system's last block updates the bookkeeping
     const long long rem = *((volatile const long long*)&st->remaining);
@@ -920,18 +955,16 @@ __global__ void __launch_bounds__(BLK) k_step_mixed(Dev d, const long long* loop
             v.x = fma(h, f.x, v.x);
             v.y = fma(h, f.y, v.y);
             v.z = fma(h, f.z, v.z);
-            const double tx = v.x * dt, ty = v.y * dt, tz = v.z * dt;
             double4 x = d.pos[i];
-            x.x += tx;
-            x.y += ty;
-            x.z += tz;
+            float tx, ty, tz;
+            drift_mixed(x, v, dt, dts, tx, ty, tz);
             d.pos[i] = x;
             need = mixed_drift(d, sp, i, x, tx, ty, tz, true, ssb);
         }
         d.vel[i] = v;
         if (sp.kind == 0) {
             double4 w = d.omg[i];
-            if (w.w != 0.0) {
+            if (dbl_nonzero(w.w)) {
                 const double4 tq = d.trq[i];
                 const double hw = 0.5 * dt * w.w;
                 if (fin) {
@@ -943,23 +976,7 @@ __global__ void __launch_bounds__(BLK) k_step_mixed(Dev d, const long long* loop
                     w.x = fma(hw, tq.x, w.x);
                     w.y = fma(hw, tq.y, w.y);
                     w.z = fma(hw, tq.z, w.z);
-                    const float wx = (float)w.x, wy = (float)w.y, wz = (float)w.z;
-                    const float om = sqrtf(wx * wx + wy * wy + wz * wz);
-                    const float angle = om * (float)dt;
-                    if (angle > 1e-14f) {
-                        const float half = 0.5f * angle;
-                        const float sq = sinf(0.5f * half);
-                        const double c1 = (double)(-2.f * sq * sq);
-                        const float k = sinf(half) / om;
-                        const double a1 = (double)(wx * k), a2 = (double)(wy * k), a3 = (double)(wz * k);
-                        const double4 q = d.quat[i];
-                        double4 r;
-                        r.x = fma(c1, q.x, q.x) - (a1 * q.y + a2 * q.z + a3 * q.w);
-                        r.y = fma(c1, q.y, q.y) + (a1 * q.x + a2 * q.w - a3 * q.z);
-                        r.z = fma(c1, q.z, q.z) + (a2 * q.x + a3 * q.y - a1 * q.w);
-                        r.w = fma(c1, q.w, q.w) + (a3 * q.x + a1 * q.z - a2 * q.y);
-                        d.quat[i] = r;
-                    }
+                    rotate_mixed(d, i, w, dtf);
                 }
                 d.omg[i] = w;
             }
@@ -1024,7 +1041,8 @@ int launch_initial_mixed(const Dev& d, cudaStream_t st, int nh_only, const long 
 }
 
 template <bool VIR, bool MT>
-void launch_lj_mixed(const Dev& d, int tpp, cudaStream_t st) {
+void launch_lj_mixed(const Dev& dall, int tpp, cudaStream_t st) {
+    const Dev d = kind_view(dall, 1);
     switch (tpp) {
         case 2: k_lj_mixed<2, VIR, MT><<<d.nrun * 2, BLK, 0, st>>>(d); break;
         case 4: k_lj_mixed<4, VIR, MT><<<d.nrun * 4, BLK, 0, st>>>(d); break;
@@ -1035,8 +1053,10 @@ void launch_lj_mixed(const Dev& d, int tpp, cudaStream_t st) {
 
 int launch_force_mixed(const Dev& d, int has_lj, int has_dem, int tpp, cudaStream_t st) {
     int n = 0;
+    has_dem = has_dem && d.nrun_kind[0] > 0;
+    has_lj = has_lj && d.nrun_kind[1] > 0;
     if (has_dem) {
-        k_dem_screen<<<d.nrun, BLK, 0, st>>>(d);
+        k_dem_screen<<<d.nrun_kind[0], BLK, 0, st>>>(kind_view(d, 0));
         if (d.vir)
             k_dem_contact<true><<<DEM_CONTACT_GRID, BLK, 0, st>>>(d);
         else
