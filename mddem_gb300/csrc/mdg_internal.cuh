@@ -293,14 +293,17 @@ __device__ __forceinline__ float3 fixed_sep(const SysParams& sp, const uint4& uj
 // ~0.6 T/s, against ~36 T/s for FFMA), so the mixed integrators convert with
 // these instead.  dbl_to_flt rounds to nearest (ties away from zero), so
 // its errors carry no bias that a long run could accumulate (|x| < 2^-126
-// gives a signed zero, |x| >= 2^128 infinity); flt_to_dbl is exact for normal
-// floats (subnormals give zero).  Finite inputs.
+// gives a signed zero, finite |x| >= 2^128 infinity); flt_to_dbl is exact for
+// normal floats (subnormals give zero).  Both keep infinities and NaNs, so a
+// non-finite force still reaches the integrators' NaN check.
 __device__ __forceinline__ float dbl_to_flt(double x) {
+    const unsigned long long raw = (unsigned long long)__double_as_longlong(x);
+    const unsigned int sign = (unsigned int)(raw >> 32) & 0x80000000u;
+    if (((raw >> 52) & 0x7ffull) == 0x7ffull)  // inf or NaN
+        return __uint_as_float(sign | 0x7f800000u | ((raw << 12) ? 0x400000u : 0u));
     // half of the 29 dropped mantissa bits; a carry moves into the exponent
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x) + (1ull << 28);
-    const unsigned int hi = (unsigned int)(b >> 32);
-    const unsigned int sign = hi & 0x80000000u;
-    const int e = (int)((hi >> 20) & 0x7ffu) - 896;  // rebias 1023 -> 127
+    const unsigned long long b = raw + (1ull << 28);
+    const int e = (int)((b >> 52) & 0x7ffull) - 896;  // rebias 1023 -> 127
     if (e <= 0) return __uint_as_float(sign);
     if (e >= 255) return __uint_as_float(sign | 0x7f800000u);
     return __uint_as_float(sign | ((unsigned int)e << 23) | ((unsigned int)(b >> 29) & 0x7fffffu));
@@ -310,8 +313,12 @@ __device__ __forceinline__ double flt_to_dbl(float f) {
     const unsigned int e = (b >> 23) & 0xffu;
     const unsigned long long sign = (unsigned long long)(b & 0x80000000u) << 32;
     if (e == 0) return __longlong_as_double((long long)sign);
-    return __longlong_as_double(
-        (long long)(sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
+    const unsigned long long de = e == 255u ? 0x7ffull : (unsigned long long)(e + 896u);
+    return __longlong_as_double((long long)(sign | (de << 52) | ((unsigned long long)(b & 0x7fffffu) << 29)));
+}
+// -x when flip, else x: a sign-bit flip (no FP64 multiply by -1)
+__device__ __forceinline__ double neg_if(double x, bool flip) {
+    return __longlong_as_double(__double_as_longlong(x) ^ (flip ? (long long)0x8000000000000000ull : 0ll));
 }
 // x != 0 for a double, by its bits (no FP64 compare)
 __device__ __forceinline__ bool dbl_nonzero(double x) {

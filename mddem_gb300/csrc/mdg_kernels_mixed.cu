@@ -20,7 +20,7 @@ struct Kahan {
         c = (t - s) - y;
         s = t;
     }
-    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+    __device__ __forceinline__ double value() const { return flt_to_dbl(s) - flt_to_dbl(c); }
 };
 
 // LJ 12-6 in FP32 with compensated per-particle sums (same list, same owner
@@ -290,7 +290,7 @@ __device__ void hm_pair_mixed(const Dev& d, const SysParams& sp, const float (&d
     const float inv_dist = 1.f / distance;
     const float nx = (dh[0] + dl[0]) * inv_dist, ny = (dh[1] + dl[1]) * inv_dist, nz = (dh[2] + dl[2]) * inv_dist;
     const float g_eff = mtf(d, sp, T_GEFF, mi, mj);
-    const float inv_m_i = (float)v_i.w, inv_m_j = (float)v_j.w;
+    const float inv_m_i = dbl_to_flt(v_i.w), inv_m_j = dbl_to_flt(v_j.w);
     const float m_r = 1.f / (inv_m_i + inv_m_j);
     const float beta = mtf(d, sp, T_BETA, mi, mj);
     const float mu = mtf(d, sp, T_FRICTION, mi, mj);
@@ -310,12 +310,12 @@ __device__ void hm_pair_mixed(const Dev& d, const SysParams& sp, const float (&d
         k_t = 8.f * g_eff * sdr;
     }
     const float r1 = r1h, r2 = r2h;
-    const float oix = (float)w_i.x, oiy = (float)w_i.y, oiz = (float)w_i.z;
-    const float ojx = (float)w_j.x, ojy = (float)w_j.y, ojz = (float)w_j.z;
+    const float oix = dbl_to_flt(w_i.x), oiy = dbl_to_flt(w_i.y), oiz = dbl_to_flt(w_i.z);
+    const float ojx = dbl_to_flt(w_j.x), ojy = dbl_to_flt(w_j.y), ojz = dbl_to_flt(w_j.z);
     const float r1nx = r1 * nx, r1ny = r1 * ny, r1nz = r1 * nz;
     const float r2nx = r2 * nx, r2ny = r2 * ny, r2nz = r2 * nz;
     // relative contact velocity: translational difference first (cancellation in fp64)
-    const float dvx = (float)(v_j.x - v_i.x), dvy = (float)(v_j.y - v_i.y), dvz = (float)(v_j.z - v_i.z);
+    const float dvx = dbl_to_flt(v_j.x - v_i.x), dvy = dbl_to_flt(v_j.y - v_i.y), dvz = dbl_to_flt(v_j.z - v_i.z);
     const float vrx = dvx + (-ojy * r2nz + ojz * r2ny) - (oiy * r1nz - oiz * r1ny);
     const float vry = dvy + (-ojz * r2nx + ojx * r2nz) - (oiz * r1nx - oix * r1nz);
     const float vrz = dvz + (-ojx * r2ny + ojy * r2nx) - (oix * r1ny - oiy * r1nx);
@@ -341,32 +341,33 @@ __device__ void hm_pair_mixed(const Dev& d, const SysParams& sp, const float (&d
     if (jkr_adhesion_only) return;
     o.tang = true;
     const float vtx = vrx - v_n * nx, vty = vry - v_n * ny, vtz = vrz - v_n * nz;
-    const double sign = tag_i < tag_j ? 1.0 : -1.0;
+    const bool flip = !(tag_i < tag_j);  // canonical (lower-tag) frame of the stored springs
     const double dt = sp.dt;
-    const double ndx = nx, ndy = ny, ndz = nz;
+    const double ndx = flt_to_dbl(nx), ndy = flt_to_dbl(ny), ndz = flt_to_dbl(nz);
     // spring integration in fp64
-    double sx = sign * stored[0], sy = sign * stored[1], sz = sign * stored[2];
+    double sx = neg_if(stored[0], flip), sy = neg_if(stored[1], flip), sz = neg_if(stored[2], flip);
     const double sdn = sx * ndx + sy * ndy + sz * ndz;
     sx -= sdn * ndx;
     sy -= sdn * ndy;
     sz -= sdn * ndz;
-    sx += (double)vtx * dt;
-    sy += (double)vty * dt;
-    sz += (double)vtz * dt;
+    sx = fma(flt_to_dbl(vtx), dt, sx);
+    sy = fma(flt_to_dbl(vty), dt, sy);
+    sz = fma(flt_to_dbl(vtz), dt, sz);
     const float ktt = hooke ? kt : k_t;
-    const float s_mag = sqrtf((float)(sx * sx + sy * sy + sz * sz));
+    const float sfx = dbl_to_flt(sx), sfy = dbl_to_flt(sy), sfz = dbl_to_flt(sz);
+    const float s_mag = sqrtf(sfx * sfx + sfy * sfy + sfz * sfz);
     const float fts = ktt * s_mag;
     const float ft_max = mu * fabsf(f_n_mag);
     if (fts > ft_max && fts > EPS) {
-        const double sc = (double)(ft_max / fts);
+        const double sc = flt_to_dbl(ft_max / fts);
         sx *= sc;
         sy *= sc;
         sz *= sc;
     }
     const float gamma_t = 2.f * SQRT_5_3 * beta * sqrtf(ktt * m_r);
-    float ftx = ktt * (float)sx - gamma_t * vtx;
-    float fty = ktt * (float)sy - gamma_t * vty;
-    float ftz = ktt * (float)sz - gamma_t * vtz;
+    float ftx = ktt * dbl_to_flt(sx) - gamma_t * vtx;
+    float fty = ktt * dbl_to_flt(sy) - gamma_t * vty;
+    float ftz = ktt * dbl_to_flt(sz) - gamma_t * vtz;
     const float ftm = sqrtf(ftx * ftx + fty * fty + ftz * ftz);
     if (ftm > ft_max && ftm > EPS) {
         const float sc = ft_max / ftm;
@@ -378,11 +379,11 @@ __device__ void hm_pair_mixed(const Dev& d, const SysParams& sp, const float (&d
     o.ti[0] = r1ny * ftz - r1nz * fty; o.ti[1] = r1nz * ftx - r1nx * ftz; o.ti[2] = r1nx * fty - r1ny * ftx;
     o.tj[0] = r2ny * ftz - r2nz * fty; o.tj[1] = r2nz * ftx - r2nx * ftz; o.tj[2] = r2nx * fty - r2ny * ftx;
     // relative spin from the fp64 angular velocities
-    const float orx = (float)(w_i.x - w_j.x), ory = (float)(w_i.y - w_j.y), orz = (float)(w_i.z - w_j.z);
+    const float orx = dbl_to_flt(w_i.x - w_j.x), ory = dbl_to_flt(w_i.y - w_j.y), orz = dbl_to_flt(w_i.z - w_j.z);
     const float odn = orx * nx + ory * ny + orz * nz;
     const float rollx = orx - odn * nx, rolly = ory - odn * ny, rollz = orz - odn * nz;
-    double rdx = sign * stored[3], rdy = sign * stored[4], rdz = sign * stored[5];
-    double twd = sign * stored[6];
+    double rdx = neg_if(stored[3], flip), rdy = neg_if(stored[4], flip), rdz = neg_if(stored[5], flip);
+    double twd = neg_if(stored[6], flip);
     o.tr[0] = o.tr[1] = o.tr[2] = 0.f;
     o.tw[0] = o.tw[1] = o.tw[2] = 0.f;
     if (mu_r > 0.f) {
@@ -392,19 +393,19 @@ __device__ void hm_pair_mixed(const Dev& d, const SysParams& sp, const float (&d
             const float g_roll = mtf(d, sp, T_GROLL, mi, mj);
             const double rdn = rdx * ndx + rdy * ndy + rdz * ndz;
             rdx -= rdn * ndx; rdy -= rdn * ndy; rdz -= rdn * ndz;
-            rdx += (double)rollx * dt; rdy += (double)rolly * dt; rdz += (double)rollz * dt;
-            float tx = -k_roll * (float)rdx - g_roll * rollx;
-            float ty = -k_roll * (float)rdy - g_roll * rolly;
-            float tz = -k_roll * (float)rdz - g_roll * rollz;
+            rdx = fma(flt_to_dbl(rollx), dt, rdx); rdy = fma(flt_to_dbl(rolly), dt, rdy); rdz = fma(flt_to_dbl(rollz), dt, rdz);
+            float tx = -k_roll * dbl_to_flt(rdx) - g_roll * rollx;
+            float ty = -k_roll * dbl_to_flt(rdy) - g_roll * rolly;
+            float tz = -k_roll * dbl_to_flt(rdz) - g_roll * rollz;
             const float trm = sqrtf(tx * tx + ty * ty + tz * tz);
             const float tau_max = mu_r * fabsf(f_n_mag) * r_eff;
             if (trm > tau_max && trm > EPS) {
                 const float sc = tau_max / trm;
                 tx *= sc; ty *= sc; tz *= sc;
                 if (k_roll > EPS) {
-                    rdx = (double)((tx + g_roll * rollx) / (-k_roll));
-                    rdy = (double)((ty + g_roll * rolly) / (-k_roll));
-                    rdz = (double)((tz + g_roll * rollz) / (-k_roll));
+                    rdx = flt_to_dbl((tx + g_roll * rollx) / (-k_roll));
+                    rdy = flt_to_dbl((ty + g_roll * rolly) / (-k_roll));
+                    rdz = flt_to_dbl((tz + g_roll * rollz) / (-k_roll));
                 }
             }
             o.tr[0] = tx; o.tr[1] = ty; o.tr[2] = tz;
@@ -418,12 +419,12 @@ __device__ void hm_pair_mixed(const Dev& d, const SysParams& sp, const float (&d
         if (sp.twisting_model == 1) {
             const float k_tw = mtf(d, sp, T_KTWIST, mi, mj);
             const float g_tw = mtf(d, sp, T_GTWIST, mi, mj);
-            twd += (double)twist_vel * dt;
-            float tau_tw = -k_tw * (float)twd - g_tw * twist_vel;
+            twd = fma(flt_to_dbl(twist_vel), dt, twd);
+            float tau_tw = -k_tw * dbl_to_flt(twd) - g_tw * twist_vel;
             const float tau_max = mu_tw * fabsf(f_n_mag) * r_eff;
             if (fabsf(tau_tw) > tau_max) {
                 tau_tw = copysignf(1.f, tau_tw) * tau_max;
-                if (k_tw > EPS) twd = (double)((tau_tw + g_tw * twist_vel) / (-k_tw));
+                if (k_tw > EPS) twd = flt_to_dbl((tau_tw + g_tw * twist_vel) / (-k_tw));
             }
             o.tw[0] = tau_tw * nx; o.tw[1] = tau_tw * ny; o.tw[2] = tau_tw * nz;
         } else if (fabsf(twist_vel) > 1e-30f) {
@@ -432,9 +433,9 @@ __device__ void hm_pair_mixed(const Dev& d, const SysParams& sp, const float (&d
             o.tw[0] = sg * tau * nx; o.tw[1] = sg * tau * ny; o.tw[2] = sg * tau * nz;
         }
     }
-    o.spring[0] = sign * sx; o.spring[1] = sign * sy; o.spring[2] = sign * sz;
-    o.spring[3] = sign * rdx; o.spring[4] = sign * rdy; o.spring[5] = sign * rdz;
-    o.spring[6] = sign * twd;
+    o.spring[0] = neg_if(sx, flip); o.spring[1] = neg_if(sy, flip); o.spring[2] = neg_if(sz, flip);
+    o.spring[3] = neg_if(rdx, flip); o.spring[4] = neg_if(rdy, flip); o.spring[5] = neg_if(rdz, flip);
+    o.spring[6] = neg_if(twd, flip);
 }
 
 __device__ __forceinline__ bool hist_find_m(const Dev& d, const SysParams& sp, int hc, long long p, int lp, uint32_t t,
@@ -523,105 +524,21 @@ __global__ void __launch_bounds__(BLK) k_dem_screen(Dev d) {
     if (contact) d.dem_cl[base + __popc(m & ((1u << lane) - 1u))] = (int)i;
 }
 
-// The contact law over the row of particle i of system s: force, torque,
-// the next history buffer, the large-overlap count and (VIR) the owner-side
-// virial sum of d_a f_b (hertz_mindlin_contact_force's add_pair,
-// contact.rs:559-569; fp32 pair terms summed in fp64).
-template <bool VIR>
-__device__ __forceinline__ void dem_contact_particle(const Dev& d, int s, long long i) {
-    const SysParams& sp = d.sp[s];
-    SysState* st = d.ss + s;
-    const int li = (int)(i - sp.p0);
-    const int hcur = st->hcur;
-    const int hn = hcur ^ 1;
-    const int nn = d.nnum[i];
-    const float4 hi = d.pos2[2 * i], lo = d.pos2[2 * i + 1];
-    const double4 vi = d.vel[i];
-    const double4 wi = d.omg[i];
-    const int ti_ = (int)d.type[i];
-    const uint32_t tag_i = d.tag[i];
-    const long long base = sp.lst0 + li;
-    const bool vir = VIR && sp.virial;
-    const float vs = sp.newton ? 1.f : 0.5f;
-    Kahan3 F, T;
-    double V[6] = {0, 0, 0, 0, 0, 0};
-    int nh = 0, nover = 0;
-    PairMixed o;
-    for (int k = 0; k < nn; k++) {
-        const uint32_t e = d.nlist[base + (long long)k * sp.npad];
-        const int lj = (int)(e & IDX_MASK);
-        const long long j = sp.p0 + lj;
-        const uint32_t code = e >> IDX_BITS;
-        const bool own = code >= 27u;
-        const int sc = (int)(own ? code - 27u : code);
-        const int sx = sc / 9 - 1, sy = (sc / 3) % 3 - 1, sz = sc % 3 - 1;
-        const float4 hj = d.pos2[2 * j], lj4 = d.pos2[2 * j + 1];
-        float dh[3], dl[3];
-        if (own) {
-            sep_df(hj.x, lj4.x, hi.x, lo.x, sx, sp.Lh[0], sp.Ll[0], dh[0], dl[0]);
-            sep_df(hj.y, lj4.y, hi.y, lo.y, sy, sp.Lh[1], sp.Ll[1], dh[1], dl[1]);
-            sep_df(hj.z, lj4.z, hi.z, lo.z, sz, sp.Lh[2], sp.Ll[2], dh[2], dl[2]);
-        } else {
-            // owner frame: owner j, partner i's image -s
-            sep_df(hi.x, lo.x, hj.x, lj4.x, -sx, sp.Lh[0], sp.Ll[0], dh[0], dl[0]);
-            sep_df(hi.y, lo.y, hj.y, lj4.y, -sy, sp.Lh[1], sp.Ll[1], dh[1], dl[1]);
-            sep_df(hi.z, lo.z, hj.z, lj4.z, -sz, sp.Lh[2], sp.Ll[2], dh[2], dl[2]);
-        }
-        if (sp.touch_only) {
-            // spheres clearly apart: no force, skip the partner's state and history
-            const float rs = hi.w + hj.w;
-            const float x = dh[0] + dl[0], y = dh[1] + dl[1], z = dh[2] + dl[2];
-            if (x * x + y * y + z * z > rs * rs * 1.00002f) continue;
-        }
-        const double4 vj = d.vel[j];
-        const double4 wj = d.omg[j];
-        const int tj_ = (int)d.type[j];
-        const uint32_t tag_j = d.tag[j];
-        double stored[7] = {0, 0, 0, 0, 0, 0, 0};
-        if (own) {
-            hist_find_m(d, sp, hcur, i, li, tag_j, stored);
-            hm_pair_mixed(d, sp, dh, dl, hi.w, lo.w, hj.w, lj4.w, vi, vj, wi, wj, ti_, tj_, tag_i, tag_j, stored, o);
-            if (!o.hit) continue;
-            F.add(-o.fn[0], -o.fn[1], -o.fn[2]);
-            if (o.overlap) nover++;
-            if (vir) {
-                // owner frame: separation owner -> partner, the owner's pair force
-                const float fx = (-o.fn[0] + (o.tang ? o.ft[0] : 0.f)) * vs;
-                const float fy = (-o.fn[1] + (o.tang ? o.ft[1] : 0.f)) * vs;
-                const float fz = (-o.fn[2] + (o.tang ? o.ft[2] : 0.f)) * vs;
-                const float x = dh[0] + dl[0], y = dh[1] + dl[1], z = dh[2] + dl[2];
-                V[0] += (double)(x * fx); V[1] += (double)(y * fy); V[2] += (double)(z * fz);
-                V[3] += (double)(x * fy); V[4] += (double)(x * fz); V[5] += (double)(y * fz);
-            }
-            if (!o.tang) continue;
-            F.add(o.ft[0], o.ft[1], o.ft[2]);
-            T.add(o.ti[0] + o.tr[0] + o.tw[0], o.ti[1] + o.tr[1] + o.tw[1], o.ti[2] + o.tr[2] + o.tw[2]);
-            if (nh < sp.hcap) {
-                d.htag[hn][sp.h0 + (long long)nh * sp.npad + li] = tag_j;
-                for (int q = 0; q < 7; q++)
-                    d.hval[hn][sp.h0 * 7 + (long long)(nh * 7 + q) * sp.npad + li] = o.spring[q];
-            }
-            nh++;
-        } else {
-            hist_find_m(d, sp, hcur, j, lj, tag_i, stored);
-            hm_pair_mixed(d, sp, dh, dl, hj.w, lj4.w, hi.w, lo.w, vj, vi, wj, wi, tj_, ti_, tag_j, tag_i, stored, o);
-            if (!o.hit) continue;
-            F.add(o.fn[0], o.fn[1], o.fn[2]);
-            if (!o.tang) continue;
-            F.add(-o.ft[0], -o.ft[1], -o.ft[2]);
-            T.add(o.tj[0] - o.tr[0] - o.tw[0], o.tj[1] - o.tr[1] - o.tw[1], o.tj[2] - o.tr[2] - o.tw[2]);
-        }
+// Lanes per contact particle in the contact pass: lane e of a group evaluates
+// row entries e, e + CG, e + 2 CG, ... of its particle, so a particle's pairs
+// run side by side instead of one after another in one thread.
+constexpr int CG = 8;
+
+// Compensated (s, c) sum over the CG lanes of a group by a fixed shuffle
+// tree (deterministic order); the total lands on the group's first lane.
+__device__ __forceinline__ void group_sum(Kahan& k) {
+#pragma unroll
+    for (int o = CG / 2; o > 0; o >>= 1) {
+        const float so = __shfl_down_sync(0xffffffffu, k.s, o, CG);
+        const float co = __shfl_down_sync(0xffffffffu, k.c, o, CG);
+        k.add(so);
+        k.c += co;
     }
-    if (nh > sp.hcap) {
-        atomicOr(&st->status, ST_HIST_OVF);
-        nh = sp.hcap;
-    }
-    d.hcnt[hn][i] = nh;
-    if (nover) atomicAdd(&st->overlap, nover);
-    d.frc[i] = make_double4(F.x.value(), F.y.value(), F.z.value(), 0.0);
-    d.trq[i] = make_double4(T.x.value(), T.y.value(), T.z.value(), 0.0);
-    if (vir)
-        for (int q = 0; q < 6; q++) d.vir[q * d.P + i] = V[q];
 }
 
 // Minimum resident blocks per SM asked of ptxas for k_dem_contact (a
@@ -631,14 +548,159 @@ __device__ __forceinline__ void dem_contact_particle(const Dev& d, int s, long l
 #endif
 constexpr int DEM_CONTACT_GRID = 152 * MDG_DEM_MINB;
 
+// The contact law over the rows of the listed particles: force, torque, the
+// next history buffer (owner tangential contacts in row order), the
+// large-overlap count and (VIR) the owner-side virial sum of d_a f_b
+// (hertz_mindlin_contact_force's add_pair, contact.rs:559-569; fp32 pair
+// terms summed in fp64).  Each warp takes 32 / CG listed particles, warps
+// numbered across blocks first so the list spreads over every SM.
 template <bool VIR>
 __global__ void __launch_bounds__(BLK, MDG_DEM_MINB) k_dem_contact(Dev d) {
     const int n = *((const volatile int*)d.dem_cl_n);
-    for (int k = blockIdx.x * BLK + threadIdx.x; k < n; k += gridDim.x * BLK) {
-        const long long i = d.dem_cl[k];
-        dem_contact_particle<VIR>(d, d.blk_sys[i / BLK], i);
+    const int lane = threadIdx.x & 31, el = lane % CG, sub = lane / CG;
+    const unsigned int gmask = ((1u << CG) - 1u) << (sub * CG);
+    const int nwarps = gridDim.x * (BLK / 32);
+    for (int w = (int)(threadIdx.x >> 5) * (int)gridDim.x + (int)blockIdx.x; w * (32 / CG) < n; w += nwarps) {
+        const int kk = w * (32 / CG) + sub;
+        const bool has = kk < n;
+        long long i = 0;
+        int s = 0, nn = 0;
+        if (has) {
+            i = d.dem_cl[kk];
+            s = d.blk_sys[i / BLK];
+            nn = d.nnum[i];
+        }
+        int maxnn = nn;  // uniform over the warp: every lane runs the same chunks
+        for (int o = 16; o > 0; o >>= 1) maxnn = max(maxnn, __shfl_xor_sync(0xffffffffu, maxnn, o));
+        const SysParams& sp = d.sp[s];
+        SysState* st = d.ss + s;
+        const int li = (int)(i - sp.p0);
+        const int hcur = st->hcur;
+        const int hn = hcur ^ 1;
+        float4 hi = make_float4(0, 0, 0, 0), lo = hi;
+        double4 vi = make_double4(0, 0, 0, 0), wi = vi;
+        int ti_ = 0;
+        uint32_t tag_i = 0;
+        if (has) {
+            hi = d.pos2[2 * i];
+            lo = d.pos2[2 * i + 1];
+            vi = d.vel[i];
+            wi = d.omg[i];
+            ti_ = (int)d.type[i];
+            tag_i = d.tag[i];
+        }
+        const long long base = sp.lst0 + li;
+        const bool vir = VIR && sp.virial;
+        const float vs = sp.newton ? 1.f : 0.5f;
+        Kahan3 F, T;
+        double V[6] = {0, 0, 0, 0, 0, 0};
+        int nh = 0, nover = 0;
+        for (int k0 = 0; k0 < maxnn; k0 += CG) {
+            const int k = k0 + el;
+            bool wh = false;  // this lane stores a history entry
+            uint32_t tag_j = 0;
+            PairMixed o;
+            if (has && k < nn) {
+                const uint32_t e = d.nlist[base + (long long)k * sp.npad];
+                const int lj = (int)(e & IDX_MASK);
+                const long long j = sp.p0 + lj;
+                const uint32_t code = e >> IDX_BITS;
+                const bool own = code >= 27u;
+                const int sc = (int)(own ? code - 27u : code);
+                const int sx = sc / 9 - 1, sy = (sc / 3) % 3 - 1, sz = sc % 3 - 1;
+                const float4 hj = d.pos2[2 * j], lj4 = d.pos2[2 * j + 1];
+                float dh[3], dl[3];
+                if (own) {
+                    sep_df(hj.x, lj4.x, hi.x, lo.x, sx, sp.Lh[0], sp.Ll[0], dh[0], dl[0]);
+                    sep_df(hj.y, lj4.y, hi.y, lo.y, sy, sp.Lh[1], sp.Ll[1], dh[1], dl[1]);
+                    sep_df(hj.z, lj4.z, hi.z, lo.z, sz, sp.Lh[2], sp.Ll[2], dh[2], dl[2]);
+                } else {
+                    // owner frame: owner j, partner i's image -s
+                    sep_df(hi.x, lo.x, hj.x, lj4.x, -sx, sp.Lh[0], sp.Ll[0], dh[0], dl[0]);
+                    sep_df(hi.y, lo.y, hj.y, lj4.y, -sy, sp.Lh[1], sp.Ll[1], dh[1], dl[1]);
+                    sep_df(hi.z, lo.z, hj.z, lj4.z, -sz, sp.Lh[2], sp.Ll[2], dh[2], dl[2]);
+                }
+                const float rs = hi.w + hj.w;
+                const float x = dh[0] + dl[0], y = dh[1] + dl[1], z = dh[2] + dl[2];
+                // spheres clearly apart: no force, skip the partner's state and history
+                if (!sp.touch_only || x * x + y * y + z * z <= rs * rs * 1.00002f) {
+                    const double4 vj = d.vel[j];
+                    const double4 wj = d.omg[j];
+                    const int tj_ = (int)d.type[j];
+                    tag_j = d.tag[j];
+                    double stored[7] = {0, 0, 0, 0, 0, 0, 0};
+                    if (own) {
+                        hist_find_m(d, sp, hcur, i, li, tag_j, stored);
+                        hm_pair_mixed(d, sp, dh, dl, hi.w, lo.w, hj.w, lj4.w, vi, vj, wi, wj, ti_, tj_, tag_i, tag_j,
+                                      stored, o);
+                        if (o.hit) {
+                            F.add(-o.fn[0], -o.fn[1], -o.fn[2]);
+                            if (o.overlap) nover++;
+                            if (vir) {
+                                // owner frame: separation owner -> partner, the owner's pair force
+                                const float fx = (-o.fn[0] + (o.tang ? o.ft[0] : 0.f)) * vs;
+                                const float fy = (-o.fn[1] + (o.tang ? o.ft[1] : 0.f)) * vs;
+                                const float fz = (-o.fn[2] + (o.tang ? o.ft[2] : 0.f)) * vs;
+                                V[0] += (double)(x * fx); V[1] += (double)(y * fy); V[2] += (double)(z * fz);
+                                V[3] += (double)(x * fy); V[4] += (double)(x * fz); V[5] += (double)(y * fz);
+                            }
+                            if (o.tang) {
+                                F.add(o.ft[0], o.ft[1], o.ft[2]);
+                                T.add(o.ti[0] + o.tr[0] + o.tw[0], o.ti[1] + o.tr[1] + o.tw[1],
+                                      o.ti[2] + o.tr[2] + o.tw[2]);
+                                wh = true;
+                            }
+                        }
+                    } else {
+                        hist_find_m(d, sp, hcur, j, lj, tag_i, stored);
+                        hm_pair_mixed(d, sp, dh, dl, hj.w, lj4.w, hi.w, lo.w, vj, vi, wj, wi, tj_, ti_, tag_j, tag_i,
+                                      stored, o);
+                        if (o.hit) {
+                            F.add(o.fn[0], o.fn[1], o.fn[2]);
+                            if (o.tang) {
+                                F.add(-o.ft[0], -o.ft[1], -o.ft[2]);
+                                T.add(o.tj[0] - o.tr[0] - o.tw[0], o.tj[1] - o.tr[1] - o.tw[1],
+                                      o.tj[2] - o.tr[2] - o.tw[2]);
+                            }
+                        }
+                    }
+                }
+            }
+            // history slots in row order within the group
+            const unsigned int bal = __ballot_sync(0xffffffffu, wh) & gmask;
+            if (wh) {
+                const int slot = nh + __popc(bal & ((1u << lane) - 1u));
+                if (slot < sp.hcap) {
+                    d.htag[hn][sp.h0 + (long long)slot * sp.npad + li] = tag_j;
+                    for (int q = 0; q < 7; q++)
+                        d.hval[hn][sp.h0 * 7 + (long long)(slot * 7 + q) * sp.npad + li] = o.spring[q];
+                }
+            }
+            nh += __popc(bal);
+        }
+        group_sum(F.x); group_sum(F.y); group_sum(F.z);
+        group_sum(T.x); group_sum(T.y); group_sum(T.z);
+#pragma unroll
+        for (int o = CG / 2; o > 0; o >>= 1) {
+            nover += __shfl_down_sync(0xffffffffu, nover, o, CG);
+            if (VIR)
+                for (int q = 0; q < 6; q++) V[q] += __shfl_down_sync(0xffffffffu, V[q], o, CG);
+        }
+        if (has && el == 0) {
+            if (nh > sp.hcap) {
+                atomicOr(&st->status, ST_HIST_OVF);
+                nh = sp.hcap;
+            }
+            d.hcnt[hn][i] = nh;
+            if (nover) atomicAdd(&st->overlap, nover);
+            d.frc[i] = make_double4(F.x.value(), F.y.value(), F.z.value(), 0.0);
+            d.trq[i] = make_double4(T.x.value(), T.y.value(), T.z.value(), 0.0);
+            if (vir)
+                for (int q = 0; q < 6; q++) d.vir[q * d.P + i] = V[q];
+        }
     }
     // every block has read the count: the last one to finish clears the list
+    __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
         if (atomicAdd((unsigned int*)d.dem_cl_n + 1, 1u) == gridDim.x - 1) {
