@@ -1,15 +1,19 @@
 """Throughput benchmark of the particle hot path on one GB300.
 
 Default workload (N=1): the served job stream -- Poisson-arriving jobs
-(50 % granular cooling gases of 100..200000 spheres, 25 % two-sphere Hertz
-rebounds, 25 % LJ FCC melts of 500..100000 atoms; 1000..50000 steps each)
-advanced by the continuous-batching server (mdg_server_*) in mixed precision.
-A "step" is one server pump: admission of the jobs that arrived, one
-multi-step device launch (200 timesteps) over every resident job, retirement
-of finished jobs.  value = particle-steps advanced inside the K timed pumps
-/ CUDA-event time on the server's stream over them.  Reported beside it:
-p50/p99 job latency (arrival to retirement) over the whole trace, and the
-same jobs run one by one on the plain FP64 path (particle-steps/s).
+(exactly 50 % granular cooling gases of 100..200000 spheres, 25 % two-sphere
+Hertz rebounds, 25 % LJ FCC melts of 500..100000 atoms; 1000..50000 steps
+each) advanced by the continuous-batching server (mdg_server_*) in mixed
+precision.  A "step" is one server pump: admission of the jobs that arrived,
+one multi-step device launch (200 timesteps) over every resident job,
+retirement of finished jobs.  The timed window is K pumps of the steady state
+while jobs keep arriving (default pumps 10..90 of a 384-job stream arriving
+at 4 per pump); value = particle-steps advanced inside it / CUDA-event time
+on the server's stream.  Reported beside it: p50/p99 job latency (arrival to
+retirement) over the whole trace once it drains, the window's saturation
+(queued jobs, resident particles, GPU share), the precision form's error
+statement, and the same jobs run one by one on the plain FP64 path.
+--sweep runs the stream at several arrival rates and admission limits.
 
 Other workloads (--workload): lj256k, lj864, dem500, gas200k, poly1m (one
 system; a step is one timestep, L2 flushed before each), ens256 (256 gas
@@ -39,8 +43,13 @@ L2_FLUSH = 512 << 20
 FALLBACK_HBM_GBS = 6800.0
 
 
-def workload(name):
+def workload(name, rsa=None):
+    """(description, config, state maker) of a single-system workload;
+    ``rsa``: the sphere generator of the gases (default the library's;
+    False when only the description is wanted)."""
     from mddem_gb300 import config, inputs
+
+    rsa = rsa or None
 
     if name == "lj256k":
         cfg = config.lj_fluid_config(box=67.06)
@@ -65,15 +74,15 @@ def workload(name):
     if name == "gas200k":
         cfg = config.granular_gas_config(box=w.gas_box(200000, 0.15), dt=w.DT_GAS)
         return ("DEM granular gas 200000 glass spheres r=1mm solid fraction 0.15", cfg,
-                lambda: w.gas(200000, phi=0.15, seed=2024)[1])
+                lambda: w.gas(200000, phi=0.15, seed=2024, rsa=rsa)[1])
     if name == "gas138k":
         cfg = config.granular_gas_config(box=w.gas_box(138195, 0.05), dt=w.DT_GAS)
         return ("DEM granular gas 138195 glass spheres r=1mm solid fraction 0.05 (thread-per-particle list build)",
-                cfg, lambda: w.gas(138195, phi=0.05, seed=3)[1])
+                cfg, lambda: w.gas(138195, phi=0.05, seed=3, rsa=rsa)[1])
     if name == "poly1m":
         cfg = w.polydisperse_config()
         return ("DEM polydisperse gas 1000000 glass spheres r~U[0.8,1.2]mm solid fraction 0.30 Maxwellian", cfg,
-                lambda: w.polydisperse_gas(seed=2024)[1])
+                lambda: w.polydisperse_gas(seed=2024, rsa=rsa)[1])
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -186,103 +195,120 @@ def cpu_baseline_sample(wl, max_seconds=15.0):
             "sample": f"{steps} timesteps of the same {n}-particle workload, single thread, after 1 warm-up step"}
 
 
-def _ref_worker(args):
-    wl, warm, steps, budget = args
+REF_BUDGET = 40.0  # seconds of stepping per core in the reference arm
+
+
+def _ref_fill(make_jobs, budget=REF_BUDGET, cap_ps=4e6):
+    """Step jobs one after another on the oracle (the CPU FP64 restatement of
+    the reference's path), each for up to its step count capped at cap_ps
+    particle-steps after one warm-up step, cycling through the list until
+    `budget` seconds of stepping are spent; setup is not timed.  The inputs
+    are made without the library (the oracle's own sphere placement).
+    Returns (particle-steps, seconds)."""
     from oracle.oracle import Oracle
 
-    desc, cfg, make = workload(wl)
-    st = make()
-    o = Oracle(cfg.replace(precision="fp64"))
-    o.load(st)
-    o.step(max(1, warm))
-    t0 = time.perf_counter()
-    done = 0
-    for _ in range(steps):
+    jobs = make_jobs()
+    work = secs = 0.0
+    k = 0
+    while secs < budget and jobs:
+        cfg, st, steps = jobs[k % len(jobs)]
+        o = Oracle(cfg.replace(precision="fp64"))
+        o.load(st)
         o.step(1)
-        done += 1
-        if time.perf_counter() - t0 > budget:
-            break
-    return len(st["tag"]) * done, time.perf_counter() - t0, done
+        n = len(st["tag"])
+        todo = max(1, min(int(steps), int(cap_ps // n)))
+        t0 = time.perf_counter()
+        done = 0
+        while done < todo and secs + (time.perf_counter() - t0) < budget:
+            o.step(1)
+            done += 1
+        secs += time.perf_counter() - t0
+        work += n * done
+        o.close()
+        k += 1
+    return work, secs
 
 
-def _ref_serve_worker(args):
-    idx, njobs, budget = args
+def _ref_single_jobs(wl):
+    from oracle import oracle
+
+    desc, cfg, make = workload(wl, rsa=oracle.rsa_spheres)
+    return [(cfg, make(), 1 << 30)]
+
+
+def _ref_serve_jobs(idx, njobs):
     import types
 
+    from oracle import oracle
+
     trace = serve_trace(types.SimpleNamespace(jobs=njobs))
-    work = secs = 0.0
+    out = []
     for k in idx:
-        if secs > budget:
-            break
-        cfg, st = trace[k].make("fp64", "reference")
-        w_, s_ = _oracle_job(cfg, st, max(1, min(trace[k].steps, int(4e6 // trace[k].n))), budget - secs + 1.0)
-        work += w_
-        secs += s_
-    return work, secs
+        cfg, st = trace[k].make("fp64", "reference", rsa=oracle.rsa_spheres)
+        out.append((cfg, st, trace[k].steps))
+    return out
 
 
-def _ref_ens_worker(args):
-    idx, budget = args
+def _ref_ens_jobs(idx):
     from mddem_gb300 import workloads as w
+    from oracle import oracle
 
-    ens = w.ensemble(precision="fp64", policy="reference")
-    work = secs = 0.0
-    for k in idx:
-        if secs > budget:
-            break
-        cfg, st = ens[k]
-        n = len(st["tag"])
-        w_, s_ = _oracle_job(cfg, st, max(1, min(5000, int(4e6 // n))), budget - secs + 1.0)
-        work += w_
-        secs += s_
-    return work, secs
+    return [(c, s, 5000) for c, s in w.ensemble(precision="fp64", policy="reference", rsa=oracle.rsa_spheres,
+                                                only=idx)]
+
+
+def _ref_worker(args):
+    kind, arg = args
+    import functools
+
+    if kind == "single":
+        return _ref_fill(functools.partial(_ref_single_jobs, arg))
+    if kind == "serve":
+        return _ref_fill(functools.partial(_ref_serve_jobs, *arg))
+    return _ref_fill(functools.partial(_ref_ens_jobs, arg))
+
+
+def _ref_pool(tasks):
+    """Run the reference workers, one per host core; the arm's rate is the sum
+    of the per-core rates (each core steps for the same wall budget)."""
+    import multiprocessing as mp
+
+    with mp.get_context("spawn").Pool(len(tasks)) as pool:
+        res = pool.map(_ref_worker, tasks)
+    return sum(w_ / s_ for w_, s_ in res if s_ > 0), len(res)
+
+
+def _ref_line(a, metric, val, cores, workload_desc, sample):
+    return {
+        "impl": "reference", "metric": metric, "value": val, "unit": "particle-steps/s",
+        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_desc, "precision": "fp64", "parallelism": f"{cores} host cores"},
+        "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
 
 
 def run_reference_ensemble(a):
-    import multiprocessing as mp
-
     cores = os.cpu_count() or 1
     parts = [list(range(c, 256, cores)) for c in range(cores)]
-    with mp.get_context("spawn").Pool(cores) as pool:
-        res = pool.map(_ref_ens_worker, [(p, 45.0) for p in parts if p])
-    val = sum(r[0] for r in res) / max(r[1] for r in res)
-    line = {
-        "impl": "reference", "metric": "particle-steps/s", "value": val, "unit": "particle-steps/s",
-        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": ENS_DESC, "precision": "fp64", "parallelism": f"{len(res)} host cores"},
-        "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": len(res), "kind": "port",
-                         "sample": f"the 256 replicas dealt round-robin to {len(res)} cores, each up to "
-                                   "4e6 particle-steps after 1 warm-up step, at most 45 s per core"},
-        "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line), flush=True)
+    val, used = _ref_pool([("ens", p) for p in parts if p])
+    sample = (f"the 256 replicas dealt round-robin to {used} cores; each core steps its replicas in turn "
+              f"(each up to 5000 steps or 4e6 particle-steps after 1 warm-up step) for {REF_BUDGET:g} s; "
+              "value = sum of the per-core rates")
+    print(json.dumps(_ref_line(a, "particle-steps/s", val, used, ENS_DESC, sample)), flush=True)
 
 
 def run_reference_serve(a):
-    import multiprocessing as mp
-
     trace = serve_trace(a)
     cores = os.cpu_count() or 1
     order = sorted(range(len(trace)), key=lambda k: trace[k].arrival)
     parts = [order[c::cores] for c in range(cores)]
-    with mp.get_context("spawn").Pool(cores) as pool:
-        res = pool.map(_ref_serve_worker, [(p, a.jobs, 45.0) for p in parts if p])
-    work = sum(r[0] for r in res)
-    wall = max(r[1] for r in res)
-    val = work / wall
-    sample = (f"the stream's jobs dealt round-robin to {len(res)} cores, each job up to 4e6 particle-steps "
-              "after 1 warm-up step, at most 45 s per core")
-    line = {
-        "impl": "reference", "metric": "particle-steps/s served", "value": val, "unit": "particle-steps/s",
-        "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup, "ms_per_step": None, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": serve_desc(trace), "precision": "fp64", "parallelism": f"{len(res)} host cores"},
-        "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": len(res), "kind": "port",
-                         "sample": sample},
-        "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line), flush=True)
+    val, used = _ref_pool([("serve", (p, a.jobs)) for p in parts if p])
+    sample = (f"the stream's jobs dealt round-robin to {used} cores; each core steps its jobs in turn "
+              f"(each up to its step count or 4e6 particle-steps after 1 warm-up step) for {REF_BUDGET:g} s; "
+              "value = sum of the per-core rates")
+    print(json.dumps(_ref_line(a, "particle-steps/s served", val, used, serve_desc(trace, a), sample)), flush=True)
 
 
 def run_reference(a):
@@ -293,38 +319,30 @@ def run_reference(a):
         return run_reference_serve(a)
     if a.workload == "ens256":
         return run_reference_ensemble(a)
-    import multiprocessing as mp
-
-    desc, cfg, make = workload(a.workload)
+    desc, _, _ = workload(a.workload, rsa=False)
     cores = os.cpu_count() or 1
-    ctxm = mp.get_context("spawn")
-    budget = 60.0
-    with ctxm.Pool(cores) as pool:
-        res = pool.map(_ref_worker, [(a.workload, a.warmup, a.steps, budget)] * cores)
-    total = sum(r[0] for r in res)
-    wall = max(r[1] for r in res)
-    val = total / wall
-    line = {
-        "impl": "reference", "metric": "particle-steps/s", "value": val, "unit": "particle-steps/s",
-        "n_gpus": a.gpus, "steps": min(r[2] for r in res), "warmup": a.warmup, "ms_per_step": None,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": desc, "replicas": cores},
-        "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{cores} independent copies x {min(r[2] for r in res)} timesteps, one per core"},
-        "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line), flush=True)
+    val, used = _ref_pool([("single", a.workload)] * cores)
+    sample = (f"{used} independent copies of the workload, one per core, each stepping for {REF_BUDGET:g} s "
+              "after 1 warm-up step; value = sum of the per-core rates")
+    print(json.dumps(_ref_line(a, "particle-steps/s", val, used, desc, sample)), flush=True)
 
 
 # ---------------------------------------------------------------------------
 # served job stream
 # ---------------------------------------------------------------------------
 SERVE_PUMP = 200            # timesteps per pump (one bench step)
-SERVE_JOBS = 128
-SERVE_BACKLOG = 48          # jobs already queued when the stream starts
-SERVE_RATE = 2.0            # Poisson arrivals per pump tick after the backlog
-SERVE_HBM_BUDGET = 12 << 30  # admission budget of resident jobs' device bytes
+SERVE_JOBS = 384
+SERVE_BACKLOG = 64          # jobs already queued when the stream starts
+SERVE_RATE = 4.0            # Poisson arrivals per pump tick after the backlog
+SERVE_BUDGET_GB = 96        # admission budget of resident jobs' device bytes (GB)
+SERVE_SLOT_MULT = 2         # times the slot counts of workloads.SERVE_*_SLOTS
+SERVE_WINDOW = 80           # timed pumps by default: the steady state while jobs keep arriving
+SERVE_WARMUP = 10           # pumps of the stream before the timed window
 PLAIN_SAMPLE_STEPS = 200
+# (jobs, backlog, arrivals per pump, budget GB, slot multiplier) of --sweep;
+# each setting's arrivals last about as long as the timed window
+SERVE_SWEEP = [(128, 32, 1.0, 96, 2), (224, 48, 2.0, 96, 2), (384, 64, 4.0, 96, 2), (704, 64, 8.0, 96, 2),
+               (704, 64, 8.0, 192, 4)]
 
 
 def reduce_over_ranks(dist, ms, work):
@@ -344,24 +362,35 @@ def reduce_over_ranks(dist, ms, work):
 def serve_trace(a):
     from mddem_gb300 import workloads as w
 
-    trace = w.serve_trace(njobs=a.jobs, rate=SERVE_RATE, seed=2024)
+    trace = w.serve_trace(njobs=a.jobs, rate=getattr(a, "serve_rate", SERVE_RATE), seed=2024)
     scale = getattr(a, "job_steps_scale", 1.0)
     for j in trace:
         j.steps = max(1, int(round(j.steps * scale)))
-    t0 = trace[SERVE_BACKLOG].arrival if len(trace) > SERVE_BACKLOG else 0.0
+    backlog = getattr(a, "backlog", SERVE_BACKLOG)
+    t0 = trace[backlog].arrival if len(trace) > backlog else 0.0
     for k, j in enumerate(trace):  # the backlog arrives at tick 0, the rest keep their gaps
-        j.arrival = 0.0 if k < SERVE_BACKLOG else j.arrival - t0 + 1.0
+        j.arrival = 0.0 if k < backlog else j.arrival - t0 + 1.0
     return trace
 
 
-def serve_desc(trace, scale=1.0):
+def serve_desc(trace, a):
     kinds = {}
     for j in trace:
         kinds[j.kind] = kinds.get(j.kind, 0) + 1
+    scale = getattr(a, "job_steps_scale", 1.0)
     return (f"served stream: {len(trace)} jobs ({kinds.get('gas', 0)} cooling gases N 100-200000, "
             f"{kinds.get('rebound', 0)} two-sphere rebounds, {kinds.get('lj', 0)} LJ FCC melts N 500-100000), "
-            f"steps {1000 * scale:g}-{50000 * scale:g} log-uniform, {SERVE_BACKLOG} queued at start then Poisson {SERVE_RATE}/pump, "
-            f"{SERVE_PUMP} timesteps per pump")
+            f"steps {1000 * scale:g}-{50000 * scale:g} log-uniform, {getattr(a, 'backlog', SERVE_BACKLOG)} queued "
+            f"at start then Poisson {getattr(a, 'serve_rate', SERVE_RATE):g}/pump, {SERVE_PUMP} timesteps per pump")
+
+
+def serve_server(a):
+    """The job server of the served-stream workload: slot classes times
+    a.slot_mult, admission budget a.budget_gb."""
+    from mddem_gb300 import capi, workloads as w
+
+    cfgs, caps = w.serve_slots(a.precision, a.policy, mult=getattr(a, "slot_mult", SERVE_SLOT_MULT))
+    return capi.Server(cfgs, caps, int(getattr(a, "budget_gb", SERVE_BUDGET_GB) * (1 << 30)))
 
 
 def state_bytes(st):
@@ -394,8 +423,17 @@ def replay(a, srv, trace, made, clk):
             sid[srv.submit(cfg, st, trace[k].steps)] = k
             h2d += state_bytes(st)
             nxt += 1
+        if "s0" in win and "s1" not in win:
+            # saturation: jobs waiting for admission and particles resident
+            # at the start of each timed pump
+            ss = srv.stats()
+            win.setdefault("pend", []).append(ss["pending"])
+            win.setdefault("res_n", []).append(sum(r["n"] for r in srv.resident()))
         if tick == warm:
             win.update(s0=srv.stats(), l0=srv.launches(), c0=clk.mark(), w0=time.perf_counter(), warm=warm)
+            ss = srv.stats()
+            win["pend"] = [ss["pending"]]
+            win["res_n"] = [sum(r["n"] for r in srv.resident())]
             e0.record(stream)
         active, pending = srv.pump(SERVE_PUMP)
         tick += 1
@@ -416,6 +454,21 @@ def replay(a, srv, trace, made, clk):
             break
     wall = time.perf_counter() - t_all
     return win, infos, {"wall_s": wall, "pumps": tick, "h2d": h2d, "d2h": d2h}
+
+
+def saturation(win):
+    """Whether the timed window ran saturated: jobs waiting for admission at
+    the start of every timed pump means the admission limits (slots, HBM
+    budget), not the arrivals, bounded the resident work; the GPU's share of
+    the window is its CUDA-event time over the window's wall time."""
+    import numpy as np
+
+    pend = np.array(win.get("pend", [0]))
+    res = np.array(win.get("res_n", [0]))
+    wall_ms = (win["w1"] - win["w0"]) * 1e3
+    return {"pumps_with_queue_frac": float(np.mean(pend > 0)), "queued_jobs_mean": float(pend.mean()),
+            "resident_particles_mean": float(res.mean()), "resident_particles_max": int(res.max()),
+            "gpu_busy_frac": float(win["ms"] / wall_ms) if wall_ms > 0 else None}
 
 
 def plain_job_by_job(trace, made):
@@ -485,6 +538,81 @@ def serve_mix(srv, trace, sid):
                     contacts_per_particle=p["contacts"] / max(1, p["n"])) for k, p in per.items()}
 
 
+def serve_samples(srv, trace, made, sid, per_kind=(("gas", 3), ("lj", 2), ("rebound", 1))):
+    """States (with contact history) of the largest resident jobs of each kind,
+    downloaded from the server's context: the sample the precision form's
+    force error is stated on."""
+    ctx = srv.context()
+    res = srv.resident()
+    out = []
+    for kind, m in per_kind:
+        ks = sorted((r for r in res if trace[sid[r["id"]]].kind == kind), key=lambda r: -r["n"])[:m]
+        for r in ks:
+            cfg = made[sid[r["id"]]][0]
+            st = ctx.download(r["slot"])
+            hist = ctx.history(r["slot"]) if cfg.kind == "dem" else None
+            out.append((kind, cfg, st, hist))
+    return out
+
+
+def precision_errors(samples):
+    """Per-particle force (and torque) error of the mixed path against the
+    plain FP64 path on each sampled job's current state (same state, same
+    contact history, one force evaluation each), with the per-particle metric
+    |F_mixed - F_fp64|_inf / max(|F_fp64|_inf, sum_pairs |f_pair|)."""
+    from mddem_gb300 import capi, validate
+
+    out = {"bound": 1e-5, "jobs": []}
+    worst = {"force": 0.0, "torque": 0.0}
+    for kind, cfg, st, hist in samples:
+        res = {}
+        for prec in ("fp64", "mixed"):
+            c = capi.Context(cfg.replace(precision=prec), len(st["tag"]))
+            c.upload(st)
+            if hist is not None and len(hist[0]):
+                c.set_history(*hist)
+            c.force_only()
+            res[prec] = (c.download(), c.pairs())
+            c.close()
+        e = validate.force_error(cfg, res["fp64"][0], res["mixed"][0], res["fp64"][1])
+        out["jobs"].append({"kind": kind, "particles": len(st["tag"]), **e})
+        for q in e:
+            worst[q] = max(worst[q], e[q])
+    out.update({"force_rel_max": worst["force"], "torque_rel_max": worst["torque"]})
+    return out
+
+
+def physics_errors():
+    """Conserved / statistical quantities of the mixed path beside the plain
+    FP64 path (whose LJ energy history equals the oracle's to 1e-6 of its
+    drift, and whose Haff time is within 2 % of the oracle's, in the GPU
+    test suite): LJ NVE energy drift over 2000 steps (864 atoms), and the
+    Haff cooling time of a frictionless gas (2000 spheres, solid fraction
+    0.2, e = 0.8, 40000 steps) with its kinetic-theory value."""
+    from mddem_gb300 import capi, config, inputs, validate, workloads
+
+    slopes = {}
+    for prec in ("fp64", "mixed"):
+        cfg = config.lj_fluid_config(nose_hoover=False, precision=prec)
+        st = inputs.lj_fcc(6, 10.06, 0.85, 0.85, seed=3)
+        c = capi.Context(cfg, len(st["tag"]))
+        c.upload(st)
+        slopes[prec] = validate.energy_drift(c)[1]
+        c.close()
+    tc = {}
+    for prec in ("fp64", "mixed"):
+        cfg, st = workloads.gas(2000, phi=0.2, restitution=0.8, friction=0.0, seed=11, precision=prec)
+        c = capi.Context(cfg, 2000)
+        c.upload(st)
+        tc[prec], theory, _ = validate.haff(c, cfg, 2000, 0.8)
+        c.close()
+    return {"lj_energy_drift": {"mixed_per_step": slopes["mixed"], "fp64_per_step": slopes["fp64"],
+                                "ratio": abs(slopes["mixed"]) / max(abs(slopes["fp64"]), 1e-300), "bound": 2.0},
+            "haff_tc": {"mixed": tc["mixed"], "fp64": tc["fp64"], "kinetic_theory": theory,
+                        "mixed_vs_fp64": tc["mixed"] / tc["fp64"] - 1.0, "fp64_vs_theory": tc["fp64"] / theory - 1.0,
+                        "bounds": {"mixed_vs_fp64": 0.02, "fp64_vs_theory": 0.15}}}
+
+
 def serve_phases(a, trace, made, at_tick, pumps=2):
     """Where the served step's time goes: the same stream replayed with
     ordinary pumps up to `at_tick` (the middle of the timed window), then
@@ -496,11 +624,10 @@ def serve_phases(a, trace, made, at_tick, pumps=2):
     import numpy as np
     from mddem_gb300 import capi, workloads as w
 
-    cfgs, caps = w.serve_slots(a.precision, a.policy)
-    srv = capi.Server(cfgs, caps, SERVE_HBM_BUDGET)
+    srv = serve_server(a)
     order = sorted(range(len(trace)), key=lambda k: trace[k].arrival)
     nxt, tick, sid = 0, 0, {}
-    rows, mix = [], None
+    rows, mix, samples = [], None, []
     while tick < at_tick + pumps:
         while nxt < len(order) and trace[order[nxt]].arrival <= tick:
             k = order[nxt]
@@ -512,6 +639,7 @@ def serve_phases(a, trace, made, at_tick, pumps=2):
             srv.pump(0)
             if mix is None:
                 mix = serve_mix(srv, trace, sid)
+                samples = serve_samples(srv, trace, made, sid)
             t, kern, rb = srv.context().timed_steps(SERVE_PUMP)
             rows.append((t, kern, rb))
             active, pending = srv.pump(0)
@@ -522,14 +650,14 @@ def serve_phases(a, trace, made, at_tick, pumps=2):
             break
     srv.close()
     if not rows:
-        return None, None
+        return None, None, []
     t = np.concatenate([r[0] for r in rows])
     kern = np.concatenate([r[1] for r in rows])
     rb = np.concatenate([r[2] for r in rows])
     names = ("initial", "rebuild", "force", "final")
     ph = {q: float(t[:, 1 + i].mean()) for i, q in enumerate(names)}
     return {"at_pump": at_tick, "timesteps": int(len(t)), "step_ms": float(t[:, 0].mean()), "phases_ms": ph,
-            "rebuild_steps_frac": float(rb.mean()), "kernels_per_step": float(kern.mean())}, mix
+            "rebuild_steps_frac": float(rb.mean()), "kernels_per_step": float(kern.mean())}, mix, samples
 
 
 def serve_roofline(a, phases, mix, served_rate):
@@ -607,8 +735,7 @@ def bench_serve(a, world, rank, local, dist):
     build.build()
     trace = serve_trace(a)
     made = [j.make(a.precision, a.policy) for j in trace]
-    cfgs, caps = w.serve_slots(a.precision, a.policy)
-    srv = capi.Server(cfgs, caps, SERVE_HBM_BUDGET)
+    srv = serve_server(a)
     if a.eager:
         srv.context().set_graph_mode(0)
     # warm-up jobs (one of each kind), drained before the stream starts
@@ -639,13 +766,19 @@ def bench_serve(a, world, rank, local, dist):
         "n_gpus": world, "steps": win["pumps"], "warmup": win["warm"], "ms_per_step": ms / win["pumps"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if a.precision == "mixed" else "f64", "data": "synthetic",
-        "config": {"workload": serve_desc(trace, a.job_steps_scale), "precision": a.precision, "rebuild_policy": a.policy,
-                   "pump_timesteps": SERVE_PUMP, "slots": {"dem": w.SERVE_DEM_SLOTS, "lj": w.SERVE_LJ_SLOTS},
-                   "hbm_budget_bytes": SERVE_HBM_BUDGET,
+        "config": {"workload": serve_desc(trace, a), "precision": a.precision, "rebuild_policy": a.policy,
+                   "pump_timesteps": SERVE_PUMP,
+                   "slots": {"dem": [[c, n * a.slot_mult] for c, n in w.SERVE_DEM_SLOTS],
+                             "lj": [[c, n * a.slot_mult] for c, n in w.SERVE_LJ_SLOTS]},
+                   "hbm_budget_bytes": int(a.budget_gb * (1 << 30)),
+                   "plain_fp64_reference": "the same jobs one by one on the plain FP64 path; each job's step time "
+                                           f"is sampled over up to {PLAIN_SAMPLE_STEPS} steps and scaled to its "
+                                           "step count (setup, upload and download timed in full)",
                    "l2": "inputs larger than L2 (resident state of all jobs, > 129 MB)",
                    "parallelism": f"replicas x{world}"},
         "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                       "max": float(lat.max()), "jobs": int(len(lat)), "failed": len(failed)},
+        "saturation": saturation(win),
         "trace": {"particle_steps": total_ps, "wall_s": run["wall_s"], "pumps": run["pumps"],
                   "host_split_s": {q: win["s1"][q] - win["s0"][q] for q in ("admit_s", "step_s", "retire_s")}},
         "gpu_launches": int(win["l1"] - win["l0"]),
@@ -656,9 +789,11 @@ def bench_serve(a, world, rank, local, dist):
     }
     srv.close()
     if rank == 0:
-        phases, mix = serve_phases(a, trace, made, win["warm"] + max(1, win["pumps"] // 2))
+        phases, mix, samples = serve_phases(a, trace, made, win["warm"] + max(1, win["pumps"] // 2))
         if phases:
             line["roofline"] = serve_roofline(a, phases, mix, line["value"] / world)
+        if a.precision == "mixed" and not a.no_error:
+            line["error"] = {"served_jobs": precision_errors(samples), **physics_errors()}
         if not a.no_plain:
             line["plain_fp64_job_by_job"] = plain_job_by_job(trace, made)
             line["served_vs_plain"] = line["value"] / world / line["plain_fp64_job_by_job"]["value"]
@@ -668,6 +803,34 @@ def bench_serve(a, world, rank, local, dist):
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def serve_sweep(a):
+    """The served stream at each SERVE_SWEEP setting (jobs, backlog, arrival
+    rate, HBM budget, slot multiplier): one JSON line per setting with the
+    window's served rate, p50 / p99 latency and its saturation figures."""
+    import numpy as np
+    from mddem_gb300 import build
+
+    build.build()
+    for jobs, backlog, rate, budget, mult in SERVE_SWEEP:
+        b = argparse.Namespace(**vars(a))
+        b.jobs, b.backlog, b.serve_rate, b.budget_gb, b.slot_mult = jobs, backlog, rate, budget, mult
+        trace = serve_trace(b)
+        made = [j.make(b.precision, b.policy) for j in trace]
+        srv = serve_server(b)
+        with ClockSampler(0) as clk:
+            win, infos, run = replay(b, srv, trace, made, clk)
+        srv.close()
+        ps = win["s1"]["particle_steps"] - win["s0"]["particle_steps"]
+        lat = np.array([infos[k]["end_s"] - infos[k]["submit_s"] for k in sorted(infos)])
+        print(json.dumps({"sweep": {"jobs": jobs, "backlog": backlog, "arrivals_per_pump": rate, "budget_gb": budget,
+                                    "slot_mult": mult},
+                          "value": ps / (win["ms"] / 1e3), "unit": "particle-steps/s", "pumps": win["pumps"],
+                          "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99))},
+                          "saturation": saturation(win), "stream_wall_s": run["wall_s"],
+                          "e2e": sum(j.n * j.steps for j in trace) / run["wall_s"],
+                          "clocks": clk.summary(win["c0"], win["c1"])}), flush=True)
 
 
 # ---------------------------------------------------------------------------
@@ -798,8 +961,9 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None,
-                    help="timed steps (default 50; served stream: every pump until it drains)")
-    ap.add_argument("--warmup", type=int, default=5)
+                    help="timed steps (default 50; served stream: 80 pumps, 0 = every pump until it drains)")
+    ap.add_argument("--warmup", type=int, default=None,
+                    help="untimed steps first (default 5; served stream: 10 pumps)")
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--workload", default="serve")
     ap.add_argument("--jobs", type=int, default=SERVE_JOBS, help="jobs in the served stream")
@@ -811,12 +975,21 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (ensemble)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison (serve, ensemble)")
+    ap.add_argument("--serve-rate", type=float, default=SERVE_RATE, help="served stream: Poisson arrivals per pump")
+    ap.add_argument("--backlog", type=int, default=SERVE_BACKLOG, help="served stream: jobs queued at the start")
+    ap.add_argument("--budget-gb", type=float, default=SERVE_BUDGET_GB, help="served stream: admission HBM budget")
+    ap.add_argument("--slot-mult", type=int, default=SERVE_SLOT_MULT, help="served stream: slot count multiplier")
+    ap.add_argument("--no-error", action="store_true", help="skip the precision-form error block (serve)")
+    ap.add_argument("--sweep", action="store_true",
+                    help="served stream at each SERVE_SWEEP setting: throughput, latency and saturation per setting")
     ap.add_argument("--job-steps-scale", type=float, default=1.0,
                     help="scale the served jobs' step counts (small cases for launch lists)")
     a = ap.parse_args()
-    a.warmup = max(3, a.warmup)
     if a.steps is None:
-        a.steps = 0 if a.workload == "serve" else 50
+        a.steps = SERVE_WINDOW if a.workload == "serve" else 50
+    if a.warmup is None:
+        a.warmup = SERVE_WARMUP if a.workload == "serve" else 5
+    a.warmup = max(3, a.warmup)
     if a.impl == "reference":
         return run_reference(a)
 
@@ -830,6 +1003,8 @@ def main():
 
         dist.init_process_group("gloo")
 
+    if a.workload == "serve" and a.sweep:
+        return serve_sweep(a)
     if a.workload == "serve":
         return bench_serve(a, world, rank, local, dist)
     if a.workload == "ens256":

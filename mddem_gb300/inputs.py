@@ -133,19 +133,25 @@ def isotropic_directions(rng, n):
 
 
 def dem_granular_gas(n=500, box=0.025, radius=1e-3, density=2500.0, speed=0.5, seed=0,
-                     sep_factor=1.1, maxwellian=False, native=False):
+                     sep_factor=1.1, maxwellian=False, native=False, rsa=None):
     """Granular-gas initial state: seeded non-overlapping spheres, speeds of
     magnitude ``speed`` in uniform random directions (or Maxwellian with RMS
     ``speed`` when ``maxwellian``), omega = 0, identity quaternions.
 
     ``native`` places the spheres with the library's grid RSA
     (``mdg_rsa_spheres``, same acceptance rule, its own random stream) --
-    needed from about 1e4 spheres on; ``radius`` may be ``(rmin, rmax)``."""
-    if native:
-        from . import capi
-
+    needed from about 1e4 spheres on; ``radius`` may be ``(rmin, rmax)``.
+    ``rsa``, when given, is another generator with mdg_rsa_spheres'
+    arguments (n, lo, hi, rmin, rmax, sep_factor, inset, seed) that places
+    the same spheres."""
+    if rsa is not None or native:
         rmin, rmax = (radius, radius) if not isinstance(radius, (tuple, list)) else radius
-        pos, rad = capi.rsa_spheres(n, (0.0, 0.0, 0.0), (box, box, box), rmin, rmax, sep_factor, True, seed)
+        if rsa is None:
+            from . import capi
+
+            rsa = capi.rsa_spheres
+        gen = rsa
+        pos, rad = gen(n, (0.0, 0.0, 0.0), (box, box, box), rmin, rmax, sep_factor, True, seed)
     else:
         pos, rad = random_spheres(n, box, radius, seed=seed, sep_factor=sep_factor)
     rng = np.random.default_rng(seed + 7919)

@@ -41,7 +41,8 @@ def sep_for(phi):
     return 1.1 if phi * 1.1 ** 3 <= 0.3 else 1.0
 
 
-def gas(n, phi=None, box=None, restitution=0.95, friction=0.4, seed=0, precision="mixed", policy="displacement"):
+def gas(n, phi=None, box=None, restitution=0.95, friction=0.4, seed=0, precision="mixed", policy="displacement",
+        rsa=None):
     """Monodisperse granular gas of n spheres at solid fraction phi (or in a
     cube of side box)."""
     if box is None:
@@ -50,7 +51,7 @@ def gas(n, phi=None, box=None, restitution=0.95, friction=0.4, seed=0, precision
     cfg = config.granular_gas_config(box=box, dt=DT_GAS, precision=precision, policy=policy)
     cfg.materials[0].restitution = float(restitution)
     cfg.materials[0].friction = float(friction)
-    st = inputs.dem_granular_gas(n, box=box, seed=seed, sep_factor=sep_for(phi), native=True)
+    st = inputs.dem_granular_gas(n, box=box, seed=seed, sep_factor=sep_for(phi), native=True, rsa=rsa)
     return cfg, st
 
 
@@ -65,15 +66,18 @@ def polydisperse_config(n=1_000_000, phi=0.30, precision="mixed", policy="displa
     return config.granular_gas_config(box=box, dt=dt, precision=precision, policy=policy)
 
 
-def polydisperse_gas(n=1_000_000, phi=0.30, seed=0, precision="mixed", policy="displacement"):
+def polydisperse_gas(n=1_000_000, phi=0.30, seed=0, precision="mixed", policy="displacement", rsa=None):
     cfg = polydisperse_config(n, phi, precision, policy)
     st = inputs.dem_granular_gas(n, box=cfg.box[0], radius=POLY_R, seed=seed, sep_factor=1.0, maxwellian=True,
-                                 native=True)
+                                 native=True, rsa=rsa)
     return cfg, st
 
 
-def ensemble(nrep=256, nmin=500, nmax=50000, seed=0, precision="mixed", policy="displacement"):
-    """Returns [(cfg, state)] for the replica ensemble."""
+def ensemble(nrep=256, nmin=500, nmax=50000, seed=0, precision="mixed", policy="displacement", rsa=None,
+             only=None):
+    """Returns [(cfg, state)] for the replica ensemble (the replicas listed in
+    ``only``, default all; each replica's parameters do not depend on which
+    are built)."""
     rng = np.random.default_rng(seed)
     out = []
     for k in range(nrep):
@@ -81,8 +85,10 @@ def ensemble(nrep=256, nmin=500, nmax=50000, seed=0, precision="mixed", policy="
         phi = rng.uniform(0.1, 0.3)
         e = rng.uniform(0.70, 0.99)
         mu = rng.uniform(0.0, 0.5)
+        if only is not None and k not in only:
+            continue
         out.append(gas(n, phi=phi, restitution=e, friction=mu, seed=seed * 100003 + k, precision=precision,
-                       policy=policy))
+                       policy=policy, rsa=rsa))
     return out
 
 
@@ -94,10 +100,13 @@ class Job:
     arrival: float     # in pump ticks
     params: dict = field(default_factory=dict)
 
-    def make(self, precision="mixed", policy="displacement"):
+    def make(self, precision="mixed", policy="displacement", rsa=None):
+        """(config, initial state); ``rsa``: the sphere generator for gases
+        (default the library's, see inputs.dem_granular_gas)."""
         p = self.params
         if self.kind == "gas":
-            return gas(self.n, phi=p["phi"], restitution=p["e"], seed=p["seed"], precision=precision, policy=policy)
+            return gas(self.n, phi=p["phi"], restitution=p["e"], seed=p["seed"], precision=precision, policy=policy,
+                       rsa=rsa)
         if self.kind == "rebound":
             st = inputs.two_sphere_rebound(speed=p["speed"])
             cfg = config.granular_gas_config(box=st["box"], dt=DT_GAS, precision=precision, policy=policy)
@@ -111,20 +120,26 @@ class Job:
         return cfg, st
 
 
-def serve_trace(njobs=64, rate=0.5, seed=0, smin=1000, smax=50000):
-    """Job stream; arrivals are a Poisson process of `rate` jobs per pump tick."""
+def serve_trace(njobs=64, rate=0.5, seed=0, smin=1000, smax=50000, mix=(0.5, 0.25, 0.25)):
+    """Job stream; arrivals are a Poisson process of `rate` jobs per pump tick.
+    The kinds (cooling gas, two-sphere rebound, LJ melt) come in the exact
+    proportions `mix` (rounded), in a seeded random order."""
     rng = np.random.default_rng(seed)
+    ngas = int(round(mix[0] * njobs))
+    nreb = int(round(mix[1] * njobs))
+    kinds = np.array(["gas"] * ngas + ["rebound"] * nreb + ["lj"] * (njobs - ngas - nreb))
+    kinds = kinds[rng.permutation(njobs)]
     t = 0.0
     jobs = []
     for k in range(njobs):
         t += rng.exponential(1.0 / rate) if k else 0.0
         steps = int(round(math.exp(rng.uniform(math.log(smin), math.log(smax)))))
-        u = rng.uniform()
-        if u < 0.5:
+        kind = kinds[k]
+        if kind == "gas":
             n = int(round(math.exp(rng.uniform(math.log(100), math.log(200000)))))
             jobs.append(Job("gas", n, steps, t, dict(phi=rng.uniform(0.05, 0.3), e=rng.uniform(0.8, 0.99),
                                                        seed=seed * 1000 + k)))
-        elif u < 0.75:
+        elif kind == "rebound":
             jobs.append(Job("rebound", 2, steps, t, dict(speed=rng.uniform(0.1, 2.0))))
         else:
             n_target = math.exp(rng.uniform(math.log(500), math.log(100000)))
@@ -141,13 +156,14 @@ SERVE_DEM_SLOTS = [(128, 32), (1024, 24), (8192, 16), (65536, 12), (200000, 8)]
 SERVE_LJ_SLOTS = [(2048, 8), (16384, 8), (100000, 6)]
 
 
-def serve_slots(precision="mixed", policy="displacement"):
-    """(slot configs, slot capacities) for a job server over serve_trace."""
+def serve_slots(precision="mixed", policy="displacement", mult=1):
+    """(slot configs, slot capacities) for a job server over serve_trace;
+    `mult` times the slot counts of SERVE_DEM_SLOTS / SERVE_LJ_SLOTS."""
     cfgs, caps = [], []
     for cap, cnt in SERVE_DEM_SLOTS:
-        cfgs += [config.granular_gas_config(precision=precision, policy=policy)] * cnt
-        caps += [cap] * cnt
+        cfgs += [config.granular_gas_config(precision=precision, policy=policy)] * (cnt * mult)
+        caps += [cap] * (cnt * mult)
     for cap, cnt in SERVE_LJ_SLOTS:
-        cfgs += [config.lj_fluid_config(precision=precision, policy=policy)] * cnt
-        caps += [cap] * cnt
+        cfgs += [config.lj_fluid_config(precision=precision, policy=policy)] * (cnt * mult)
+        caps += [cap] * (cnt * mult)
     return cfgs, caps

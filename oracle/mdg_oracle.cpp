@@ -1455,3 +1455,98 @@ int orc_lj_tails(void* h, double* e_tail, double* p_tail) {
 }
 
 }  // extern "C"
+
+// ---- seeded random sequential addition (input generation for the CPU arm) --
+// The same stream and acceptance rule as the library's mdg_rsa_spheres:
+// candidate centres uniform in the box (inset by rmax when asked), radius
+// uniform in [rmin, rmax], rejected when a placed sphere lies within
+// sep_factor (r_i + r_j) under the minimum image (insert.rs:523-571), with
+// xoshiro256** (Blackman & Vigna 2018) seeded through splitmix64 and a
+// cell grid of side >= sep_factor 2 rmax.  Same seed, same spheres.
+namespace {
+struct OrcRng {
+    uint64_t s[4];
+    explicit OrcRng(uint64_t seed) {
+        for (auto& v : s) {
+            uint64_t z = (seed += 0x9e3779b97f4a7c15ull);
+            z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+            z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+            v = z ^ (z >> 31);
+        }
+    }
+    static uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
+    double uniform() {
+        const uint64_t r = rotl(s[1] * 5, 7) * 9, t = s[1] << 17;
+        s[2] ^= s[0];
+        s[3] ^= s[1];
+        s[1] ^= s[2];
+        s[0] ^= s[3];
+        s[2] ^= t;
+        s[3] = rotl(s[3], 45);
+        return (double)(r >> 11) * 0x1.0p-53;
+    }
+};
+}  // namespace
+
+extern "C" int orc_rsa_spheres(size_t n, const double* box_lo, const double* box_hi, double rmin, double rmax,
+                               double sep_factor, int inset, uint64_t seed, uint64_t max_attempts, double* pos,
+                               double* rad, size_t* placed) {
+    *placed = 0;
+    if (!(rmin > 0.0) || !(rmax >= rmin) || !(sep_factor > 0.0)) return 9;
+    double L[3], lo[3], hi[3], cell[3];
+    int nc[3];
+    const double reach = sep_factor * 2.0 * rmax;
+    for (int d = 0; d < 3; d++) {
+        L[d] = box_hi[d] - box_lo[d];
+        lo[d] = box_lo[d] + (inset ? rmax : 0.0);
+        hi[d] = box_hi[d] - (inset ? rmax : 0.0);
+        if (!(L[d] > 0.0) || !(hi[d] > lo[d])) return 9;
+        const double c = std::floor(L[d] / reach);
+        nc[d] = c < 1.0 ? 1 : (c > 1024.0 ? 1024 : (int)c);
+        cell[d] = L[d] / nc[d];
+    }
+    std::vector<int64_t> head((size_t)nc[0] * nc[1] * nc[2], -1), link;
+    link.reserve(n);
+    const uint64_t limit = max_attempts ? max_attempts : (uint64_t)n * 20000ull;
+    const bool poly = rmax > rmin;
+    OrcRng rng(seed);
+    auto cell_of = [&](double x, int d) {
+        int c = (int)std::floor((x - box_lo[d]) / cell[d]) % nc[d];
+        return c < 0 ? c + nc[d] : c;
+    };
+    // the cells around a candidate: all of an axis with fewer than 3 cells
+    auto nb = [&](int ci, int d, int k) { return nc[d] >= 3 ? (ci + k - 1 + nc[d]) % nc[d] : k; };
+    size_t count = 0;
+    for (uint64_t att = 0; att < limit && count < n; att++) {
+        double c[3];
+        for (int d = 0; d < 3; d++) c[d] = lo[d] + (hi[d] - lo[d]) * rng.uniform();
+        const double r = poly ? rmin + (rmax - rmin) * rng.uniform() : rmin;
+        const int ci[3] = {cell_of(c[0], 0), cell_of(c[1], 1), cell_of(c[2], 2)};
+        const int m[3] = {nc[0] >= 3 ? 3 : nc[0], nc[1] >= 3 ? 3 : nc[1], nc[2] >= 3 ? 3 : nc[2]};
+        bool ok = true;
+        for (int a = 0; a < m[0] && ok; a++)
+            for (int b = 0; b < m[1] && ok; b++)
+                for (int e = 0; e < m[2] && ok; e++) {
+                    const size_t k = ((size_t)nb(ci[0], 0, a) * nc[1] + nb(ci[1], 1, b)) * nc[2] + nb(ci[2], 2, e);
+                    for (int64_t j = head[k]; j >= 0 && ok; j = link[j]) {
+                        double r2 = 0.0;
+                        for (int d = 0; d < 3; d++) {
+                            double dx = pos[3 * j + d] - c[d];
+                            dx -= L[d] * std::nearbyint(dx / L[d]);
+                            r2 += dx * dx;
+                        }
+                        const double md = sep_factor * (r + rad[j]);
+                        ok = !(r2 <= md * md);
+                    }
+                }
+        if (!ok) continue;
+        for (int d = 0; d < 3; d++) pos[3 * count + d] = c[d];
+        rad[count] = r;
+        const size_t k = ((size_t)ci[0] * nc[1] + ci[1]) * nc[2] + ci[2];
+        link.push_back(head[k]);
+        head[k] = (int64_t)count;
+        count++;
+    }
+    *placed = count;
+    return count == n ? 0 : 9;
+}

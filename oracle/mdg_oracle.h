@@ -124,6 +124,12 @@ long   orc_overlap_count(void* h);
 /* LJ long-range tail corrections E_tail, P_tail (equimolar weights over the
  * type pairs, setup_lj_tails). */
 int    orc_lj_tails(void* h, double* e_tail, double* p_tail);
+/* Seeded random sequential addition of spheres, the same stream and
+ * acceptance rule as the library's mdg_rsa_spheres (same seed, same spheres):
+ * inputs for the CPU arm made without the library.  Returns 0 when all n fit. */
+int    orc_rsa_spheres(size_t n, const double* box_lo, const double* box_hi, double rmin, double rmax,
+                       double sep_factor, int inset, uint64_t seed, uint64_t max_attempts, double* pos,
+                       double* rad, size_t* placed);
 
 #ifdef __cplusplus
 }

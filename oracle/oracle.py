@@ -86,6 +86,9 @@ def _load():
         lib.orc_get_tags.argtypes = [C.c_void_p, P(C.c_uint32)]
         lib.orc_get_types.argtypes = [C.c_void_p, P(C.c_uint32)]
         lib.orc_get_scale.argtypes = [C.c_void_p, P(C.c_double), P(C.c_double)]
+        lib.orc_rsa_spheres.argtypes = [C.c_size_t, P(C.c_double), P(C.c_double), C.c_double, C.c_double,
+                                        C.c_double, C.c_int, C.c_uint64, C.c_uint64, P(C.c_double), P(C.c_double),
+                                        P(C.c_size_t)]
         lib.orc_get_image.argtypes = [C.c_void_p, P(C.c_int32)]
         lib.orc_get_pairs.argtypes = [C.c_void_p, P(C.c_uint32), C.c_size_t]
         lib.orc_get_pairs.restype = C.c_size_t
@@ -97,6 +100,24 @@ def _load():
         lib.orc_overlap_count.restype = C.c_long
         _lib = lib
     return _lib
+
+
+def rsa_spheres(n, box_lo, box_hi, rmin, rmax, sep_factor=1.1, inset=True, seed=0, max_attempts=0):
+    """Seeded random sequential addition of spheres by the oracle: the same
+    spheres as the library's mdg_rsa_spheres for the same arguments, made
+    without loading the library (inputs of the CPU arm)."""
+    lib = _load()
+    pos = np.zeros((n, 3))
+    rad = np.zeros(n)
+    lo = (C.c_double * 3)(*box_lo)
+    hi = (C.c_double * 3)(*box_hi)
+    placed = C.c_size_t()
+    r = lib.orc_rsa_spheres(n, lo, hi, rmin, rmax, sep_factor, int(inset), seed, max_attempts,
+                            pos.ctypes.data_as(C.POINTER(C.c_double)), rad.ctypes.data_as(C.POINTER(C.c_double)),
+                            C.byref(placed))
+    if r:
+        raise RuntimeError(f"orc_rsa_spheres placed {placed.value}/{n}")
+    return pos, rad
 
 
 def _p(a, ct=C.c_double):

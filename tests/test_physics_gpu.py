@@ -14,8 +14,6 @@ reference's own validation bounds.
   GPU paths within 2 % of the oracle's and within 15 % of the kinetic-theory
   value of examples/granular_gas_benchmark/haff_analysis.py:82-104.
 """
-import math
-
 import numpy as np
 import pytest
 
@@ -23,7 +21,7 @@ pytestmark = pytest.mark.gpu
 
 
 def _lj_energy(backend, prec, steps=2000, every=50):
-    from mddem_gb300 import capi, config, inputs
+    from mddem_gb300 import capi, config, inputs, validate
 
     cfg = config.lj_fluid_config(nose_hoover=False, precision=prec)
     st = inputs.lj_fcc(6, 10.06, 0.85, 0.85, seed=3)
@@ -35,15 +33,7 @@ def _lj_energy(backend, prec, steps=2000, every=50):
     else:
         o = capi.Context(cfg, len(st["tag"]))
         o.upload(st)
-    o.force_only()
-    E = []
-    for k in range(steps // every + 1):
-        t = o.thermo()
-        E.append(t["ke"] + t["pe"])
-        if k < steps // every:
-            o.step(every)
-    E = np.array(E)
-    return E, np.polyfit(np.arange(len(E)) * every, E, 1)[0]
+    return validate.energy_drift(o, steps, every)
 
 
 def test_lj_energy_drift(gpu_lib):
@@ -82,7 +72,7 @@ def test_lj_structure_and_diffusion(gpu_lib):
 
 
 def _haff(backend, prec, n=2000, phi=0.2, e=0.8, steps=40000, every=2000):
-    from mddem_gb300 import capi, workloads
+    from mddem_gb300 import capi, validate, workloads
 
     cfg, st = workloads.gas(n, phi=phi, restitution=e, friction=0.0, seed=11, precision=prec)
     if backend == "oracle":
@@ -93,20 +83,7 @@ def _haff(backend, prec, n=2000, phi=0.2, e=0.8, steps=40000, every=2000):
     else:
         o = capi.Context(cfg, n)
         o.upload(st)
-    T = []
-    for k in range(steps // every + 1):
-        T.append(o.thermo()["granular_temp"])
-        if k < steps // every:
-            o.step(every)
-    T = np.array(T)
-    t = np.arange(len(T)) * every * cfg.dt
-    a, b = np.polyfit(t, 1.0 / np.sqrt(T), 1)
-    L = cfg.box[0]
-    nd = n / L ** 3
-    ph = nd * 4.0 / 3.0 * math.pi * 1e-9
-    g0 = (1.0 - ph / 2.0) / (1.0 - ph) ** 3
-    om = 4.0 / 3.0 * nd * (2e-3) ** 2 * g0 * math.sqrt(math.pi) * (1.0 - e * e)
-    return b / a, 2.0 / (om * math.sqrt(T[0])), T[-1] / T[0]
+    return validate.haff(o, cfg, n, e, steps=steps, every=every)
 
 
 def test_haff_cooling(gpu_lib):

@@ -70,3 +70,24 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
     a = types.SimpleNamespace(workload="serve", warmup=3, steps=0, gpus=2)
     assert bench.run_reference(a) is None
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_inputs_do_not_load_the_library():
+    """The reference arm makes its jobs' inputs with the oracle's own sphere
+    placement: building a stretch of the served stream's jobs and stepping
+    them maps the oracle's library and never libmddem_gb300.so."""
+    import subprocess
+    import sys
+
+    code = (
+        "import sys; sys.path.insert(0, %r)\n"
+        "import bench\n"
+        "bench.REF_BUDGET = 0.5\n"
+        "w, s = bench._ref_worker(('serve', (list(range(0, 16)), 16)))\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "assert w > 0 and s > 0\n"
+        "assert 'libmdg_oracle' in maps\n"
+        "assert 'libmddem_gb300' not in maps, 'library mapped'\n"
+        "print('ok')\n" % ROOT)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and "ok" in r.stdout, r.stderr[-2000:]

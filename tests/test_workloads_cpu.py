@@ -13,7 +13,7 @@ def test_serve_trace_is_seeded_and_has_the_stated_mix():
     b = w.serve_trace(njobs=128, rate=2.0, seed=2024)
     assert [(j.kind, j.n, j.steps, j.arrival) for j in a] == [(j.kind, j.n, j.steps, j.arrival) for j in b]
     kinds = [j.kind for j in a]
-    assert (kinds.count("gas"), kinds.count("rebound"), kinds.count("lj")) == (56, 40, 32)
+    assert (kinds.count("gas"), kinds.count("rebound"), kinds.count("lj")) == (64, 32, 32)  # exactly 50/25/25
     assert all(1000 <= j.steps <= 50000 for j in a)
     assert all(100 <= j.n <= 200000 for j in a if j.kind == "gas")
     assert all(j.n == 2 for j in a if j.kind == "rebound")
@@ -29,9 +29,11 @@ def test_every_job_fits_a_slot_class():
     lj_cap = max(c for c, _ in w.SERVE_LJ_SLOTS)
     for j in w.serve_trace(njobs=128, rate=2.0, seed=2024):
         assert j.n <= (lj_cap if j.kind == "lj" else dem_cap)
-    cfgs, caps = w.serve_slots("mixed")
-    assert len(cfgs) == len(caps) == sum(c for _, c in w.SERVE_DEM_SLOTS) + sum(c for _, c in w.SERVE_LJ_SLOTS)
-    assert all(c.precision == "mixed" for c in cfgs)
+    for mult in (1, 2):
+        cfgs, caps = w.serve_slots("mixed", mult=mult)
+        assert len(cfgs) == len(caps) == mult * (sum(c for _, c in w.SERVE_DEM_SLOTS) +
+                                                 sum(c for _, c in w.SERVE_LJ_SLOTS))
+        assert all(c.precision == "mixed" for c in cfgs)
 
 
 def test_job_states_are_reproducible():
@@ -46,3 +48,22 @@ def test_job_states_are_reproducible():
         assert len(s1["tag"]) == j.n
         assert np.array_equal(s1["pos"], s2["pos"]) and np.array_equal(s1["vel"], s2["vel"])
         assert c1 == c2
+
+
+def test_oracle_rsa_places_the_library_spheres():
+    """The oracle's seeded sphere placement (inputs of the CPU arm, made
+    without the library) gives exactly the library's spheres: mono- and
+    polydisperse, inset and periodic, several seeds."""
+    import numpy as np
+
+    from mddem_gb300 import build, capi
+    from oracle import oracle
+
+    build.build()
+    oracle.build()
+    for n, box, rmin, rmax, sep, inset, seed in [(500, 0.025, 1e-3, 1e-3, 1.1, True, 0),
+                                                  (3000, 0.04, 0.8e-3, 1.2e-3, 1.0, False, 7),
+                                                  (20000, 0.08, 1e-3, 1e-3, 1.1, True, 12345)]:
+        a = capi.rsa_spheres(n, (0.0,) * 3, (box,) * 3, rmin, rmax, sep, inset, seed)
+        b = oracle.rsa_spheres(n, (0.0,) * 3, (box,) * 3, rmin, rmax, sep, inset, seed)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
