@@ -348,13 +348,15 @@ int cuda_err(cudaError_t e) {
 // neighbor_setup + compute_bin_grid (crates/mddem_core/src/neighbor.rs:480-541,
 // 290-371) for one rank, from the uploaded cutoff radii.
 // List build mode (all give the same rows): under about 6 particles per bin
-// a thread per particle; a warp per bin when there are enough bins to fill
-// the GPU (and no more bins than particles, as bins take particle slots);
-// else a warp per particle.
+// a thread per particle; a warp per bin from 512 bins on (and no more bins
+// than particles, as bins take particle slots); else a warp per particle.
+// Measured on GB300 (LJ melts, rho 0.85): a warp per particle is faster up
+// to about 7000 atoms (343 bins: 59 against 75 us), a warp per bin from
+// about 1300 bins on (27436 atoms: 99 against 203 us).
 int auto_build_mode(const SysParams& p, size_t n) {
     const double nbins = (double)p.nc[0] * (double)p.nc[1] * (double)p.nc[2];
     if ((double)n < 6.0 * nbins) return 2;
-    if (nbins >= 2048.0 && (size_t)p.ncell <= n) return 0;
+    if (nbins >= 512.0 && (size_t)p.ncell <= n) return 0;
     return 1;
 }
 

@@ -652,7 +652,7 @@ constexpr int BUILD_SUBS = BLK / BUILD_WARPS;  // work units per 128-particle bl
 
 // Row of particle li of system s by one thread (dilute systems, and the
 // rare particles whose window has particles in ghost-layer bins).
-__device__ void build_one(const Dev& d, int s, int li) {
+__device__ __noinline__ void build_one(const Dev& d, int s, int li) {
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
     const long long i = (long long)sp.p0 + li;
@@ -756,7 +756,7 @@ __device__ void build_one(const Dev& d, int s, int li) {
 // One warp per bin (large dense systems): bin `sub * BUILD_WARPS + warp` of
 // block `lcb` of system s; the lanes are the bin's particles, 32 at a time.
 // Warp-synchronous only (no block barrier), so warps may leave early.
-__device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
+__device__ __noinline__ void build_cells(const Dev& d, int s, int lcb, int sub) {
     __shared__ float4 tile_h[BUILD_WARPS][32], tile_l[BUILD_WARPS][32];
     __shared__ int tile_e[BUILD_WARPS][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -945,7 +945,7 @@ __device__ void build_cells(const Dev& d, int s, int lcb, int sub) {
 // hits are written in candidate order at ballot offsets.  A window with
 // particles in a ghost-layer bin (rounding at the box face) falls back to
 // build_one on lane 0.
-__device__ void build_warp(const Dev& d, int s, int li) {
+__device__ __noinline__ void build_warp(const Dev& d, int s, int li) {
     __shared__ int s_pre[BUILD_WARPS][33], s_m0[BUILD_WARPS][32], s_q[BUILD_WARPS][32], s_E[BUILD_WARPS][32];
     const SysParams& sp = d.sp[s];
     SysState* st = d.ss + s;
@@ -1117,6 +1117,257 @@ __device__ void build_warp(const Dev& d, int s, int li) {
     }
 }
 
+// Candidates one warp stages at a time in build_cells_staged.
+constexpr int STAGE_CAP = 384;
+
+// One warp per bin, staged (systems with many dense bins): the candidates of
+// the bin's window are gathered into shared memory in passes of 32 (every
+// lane issues its loads together: one memory latency per pass instead of one
+// per window bin), moved by their periodic image, and those farther than the
+// list cutoff from the centre bin's box are dropped (no particle of the bin
+// can pair with them; about 30 % of a dense window).  The staged candidates
+// are screened from shared memory against the bin's particles (the lanes),
+// with the system's parameters and each window bin's owner rule and image
+// code in registers and shared memory.  Same candidates in the same order as
+// build_cells, hence identical rows.  Falls back to build_cells for a window
+// of more than 32 bins (bins smaller than the list cutoff) and when a window
+// bin on a box face has particles in its adjacent ghost-layer bin (placed
+// there by rounding).
+__device__ void build_cells_staged(const Dev& d, int s, int lcb, int sub) {
+    __shared__ float4 st_p[BUILD_WARPS][STAGE_CAP];  // hi part + image shift, cutoff radius
+    __shared__ int st_m[BUILD_WARPS][STAGE_CAP];     // the row entry: local index | image code << 26 | edge << 31
+    __shared__ int st_f[BUILD_WARPS][STAGE_CAP];     // own | oth << 1 | same << 2 | shifted << 3 | entry << 4
+    __shared__ int st_pre[BUILD_WARPS][33], st_q[BUILD_WARPS][32], st_E[BUILD_WARPS][32], st_m0[BUILD_WARPS][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const SysParams& sp = d.sp[s];
+    SysState* st = d.ss + s;
+    if (!do_rebuild(st)) return;
+    const int c = lcb * BLK + sub * BUILD_WARPS + warp;
+    if (c >= sp.ncell) return;
+    const int a0 = d.cstart[sp.c0 + c], a1 = d.cstart[sp.c0 + c + 1];
+    if (a0 == a1) return;
+    const int wy = 2 * sp.win[1] + 1, wz = 2 * sp.win[2] + 1;
+    const int nent = (2 * sp.win[0] + 1) * wy * wz;
+    if (nent > 32) {  // uniform over the warp
+        build_cells(d, s, lcb, sub);
+        return;
+    }
+    const int ez = c % sp.ext[2];
+    const int ey = (c / sp.ext[2]) % sp.ext[1];
+    const int ex = c / (sp.ext[2] * sp.ext[1]);
+    const int qx0 = min(max(ex - sp.sl[0], 0), sp.nc[0] - 1);
+    const int qy0 = min(max(ey - sp.sl[1], 0), sp.nc[1] - 1);
+    const int qz0 = min(max(ez - sp.sl[2], 0), sp.nc[2] - 1);
+    // window entry `lane` (reference stencil order): image shift, tile rule
+    // and candidate range of its bin
+    int nseg = 0, eq = 0, eE = 0, em0 = 0;
+    bool ghost = false;
+    if (lane < nent) {
+        const int e = lane;
+        int qx = qx0 + e / (wy * wz) - sp.win[0], sx = 0;
+        int qy = qy0 + (e / wz) % wy - sp.win[1], sy = 0;
+        int qz = qz0 + e % wz - sp.win[2], sz = 0;
+        if (qx < 0) { qx += sp.nc[0]; sx = -1; } else if (qx >= sp.nc[0]) { qx -= sp.nc[0]; sx = 1; }
+        if (qy < 0) { qy += sp.nc[1]; sy = -1; } else if (qy >= sp.nc[1]) { qy -= sp.nc[1]; sy = 1; }
+        if (qz < 0) { qz += sp.nc[2]; sz = -1; } else if (qz >= sp.nc[2]) { qz -= sp.nc[2]; sz = 1; }
+        const bool ok = !(sx && !sp.per[0]) && !(sy && !sp.per[1]) && !(sz && !sp.per[2]) && qx >= 0 &&
+                        qx < sp.nc[0] && qy >= 0 && qy < sp.nc[1] && qz >= 0 && qz < sp.nc[2];
+        if (ok) {
+            const int Ex = qx + sp.sl[0], Ey = qy + sp.sl[1], Ez = qz + sp.sl[2];
+            const int flatE = (Ex * sp.ext[1] + Ey) * sp.ext[2] + Ez;
+            const TileRule tr = tile_rule(sp, ex, ey, ez, Ex, Ey, Ez, sx, sy, sz);
+            eE = flatE;
+            eq = ((sx + 1) << 1) | ((sy + 1) << 3) | ((sz + 1) << 5) | (tr.own ? 1 << 13 : 0) |
+                 (tr.oth ? 1 << 14 : 0) | (tr.same ? 1 << 15 : 0);
+            if (tr.own || tr.oth || tr.same || (sx | sy | sz)) {
+                em0 = d.cstart[sp.c0 + flatE];
+                nseg = d.cstart[sp.c0 + flatE + 1] - em0;
+            }
+            const int axa = (qx == 0) ? -1 : 0, axb = (qx == sp.nc[0] - 1) ? 1 : 0;
+            const int aya = (qy == 0) ? -1 : 0, ayb = (qy == sp.nc[1] - 1) ? 1 : 0;
+            const int aza = (qz == 0) ? -1 : 0, azb = (qz == sp.nc[2] - 1) ? 1 : 0;
+            for (int ax = axa; ax <= axb; ax++)
+                for (int ay = aya; ay <= ayb; ay++)
+                    for (int az = aza; az <= azb; az++) {
+                        if ((ax | ay | az) == 0) continue;
+                        const int g = ((Ex + ax) * sp.ext[1] + (Ey + ay)) * sp.ext[2] + (Ez + az);
+                        if (d.cstart[sp.c0 + g] != d.cstart[sp.c0 + g + 1]) ghost = true;
+                    }
+        }
+    }
+    if (__any_sync(0xffffffffu, ghost)) {
+        build_cells(d, s, lcb, sub);
+        return;
+    }
+    int incl = nseg;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    st_pre[warp][lane] = incl - nseg;
+    st_q[warp][lane] = eq;
+    st_E[warp][lane] = eE;
+    st_m0[warp][lane] = em0;
+    if (lane == 0) st_pre[warp][32] = total;
+    // the system's parameters the loops use, in registers (the list stores
+    // could alias the global SysParams for all the compiler knows)
+    const float brel = sp.band_rel;
+    const bool uniform = sp.uniform != 0, newton = sp.newton != 0;
+    const float ucut2 = sp.ucut2f, sf2 = sp.sf2f;
+    const float in_f = 1.f + brel, near_f = 1.f - brel;
+    const float Lx = sp.Lh[0], Ly = sp.Lh[1], Lz = sp.Lh[2];
+    const long long sp0 = sp.p0;
+    const int ncap = sp.ncap, npad = sp.npad;
+    // the centre bin's box in the frame of the geometry copy (x - lo),
+    // widened by 1e-6 of the box for rounding; uniform systems drop staged
+    // candidates farther than the list cutoff (plus the band) from it
+    const float bx0 = (float)((ex - sp.sl[0]) * sp.bin[0] - 1e-6 * sp.L[0]);
+    const float by0 = (float)((ey - sp.sl[1]) * sp.bin[1] - 1e-6 * sp.L[1]);
+    const float bz0 = (float)((ez - sp.sl[2]) * sp.bin[2] - 1e-6 * sp.L[2]);
+    const float bx1 = (float)((ex - sp.sl[0] + 1) * sp.bin[0] + 1e-6 * sp.L[0]);
+    const float by1 = (float)((ey - sp.sl[1] + 1) * sp.bin[1] + 1e-6 * sp.L[1]);
+    const float bz1 = (float)((ez - sp.sl[2] + 1) * sp.bin[2] + 1e-6 * sp.L[2]);
+    const float cull2 = ucut2 * in_f;
+    for (int ib = a0; ib < a1; ib += 32) {
+        const long long i = ib + lane;
+        const bool act = i < a1;
+        float4 hi = make_float4(0, 0, 0, 0), lo = make_float4(0, 0, 0, 0);
+        bool edge_i = false;
+        if (act) {
+            d.lbp[i] = d.pos[i];
+            hi = d.pos2[2 * i];
+            lo = d.pos2[2 * i + 1];
+            edge_i = d.cell[i] < 0;
+        }
+        uint32_t* row = d.nlist + sp.lst0 + (i - sp0);
+        const int li = (int)(i - sp0);
+        int count = 0;
+        int q0 = 0;  // next candidate of the window sequence to stage
+        while (q0 < total) {
+            // stage: passes of 32 candidates, kept ones compacted by ballot
+            __syncwarp();
+            int np = 0;
+            while (q0 < total && np + 32 <= STAGE_CAP) {
+                const int q = q0 + lane;
+                bool keep = false;
+                float4 hj = make_float4(0, 0, 0, 0);
+                int meta = 0, fl = 0;
+                if (q < total) {
+                    int k = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1)
+                        if (st_pre[warp][k + step] <= q) k += step;
+                    const int ek = st_q[warp][k];
+                    const long long j = st_m0[warp][k] + (q - st_pre[warp][k]);
+                    const int sx = ((ek >> 1) & 3) - 1, sy = ((ek >> 3) & 3) - 1, sz = ((ek >> 5) & 3) - 1;
+                    hj = d.pos2[2 * j];
+                    hj.x += (float)sx * Lx;
+                    hj.y += (float)sy * Ly;
+                    hj.z += (float)sz * Lz;
+                    keep = true;
+                    if (uniform) {
+                        const float ox = fmaxf(fmaxf(bx0 - hj.x, hj.x - bx1), 0.f);
+                        const float oy = fmaxf(fmaxf(by0 - hj.y, hj.y - by1), 0.f);
+                        const float oz = fmaxf(fmaxf(bz0 - hj.z, hj.z - bz1), 0.f);
+                        keep = ox * ox + oy * oy + oz * oz <= cull2;
+                    }
+                    const bool shifted = (sx | sy | sz) != 0;
+                    const bool edge = keep && shifted && d.cell[j] < 0;
+                    const int sc = (sx + 1) * 9 + (sy + 1) * 3 + (sz + 1);
+                    meta = (int)(j - sp0) | (sc << IDX_BITS) | (edge ? (int)0x80000000u : 0);
+                    fl = ((ek >> 13) & 7) | (shifted ? 8 : 0) | (k << 4);
+                }
+                const unsigned int kb = __ballot_sync(0xffffffffu, keep);
+                if (keep) {
+                    const int slot = np + __popc(kb & ((1u << lane) - 1u));
+                    st_p[warp][slot] = hj;
+                    st_m[warp][slot] = meta;
+                    st_f[warp][slot] = fl;
+                }
+                np += __popc(kb);
+                q0 += 32;
+            }
+            __syncwarp();
+            if (!act) continue;
+            for (int t0 = 0; t0 < np; t0 += 32) {
+                const int nt = min(32, np - t0);
+                // hi-part fp32 screen of 32 staged candidates into two bit masks:
+                // within the cutoff band / near the cutoff (precise path)
+                unsigned int mask = 0u, near = 0u;
+                const float4* tile = &st_p[warp][t0];
+                if (uniform) {
+                    const float cin = ucut2 * in_f, cnear = ucut2 * near_f;
+#pragma unroll 8
+                    for (int t = 0; t < nt; t++) {
+                        const float4 hj = tile[t];
+                        const float px = hj.x - hi.x, py = hj.y - hi.y, pz = hj.z - hi.z;
+                        const float r2h = px * px + py * py + pz * pz;
+                        mask |= (r2h <= cin ? 1u : 0u) << t;
+                        near |= (r2h > cnear ? 1u : 0u) << t;
+                    }
+                } else {
+#pragma unroll 4
+                    for (int t = 0; t < nt; t++) {
+                        const float4 hj = tile[t];
+                        const float px = hj.x - hi.x, py = hj.y - hi.y, pz = hj.z - hi.z;
+                        const float r2h = px * px + py * py + pz * pz;
+                        const float ssum = hi.w + hj.w;
+                        const float c2h = ssum * ssum * sf2;
+                        mask |= (r2h <= c2h * in_f ? 1u : 0u) << t;
+                        near |= (r2h > c2h * near_f ? 1u : 0u) << t;
+                    }
+                }
+                while (mask) {
+                    const int t = __ffs(mask) - 1;
+                    mask &= mask - 1u;
+                    const int meta = st_m[warp][t0 + t];
+                    const int fl = st_f[warp][t0 + t];
+                    const int jl = meta & (int)IDX_MASK;
+                    if (!(fl & 8) && jl == li) continue;  // itself
+                    const bool edge = (fl & 8) && (edge_i || meta < 0);
+                    int bits;
+                    if (!((near >> t) & 1u) && !edge) {
+                        // owner rule of the pair's two bins; same bin: by index
+                        const bool same = (fl & 4) != 0;
+                        bits = (((fl & 1) || (same && (!newton || jl > li))) ? 1 : 0) |
+                               (((fl & 2) || (same && newton && jl < li)) ? 2 : 0);
+                    } else {
+                        const int sc = (meta >> IDX_BITS) & 31;
+                        const int k = fl >> 4;
+                        const int fE = st_E[warp][k];
+                        const int Ez = fE % sp.ext[2], Ey = (fE / sp.ext[2]) % sp.ext[1],
+                                  Ex = fE / (sp.ext[2] * sp.ext[1]);
+                        bits = near_pair(d, sp, i, sp0 + jl, hi, lo, d.pos2[2 * (sp0 + jl)],
+                                         d.pos2[2 * (sp0 + jl) + 1], sc / 9 - 1, (sc / 3) % 3 - 1, sc % 3 - 1, edge,
+                                         ex, ey, ez, Ex, Ey, Ez,
+                                         TileRule{(fl & 1) != 0, (fl & 2) != 0, (fl & 4) != 0});
+                    }
+                    const uint32_t code = (uint32_t)meta & 0x7fffffffu;  // local index | image code << 26
+                    if (bits & 1) {
+                        if (count < ncap) row[(size_t)count * npad] = code + (27u << IDX_BITS);
+                        count++;
+                    }
+                    if (bits & 2) {
+                        if (count < ncap) row[(size_t)count * npad] = code;
+                        count++;
+                    }
+                }
+            }
+        }
+        if (act) {
+            if (count > ncap) {
+                atomicOr(&st->status, ST_NBR_OVF);
+                atomicMax(&st->max_nbr, count);
+                count = ncap;
+            } else if (count > vload(&st->max_nbr)) {  // skip the atomic on one word when it cannot raise it
+                atomicMax(&st->max_nbr, count);
+            }
+            d.nnum[i] = count;
+        }
+    }
+}
+
 // Work unit (particle block pb, sub-unit sub) of system s, by the system's
 // build mode: 2 (dilute) the block's particles with a thread each (sub-unit
 // 0); 0 (many dense bins) a bin per warp, bins numbered like particle slots;
@@ -1131,18 +1382,20 @@ __device__ void build_unit(const Dev& d, int s, int pb, int sub) {
         return;
     }
     if (sp.build_mode == 0) {
-        build_cells(d, s, pb, sub);  // the system has no more bins than particle slots
+        build_cells_staged(d, s, pb, sub);  // the system has no more bins than particle slots
         return;
     }
     const int li = pb * BLK + sub * BUILD_WARPS + (int)(threadIdx.x >> 5);
     if (li < sp.n) build_warp(d, s, li);  // uniform over the warp
 }
 
-// Minimum resident blocks per SM asked of ptxas for k_build: 5 caps it at
-// 96 registers (from 125) with ~100 B of spills and runs 22 % faster on GB300
-// (LJ 256k) than no cap; a compile-time tuning knob.
+// Minimum resident blocks per SM asked of ptxas for k_build: 4 caps it at
+// 128 registers with ~20 B of spills (5, at 96 registers, spilled in the
+// staged build's inner loop: 10 M local-memory requests per LJ 256k build,
+// 11 % slower); shared memory (45.6 KB per block) allows 4 as well; a
+// compile-time tuning knob.
 #ifndef MDG_BUILD_MINB
-#define MDG_BUILD_MINB 5
+#define MDG_BUILD_MINB 4
 #endif
 __global__ void __launch_bounds__(BUILD_WARPS * 32, MDG_BUILD_MINB) k_build(Dev d)
     RB_FOR_PARTICLE_SUBS(build_unit, BUILD_SUBS)
