@@ -524,16 +524,15 @@ def force_bytes(kind, nfull, contacts, prec="fp64"):
 def serve_mix(srv, trace, sid):
     """Particles, mean full-list row length and stored contacts per particle
     of the jobs resident now, by kind."""
-    ctx = srv.context()
     per = {}
     for r in srv.resident():
         kind = "lj" if trace[sid[r["id"]]].kind == "lj" else "dem"
         p = per.setdefault(kind, dict(n=0, pairs=0, contacts=0, jobs=0))
         p["n"] += int(r["n"])
         p["jobs"] += 1
-        p["pairs"] += len(ctx.pairs(r["slot"]))
+        p["pairs"] += len(srv.pairs_resident(r["slot"]))
         if kind == "dem":
-            p["contacts"] += len(ctx.history(r["slot"])[0])
+            p["contacts"] += len(srv.history_resident(r["slot"])[0])
     return {k: dict(particles=p["n"], jobs=p["jobs"], avg_full_neighbors=2.0 * p["pairs"] / max(1, p["n"]),
                     contacts_per_particle=p["contacts"] / max(1, p["n"])) for k, p in per.items()}
 
@@ -542,15 +541,14 @@ def serve_samples(srv, trace, made, sid, per_kind=(("gas", 3), ("lj", 2), ("rebo
     """States (with contact history) of the largest resident jobs of each kind,
     downloaded from the server's context: the sample the precision form's
     force error is stated on."""
-    ctx = srv.context()
     res = srv.resident()
     out = []
     for kind, m in per_kind:
         ks = sorted((r for r in res if trace[sid[r["id"]]].kind == kind), key=lambda r: -r["n"])[:m]
         for r in ks:
             cfg = made[sid[r["id"]]][0]
-            st = ctx.download(r["slot"])
-            hist = ctx.history(r["slot"]) if cfg.kind == "dem" else None
+            st = srv.download_resident(r["slot"])
+            hist = srv.history_resident(r["slot"]) if cfg.kind == "dem" else None
             out.append((kind, cfg, st, hist))
     return out
 
@@ -613,6 +611,90 @@ def physics_errors():
                         "bounds": {"mixed_vs_fp64": 0.02, "fp64_vs_theory": 0.15}}}
 
 
+# run lengths of the workloads' own error statements (the configs' run lengths)
+LJ_RDF_STEPS = 100000
+LJ_RDF_FRAMES = 20
+COOL_STEPS = {"dem500": 10000, "gas200k": 20000, "gas138k": 20000, "poly1m": 20000}
+
+
+def lj_structure(cfg, st, steps=LJ_RDF_STEPS, frames=LJ_RDF_FRAMES):
+    """g(r) of an NH LJ melt on the mixed and on the plain FP64 path, both
+    from the same FCC state: `steps` steps, g averaged over `frames` frames of
+    the second half; the reference's structure checks on each and the largest
+    |g_mixed - g_fp64| over r < 3 sigma."""
+    import numpy as np
+    from mddem_gb300 import capi, validate
+
+    out, gs = {}, {}
+    nb, rmax = 200, 3.0
+    for prec in ("fp64", "mixed"):
+        c = capi.Context(cfg.replace(precision=prec), len(st["tag"]))
+        c.upload(st)
+        c.step(steps // 2)
+        acc = []
+        for _ in range(frames):
+            c.step(steps // 2 // frames)
+            acc.append(c.rdf(r_max=rmax, nbins=nb)[1])
+        c.close()
+        gs[prec] = np.mean(acc, axis=0)
+        out[prec] = validate.rdf_checks((np.arange(nb) + 0.5) * rmax / nb, gs[prec])
+    out["max_abs_diff"] = float(np.max(np.abs(gs["mixed"] - gs["fp64"])))
+    out["steps"], out["frames"] = steps, frames
+    return out
+
+
+def workload_errors(name, cfg, make, ctx, sys_=None):
+    """The precision form's error statement for a single-system workload (or
+    the listed replicas of a batch): the per-particle force / torque error
+    against the plain FP64 path on the state the timed steps left (with its
+    contact history); for LJ the NVE energy drift over 2000 steps and g(r)
+    after the NH run; for the gases the cooling fit over the workload's run
+    length.  The plain FP64 path is the one the GPU parity tests hold to the
+    oracle (1e-12 per force, identical pair sets and histories)."""
+    from mddem_gb300 import capi, validate
+
+    samples = []
+    for q in (sys_ if sys_ is not None else [0]):
+        c = cfg[q] if isinstance(cfg, list) else cfg
+        samples.append((f"{name}[{q}]" if sys_ is not None else name, c, ctx.download(q),
+                        ctx.history(q) if c.kind == "dem" else None))
+    out = {"force": precision_errors(samples)}
+    if isinstance(cfg, list):
+        return out
+    st = make()
+    n = len(st["tag"])
+    if cfg.kind == "lj":
+        slopes = {}
+        for prec in ("fp64", "mixed"):
+            c = capi.Context(cfg.replace(precision=prec, nose_hoover=False), n)
+            c.upload(st)
+            slopes[prec] = validate.energy_drift(c)[1] / n
+            c.close()
+        out["lj_energy_drift"] = {"mixed_per_step_per_atom": slopes["mixed"], "fp64_per_step_per_atom": slopes["fp64"],
+                                  "ratio": abs(slopes["mixed"]) / max(abs(slopes["fp64"]), 1e-300), "bound": 2.0,
+                                  "steps": 2000, "ensemble": "NVE (thermostat off)"}
+        out["rdf"] = lj_structure(cfg, st)
+    elif name in COOL_STEPS:
+        steps = COOL_STEPS[name]
+        res = {}
+        for prec in ("fp64", "mixed"):
+            c = capi.Context(cfg.replace(precision=prec), n)
+            c.upload(st)
+            res[prec] = validate.cooling(c, cfg.dt, steps, steps // 20)
+            c.close()
+        m = cfg.materials[0]
+        mono = float(st["radius"].min()) == float(st["radius"].max())
+        theory = (validate.haff_theory(n, cfg.box[0], float(st["radius"][0]), m.restitution, res["fp64"][2][0])
+                  if mono else None)
+        out["cooling"] = {"steps": steps, "tc_mixed": res["mixed"][0], "tc_fp64": res["fp64"][0],
+                          "mixed_vs_fp64": res["mixed"][0] / res["fp64"][0] - 1.0,
+                          "T_end_over_T0": {"mixed": res["mixed"][1], "fp64": res["fp64"][1]},
+                          "frictionless_kinetic_theory_tc": theory, "bound_mixed_vs_fp64": 0.02,
+                          "note": "T(t) = T0 / (1 + t/t_c)^2 fitted on 1/sqrt(T); frictional spheres, so kinetic "
+                                  "theory (smooth spheres) is context only"}
+    return out
+
+
 def serve_phases(a, trace, made, at_tick, pumps=2):
     """Where the served step's time goes: the same stream replayed with
     ordinary pumps up to `at_tick` (the middle of the timed window), then
@@ -640,8 +722,9 @@ def serve_phases(a, trace, made, at_tick, pumps=2):
             if mix is None:
                 mix = serve_mix(srv, trace, sid)
                 samples = serve_samples(srv, trace, made, sid)
-            t, kern, rb = srv.context().timed_steps(SERVE_PUMP)
-            rows.append((t, kern, rb))
+            # each context's timesteps, one context after the other
+            per = [c.timed_steps(SERVE_PUMP) for c in srv.contexts()]
+            rows.append((sum(q[0] for q in per), sum(q[1] for q in per), np.max([q[2] for q in per], axis=0)))
             active, pending = srv.pump(0)
         for info in srv.poll():
             srv.fetch(info["id"])
@@ -737,7 +820,8 @@ def bench_serve(a, world, rank, local, dist):
     made = [j.make(a.precision, a.policy) for j in trace]
     srv = serve_server(a)
     if a.eager:
-        srv.context().set_graph_mode(0)
+        for c in srv.contexts():
+            c.set_graph_mode(0)
     # warm-up jobs (one of each kind), drained before the stream starts
     wsteps = 2 * SERVE_PUMP if a.job_steps_scale >= 1.0 else SERVE_PUMP // 4
     for j in (w.Job("gas", 300, wsteps, 0, dict(phi=0.1, e=0.9, seed=7)),
@@ -902,6 +986,12 @@ def bench_ensemble(a, world, rank, local, dist):
                             "frac": ach / peak, "peak_source": src, "traffic": ncu_traffic(name + "/ens256"),
                             "algorithmic_bytes_per_launch": nbytes, "launch_ms": kms,
                             "kernels_ms": {q: v[0] for q, v in cands.items()}}
+        if a.precision == "mixed" and not a.no_error:
+            sizes = [len(q["tag"]) for q in sts]
+            pick = sorted(set(sorted(range(len(sts)), key=lambda q: -sizes[q])[:2]
+                              + [min(range(len(sts)), key=lambda q: cfgs[q].materials[0].restitution),
+                                 max(range(len(sts)), key=lambda q: cfgs[q].materials[0].friction)]))
+            line["error"] = workload_errors("ens256", cfgs, None, ctx, pick)
         if not a.no_e2e:
             line["e2e"] = ensemble_e2e(cfgs, sts, a.steps)
         if not a.no_plain:
@@ -979,7 +1069,7 @@ def main():
     ap.add_argument("--backlog", type=int, default=SERVE_BACKLOG, help="served stream: jobs queued at the start")
     ap.add_argument("--budget-gb", type=float, default=SERVE_BUDGET_GB, help="served stream: admission HBM budget")
     ap.add_argument("--slot-mult", type=int, default=SERVE_SLOT_MULT, help="served stream: slot count multiplier")
-    ap.add_argument("--no-error", action="store_true", help="skip the precision-form error block (serve)")
+    ap.add_argument("--no-error", action="store_true", help="skip the precision-form error block")
     ap.add_argument("--sweep", action="store_true",
                     help="served stream at each SERVE_SWEEP setting: throughput, latency and saturation per setting")
     ap.add_argument("--job-steps-scale", type=float, default=1.0,
@@ -1064,6 +1154,8 @@ def main():
                      "kernels_ms": {q: v[0] for q, v in cands.items()}},
         "clocks": clk.summary(),
     }
+    if rank == 0 and a.precision == "mixed" and not a.no_error:
+        line["error"] = workload_errors(a.workload, cfg, make, ctx)
     if rank == 0 and not a.no_e2e:
         line["e2e"] = e2e(cfg, make, a.steps)
     if rank == 0 and not a.no_cpu_baseline:

@@ -244,6 +244,13 @@ int  mdg_get_history(mdg_ctx* ctx, int sys, uint32_t* keys, double* vals, size_t
  * mode: one launch of a device-side loop).  Returns the first non-zero system
  * status, if any. */
 int  mdg_step(mdg_ctx* ctx, int64_t nsteps);
+/* mdg_step in two halves, for a caller that advances several contexts at
+ * once (each on its own stream, so their launches overlap on the GPU):
+ * mdg_step_async queues the nsteps on the context's stream and returns;
+ * mdg_step_wait blocks until they are done and returns what mdg_step would.
+ * No other call on the context between the two. */
+int  mdg_step_async(mdg_ctx* ctx, int64_t nsteps);
+int  mdg_step_wait(mdg_ctx* ctx);
 /* Step budget of one system: it advances `steps` more timesteps and then
  * freezes (its kernels skip it) until given a new budget; -1 = unlimited (the
  * default after upload).  Used by batching and serving to stop finished jobs
@@ -362,14 +369,16 @@ int  mdg_timed_steps(mdg_ctx* ctx, int64_t nsteps, size_t l2_flush_bytes, mdg_st
 int  mdg_granular_temp_noalloc(const double* vel, const double* mass, size_t n, double* out3, void* stream);
 
 /* ---- Serving: continuous batching of independent jobs --------------------
- * A server owns one batch context whose systems are slots (kind and particle
- * capacity from slot_cfgs / slot_capacity).  Submitted jobs (config + initial
- * state + step count) queue on the host; mdg_server_pump admits queued jobs
- * into free slots of their kind while the resident jobs' estimated device
- * footprint stays within hbm_budget bytes, advances all resident jobs with one
- * multi-step device launch of at most max_steps steps (each job freezes at its
- * own step count), and retires finished jobs (final state kept on the host
- * until fetched).  Times are seconds since server creation. */
+ * A server's slots (kind and particle capacity from slot_cfgs /
+ * slot_capacity) are the systems of one batch context per particle kind, each
+ * on its own stream.  Submitted jobs (config + initial state + step count)
+ * queue on the host; mdg_server_pump admits queued jobs into free slots of
+ * their kind while the resident jobs' estimated device footprint stays within
+ * hbm_budget bytes, advances all resident jobs with one multi-step device
+ * launch of at most max_steps steps per context (all launched before any is
+ * waited for, so the kinds run side by side; each job freezes at its own step
+ * count), and retires finished jobs (final state kept on the host until
+ * fetched).  Times are seconds since server creation. */
 typedef struct mdg_server mdg_server;
 typedef struct mdg_job_info {
     int64_t id;
@@ -386,12 +395,16 @@ int  mdg_server_submit(mdg_server* srv, const mdg_config* cfg, const mdg_state_v
 int  mdg_server_pump(mdg_server* srv, int64_t max_steps, int* active, int* pending);
 int  mdg_server_poll(mdg_server* srv, mdg_job_info* out, int cap, int* n);
 int  mdg_server_fetch(mdg_server* srv, int64_t id, mdg_state_view* out);
+/* The context holding slot 0; mdg_server_slot_context gives the context
+ * holding any slot and the slot's system index there (diagnostics: timed
+ * steps, pairs, a resident job's state). */
 int  mdg_server_context(mdg_server* srv, mdg_ctx** ctx);
+int  mdg_server_slot_context(mdg_server* srv, int slot, mdg_ctx** ctx, int* sys);
 /* Running totals: particle-steps advanced by all pumps, pumps that launched
  * work, jobs retired; resident and queued jobs and their estimated device
  * bytes now; seconds since creation; host seconds spent in admission
  * (configure + upload), in the multi-step launches (to completion) and in
- * retirement (progress read + download). */
+ * retirement (progress read + download); kernels launched; contexts. */
 typedef struct mdg_server_stats_t {
     double particle_steps;
     int64_t pumps, retired;
@@ -399,6 +412,8 @@ typedef struct mdg_server_stats_t {
     size_t hbm_used;
     double time_s;
     double admit_s, step_s, retire_s;
+    int64_t launches;        /* device kernels launched by all of the server's contexts */
+    int32_t contexts;        /* batch contexts (one per particle kind among the slots) */
 } mdg_server_stats_t;
 int  mdg_server_stats(mdg_server* srv, mdg_server_stats_t* out);
 /* The jobs resident in slots now (steps = steps done so far, end_s = -1);

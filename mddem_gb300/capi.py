@@ -28,10 +28,11 @@ STATUS_NAMES = {
 EXPORTS = [
     "mdg_abi_version", "mdg_status_string", "mdg_device_count", "mdg_create", "mdg_batch_create", "mdg_destroy",
     "mdg_num_systems", "mdg_upload_state", "mdg_download_state", "mdg_set_history", "mdg_get_history",
-    "mdg_step", "mdg_force_only", "mdg_get_pairs", "mdg_thermo", "mdg_synchronize", "mdg_kernel_launches",
+    "mdg_step", "mdg_step_async", "mdg_step_wait", "mdg_force_only", "mdg_get_pairs", "mdg_thermo", "mdg_synchronize", "mdg_kernel_launches",
     "mdg_set_graph_mode", "mdg_timed_steps", "mdg_granular_temp_noalloc", "mdg_set_remaining",
     "mdg_get_remaining", "mdg_get_status", "mdg_configure_system", "mdg_server_create", "mdg_server_destroy",
     "mdg_server_submit", "mdg_server_pump", "mdg_server_poll", "mdg_server_fetch", "mdg_server_context",
+    "mdg_server_slot_context",
     "mdg_rsa_spheres", "mdg_get_progress", "mdg_get_stream", "mdg_server_stats",
     "mdg_server_resident", "mdg_get_config", "mdg_set_threads_per_particle", "mdg_get_threads_per_particle",
     "mdg_set_build_mode", "mdg_autotune", "mdg_rdf", "mdg_msd_reset", "mdg_msd",
@@ -110,7 +111,8 @@ class JobInfo(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("particle_steps", C.c_double), ("pumps", C.c_int64), ("retired", C.c_int64),
                 ("resident", C.c_int32), ("pending", C.c_int32), ("hbm_used", C.c_size_t), ("time_s", C.c_double),
-                ("admit_s", C.c_double), ("step_s", C.c_double), ("retire_s", C.c_double)]
+                ("admit_s", C.c_double), ("step_s", C.c_double), ("retire_s", C.c_double),
+                ("launches", C.c_int64), ("contexts", C.c_int32)]
 
 
 class TuneOpts(C.Structure):
@@ -176,6 +178,9 @@ def load(path: str = LIB_PATH):
     lib.mdg_server_poll.argtypes = [C.c_void_p, C.POINTER(JobInfo), C.c_int, C.POINTER(C.c_int)]
     lib.mdg_server_fetch.argtypes = [C.c_void_p, C.c_int64, C.POINTER(StateView)]
     lib.mdg_server_context.argtypes = [C.c_void_p, C.POINTER(C.c_void_p)]
+    lib.mdg_server_slot_context.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_int)]
+    lib.mdg_step_async.argtypes = [C.c_void_p, C.c_int64]
+    lib.mdg_step_wait.argtypes = [C.c_void_p]
     lib.mdg_get_progress.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.POINTER(C.c_int64)]
     lib.mdg_rdf.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_uint64)]
     lib.mdg_msd_reset.argtypes = [C.c_void_p, C.c_int]
@@ -373,23 +378,56 @@ class Server:
             if n.value < 256:
                 return out
 
-    def context(self):
-        """The server's batch context as a non-owning Context (diagnostics:
-        timed steps, thermo, pairs or the state of a resident slot; particle
-        counts are those of the jobs resident at this call)."""
-        ctx = C.c_void_p()
-        _check(self.lib.mdg_server_context(self.h, C.byref(ctx)), "mdg_server_context")
+    def _ctx_of(self, slot):
+        ctx, sys_ = C.c_void_p(), C.c_int()
+        _check(self.lib.mdg_server_slot_context(self.h, int(slot), C.byref(ctx), C.byref(sys_)),
+               "mdg_server_slot_context")
+        return ctx.value, sys_.value
+
+    def _view(self, handle):
+        """Non-owning Context over the server's context `handle`; particle
+        counts are those of the jobs resident now."""
+        slots = [k for k in range(self.nslots) if self._ctx_of(k)[0] == handle]
         c = Context.__new__(Context)
-        c.lib, c.h, c.nsys, c.owner = self.lib, ctx, self.nslots, False
-        c.configs, c._keep, c.n = list(self.slot_configs), [], [0] * self.nslots
+        c.lib, c.h, c.owner = self.lib, C.c_void_p(handle), False
+        c.nsys = len(slots)
+        c.configs, c._keep, c.n = [self.slot_configs[k] for k in slots], [], [0] * len(slots)
         for r in self.resident():
-            c.n[r["slot"]] = int(r["n"])
+            if r["slot"] in slots:
+                c.n[self._ctx_of(r["slot"])[1]] = int(r["n"])
         return c
 
+    def slot_context(self, slot):
+        """(non-owning Context holding `slot`, the slot's system index in it):
+        diagnostics -- timed steps, pairs, history, a resident job's state."""
+        h, q = self._ctx_of(slot)
+        return self._view(h), q
+
+    def contexts(self):
+        """Every batch context of the server (one per particle kind), as
+        non-owning Contexts."""
+        hs = []
+        for k in range(self.nslots):
+            h = self._ctx_of(k)[0]
+            if h not in hs:
+                hs.append(h)
+        return [self._view(h) for h in hs]
+
+    def download_resident(self, slot):
+        """State of the job resident in `slot` now (diagnostics)."""
+        c, q = self.slot_context(slot)
+        return c.download(q)
+
+    def history_resident(self, slot):
+        c, q = self.slot_context(slot)
+        return c.history(q)
+
+    def pairs_resident(self, slot):
+        c, q = self.slot_context(slot)
+        return c.pairs(q)
+
     def launches(self):
-        ctx = C.c_void_p()
-        _check(self.lib.mdg_server_context(self.h, C.byref(ctx)), "mdg_server_context")
-        return int(self.lib.mdg_kernel_launches(ctx))
+        return int(self.stats()["launches"])
 
     def resident(self):
         buf = (JobInfo * 1024)()

@@ -187,6 +187,11 @@ struct mdg_ctx {
     void* flush_buf = nullptr;
     size_t flush_bytes = 0;
     long long launches = 0;
+    // mdg_step_async / mdg_step_wait: the launched step count (0 = none in
+    // flight) and pinned copies of the rebuild-branch counter before and
+    // after the launch
+    int64_t pending_steps = 0;
+    unsigned long long* h_stat = nullptr;
     std::vector<void*> allocs;
 
     ~mdg_ctx() {
@@ -198,6 +203,7 @@ struct mdg_ctx {
         for (void* p : allocs) cudaFree(p);
         if (stream) cudaStreamDestroy(stream);
         if (stream2) cudaStreamDestroy(stream2);
+        if (h_stat) cudaFreeHost(h_stat);
     }
     template <class T>
     T* alloc(size_t n, int& err) {
@@ -566,13 +572,16 @@ int update_run_maps(mdg_ctx* c) {
         for (int b = 0; b < c->cseg_blocks[s]; b++) cb.push_back(c->cblk0_host[s] + b);
     }
     if (!pb.empty() &&
-        (cudaMemcpy(c->d_blk_run, pb.data(), pb.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
-         cudaMemcpy(c->d_cblk_run, cb.data(), cb.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess ||
-         cudaMemcpy(c->d_run_sys, run.data(), run.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess))
+        (cudaMemcpyAsync(c->d_blk_run, pb.data(), pb.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream) !=
+             cudaSuccess ||
+         cudaMemcpyAsync(c->d_cblk_run, cb.data(), cb.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream) !=
+             cudaSuccess ||
+         cudaMemcpyAsync(c->d_run_sys, run.data(), run.size() * sizeof(int), cudaMemcpyHostToDevice, c->stream) !=
+             cudaSuccess))
         return -MDG_ERR_CUDA;
     for (int q = 0; q < 2; q++) {
-        if (!pk[q].empty() && cudaMemcpy(c->d_blk_run_kind[q], pk[q].data(), pk[q].size() * sizeof(int),
-                                         cudaMemcpyHostToDevice) != cudaSuccess)
+        if (!pk[q].empty() && cudaMemcpyAsync(c->d_blk_run_kind[q], pk[q].data(), pk[q].size() * sizeof(int),
+                                              cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
             return -MDG_ERR_CUDA;
         c->d.blk_run_kind[q] = c->d_blk_run_kind[q];
         c->d.nrun_kind[q] = (int)pk[q].size();
@@ -865,7 +874,9 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
     if (!c) return MDG_ERR_OOM;
     cudaGetDevice(&c->device);
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMallocHost(&c->h_stat, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+        cudaGetLastError();
         delete c;
         return MDG_ERR_CUDA;
     }
@@ -1318,15 +1329,15 @@ static bool any_uploaded(const mdg_ctx* c) {
     return false;
 }
 
-int mdg_step(mdg_ctx* c, int64_t nsteps) {
+int mdg_step_async(mdg_ctx* c, int64_t nsteps) {
     if (!c || nsteps < 0) return MDG_ERR_ARG;
     if (!any_uploaded(c)) return MDG_ERR_STATE;
+    if (c->pending_steps) return MDG_ERR_STATE;  // the previous launch was not waited for
     if (nsteps == 0) return MDG_OK;
     const int nrun = update_run_maps(c);
     if (nrun < 0) return -nrun;
     if (nrun == 0) return MDG_OK;  // every system's budget is spent
-    unsigned long long rb0 = 0, rb1 = 0;
-    cudaMemcpy(&rb0, c->d.stat_ctr, sizeof(rb0), cudaMemcpyDeviceToHost);
+    cudaMemcpyAsync(c->h_stat, c->d.stat_ctr, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream);
     if (c->graph_mode) {
         // one launch: the WHILE graph counts the steps down on the device
         if (!c->wgraph) {
@@ -1341,11 +1352,21 @@ int mdg_step(mdg_ctx* c, int64_t nsteps) {
     } else {
         for (int64_t k = 0; k < nsteps; k++) enqueue_step(c, c->stream);
     }
+    cudaMemcpyAsync(c->h_stat + 1, c->d.stat_ctr, sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream);
+    c->pending_steps = nsteps;
+    return cuda_err(cudaGetLastError());
+}
+
+int mdg_step_wait(mdg_ctx* c) {
+    if (!c) return MDG_ERR_ARG;
+    const int64_t nsteps = c->pending_steps;
+    if (!nsteps) return MDG_OK;  // nothing in flight
+    c->pending_steps = 0;
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_err(e);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(e);
-    cudaMemcpy(&rb1, c->d.stat_ctr, sizeof(rb1), cudaMemcpyDeviceToHost);
+    const unsigned long long rb0 = c->h_stat[0], rb1 = c->h_stat[1];
     advance_budgets(c, nsteps);
     // kernels that ran: per step initial + force + final (+ loop control),
     // plus the rebuild kernels on the steps whose rebuild branch opened
@@ -1362,6 +1383,12 @@ int mdg_step(mdg_ctx* c, int64_t nsteps) {
     }
     c->launches += nsteps * base + (long long)rb_kernels(c) * (long long)(c->graph_mode ? (rb1 - rb0) : nsteps);
     return check_status(c);
+}
+
+int mdg_step(mdg_ctx* c, int64_t nsteps) {
+    const int r = mdg_step_async(c, nsteps);
+    if (r) return r;
+    return mdg_step_wait(c);
 }
 
 int mdg_force_only(mdg_ctx* c) {

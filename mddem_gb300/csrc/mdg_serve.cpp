@@ -1,12 +1,15 @@
 // mdg_serve.cpp -- continuous-batching server for independent simulation jobs.
 //
-// The server owns one batch context whose systems are slots (typed by kind,
-// sized by particle capacity).  Jobs are submitted with their config, initial
-// state and step count; pump() admits queued jobs into free slots while the
-// estimated device footprint of the resident jobs stays within the HBM budget,
-// advances every resident job on the GPU with one multi-step launch (each
-// job's step budget freezes it when done, so short jobs never run past their
-// end), retires finished jobs (state downloaded, slot freed) and records
+// The server's slots (typed by kind, sized by particle capacity) live in one
+// batch context per particle kind, each with its own CUDA stream.  Jobs are
+// submitted with their config, initial state and step count; pump() admits
+// queued jobs into free slots while the estimated device footprint of the
+// resident jobs stays within the HBM budget, advances every resident job with
+// one multi-step launch per context -- all contexts' launches are queued
+// before any is waited for, so the kinds' kernels run side by side on the GPU
+// and one kind's latency-bound kernels fill the SMs the other leaves idle --
+// (each job's step budget freezes it when done, so short jobs never run past
+// their end), retires finished jobs (state downloaded, slot freed) and records
 // submit / start / end times.  Job state stays on the device between pumps.
 #include <chrono>
 #include <cstring>
@@ -118,7 +121,9 @@ size_t job_bytes(const mdg_config& c, size_t n) {
 }  // namespace
 
 struct mdg_server {
-    mdg_ctx* ctx = nullptr;
+    std::vector<mdg_ctx*> ctxs;    // one batch context per particle kind present
+    std::vector<int> slot_ctx;     // slot -> its context
+    std::vector<int> slot_sys;     // slot -> its system index in that context
     int nslots = 0;
     std::vector<int> slot_kind;
     std::vector<size_t> slot_cap;
@@ -143,17 +148,44 @@ int mdg_server_create(const mdg_config* slot_cfgs, const size_t* slot_capacity, 
     *out = nullptr;
     auto* s = new (std::nothrow) mdg_server();
     if (!s) return MDG_ERR_OOM;
-    int r = mdg_batch_create(slot_cfgs, slot_capacity, nslots, &s->ctx);
-    if (r) {
-        delete s;
-        return r;
-    }
     s->nslots = nslots;
+    s->slot_ctx.assign(nslots, -1);
+    s->slot_sys.assign(nslots, -1);
+    // the slots of each kind, in order, make one batch context
+    for (int kind : {MDG_KIND_DEM, MDG_KIND_LJ}) {
+        std::vector<mdg_config> cfgs;
+        std::vector<size_t> caps;
+        std::vector<int> ids;
+        for (int k = 0; k < nslots; k++)
+            if (slot_cfgs[k].kind == kind) {
+                cfgs.push_back(slot_cfgs[k]);
+                caps.push_back(slot_capacity[k]);
+                ids.push_back(k);
+            }
+        if (cfgs.empty()) continue;
+        mdg_ctx* ctx = nullptr;
+        const int r = mdg_batch_create(cfgs.data(), caps.data(), (int)cfgs.size(), &ctx);
+        if (r) {
+            for (mdg_ctx* c : s->ctxs) mdg_destroy(c);
+            delete s;
+            return r;
+        }
+        for (size_t q = 0; q < ids.size(); q++) {
+            s->slot_ctx[ids[q]] = (int)s->ctxs.size();
+            s->slot_sys[ids[q]] = (int)q;
+            mdg_set_remaining(ctx, (int)q, 0);
+        }
+        s->ctxs.push_back(ctx);
+    }
     for (int k = 0; k < nslots; k++) {
+        if (s->slot_ctx[k] < 0) {  // a kind other than DEM and LJ
+            for (mdg_ctx* c : s->ctxs) mdg_destroy(c);
+            delete s;
+            return MDG_ERR_CONFIG;
+        }
         s->slot_kind.push_back(slot_cfgs[k].kind);
         s->slot_cap.push_back(slot_capacity[k]);
         s->slot_job.push_back(-1);
-        mdg_set_remaining(s->ctx, k, 0);
     }
     s->budget = hbm_budget;
     *out = s;
@@ -162,7 +194,7 @@ int mdg_server_create(const mdg_config* slot_cfgs, const size_t* slot_capacity, 
 
 void mdg_server_destroy(mdg_server* s) {
     if (!s) return;
-    mdg_destroy(s->ctx);
+    for (mdg_ctx* c : s->ctxs) mdg_destroy(c);
     delete s;
 }
 
@@ -218,10 +250,12 @@ int mdg_server_pump(mdg_server* s, int64_t max_steps, int* active, int* pending)
             ++it;
             continue;
         }
-        int r = mdg_configure_system(s->ctx, slot, &j->cfg);
+        mdg_ctx* ctx = s->ctxs[s->slot_ctx[slot]];
+        const int sys = s->slot_sys[slot];
+        int r = mdg_configure_system(ctx, sys, &j->cfg);
         mdg_state_view v = j->state.view();
-        if (!r) r = mdg_upload_state(s->ctx, slot, &v);
-        if (!r) r = mdg_set_remaining(s->ctx, slot, j->steps);
+        if (!r) r = mdg_upload_state(ctx, sys, &v);
+        if (!r) r = mdg_set_remaining(ctx, sys, j->steps);
         if (r) {  // the job cannot run: finish it with its error
             j->status = r;
             j->t_start = j->t_end = s->now();
@@ -236,54 +270,76 @@ int mdg_server_pump(mdg_server* s, int64_t max_steps, int* active, int* pending)
         s->used += j->bytes;
         it = s->pending.erase(it);
     }
+    const int nctx = (int)s->ctxs.size();
     int nactive = 0;
-    int64_t most = 0;
+    std::vector<int64_t> most(nctx, 0);
     for (int k = 0; k < s->nslots; k++)
         if (s->slot_job[k] >= 0) {
             // a resident job's budget is exactly its steps left: the host
             // tracks it, the device counts it down
             const int64_t left = s->jobs[s->slot_job[k]]->left;
-            most = left > most ? left : most;
+            int64_t& m = most[s->slot_ctx[k]];
+            m = left > m ? left : m;
             nactive++;
         }
     const double tb = s->now();
     s->admit_s += tb - ta;
     int rstep = MDG_OK;
-    const int64_t adv = most < max_steps ? most : max_steps;
-    if (nactive && adv > 0) {
-        rstep = mdg_step(s->ctx, adv);
+    // every context's launch is queued before any is waited for
+    std::vector<int64_t> adv(nctx, 0);
+    bool stepped = false;
+    for (int g = 0; g < nctx; g++) {
+        adv[g] = most[g] < max_steps ? most[g] : max_steps;
+        if (adv[g] <= 0) continue;
+        const int r = mdg_step_async(s->ctxs[g], adv[g]);
+        if (r && rstep == MDG_OK) rstep = r;
+        if (r) adv[g] = 0;
+        stepped = true;
+    }
+    for (int g = 0; g < nctx; g++) {
+        if (adv[g] <= 0) continue;
+        const int r = mdg_step_wait(s->ctxs[g]);
+        if (r && rstep == MDG_OK) rstep = r;
+    }
+    if (stepped) {
         for (int k = 0; k < s->nslots; k++)
             if (s->slot_job[k] >= 0) {
                 const Job* j = s->jobs[s->slot_job[k]].get();
-                s->particle_steps += (double)j->state.n * (double)(j->left < adv ? j->left : adv);
+                const int64_t a = adv[s->slot_ctx[k]];
+                s->particle_steps += (double)j->state.n * (double)(j->left < a ? j->left : a);
             }
         s->pumps++;
     }
     const double tc = s->now();
     s->step_s += tc - tb;
-    // retirement: one read of every slot's budget and status
-    std::vector<int64_t> left(s->nslots, 0);
-    std::vector<int32_t> stw(s->nslots, 0);
-    if (nactive) {
-        const int r = mdg_get_progress(s->ctx, left.data(), stw.data(), nullptr);
-        if (r) return r;
-    }
+    // retirement: one read of every context's budgets and statuses
+    std::vector<std::vector<int64_t>> left(nctx);
+    std::vector<std::vector<int32_t>> stw(nctx);
+    if (nactive)
+        for (int g = 0; g < nctx; g++) {
+            const int ns = mdg_num_systems(s->ctxs[g]);
+            left[g].assign(ns, 0);
+            stw[g].assign(ns, 0);
+            const int r = mdg_get_progress(s->ctxs[g], left[g].data(), stw[g].data(), nullptr);
+            if (r) return r;
+        }
     for (int k = 0; k < s->nslots; k++) {
         if (s->slot_job[k] < 0) continue;
-        s->jobs[s->slot_job[k]]->left = left[k];
-        const bool failed = stw[k] != 0;
-        if (left[k] != 0 && !failed) continue;
+        const int g = s->slot_ctx[k], sys = s->slot_sys[k];
+        s->jobs[s->slot_job[k]]->left = left[g][sys];
+        const bool failed = stw[g][sys] != 0;
+        if (left[g][sys] != 0 && !failed) continue;
         Job* j = s->jobs[s->slot_job[k]].get();
         j->state.alloc(j->state.n, j->cfg.kind == MDG_KIND_DEM);
         mdg_state_view v = j->state.view();
-        const int rd = mdg_download_state(s->ctx, k, &v);
+        const int rd = mdg_download_state(s->ctxs[g], sys, &v);
         j->status = failed ? (rstep != MDG_OK ? rstep : MDG_ERR_STATE) : rd;
         j->t_end = s->now();
         s->finished.push_back(j->id);
         s->retired++;
         s->used -= j->bytes;
         s->slot_job[k] = -1;
-        mdg_set_remaining(s->ctx, k, 0);
+        mdg_set_remaining(s->ctxs[g], sys, 0);
         nactive--;
     }
     s->retire_s += s->now() - tc;
@@ -307,6 +363,9 @@ int mdg_server_stats(mdg_server* s, mdg_server_stats_t* out) {
     out->admit_s = s->admit_s;
     out->step_s = s->step_s;
     out->retire_s = s->retire_s;
+    out->launches = 0;
+    for (mdg_ctx* c : s->ctxs) out->launches += mdg_kernel_launches(c);
+    out->contexts = (int32_t)s->ctxs.size();
     return MDG_OK;
 }
 
@@ -385,7 +444,14 @@ int mdg_server_fetch(mdg_server* s, int64_t id, mdg_state_view* out) {
 
 int mdg_server_context(mdg_server* s, mdg_ctx** ctx) {
     if (!s || !ctx) return MDG_ERR_ARG;
-    *ctx = s->ctx;
+    *ctx = s->ctxs[s->slot_ctx[0]];
+    return MDG_OK;
+}
+
+int mdg_server_slot_context(mdg_server* s, int slot, mdg_ctx** ctx, int* sys) {
+    if (!s || !ctx || !sys || slot < 0 || slot >= s->nslots) return MDG_ERR_ARG;
+    *ctx = s->ctxs[s->slot_ctx[slot]];
+    *sys = s->slot_sys[slot];
     return MDG_OK;
 }
 

@@ -124,20 +124,45 @@ def energy_drift(sim, steps=2000, every=50):
     return E, float(np.polyfit(np.arange(len(E)) * every, E, 1)[0])
 
 
-def haff(sim, cfg, n, restitution, radius=1e-3, steps=40000, every=2000):
-    """Haff cooling of a frictionless granular gas: (t_c fitted on
-    1/sqrt(T) = (1 + t/t_c) / sqrt(T0), t_c of kinetic theory, T_end / T_0)."""
+def cooling(sim, dt, steps=40000, every=2000):
+    """Granular temperature sampled every `every` steps: (t_c fitted on
+    1/sqrt(T) = (1 + t/t_c) / sqrt(T0), T_end / T_0, the samples)."""
     T = []
     for k in range(steps // every + 1):
         T.append(sim.thermo()["granular_temp"])
         if k < steps // every:
             sim.step(every)
     T = np.array(T)
-    t = np.arange(len(T)) * every * cfg.dt
+    t = np.arange(len(T)) * every * dt
     a, b = np.polyfit(t, 1.0 / np.sqrt(T), 1)
-    L = cfg.box[0]
-    nd = n / L ** 3
+    return float(b / a), float(T[-1] / T[0]), T
+
+
+def haff_theory(n, box, radius, restitution, T0):
+    """t_c = 2 / (omega_0 sqrt(T0)) with omega_0 = 4/3 n d^2 g0 sqrt(pi)
+    (1 - e^2) and the Carnahan-Starling g0 (monodisperse spheres)."""
+    nd = n / box ** 3
     ph = nd * 4.0 / 3.0 * math.pi * radius ** 3
     g0 = (1.0 - ph / 2.0) / (1.0 - ph) ** 3
     om = 4.0 / 3.0 * nd * (2.0 * radius) ** 2 * g0 * math.sqrt(math.pi) * (1.0 - restitution ** 2)
-    return float(b / a), float(2.0 / (om * math.sqrt(T[0]))), float(T[-1] / T[0])
+    return float(2.0 / (om * math.sqrt(T0)))
+
+
+def haff(sim, cfg, n, restitution, radius=1e-3, steps=40000, every=2000):
+    """Haff cooling of a frictionless granular gas: (t_c fitted on
+    1/sqrt(T) = (1 + t/t_c) / sqrt(T0), t_c of kinetic theory, T_end / T_0)."""
+    tc, ratio, T = cooling(sim, cfg.dt, steps, every)
+    return tc, haff_theory(n, cfg.box[0], radius, restitution, T[0]), ratio
+
+
+def rdf_checks(r, g):
+    """The LJ liquid structure checks of the reference's
+    examples/lj_argon/validate.py:66-110: first peak position in
+    [0.95, 1.15] sigma and height in [2.4, 3.5] (r in (0.8, 1.5)), mean g
+    over r in (2.0, 2.8) within [0.7, 1.3]."""
+    sel = (r > 0.8) & (r < 1.5)
+    k = int(np.argmax(g[sel]))
+    peak_r, peak_g = float(r[sel][k]), float(g[sel][k])
+    far = float(np.mean(g[(r > 2.0) & (r < 2.8)]))
+    return {"peak_r": peak_r, "peak_g": peak_g, "far_mean": far,
+            "pass": bool(0.95 <= peak_r <= 1.15 and 2.4 <= peak_g <= 3.5 and 0.7 <= far <= 1.3)}

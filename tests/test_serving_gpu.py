@@ -79,12 +79,12 @@ def test_server_results_equal_alone(gpu_lib, precision):
     srv = capi.Server(slots, caps, hbm_budget=16 << 20)
     ids = [srv.submit(c, s, n) for c, s, n in jobs[:3]]
     srv.pump(25)
-    # diagnostics view of the server's context: resident slots download
-    ctx = srv.context()
+    # diagnostics view of the server's contexts: resident slots download
     res = srv.resident()
     assert res
     for r in res:
-        assert len(ctx.download(r["slot"])["tag"]) == r["n"]
+        assert len(srv.download_resident(r["slot"])["tag"]) == r["n"]
+    assert srv.stats()["contexts"] == 2  # one per particle kind
     ids += [srv.submit(c, s, n) for c, s, n in jobs[3:]]
     done = {}
     for _ in range(1000):
