@@ -29,6 +29,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -105,6 +106,9 @@ class ClockSampler:
                  "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            t0 = time.perf_counter()  # the timed region starts once sampling has
+            while not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < 3.0:
+                time.sleep(0.01)
         except OSError:
             self.proc = None
         return self
@@ -338,6 +342,7 @@ SERVE_BUDGET_GB = 96        # admission budget of resident jobs' device bytes (G
 SERVE_SLOT_MULT = 2         # times the slot counts of workloads.SERVE_*_SLOTS
 SERVE_WINDOW = 80           # timed pumps by default: the steady state while jobs keep arriving
 SERVE_WARMUP = 10           # pumps of the stream before the timed window
+SERVE_GROUPS = "kind"       # slots per batch context (workloads.serve_groups)
 PLAIN_SAMPLE_STEPS = 200
 # (jobs, backlog, arrivals per pump, budget GB, slot multiplier) of --sweep;
 # each setting's arrivals last about as long as the timed window
@@ -390,7 +395,8 @@ def serve_server(a):
     from mddem_gb300 import capi, workloads as w
 
     cfgs, caps = w.serve_slots(a.precision, a.policy, mult=getattr(a, "slot_mult", SERVE_SLOT_MULT))
-    return capi.Server(cfgs, caps, int(getattr(a, "budget_gb", SERVE_BUDGET_GB) * (1 << 30)))
+    groups = w.serve_groups(cfgs, caps, getattr(a, "groups", SERVE_GROUPS))
+    return capi.Server(cfgs, caps, int(getattr(a, "budget_gb", SERVE_BUDGET_GB) * (1 << 30)), groups=groups)
 
 
 def state_bytes(st):
@@ -508,6 +514,20 @@ def plain_job_by_job(trace, made):
 # torque) read, v (+ omega) written.
 INIT_BYTES = {("dem", "mixed"): 416, ("dem", "fp64"): 352, ("lj", "mixed"): 192, ("lj", "fp64"): 192}
 FINAL_BYTES = {"dem": 232, "lj": 136}
+
+
+def rebuild_bytes(kind, nfull, contacts, prec="mixed"):
+    """Per particle whose system rebuilds (every rebuild sorts by bin, as
+    sort_atoms_by_bin): the bin of its position (32 read, 4 written), the
+    counting sort's permutation entry (4 + 4), its state permuted once (read and
+    written: x, v, m, cutoff, tag, type, image 104; DEM adds omega and q 64 and
+    the history count 4 + 60 per contact), the geometry copies written
+    (two-float x 32; mixed adds the build copy 32, mixed LJ the fixed-point
+    positions 32), and the list build (two-float x 32, bin start and count 8,
+    4 per row entry, row length 4)."""
+    row = 104 + (64 + 4 + 60 * contacts if kind == "dem" else 0)
+    geo = 32 + (32 if prec == "mixed" else 0) + (32 if (kind, prec) == ("lj", "mixed") else 0)
+    return 36 + 8 + 2 * row + geo + 44 + 4 * nfull
 
 
 def force_bytes(kind, nfull, contacts, prec="fp64"):
@@ -709,7 +729,7 @@ def serve_phases(a, trace, made, at_tick, pumps=2):
     srv = serve_server(a)
     order = sorted(range(len(trace)), key=lambda k: trace[k].arrival)
     nxt, tick, sid = 0, 0, {}
-    rows, mix, samples = [], None, []
+    rows, mix, samples, rebuilt = [], None, [], {}
     while tick < at_tick + pumps:
         while nxt < len(order) and trace[order[nxt]].arrival <= tick:
             k = order[nxt]
@@ -722,8 +742,16 @@ def serve_phases(a, trace, made, at_tick, pumps=2):
             if mix is None:
                 mix = serve_mix(srv, trace, sid)
                 samples = serve_samples(srv, trace, made, sid)
-            # each context's timesteps, one context after the other
-            per = [c.timed_steps(SERVE_PUMP) for c in srv.contexts()]
+            # each context's timesteps, one context after the other; the
+            # systems' build counters give the particles rebuilt
+            per = []
+            for c in srv.contexts():
+                live = [q for q in range(c.nsys) if c.n[q]]
+                nb0 = {q: c.thermo(q)["nbuilds"] for q in live}
+                per.append(c.timed_steps(SERVE_PUMP))
+                for q in live:
+                    kind = c.configs[q].kind
+                    rebuilt[kind] = rebuilt.get(kind, 0) + c.n[q] * (c.thermo(q)["nbuilds"] - nb0[q])
             rows.append((sum(q[0] for q in per), sum(q[1] for q in per), np.max([q[2] for q in per], axis=0)))
             active, pending = srv.pump(0)
         for info in srv.poll():
@@ -740,7 +768,8 @@ def serve_phases(a, trace, made, at_tick, pumps=2):
     names = ("initial", "rebuild", "force", "final")
     ph = {q: float(t[:, 1 + i].mean()) for i, q in enumerate(names)}
     return {"at_pump": at_tick, "timesteps": int(len(t)), "step_ms": float(t[:, 0].mean()), "phases_ms": ph,
-            "rebuild_steps_frac": float(rb.mean()), "kernels_per_step": float(kern.mean())}, mix, samples
+            "rebuild_steps_frac": float(rb.mean()), "kernels_per_step": float(kern.mean()),
+            "rebuilt_particles_per_step": {k: v / len(t) for k, v in rebuilt.items()}}, mix, samples
 
 
 def serve_roofline(a, phases, mix, served_rate):
@@ -754,14 +783,17 @@ def serve_roofline(a, phases, mix, served_rate):
     fin_b = sum(m["particles"] * FINAL_BYTES[k] for k, m in mix.items())
     force_b = sum(m["particles"] * force_bytes(k, m["avg_full_neighbors"], m["contacts_per_particle"], prec)
                   for k, m in mix.items())
+    rb_b = sum(v * rebuild_bytes(k, mix[k]["avg_full_neighbors"], mix[k]["contacts_per_particle"], prec)
+               for k, v in phases.get("rebuilt_particles_per_step", {}).items() if k in mix)
     ph = phases["phases_ms"]
     cands = {"initial": (ph["initial"], init_b), "force": (ph["force"], force_b), "final": (ph["final"], fin_b),
-             "rebuild": (ph["rebuild"], None)}
+             "rebuild": (ph["rebuild"], rb_b or None)}
     name = max(cands, key=lambda q: cands[q][0])
     ms, nbytes = cands[name]
     peak, src = peak_hbm()
-    kernel = {"initial": f"k_initial_{prec}", "final": f"k_final_{prec}", "rebuild": "rebuild pipeline",
-              "force": "k_dem_" + prec + " + k_lj_" + prec}[name]
+    kernel = {"initial": f"k_initial_{prec}", "final": f"k_final_{prec}",
+              "rebuild": "rebuild pipeline (bin sort, permutation, k_build)",
+              "force": ("k_dem_screen + k_dem_contact + k_lj_mixed" if prec == "mixed" else "k_dem_fp64 + k_lj_fp64")}[name]
     step_b = init_b + fin_b + force_b
     bpps = step_b / sum(m["particles"] for m in mix.values())
     out = {"bound": "hbm", "kernel": kernel, "phase": name, "share": ms / phases["step_ms"],
@@ -855,6 +887,8 @@ def bench_serve(a, world, rank, local, dist):
                    "slots": {"dem": [[c, n * a.slot_mult] for c, n in w.SERVE_DEM_SLOTS],
                              "lj": [[c, n * a.slot_mult] for c, n in w.SERVE_LJ_SLOTS]},
                    "hbm_budget_bytes": int(a.budget_gb * (1 << 30)),
+                   "slot_groups": f"{a.groups}: one batch context and stream per group; every context's "
+                                  "multi-step launch is queued before any is waited on",
                    "plain_fp64_reference": "the same jobs one by one on the plain FP64 path; each job's step time "
                                            f"is sampled over up to {PLAIN_SAMPLE_STEPS} steps and scaled to its "
                                            "step count (setup, upload and download timed in full)",
@@ -976,7 +1010,8 @@ def bench_ensemble(a, world, rank, local, dist):
         contacts = sum(len(ctx.history(q)[0]) for q in range(len(sts))) / n
         nfull = sum(2.0 * len(ctx.pairs(q)) for q in range(len(sts))) / n
         cands = {"k_initial": (float(t[:, 1].mean()), n * INIT_BYTES[("dem", a.precision)]),
-                 "k_dem_" + a.precision: (float(t[:, 3].mean()), n * force_bytes("dem", nfull, contacts, a.precision)),
+                 ("k_dem_screen + k_dem_contact" if a.precision == "mixed" else "k_dem_fp64"):
+                     (float(t[:, 3].mean()), n * force_bytes("dem", nfull, contacts, a.precision)),
                  "k_final": (float(t[:, 4].mean()), n * FINAL_BYTES["dem"])}
         name = max(cands, key=lambda q: cands[q][0])
         kms, nbytes = cands[name]
@@ -1069,12 +1104,15 @@ def main():
     ap.add_argument("--backlog", type=int, default=SERVE_BACKLOG, help="served stream: jobs queued at the start")
     ap.add_argument("--budget-gb", type=float, default=SERVE_BUDGET_GB, help="served stream: admission HBM budget")
     ap.add_argument("--slot-mult", type=int, default=SERVE_SLOT_MULT, help="served stream: slot count multiplier")
+    ap.add_argument("--groups", default=SERVE_GROUPS, choices=("kind", "size", "class"),
+                    help="served stream: slots per batch context (one context and stream per group)")
     ap.add_argument("--no-error", action="store_true", help="skip the precision-form error block")
     ap.add_argument("--sweep", action="store_true",
                     help="served stream at each SERVE_SWEEP setting: throughput, latency and saturation per setting")
     ap.add_argument("--job-steps-scale", type=float, default=1.0,
                     help="scale the served jobs' step counts (small cases for launch lists)")
     a = ap.parse_args()
+    a.steps_auto = a.steps is None and a.workload not in ("serve", "ens256")
     if a.steps is None:
         a.steps = SERVE_WINDOW if a.workload == "serve" else 50
     if a.warmup is None:
@@ -1104,13 +1142,19 @@ def main():
     build.build()
     desc, cfg, make = workload(a.workload)
     cfg = cfg.replace(precision=a.precision, rebuild_policy=a.policy, threads_per_particle=a.tpp)
+    t0 = time.perf_counter()
     st = make()
+    host_setup = time.perf_counter() - t0
     n = len(st["tag"])
     ctx = capi.Context(cfg, n)
     ctx.upload(st)
     if a.eager:
         ctx.set_graph_mode(0)
     ctx.timed_steps(a.warmup, L2_FLUSH)
+    if a.steps_auto:
+        # long enough for the clock sampler (200 ms period) to see the region
+        probe = float(ctx.timed_steps(5, L2_FLUSH)[0][:, 0].mean())
+        a.steps = int(min(100000, max(a.steps, math.ceil(1500.0 / max(probe, 1e-3)))))
     if dist:
         dist.barrier()
     with ClockSampler(local) as clk:
@@ -1127,7 +1171,9 @@ def main():
     suffix = "mixed" if a.precision == "mixed" else "fp64"
     # the dominant per-particle kernel of the step: force, initial or final
     # integration (phases timed by CUDA events; rebuild steps averaged in)
-    cands = {("k_dem_" if kind == "dem" else "k_lj_") + suffix: (force_ms, force_bytes(kind, nfull_avg, contacts, a.precision)),
+    fname = {("dem", "mixed"): "k_dem_screen + k_dem_contact", ("dem", "fp64"): "k_dem_fp64",
+             ("lj", "mixed"): "k_lj_mixed", ("lj", "fp64"): "k_lj_fp64"}[(kind, a.precision)]
+    cands = {fname: (force_ms, force_bytes(kind, nfull_avg, contacts, a.precision)),
              ("k_initial_mixed" if a.precision == "mixed" else "k_initial"):
                  (float(t[:, 1].mean()), INIT_BYTES[(kind, a.precision)]),
              ("k_final_mixed" if a.precision == "mixed" else "k_final"):
@@ -1143,6 +1189,8 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64" if a.precision == "mixed" else "f64",
         "data": "synthetic",
         "config": {"workload": desc, "precision": a.precision, "rebuild_policy": a.policy, "particles": n,
+                   "steps_rule": ("timed steps chosen to last >= 1.5 s (clock sampling)" if a.steps_auto
+                                  else "as given"),
                    "l2": "flushed before every timed step (512 MB write)", "parallelism": f"replicas x{world}"},
         "phases_ms": {"initial": float(t[:, 1].mean()), "rebuild": float(t[:, 2].mean()), "force": force_ms,
                       "final": float(t[:, 4].mean())},
@@ -1154,6 +1202,8 @@ def main():
                      "kernels_ms": {q: v[0] for q, v in cands.items()}},
         "clocks": clk.summary(),
     }
+    if rank == 0:
+        line["setup"] = setup_times(a.workload, cfg, st, host_setup)
     if rank == 0 and a.precision == "mixed" and not a.no_error:
         line["error"] = workload_errors(a.workload, cfg, make, ctx)
     if rank == 0 and not a.no_e2e:
@@ -1165,6 +1215,33 @@ def main():
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def setup_times(name, cfg, st, host_s):
+    """Initial-condition set-up: the host generator the workload's inputs come
+    from (shared with the reference arm) beside the device generator making a
+    system of the same kind and size in a context (mdg_generate_fcc / _gas,
+    wall clock of the call)."""
+    from mddem_gb300 import capi, workloads as w
+
+    out = {"host_generator_s": host_s}
+    n = len(st["tag"])
+    c = capi.Context(cfg, n)
+    t0 = time.perf_counter()
+    if cfg.kind == "lj":
+        dens = n / float(cfg.box[0] * cfg.box[1] * cfg.box[2])
+        c.generate_fcc(dens, 0.85 if name != "lj500" else 1.0, seed=2024)
+        what = "FCC lattice with Gaussian velocities (mdg_generate_fcc)"
+    else:
+        rad = st["radius"]
+        poly = float(rad.min()) != float(rad.max())
+        c.generate_gas(n, w.POLY_R if poly else float(rad[0]), sep_factor=1.0 if poly else 1.1,
+                       velocity="maxwell_rms" if poly else "speed", speed=0.5, seed=2024)
+        what = "grid-parallel RSA and velocities (mdg_generate_gas)"
+    out["device_generator_s"] = time.perf_counter() - t0
+    out["device_generator"] = what
+    c.close()
+    return out
 
 
 def e2e(cfg, make, steps):

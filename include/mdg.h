@@ -390,6 +390,12 @@ typedef struct mdg_job_info {
 } mdg_job_info;
 int  mdg_server_create(const mdg_config* slot_cfgs, const size_t* slot_capacity, int nslots, size_t hbm_budget,
                        mdg_server** out);
+/* As mdg_server_create, with the slots placed by slot_group: the slots that
+ * share a group id (which must share a kind) make one batch context on its
+ * own stream, so e.g. small and large jobs of one kind can also run side by
+ * side.  mdg_server_create groups by kind. */
+int  mdg_server_create_grouped(const mdg_config* slot_cfgs, const size_t* slot_capacity, const int* slot_group,
+                               int nslots, size_t hbm_budget, mdg_server** out);
 void mdg_server_destroy(mdg_server* srv);
 int  mdg_server_submit(mdg_server* srv, const mdg_config* cfg, const mdg_state_view* st, int64_t steps, int64_t* id);
 int  mdg_server_pump(mdg_server* srv, int64_t max_steps, int* active, int* pending);
@@ -434,6 +440,65 @@ int  mdg_server_resident(mdg_server* srv, mdg_job_info* out, int cap, int* n);
 int  mdg_rsa_spheres(size_t n, const double box_lo[3], const double box_hi[3], double rmin, double rmax,
                      double sep_factor, int inset, uint64_t seed, uint64_t max_attempts, double* pos_out,
                      double* rad_out, size_t* placed);
+
+/* Generators on the device: they write system `sys` of a context directly
+ * (no host state, no host->device copy), then arm it like mdg_upload_state.
+ * Their random numbers are counter based -- mdg_counter_draw(seed, stream, i)
+ * is the 64-bit draw i of a stream, a uniform takes its top 53 bits, a normal
+ * comes from the Box-Muller transform of draws (2k, 2k+1) -- so the results do
+ * not depend on the launch shape and are the same on every GPU. */
+uint64_t mdg_counter_draw(uint64_t seed, uint32_t stream, uint64_t index);
+
+/* FCC lattice of an LJ system, restating fcc_insert
+ * (crates/md_lattice/src/lib.rs:232-454): lattice constant (4/density)^(1/3),
+ * cells per axis floor(L / a) (MDG_ERR_CONFIG when 0 on an axis), cells
+ * stretched to tile the box from box_lo, 4-atom basis in (ix, iy, iz, basis)
+ * order, tags 0..N-1; atom k takes the first type whose cumulative fraction
+ * exceeds (k + 0.5) / N (the last type past them); velocities N(0, sqrt(T/m))
+ * per component from draws 4k..4k+3 of stream 2, the plain mean removed,
+ * rescaled to exactly T with 3N - 3 degrees of freedom.  *n_out receives N
+ * (MDG_ERR_ARG when above the system's capacity). */
+#define MDG_GEN_MAX_TYPES 8
+typedef struct mdg_fcc_spec {
+    double density;          /* reduced number density rho */
+    double temperature;      /* T (reduced units) */
+    double mass;             /* atom mass (every type without its own) */
+    double skin;             /* cutoff_radius of every atom (the lattice skin) */
+    uint64_t seed;
+    int32_t n_types;         /* 0 or 1: every atom type 0 */
+    double type_fractions[MDG_GEN_MAX_TYPES];  /* cumulative thresholds */
+    double type_masses[MDG_GEN_MAX_TYPES];     /* > 0: that type's mass */
+} mdg_fcc_spec;
+int  mdg_generate_fcc(mdg_ctx* ctx, int sys, const mdg_fcc_spec* spec, size_t* n_out);
+
+/* Granular gas of a DEM system: the acceptance rule of insert.rs:523-571 over
+ * the proposal stream g = 0, 1, ... (centre uniform in the box of the system's
+ * config, inset by rmax when `inset`, from draws 4g..4g+2 of stream 1; radius
+ * rmin + (rmax - rmin) u from draw 4g+3), placed by a grid-parallel random
+ * sequential addition whose result equals the sequential one on that stream;
+ * tags in acceptance order.  Velocities by velocity_mode from stream 2:
+ * MDG_VEL_SPEED |v| = speed in an isotropic direction (z = 1 - 2 u_{4k},
+ * azimuth 2 pi u_{4k+1}); MDG_VEL_MAXWELL_RMS Gaussian components of sigma
+ * speed / sqrt(3); MDG_VEL_GAUSSIAN sigma = speed per component (the
+ * reference's `velocity`, insert.rs:580-592).  omega 0, identity quaternions,
+ * mass density 4/3 pi r^3 and 1 / (0.4 m r^2) as insert.rs:343-349,
+ * cutoff_radius = r, type = material.  *placed receives the spheres placed;
+ * MDG_ERR_ARG (and nothing written) when fewer than n fit within
+ * max_proposals (0 = 20000 n). */
+enum { MDG_VEL_SPEED = 0, MDG_VEL_MAXWELL_RMS = 1, MDG_VEL_GAUSSIAN = 2 };
+typedef struct mdg_gas_spec {
+    size_t n;
+    double rmin, rmax;       /* radius uniform in [rmin, rmax] */
+    double density;          /* kg/m^3 */
+    double sep_factor;       /* rejection distance sep_factor (r_i + r_j); the reference uses 1.1 */
+    int32_t inset;
+    int32_t velocity_mode;   /* MDG_VEL_* */
+    double speed;
+    uint32_t material;
+    uint64_t seed;
+    uint64_t max_proposals;
+} mdg_gas_spec;
+int  mdg_generate_gas(mdg_ctx* ctx, int sys, const mdg_gas_spec* spec, size_t* placed);
 
 #ifdef __cplusplus
 }

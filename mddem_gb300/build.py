@@ -37,6 +37,7 @@ UNITS = [
     ("mdg_api.cu", ["-fmad=false"]),
     ("mdg_noalloc.cu", ["-fmad=false"]),
     ("mdg_measure.cu", ["-fmad=false"]),
+    ("mdg_generate.cu", ["-fmad=false"]),
     ("mdg_serve.cpp", []),
     ("mdg_insert.cpp", []),
     ("mdg_tune.cpp", []),

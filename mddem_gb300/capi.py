@@ -30,10 +30,10 @@ EXPORTS = [
     "mdg_num_systems", "mdg_upload_state", "mdg_download_state", "mdg_set_history", "mdg_get_history",
     "mdg_step", "mdg_step_async", "mdg_step_wait", "mdg_force_only", "mdg_get_pairs", "mdg_thermo", "mdg_synchronize", "mdg_kernel_launches",
     "mdg_set_graph_mode", "mdg_timed_steps", "mdg_granular_temp_noalloc", "mdg_set_remaining",
-    "mdg_get_remaining", "mdg_get_status", "mdg_configure_system", "mdg_server_create", "mdg_server_destroy",
+    "mdg_get_remaining", "mdg_get_status", "mdg_configure_system", "mdg_server_create", "mdg_server_create_grouped", "mdg_server_destroy",
     "mdg_server_submit", "mdg_server_pump", "mdg_server_poll", "mdg_server_fetch", "mdg_server_context",
     "mdg_server_slot_context",
-    "mdg_rsa_spheres", "mdg_get_progress", "mdg_get_stream", "mdg_server_stats",
+    "mdg_rsa_spheres", "mdg_counter_draw", "mdg_generate_fcc", "mdg_generate_gas", "mdg_get_progress", "mdg_get_stream", "mdg_server_stats",
     "mdg_server_resident", "mdg_get_config", "mdg_set_threads_per_particle", "mdg_get_threads_per_particle",
     "mdg_set_build_mode", "mdg_autotune", "mdg_rdf", "mdg_msd_reset", "mdg_msd",
 ]
@@ -115,6 +115,23 @@ class ServerStats(C.Structure):
                 ("launches", C.c_int64), ("contexts", C.c_int32)]
 
 
+GEN_MAX_TYPES = 8
+VEL_MODES = {"speed": 0, "maxwell_rms": 1, "gaussian": 2}
+
+
+class FccSpec(C.Structure):
+    _fields_ = [("density", C.c_double), ("temperature", C.c_double), ("mass", C.c_double), ("skin", C.c_double),
+                ("seed", C.c_uint64), ("n_types", C.c_int32), ("type_fractions", C.c_double * GEN_MAX_TYPES),
+                ("type_masses", C.c_double * GEN_MAX_TYPES)]
+
+
+class GasSpec(C.Structure):
+    _fields_ = [("n", C.c_size_t), ("rmin", C.c_double), ("rmax", C.c_double), ("density", C.c_double),
+                ("sep_factor", C.c_double), ("inset", C.c_int32), ("velocity_mode", C.c_int32),
+                ("speed", C.c_double), ("material", C.c_uint32), ("seed", C.c_uint64),
+                ("max_proposals", C.c_uint64)]
+
+
 class TuneOpts(C.Structure):
     _fields_ = [("steps", C.c_int), ("tune_tpp", C.c_int), ("tune_skin", C.c_int), ("tune_bin", C.c_int)]
 
@@ -170,6 +187,8 @@ def load(path: str = LIB_PATH):
     lib.mdg_configure_system.argtypes = [C.c_void_p, C.c_int, C.POINTER(Config)]
     lib.mdg_server_create.argtypes = [C.POINTER(Config), C.POINTER(C.c_size_t), C.c_int, C.c_size_t,
                                       C.POINTER(C.c_void_p)]
+    lib.mdg_server_create_grouped.argtypes = [C.POINTER(Config), C.POINTER(C.c_size_t), C.POINTER(C.c_int), C.c_int,
+                                              C.c_size_t, C.POINTER(C.c_void_p)]
     lib.mdg_server_destroy.argtypes = [C.c_void_p]
     lib.mdg_server_destroy.restype = None
     lib.mdg_server_submit.argtypes = [C.c_void_p, C.POINTER(Config), C.POINTER(StateView), C.c_int64,
@@ -195,6 +214,10 @@ def load(path: str = LIB_PATH):
     lib.mdg_rsa_spheres.argtypes = [C.c_size_t, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double,
                                     C.c_double, C.c_double, C.c_int, C.c_uint64, C.c_uint64,
                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_size_t)]
+    lib.mdg_counter_draw.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64]
+    lib.mdg_counter_draw.restype = C.c_uint64
+    lib.mdg_generate_fcc.argtypes = [C.c_void_p, C.c_int, C.POINTER(FccSpec), C.POINTER(C.c_size_t)]
+    lib.mdg_generate_gas.argtypes = [C.c_void_p, C.c_int, C.POINTER(GasSpec), C.POINTER(C.c_size_t)]
     lib.mdg_granular_temp_noalloc.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]
     _lib = lib
     return lib
@@ -321,12 +344,19 @@ def rsa_spheres(n, box_lo, box_hi, rmin, rmax, sep_factor=1.1, inset=True, seed=
     return pos, rad
 
 
+def counter_draw(seed, stream, index):
+    """mdg_counter_draw: draw `index` of the generators' counter-based stream."""
+    return int(load().mdg_counter_draw(int(seed), int(stream), int(index)))
+
+
 class Server:
     """Continuous-batching server (mdg_server_*): typed slots, HBM-budget
     admission, one multi-step device launch per pump, retirement of finished
     jobs."""
 
-    def __init__(self, slot_configs, slot_capacities, hbm_budget):
+    def __init__(self, slot_configs, slot_capacities, hbm_budget, groups=None):
+        """``groups``: per-slot group ids (slots of one group, one kind,
+        share a batch context and stream); default one group per kind."""
         self.lib = load()
         n = len(slot_configs)
         arr = (Config * n)()
@@ -337,7 +367,12 @@ class Server:
             self._keep.append(mats)
         caps = (C.c_size_t * n)(*[int(x) for x in slot_capacities])
         h = C.c_void_p()
-        _check(self.lib.mdg_server_create(arr, caps, n, int(hbm_budget), C.byref(h)), "mdg_server_create")
+        if groups is None:
+            _check(self.lib.mdg_server_create(arr, caps, n, int(hbm_budget), C.byref(h)), "mdg_server_create")
+        else:
+            g = (C.c_int * n)(*[int(x) for x in groups])
+            _check(self.lib.mdg_server_create_grouped(arr, caps, g, n, int(hbm_budget), C.byref(h)),
+                   "mdg_server_create_grouped")
         self.h = h
         self.nslots = n
         self.slot_configs = list(slot_configs)
@@ -494,6 +529,39 @@ class Context:
         self.close()
 
     # -- state -------------------------------------------------------------------
+    def generate_fcc(self, density, temperature, mass=1.0, skin=1.25, seed=0, sys=0, type_fractions=None,
+                     type_masses=None):
+        """mdg_generate_fcc: the FCC lattice of fcc_insert made on the device
+        in system `sys` (cells per axis from the config's box); returns N."""
+        f = FccSpec(density=float(density), temperature=float(temperature), mass=float(mass), skin=float(skin),
+                    seed=int(seed))
+        fr = list(type_fractions or [])
+        f.n_types = len(fr)
+        for k, v in enumerate(fr):
+            f.type_fractions[k] = float(v)
+        for k, v in enumerate(type_masses or []):
+            f.type_masses[k] = float(v)
+        n = C.c_size_t()
+        _check(self.lib.mdg_generate_fcc(self.h, sys, C.byref(f), C.byref(n)), "mdg_generate_fcc")
+        self.n[sys] = n.value
+        return n.value
+
+    def generate_gas(self, n, radius, density=2500.0, sep_factor=1.1, inset=True, velocity="speed", speed=0.5,
+                     material=0, seed=0, max_proposals=0, sys=0):
+        """mdg_generate_gas: the granular gas of the grid-parallel RSA made on
+        the device in system `sys`; ``radius`` r or (rmin, rmax); ``velocity``
+        "speed", "maxwell_rms" or "gaussian".  Returns the spheres placed."""
+        rmin, rmax = (radius, radius) if not isinstance(radius, (tuple, list)) else radius
+        g = GasSpec(n=int(n), rmin=float(rmin), rmax=float(rmax), density=float(density),
+                    sep_factor=float(sep_factor), inset=int(bool(inset)), velocity_mode=VEL_MODES[velocity],
+                    speed=float(speed), material=int(material), seed=int(seed), max_proposals=int(max_proposals))
+        placed = C.c_size_t()
+        st = self.lib.mdg_generate_gas(self.h, sys, C.byref(g), C.byref(placed))
+        if st != MDG_OK:
+            raise MdgError(st, f"mdg_generate_gas placed {placed.value}/{n}")
+        self.n[sys] = int(n)
+        return placed.value
+
     def upload(self, state, sys=0):
         n = len(state["tag"])
         keep = {k: np.ascontiguousarray(v) for k, v in state.items() if isinstance(v, np.ndarray)}

@@ -366,12 +366,7 @@ int auto_build_mode(const SysParams& p, size_t n) {
     return 1;
 }
 
-int setup_grid(const mdg_config& c, const double* cutr, size_t n, SysParams& p) {
-    double max_skin = 0.0, min_skin = std::numeric_limits<double>::max();
-    for (size_t i = 0; i < n; i++) {
-        max_skin = std::fmax(max_skin, cutr[i]);
-        min_skin = std::fmin(min_skin, cutr[i]);
-    }
+int setup_grid(const mdg_config& c, double min_skin, double max_skin, size_t n, SysParams& p) {
     const double sf = c.skin_fraction;
     double bin_min = c.bin_size;
     const double max_cutoff = max_skin > 0.0 ? 2.0 * max_skin * sf : bin_min;
@@ -1089,6 +1084,54 @@ void mdg_destroy(mdg_ctx* c) { delete c; }
 
 int mdg_num_systems(const mdg_ctx* c) { return c ? c->nsys : 0; }
 
+// Grid, list capacity and thermostat of system `sys` for n particles whose
+// list cutoff radii span [min_cut, max_cut], then the context's layout; the
+// particle arrays are written next (from the host or by a generator) and
+// finish_upload arms the first step.
+static int prepare_system(mdg_ctx* c, int sys, size_t n, double min_cut, double max_cut) {
+    const mdg_config& k = c->cfg[sys];
+    SysParams& p = c->sp[sys];
+    int r = setup_grid(k, min_cut, max_cut, n, p);
+    if (r) return r;
+    if (c->build_mode >= 0) p.build_mode = c->build_mode;
+    p.n = (int)n;
+    p.nb = (int)((n + BLK - 1) / BLK);
+    c->maps_dirty = true;
+    p.ncap = auto_ncap(k, p, n);
+    if (k.nose_hoover) {
+        // setup_nose_hoover (crates/md_thermostat/src/lib.rs:195-243)
+        p.nh = 1;
+        p.nh_ndof = 3.0 * (double)n - 3.0;
+        p.nh_T = k.nh_temperature;
+        p.nh_Q = p.nh_ndof * p.nh_T * k.nh_coupling * k.nh_coupling;
+    } else {
+        p.nh = 0;
+    }
+    return ensure_layout(c, sys);
+}
+
+// The first step of a freshly written system performs a full rebuild
+// (CommState::FullRebuild); the kinetic energies of every system are
+// refreshed.
+static int finish_upload(mdg_ctx* c, int sys) {
+    Dev& d = c->d;
+    cudaStream_t s0 = c->stream;
+    SysState ss{};
+    ss.rebuild = 1;
+    ss.remaining = -1;
+    cudaMemcpyAsync(d.ss + sys, &ss, sizeof(SysState), cudaMemcpyHostToDevice, s0);
+    cudaError_t e = cudaStreamSynchronize(s0);
+    if (e != cudaSuccess) return cuda_err(e);
+    c->launches += launch_ke_init(d, s0);
+    e = cudaStreamSynchronize(s0);
+    if (e != cudaSuccess) return cuda_err(e);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(e);
+    c->uploaded[sys] = 1;
+    c->rem_host[sys] = -1;
+    return MDG_OK;
+}
+
 int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
     if (!c || !st || sys < 0 || sys >= c->nsys) return MDG_ERR_ARG;
     const mdg_config& k = c->cfg[sys];
@@ -1106,24 +1149,12 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
         if (k.kind == MDG_KIND_LJ && c->ljn[sys] > 1 && (!st->type || st->type[i] >= (uint32_t)c->ljn[sys]))
             return MDG_ERR_ARG;
     }
-    int r = setup_grid(k, st->cutoff_radius, n, p);
-    if (r) return r;
-    if (c->build_mode >= 0) p.build_mode = c->build_mode;
-    p.n = (int)n;
-    p.nb = (int)((n + BLK - 1) / BLK);
-    c->maps_dirty = true;
-    const int ncap = auto_ncap(k, p, n);
-    p.ncap = ncap;
-    if (k.nose_hoover) {
-        // setup_nose_hoover (crates/md_thermostat/src/lib.rs:195-243)
-        p.nh = 1;
-        p.nh_ndof = 3.0 * (double)n - 3.0;
-        p.nh_T = k.nh_temperature;
-        p.nh_Q = p.nh_ndof * p.nh_T * k.nh_coupling * k.nh_coupling;
-    } else {
-        p.nh = 0;
+    double min_cut = std::numeric_limits<double>::max(), max_cut = 0.0;
+    for (size_t i = 0; i < n; i++) {
+        max_cut = std::fmax(max_cut, st->cutoff_radius[i]);
+        min_cut = std::fmin(min_cut, st->cutoff_radius[i]);
     }
-    r = ensure_layout(c, sys);
+    int r = prepare_system(c, sys, n, min_cut, max_cut);
     if (r) return r;
     const size_t np = (size_t)p.npad;
     std::vector<double4> pos(np), vel(np), zero4(np), frc(np), trq, omg, quat;
@@ -1180,20 +1211,86 @@ int mdg_upload_state(mdg_ctx* c, int sys, const mdg_state_view* st) {
         cudaMemcpyAsync(d.quat + o, quat.data(), np * sizeof(double4), cudaMemcpyHostToDevice, s0);
         for (int b = 0; b < 2; b++) cudaMemcpyAsync(d.hcnt[b] + o, zi.data(), np * sizeof(int), cudaMemcpyHostToDevice, s0);
     }
-    SysState ss{};
-    ss.rebuild = 1;  // the first step performs a full rebuild (CommState::FullRebuild)
-    ss.remaining = -1;
-    cudaMemcpyAsync(d.ss + sys, &ss, sizeof(SysState), cudaMemcpyHostToDevice, s0);
-    cudaError_t e = cudaStreamSynchronize(s0);
-    if (e != cudaSuccess) return cuda_err(e);
-    c->launches += launch_ke_init(d, s0);
-    e = cudaStreamSynchronize(s0);
-    if (e != cudaSuccess) return cuda_err(e);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_err(e);
-    c->uploaded[sys] = 1;
-    c->rem_host[sys] = -1;
-    return MDG_OK;
+    return finish_upload(c, sys);
+}
+
+int mdg_generate_fcc(mdg_ctx* c, int sys, const mdg_fcc_spec* f, size_t* n_out) {
+    if (!c || !f || sys < 0 || sys >= c->nsys) return MDG_ERR_ARG;
+    if (n_out) *n_out = 0;
+    const mdg_config& k = c->cfg[sys];
+    if (k.kind != MDG_KIND_LJ) return MDG_ERR_CONFIG;
+    // fcc_insert's checks (md_lattice/src/lib.rs:257-269, 395-405)
+    if (!(f->density > 0.0) || !std::isfinite(f->density) || !(f->temperature >= 0.0) ||
+        !std::isfinite(f->temperature) || !(f->mass > 0.0) || !(f->skin > 0.0) || f->n_types < 0 ||
+        f->n_types > MDG_GEN_MAX_TYPES)
+        return MDG_ERR_CONFIG;
+    FccArgs a{};
+    const double a_ideal = std::cbrt(4.0 / f->density);
+    long long n = 4;
+    for (int d = 0; d < 3; d++) {
+        const double L = k.box_hi[d] - k.box_lo[d];
+        const double cells = std::floor(L / a_ideal);
+        if (!(cells >= 1.0) || cells > 4096.0) return MDG_ERR_CONFIG;
+        a.nc[d] = (int)cells;
+        a.a[d] = L / cells;
+        a.lo[d] = k.box_lo[d];
+        n *= a.nc[d];
+    }
+    if ((size_t)n > c->capacity[sys]) return MDG_ERR_ARG;
+    a.temperature = f->temperature;
+    a.skin = f->skin;
+    a.seed = f->seed;
+    a.ntypes = f->n_types > 1 ? f->n_types : 1;
+    for (int t = 0; t < a.ntypes; t++) {
+        a.frac[t] = f->n_types > 1 ? f->type_fractions[t] : 1.0;
+        a.tmass[t] = f->type_masses[t] > 0.0 && f->n_types > 1 ? f->type_masses[t] : f->mass;
+    }
+    // multi-type LJ: the type indexes the pair table
+    if (c->ljn[sys] > 1 ? a.ntypes > c->ljn[sys] : a.ntypes > 1) return MDG_ERR_ARG;
+    int r = prepare_system(c, sys, (size_t)n, f->skin, f->skin);
+    if (r) return r;
+    r = gen_fcc(c->d, c->sp[sys], a, c->stream, &c->launches);
+    if (r) return r;
+    if (n_out) *n_out = (size_t)n;
+    return finish_upload(c, sys);
+}
+
+int mdg_generate_gas(mdg_ctx* c, int sys, const mdg_gas_spec* g, size_t* placed) {
+    if (!c || !g || sys < 0 || sys >= c->nsys) return MDG_ERR_ARG;
+    if (placed) *placed = 0;
+    const mdg_config& k = c->cfg[sys];
+    if (k.kind != MDG_KIND_DEM) return MDG_ERR_CONFIG;
+    if (g->n < 1 || g->n > c->capacity[sys]) return MDG_ERR_ARG;
+    if (!(g->rmin > 0.0) || !(g->rmax >= g->rmin) || !std::isfinite(g->rmax) || !(g->sep_factor > 0.0) ||
+        !(g->density > 0.0) || !(g->speed >= 0.0) || !std::isfinite(g->speed) ||
+        g->velocity_mode < MDG_VEL_SPEED || g->velocity_mode > MDG_VEL_GAUSSIAN ||
+        (int)g->material >= k.n_materials)
+        return MDG_ERR_ARG;
+    GasArgs a{};
+    a.n = (long long)g->n;
+    a.rmin = g->rmin;
+    a.rmax = g->rmax;
+    a.density = g->density;
+    a.sep = g->sep_factor;
+    a.inset = g->inset ? 1 : 0;
+    a.vel_mode = g->velocity_mode;
+    a.speed = g->speed;
+    a.material = g->material;
+    a.seed = g->seed;
+    a.max_proposals = g->max_proposals;
+    GasPlacement gp;
+    int r = gen_gas_place(a, k.box_lo, k.box_hi, c->stream, &gp, &c->launches);
+    if (placed) *placed = gp.count;
+    if (r) {
+        gp.release(c->stream);
+        cudaStreamSynchronize(c->stream);
+        return r;
+    }
+    r = prepare_system(c, sys, g->n, gp.rmin, gp.rmax);
+    if (!r) r = gen_gas_write(c->d, c->sp[sys], a, gp, c->stream, &c->launches);
+    gp.release(c->stream);
+    if (r) return r;
+    return finish_upload(c, sys);
 }
 
 int mdg_download_state(mdg_ctx* c, int sys, mdg_state_view* st) {

@@ -604,4 +604,39 @@ int launch_ke_init(const Dev& d, cudaStream_t st);
 int launch_thermo(const Dev& d, double* out, cudaStream_t st);
 // history injection/extraction helpers run on the host side of the API
 
+// ---- seeded initial conditions on the device (mdg_generate.cu)
+constexpr int GEN_MAX_TYPES = 8;
+struct FccArgs {
+    int nc[3];
+    double lo[3], a[3];
+    double temperature, skin;
+    uint64_t seed;
+    int ntypes;
+    double frac[GEN_MAX_TYPES];   // cumulative type thresholds
+    double tmass[GEN_MAX_TYPES];  // mass of each type (index 0 for a single type)
+};
+struct GasArgs {
+    long long n;
+    double rmin, rmax, density, sep;
+    int inset, vel_mode;
+    double speed;
+    uint32_t material;
+    uint64_t seed, max_proposals;
+};
+struct GasPlacement {
+    double4* placed = nullptr;  // (x, y, z, r) in acceptance order
+    size_t count = 0;
+    uint64_t proposals = 0;
+    double rmin = 0.0, rmax = 0.0;  // of the placed radii
+    void release(cudaStream_t s);
+};
+// FCC lattice into system segment p (p.n atoms); velocities fixed to T
+int gen_fcc(const Dev& d, const SysParams& p, const FccArgs& f, cudaStream_t s, long long* launches);
+// parallel RSA into scratch (MDG_ERR_ARG when fewer than n fit in the proposal budget)
+int gen_gas_place(const GasArgs& a, const double box_lo[3], const double box_hi[3], cudaStream_t s,
+                  GasPlacement* out, long long* launches);
+// placed spheres and their velocities into system segment p
+int gen_gas_write(const Dev& d, const SysParams& p, const GasArgs& a, const GasPlacement& gp, cudaStream_t s,
+                  long long* launches);
+
 }  // namespace mdg

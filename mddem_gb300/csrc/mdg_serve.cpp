@@ -1,7 +1,8 @@
 // mdg_serve.cpp -- continuous-batching server for independent simulation jobs.
 //
 // The server's slots (typed by kind, sized by particle capacity) live in one
-// batch context per particle kind, each with its own CUDA stream.  Jobs are
+// batch context per slot group (default: per particle kind), each with its
+// own CUDA stream.  Jobs are
 // submitted with their config, initial state and step count; pump() admits
 // queued jobs into free slots while the estimated device footprint of the
 // resident jobs stays within the HBM budget, advances every resident job with
@@ -142,27 +143,33 @@ struct mdg_server {
 
 extern "C" {
 
-int mdg_server_create(const mdg_config* slot_cfgs, const size_t* slot_capacity, int nslots, size_t hbm_budget,
-                      mdg_server** out) {
-    if (!slot_cfgs || !slot_capacity || nslots < 1 || !out) return MDG_ERR_ARG;
+int mdg_server_create_grouped(const mdg_config* slot_cfgs, const size_t* slot_capacity, const int* slot_group,
+                              int nslots, size_t hbm_budget, mdg_server** out) {
+    if (!slot_cfgs || !slot_capacity || !slot_group || nslots < 1 || !out) return MDG_ERR_ARG;
     *out = nullptr;
+    for (int k = 0; k < nslots; k++) {
+        if (slot_cfgs[k].kind != MDG_KIND_DEM && slot_cfgs[k].kind != MDG_KIND_LJ) return MDG_ERR_CONFIG;
+        for (int q = 0; q < k; q++)  // a group holds one kind
+            if (slot_group[q] == slot_group[k] && slot_cfgs[q].kind != slot_cfgs[k].kind) return MDG_ERR_CONFIG;
+    }
     auto* s = new (std::nothrow) mdg_server();
     if (!s) return MDG_ERR_OOM;
     s->nslots = nslots;
     s->slot_ctx.assign(nslots, -1);
     s->slot_sys.assign(nslots, -1);
-    // the slots of each kind, in order, make one batch context
-    for (int kind : {MDG_KIND_DEM, MDG_KIND_LJ}) {
+    // the slots of each group, in slot order, make one batch context; groups
+    // in order of their first slot
+    for (int k0 = 0; k0 < nslots; k0++) {
+        if (s->slot_ctx[k0] >= 0) continue;
         std::vector<mdg_config> cfgs;
         std::vector<size_t> caps;
         std::vector<int> ids;
-        for (int k = 0; k < nslots; k++)
-            if (slot_cfgs[k].kind == kind) {
+        for (int k = k0; k < nslots; k++)
+            if (slot_group[k] == slot_group[k0]) {
                 cfgs.push_back(slot_cfgs[k]);
                 caps.push_back(slot_capacity[k]);
                 ids.push_back(k);
             }
-        if (cfgs.empty()) continue;
         mdg_ctx* ctx = nullptr;
         const int r = mdg_batch_create(cfgs.data(), caps.data(), (int)cfgs.size(), &ctx);
         if (r) {
@@ -178,11 +185,6 @@ int mdg_server_create(const mdg_config* slot_cfgs, const size_t* slot_capacity, 
         s->ctxs.push_back(ctx);
     }
     for (int k = 0; k < nslots; k++) {
-        if (s->slot_ctx[k] < 0) {  // a kind other than DEM and LJ
-            for (mdg_ctx* c : s->ctxs) mdg_destroy(c);
-            delete s;
-            return MDG_ERR_CONFIG;
-        }
         s->slot_kind.push_back(slot_cfgs[k].kind);
         s->slot_cap.push_back(slot_capacity[k]);
         s->slot_job.push_back(-1);
@@ -190,6 +192,14 @@ int mdg_server_create(const mdg_config* slot_cfgs, const size_t* slot_capacity, 
     s->budget = hbm_budget;
     *out = s;
     return MDG_OK;
+}
+
+int mdg_server_create(const mdg_config* slot_cfgs, const size_t* slot_capacity, int nslots, size_t hbm_budget,
+                      mdg_server** out) {
+    if (!slot_cfgs || nslots < 1) return MDG_ERR_ARG;
+    std::vector<int> group(nslots);
+    for (int k = 0; k < nslots; k++) group[k] = slot_cfgs[k].kind;  // one context per particle kind
+    return mdg_server_create_grouped(slot_cfgs, slot_capacity, group.data(), nslots, hbm_budget, out);
 }
 
 void mdg_server_destroy(mdg_server* s) {

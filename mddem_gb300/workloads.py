@@ -156,6 +156,25 @@ SERVE_DEM_SLOTS = [(128, 32), (1024, 24), (8192, 16), (65536, 12), (200000, 8)]
 SERVE_LJ_SLOTS = [(2048, 8), (16384, 8), (100000, 6)]
 
 
+def serve_groups(cfgs, caps, policy="kind", small=1024):
+    """Per-slot group ids for capi.Server(groups=...): "kind" one batch
+    context per particle kind; "size" the slots of capacity <= `small` apart
+    from the larger ones of their kind; "class" one context per (kind,
+    capacity)."""
+    keys = []
+    for c, cap in zip(cfgs, caps):
+        if policy == "kind":
+            keys.append(c.kind)
+        elif policy == "size":
+            keys.append((c.kind, cap <= small))
+        elif policy == "class":
+            keys.append((c.kind, cap))
+        else:
+            raise ValueError(f"unknown grouping {policy}")
+    ids = {}
+    return [ids.setdefault(k, len(ids)) for k in keys]
+
+
 def serve_slots(precision="mixed", policy="displacement", mult=1):
     """(slot configs, slot capacities) for a job server over serve_trace;
     `mult` times the slot counts of SERVE_DEM_SLOTS / SERVE_LJ_SLOTS."""
