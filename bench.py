@@ -512,7 +512,29 @@ def plain_job_by_job(trace, made):
 # fp64: build-time x) (+ DEM: omega, torque, quaternion) read, v, x (+ the
 # geometry copy) (+ omega, quaternion) written.  k_final: f, v, m, x (+ omega,
 # torque) read, v (+ omega) written.
-INIT_BYTES = {("dem", "mixed"): 416, ("dem", "fp64"): 352, ("lj", "mixed"): 192, ("lj", "fp64"): 192}
+INIT_BYTES = {("dem", "mixed"): 352, ("dem", "fp64"): 352, ("lj", "mixed"): 192, ("lj", "fp64"): 192}
+
+
+def init_bytes(kind, prec, spinning=1.0):
+    """k_initial / k_initial_mixed per particle: v, f, x read and v, x written;
+    DEM adds omega and the torque read, omega written and the quaternion read
+    and written; the mixed kernels also read and write the geometry copy and
+    read its build copy.  The mixed DEM kernel leaves the quaternion of a
+    sphere that has never spun (omega = 0: nothing to rotate) untouched, so its
+    64 B count only for the `spinning` fraction."""
+    b = INIT_BYTES[(kind, prec)]
+    if (kind, prec) == ("dem", "mixed"):
+        b += 64 * spinning
+    return b
+
+
+def spinning_fraction(states):
+    """Share of DEM particles with nonzero angular velocity over `states`."""
+    import numpy as np
+
+    n = sum(len(st["tag"]) for st in states)
+    k = sum(int(np.count_nonzero(np.any(st["omega"] != 0.0, axis=1))) for st in states)
+    return k / max(1, n)
 FINAL_BYTES = {"dem": 232, "lj": 136}
 
 
@@ -544,17 +566,22 @@ def force_bytes(kind, nfull, contacts, prec="fp64"):
 def serve_mix(srv, trace, sid):
     """Particles, mean full-list row length and stored contacts per particle
     of the jobs resident now, by kind."""
+    import numpy as np
+
     per = {}
     for r in srv.resident():
         kind = "lj" if trace[sid[r["id"]]].kind == "lj" else "dem"
-        p = per.setdefault(kind, dict(n=0, pairs=0, contacts=0, jobs=0))
+        p = per.setdefault(kind, dict(n=0, pairs=0, contacts=0, jobs=0, spin=0))
         p["n"] += int(r["n"])
         p["jobs"] += 1
         p["pairs"] += len(srv.pairs_resident(r["slot"]))
         if kind == "dem":
             p["contacts"] += len(srv.history_resident(r["slot"])[0])
+            w = srv.download_resident(r["slot"])["omega"]
+            p["spin"] += int(np.count_nonzero(np.any(w != 0.0, axis=1)))
     return {k: dict(particles=p["n"], jobs=p["jobs"], avg_full_neighbors=2.0 * p["pairs"] / max(1, p["n"]),
-                    contacts_per_particle=p["contacts"] / max(1, p["n"])) for k, p in per.items()}
+                    contacts_per_particle=p["contacts"] / max(1, p["n"]),
+                    spinning_fraction=p["spin"] / max(1, p["n"])) for k, p in per.items()}
 
 
 def serve_samples(srv, trace, made, sid, per_kind=(("gas", 3), ("lj", 2), ("rebound", 1))):
@@ -632,7 +659,7 @@ def physics_errors():
 
 
 # run lengths of the workloads' own error statements (the configs' run lengths)
-LJ_RDF_STEPS = 100000
+LJ_RDF_STEPS = 100000       # 864 atoms; 10000 from 10^4 atoms on (a large melt's g(r) converges sooner)
 LJ_RDF_FRAMES = 20
 COOL_STEPS = {"dem500": 10000, "gas200k": 20000, "gas138k": 20000, "poly1m": 20000}
 
@@ -693,7 +720,7 @@ def workload_errors(name, cfg, make, ctx, sys_=None):
         out["lj_energy_drift"] = {"mixed_per_step_per_atom": slopes["mixed"], "fp64_per_step_per_atom": slopes["fp64"],
                                   "ratio": abs(slopes["mixed"]) / max(abs(slopes["fp64"]), 1e-300), "bound": 2.0,
                                   "steps": 2000, "ensemble": "NVE (thermostat off)"}
-        out["rdf"] = lj_structure(cfg, st)
+        out["rdf"] = lj_structure(cfg, st, steps=LJ_RDF_STEPS if n < 10000 else 10000)
     elif name in COOL_STEPS:
         steps = COOL_STEPS[name]
         res = {}
@@ -779,7 +806,7 @@ def serve_roofline(a, phases, mix, served_rate):
     reported, plus the whole step's bytes per particle-step times the
     window's served rate."""
     prec = a.precision
-    init_b = sum(m["particles"] * INIT_BYTES[(k, prec)] for k, m in mix.items())
+    init_b = sum(m["particles"] * init_bytes(k, prec, m.get("spinning_fraction", 1.0)) for k, m in mix.items())
     fin_b = sum(m["particles"] * FINAL_BYTES[k] for k, m in mix.items())
     force_b = sum(m["particles"] * force_bytes(k, m["avg_full_neighbors"], m["contacts_per_particle"], prec)
                   for k, m in mix.items())
@@ -794,11 +821,17 @@ def serve_roofline(a, phases, mix, served_rate):
     kernel = {"initial": f"k_initial_{prec}", "final": f"k_final_{prec}",
               "rebuild": "rebuild pipeline (bin sort, permutation, k_build)",
               "force": ("k_dem_screen + k_dem_contact + k_lj_mixed" if prec == "mixed" else "k_dem_fp64 + k_lj_fp64")}[name]
-    step_b = init_b + fin_b + force_b
+    step_b = init_b + fin_b + force_b + (rb_b or 0.0)
     bpps = step_b / sum(m["particles"] for m in mix.values())
+    traffic = ncu_traffic(name + "/serve")
+    per = ncu_traffic("rebuild_per_particle")
+    if name == "rebuild" and per:
+        # the pipeline's measured DRAM bytes per rebuilt particle (LJ 256k, gas
+        # 200k) times the particles the mix rebuilt per step
+        traffic = sum(v * per[k] for k, v in phases.get("rebuilt_particles_per_step", {}).items() if k in per)
     out = {"bound": "hbm", "kernel": kernel, "phase": name, "share": ms / phases["step_ms"],
            "achieved": nbytes / (ms / 1e3) / 1e9 if nbytes else None, "peak": peak, "unit": "GB/s",
-           "peak_source": src, "traffic": ncu_traffic(name + "/serve"), "algorithmic_bytes_per_launch": nbytes,
+           "peak_source": src, "traffic": traffic, "algorithmic_bytes_per_launch": nbytes,
            "launch_ms": ms,
            "phases": {q: {"ms": v[0], "share": v[0] / phases["step_ms"],
                           "algorithmic_bytes": v[1],
@@ -806,8 +839,8 @@ def serve_roofline(a, phases, mix, served_rate):
                       for q, v in cands.items()},
            "whole_step": {"bytes_per_particle_step": bpps, "served_particle_steps_per_s": served_rate,
                           "achieved": bpps * served_rate / 1e9, "frac": bpps * served_rate / 1e9 / peak,
-                          "note": "the mix's algorithmic bytes per particle-step (integrators + force) x the "
-                                  "window's served rate, over the measured copy peak"},
+                          "note": "the mix's algorithmic bytes per particle-step (integrators, force and the "
+                                  "rebuilds it made) x the window's served rate, over the measured copy peak"},
            "attribution": phases, "mix": mix}
     out["frac"] = out["achieved"] / peak if out["achieved"] else None
     return out
@@ -1009,17 +1042,20 @@ def bench_ensemble(a, world, rank, local, dist):
         ctx.set_graph_mode(0 if a.eager else 1)
         contacts = sum(len(ctx.history(q)[0]) for q in range(len(sts))) / n
         nfull = sum(2.0 * len(ctx.pairs(q)) for q in range(len(sts))) / n
-        cands = {"k_initial": (float(t[:, 1].mean()), n * INIT_BYTES[("dem", a.precision)]),
+        spin = spinning_fraction([ctx.download(q) for q in range(len(sts))])
+        cands = {("k_initial_mixed" if a.precision == "mixed" else "k_initial"):
+                     (float(t[:, 1].mean()), n * init_bytes("dem", a.precision, spin)),
                  ("k_dem_screen + k_dem_contact" if a.precision == "mixed" else "k_dem_fp64"):
                      (float(t[:, 3].mean()), n * force_bytes("dem", nfull, contacts, a.precision)),
-                 "k_final": (float(t[:, 4].mean()), n * FINAL_BYTES["dem"])}
+                 ("k_final_mixed" if a.precision == "mixed" else "k_final"):
+                     (float(t[:, 4].mean()), n * FINAL_BYTES["dem"])}
         name = max(cands, key=lambda q: cands[q][0])
         kms, nbytes = cands[name]
         peak, src = peak_hbm()
         ach = nbytes / (kms / 1e3) / 1e9
         line["roofline"] = {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "unit": "GB/s",
                             "frac": ach / peak, "peak_source": src, "traffic": ncu_traffic(name + "/ens256"),
-                            "algorithmic_bytes_per_launch": nbytes, "launch_ms": kms,
+                            "algorithmic_bytes_per_launch": nbytes, "launch_ms": kms, "spinning_fraction": spin,
                             "kernels_ms": {q: v[0] for q, v in cands.items()}}
         if a.precision == "mixed" and not a.no_error:
             sizes = [len(q["tag"]) for q in sts]
@@ -1114,7 +1150,8 @@ def main():
     a = ap.parse_args()
     a.steps_auto = a.steps is None and a.workload not in ("serve", "ens256")
     if a.steps is None:
-        a.steps = SERVE_WINDOW if a.workload == "serve" else 50
+        # ens256: the ensemble's 5000 steps per replica in one launch
+        a.steps = SERVE_WINDOW if a.workload == "serve" else (5000 if a.workload == "ens256" else 50)
     if a.warmup is None:
         a.warmup = SERVE_WARMUP if a.workload == "serve" else 5
     a.warmup = max(3, a.warmup)
@@ -1168,6 +1205,7 @@ def main():
     force_ms = float(t[:, 3].mean())
     kind = cfg.kind
     contacts = len(ctx.history()[0]) / n if kind == "dem" else 0.0
+    spin = spinning_fraction([ctx.download()]) if kind == "dem" else 0.0
     suffix = "mixed" if a.precision == "mixed" else "fp64"
     # the dominant per-particle kernel of the step: force, initial or final
     # integration (phases timed by CUDA events; rebuild steps averaged in)
@@ -1175,7 +1213,7 @@ def main():
              ("lj", "mixed"): "k_lj_mixed", ("lj", "fp64"): "k_lj_fp64"}[(kind, a.precision)]
     cands = {fname: (force_ms, force_bytes(kind, nfull_avg, contacts, a.precision)),
              ("k_initial_mixed" if a.precision == "mixed" else "k_initial"):
-                 (float(t[:, 1].mean()), INIT_BYTES[(kind, a.precision)]),
+                 (float(t[:, 1].mean()), init_bytes(kind, a.precision, spin)),
              ("k_final_mixed" if a.precision == "mixed" else "k_final"):
                  (float(t[:, 4].mean()), FINAL_BYTES[kind])}
     kname = max(cands, key=lambda q: cands[q][0])
@@ -1199,6 +1237,7 @@ def main():
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": src, "traffic": traffic,
                      "algorithmic_bytes_per_particle": bpp, "avg_full_neighbors": nfull_avg, "launch_ms": kms,
+                     "spinning_fraction": spin,
                      "kernels_ms": {q: v[0] for q, v in cands.items()}},
         "clocks": clk.summary(),
     }

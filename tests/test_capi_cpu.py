@@ -264,3 +264,13 @@ seed = 9
     assert c.langevin and c.lv_temperature == 1.1 and c.lv_damping == 0.5 and c.lv_seed == 9
     with pytest.raises(config.ConfigError):
         config.from_toml(txt.replace("seed = 9", "seed = 9\nfriction = 1.0"))
+
+
+def test_grouped_server_refuses_a_group_of_two_kinds(lib):
+    """A slot group shares one batch context, so it must hold one particle
+    kind; the check runs before any device work."""
+    from mddem_gb300 import capi, config
+
+    with pytest.raises(capi.MdgError) as e:
+        capi.Server([config.granular_gas_config(), config.lj_fluid_config()], [100, 100], 1 << 30, groups=[0, 0])
+    assert e.value.status == 1  # MDG_ERR_CONFIG

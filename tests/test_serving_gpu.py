@@ -106,6 +106,30 @@ def test_server_results_equal_alone(gpu_lib, precision):
     srv.close()
 
 
+def test_grouped_server_results_equal_alone(gpu_lib):
+    """Every slot in its own context (mdg_server_create_grouped): four
+    contexts on four streams, all launched before any is waited on; each job
+    still ends bitwise where it ends alone."""
+    from mddem_gb300 import capi, config
+
+    jobs = _jobs("mixed")
+    slots = [config.granular_gas_config(precision="mixed")] * 2 + [config.lj_fluid_config(precision="mixed")] * 2
+    srv = capi.Server(slots, [2000, 2000, 1000, 1000], hbm_budget=1 << 30, groups=[0, 1, 2, 3])
+    assert srv.stats()["contexts"] == 4
+    ids = [srv.submit(c, s, n) for c, s, n in jobs]
+    done = {}
+    for _ in range(1000):
+        active, pending = srv.pump(25)
+        done.update({i["id"]: i for i in srv.poll()})
+        if active == 0 and pending == 0:
+            break
+    assert sorted(done) == sorted(ids)
+    for jid, (cfg, st, steps) in zip(ids, jobs):
+        f = ("pos", "vel", "omega") if cfg.kind == "dem" else ("pos", "vel")
+        assert _same(srv.fetch(jid), _alone(cfg, st, steps), f), jid
+    srv.close()
+
+
 def test_server_rejects_jobs_without_a_slot(gpu_lib):
     from mddem_gb300 import capi, config, inputs
 
