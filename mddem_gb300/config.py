@@ -112,7 +112,7 @@ _SECTIONS = {
     "thermostat": {"temperature", "coupling", "group"},
     "langevin": {"temperature", "damping", "seed", "group"},
     "gpu": {"precision", "rebuild_policy", "threads_per_particle", "neighbor_capacity", "history_capacity",
-            "virial"},
+            "virial", "generate"},
 }
 _MATERIAL_KEYS = {f.name for f in dataclasses.fields(Material)}
 _WALL_KEYS = {"type", "point_x", "point_y", "point_z", "normal_x", "normal_y", "normal_z", "material", "name",

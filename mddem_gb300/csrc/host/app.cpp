@@ -266,6 +266,42 @@ struct PrintPlugin : Plugin {
     }
 };
 
+// The generated system's state, back on the host for the plugins that read
+// it later (restart files, measurement normalisation).
+void download_state(App& a) {
+    const size_t n = a.device_gen_n;
+    HostState& h = a.state;
+    h = HostState{};
+    h.dem = a.dem;
+    h.tag.resize(n);
+    h.type.resize(n);
+    h.pos.resize(3 * n);
+    h.vel.resize(3 * n);
+    h.mass.resize(n);
+    h.cutoff_radius.resize(n);
+    mdg_state_view v{};
+    v.n = n;
+    v.tag = h.tag.data();
+    v.type = h.type.data();
+    v.pos = h.pos.data();
+    v.vel = h.vel.data();
+    v.mass = h.mass.data();
+    v.cutoff_radius = h.cutoff_radius.data();
+    if (h.dem) {
+        h.radius.resize(n);
+        h.inv_inertia.resize(n);
+        h.omega.resize(3 * n);
+        h.quat.resize(4 * n);
+        h.density.assign(n, a.device_gen_density);
+        v.radius = h.radius.data();
+        v.inv_inertia = h.inv_inertia.data();
+        v.omega = h.omega.data();
+        v.quat = h.quat.data();
+    }
+    const int st = mdg_download_state(a.ctx, 0, &v);
+    if (st != MDG_OK) throw ConfigError(std::string("mdg_download_state: ") + mdg_status_string(st));
+}
+
 // The device plugin: [gpu] settings, then (PostSetup, after the state
 // plugins) the context and the upload.  It provides the systems the
 // reference's NeighborPlugin, force plugins and integrators run on the host.
@@ -276,7 +312,10 @@ struct GpuPlugin : Plugin {
             const toml::Table* g = section(a, "gpu");
             if (g)
                 check_keys("gpu", *g, {"precision", "rebuild_policy", "threads_per_particle", "neighbor_capacity",
-                                       "history_capacity", "virial"});
+                                       "history_capacity", "virial", "generate"});
+            const std::string gen = text(g, "generate", "host");
+            if (gen != "host" && gen != "device") throw ConfigError("generate = \"" + gen + "\": host or device");
+            a.gen_device = gen == "device";
             std::string prec = text(g, "precision", "fp64");
             if (!a.opts.precision.empty()) prec = a.opts.precision;
             if (prec != "fp64" && prec != "mixed") throw ConfigError("precision = \"" + prec + "\": fp64 or mixed");
@@ -304,6 +343,16 @@ struct GpuPlugin : Plugin {
         if (a.opts.check) {
             if (!a.opts.write_restart.empty()) write_initial_restart(a, a.opts.write_restart);
             std::printf("%s\n", config_json(a).c_str());
+            return;
+        }
+        if (a.device_gen && a.state.size() == 0) {  // no restart state: make the system on the device
+            int st = mdg_create(&a.cfg, a.device_gen_n, &a.ctx);
+            if (st != MDG_OK) throw ConfigError(std::string("mdg_create: ") + mdg_status_string(st));
+            st = a.device_gen(a);
+            if (st != MDG_OK) throw ConfigError(std::string("device generator: ") + mdg_status_string(st));
+            download_state(a);
+            std::printf("# %s N=%zu dt=%.6e steps=%lld precision=%s (generated on the device)\n", a.dem ? "dem" : "lj",
+                        a.state.size(), a.cfg.dt, a.run_steps, a.cfg.precision == MDG_MIXED ? "mixed" : "fp64");
             return;
         }
         int st = mdg_create(&a.cfg, a.state.size(), &a.ctx);

@@ -84,6 +84,14 @@ public:
     int lj_types = 0;                       // [lj] types: > 1 = multi-type mode
     std::vector<mdg_lj_pair> lj_pairs;      // its n x n pair table
     HostState state;
+    // [gpu] generate = "device": the state plugins leave `state` empty and
+    // register the device generator of their system instead; the device
+    // plugin creates the context for device_gen_n particles, runs it, and
+    // downloads the generated state into `state` (densities: device_gen_density)
+    bool gen_device = false;
+    size_t device_gen_n = 0;
+    double device_gen_density = 0.0;
+    std::function<int(App&)> device_gen;
     long long run_steps = 1000, thermo_every = 100;
     std::vector<long long> intervals;   // other output intervals (measurements)
     long long step = 0;             // step counter: first_step + the steps done in this run

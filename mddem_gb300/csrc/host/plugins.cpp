@@ -131,6 +131,52 @@ double rayleigh_dt(double r, double density, double E, double nu) {
     return 0.15 * (kPi * r / alpha * std::sqrt(density / g));
 }
 
+// [gpu] generate = "device" for a granular config: one random insertion block
+// in the domain (inset by the radius), made by mdg_generate_gas with the same
+// rejection rule (1.1 (r_i + r_j)) and Gaussian components of std `velocity`;
+// block regions, files, several blocks and directional velocities stay on the
+// host generator.  dt from the smallest radius the block allows.
+void device_gas(App& a, const std::vector<const toml::Table*>& blocks) {
+    if (blocks.size() != 1) throw ConfigError("generate = \"device\": one [[particles.insert]] block");
+    const toml::Table* b = blocks[0];
+    if (text(b, "source", "random") != "random" || toml::find(*b, "rate") || toml::find(*b, "region"))
+        throw ConfigError("generate = \"device\": random insertion in the whole domain only");
+    for (const char* k : {"velocity_x", "velocity_y", "velocity_z"})
+        if (num(b, k, 0.0) != 0.0) throw ConfigError(std::string("generate = \"device\": ") + k + " is not supported");
+    const long long n = integer(b, "count", -1);
+    if (n < 1) throw ConfigError("[[particles.insert]] needs count");
+    mdg_gas_spec g{};
+    g.n = (size_t)n;
+    const toml::Value* rv = toml::find(*b, "radius");
+    if (!rv) throw ConfigError("[[particles.insert]] needs radius");
+    if (rv->kind == toml::Value::TABLE) {
+        if (text(rv->t.get(), "distribution", "") != "uniform") throw ConfigError("radius distribution: fixed or uniform only");
+        g.rmin = num(rv->t.get(), "min", 0.0);
+        g.rmax = num(rv->t.get(), "max", 0.0);
+    } else {
+        g.rmin = g.rmax = rv->number();
+    }
+    g.density = num(b, "density", 2500.0);
+    g.sep_factor = 1.1;
+    g.inset = 1;
+    g.velocity_mode = MDG_VEL_GAUSSIAN;
+    g.speed = num(b, "velocity", 0.0);
+    const std::string mat = text(b, "material", a.material_names[0]);
+    size_t mi = 0;
+    while (mi < a.material_names.size() && a.material_names[mi] != mat) mi++;
+    if (mi == a.material_names.size()) throw ConfigError("material \"" + mat + "\" is not in [[dem.materials]]");
+    g.material = (uint32_t)mi;
+    g.seed = a.opts.seed;
+    a.device_gen_n = (size_t)n;
+    a.device_gen_density = g.density;
+    a.device_gen = [g](App& app) {
+        size_t placed = 0;
+        return mdg_generate_gas(app.ctx, 0, &g, &placed);
+    };
+    if (a.cfg.dt == 0.0)
+        a.cfg.dt = rayleigh_dt(g.rmin, g.density, a.materials[0].youngs_mod, a.materials[0].poisson_ratio);
+}
+
 // DemAtomInsertPlugin: [[particles.insert]] (crates/dem_atom/src/insert.rs:
 // 417-614): random insertion in the domain inset by the radius or in a block
 // region, rejection at 1.1 (r_i + r_j) (mdg_rsa_spheres), Gaussian velocity
@@ -147,6 +193,10 @@ struct DemAtomInsertPlugin : Plugin {
             HostState& h = a.state;
             h = HostState{};
             h.dem = true;
+            if (a.gen_device) {
+                device_gas(a, blocks);
+                return;
+            }
             double rmin_all = std::numeric_limits<double>::infinity(), dmax = 0.0;
             for (size_t k = 0; k < blocks.size(); k++) {
                 const toml::Table* b = blocks[k];
@@ -302,6 +352,32 @@ struct LatticePlugin : Plugin {
             HostState& h = a.state;
             h = HostState{};
             h.dem = false;
+            if (a.gen_device) {  // mdg_generate_fcc: the same lattice, types and masses, T fixed on the device
+                if ((int)fractions.size() > MDG_GEN_MAX_TYPES) throw ConfigError("[lattice] more than 8 types");
+                if (a.lj_types > 1 && (int)fractions.size() > a.lj_types)
+                    throw ConfigError("[lattice] type_fractions give more types than [lj] types");
+                mdg_fcc_spec f{};
+                f.density = rho;
+                f.temperature = T;
+                f.mass = mass;
+                f.skin = skin;
+                f.seed = a.opts.seed;
+                f.n_types = (int32_t)fractions.size();
+                for (size_t q = 0; q < fractions.size(); q++) {
+                    f.type_fractions[q] = fractions[q];
+                    f.type_masses[q] = q < tmass.size() ? tmass[q] : 0.0;
+                }
+                long long n = 4;
+                for (int d = 0; d < 3; d++)
+                    n *= (long long)std::floor((a.cfg.box_hi[d] - a.cfg.box_lo[d]) / std::cbrt(4.0 / rho));
+                a.device_gen_n = (size_t)n;
+                a.device_gen = [f](App& app) {
+                    size_t made = 0;
+                    return mdg_generate_fcc(app.ctx, 0, &f, &made);
+                };
+                if (a.cfg.dt == 0.0) a.cfg.dt = 0.005;
+                return;
+            }
             std::mt19937_64 gen(a.opts.seed);
             std::normal_distribution<double> nd(0.0, std::sqrt(T / mass)), n01(0.0, 1.0);
             // types by index (fcc_insert, md_lattice/src/lib.rs:291-327): the
@@ -769,8 +845,9 @@ std::string config_json(const App& a) {
         ms += h.mass[i];
         if (h.dem) rs += h.radius[i];
     }
-    o << "], \"steps\": " << a.run_steps << ", \"thermo\": " << a.thermo_every << ", \"n\": " << h.size()
-      << ", \"pos_sum\": ";
+    o << "], \"steps\": " << a.run_steps << ", \"thermo\": " << a.thermo_every
+      << ", \"n\": " << (h.size() ? h.size() : a.device_gen_n)
+      << ", \"generate\": \"" << (a.device_gen ? "device" : "host") << "\", \"pos_sum\": ";
     json_vec(o, ps, 3);
     o << ", \"radius_sum\": ";
     json_num(o, rs);

@@ -1117,8 +1117,9 @@ __device__ __noinline__ void build_warp(const Dev& d, int s, int li) {
     }
 }
 
-// Candidates one warp stages at a time in build_cells_staged.
-constexpr int STAGE_CAP = 384;
+// Candidates one warp stages at a time in build_cells_staged (192: 27 KB of
+// shared memory per block, which leaves room for the 6 blocks per SM below).
+constexpr int STAGE_CAP = 192;
 
 // One warp per bin, staged (systems with many dense bins): the candidates of
 // the bin's window are gathered into shared memory in passes of 32 (every
@@ -1389,13 +1390,13 @@ __device__ void build_unit(const Dev& d, int s, int pb, int sub) {
     if (li < sp.n) build_warp(d, s, li);  // uniform over the warp
 }
 
-// Minimum resident blocks per SM asked of ptxas for k_build: 4 caps it at
-// 128 registers with ~20 B of spills (5, at 96 registers, spilled in the
-// staged build's inner loop: 10 M local-memory requests per LJ 256k build,
-// 11 % slower); shared memory (45.6 KB per block) allows 4 as well; a
-// compile-time tuning knob.
+// Minimum resident blocks per SM asked of ptxas for k_build: 6 caps it at 80
+// registers (~180 B of spills in the staged loop).  Measured on GB300 against
+// 4 blocks at 128 registers: warp per particle 12 % faster (LJ 256k 2.04 ->
+// 1.79 ms per rebuild and force, polydisperse 200k 0.97 -> 0.86 ms), warp per
+// bin 2 % faster (0.83 -> 0.81 ms); a compile-time tuning knob.
 #ifndef MDG_BUILD_MINB
-#define MDG_BUILD_MINB 4
+#define MDG_BUILD_MINB 6
 #endif
 __global__ void __launch_bounds__(BUILD_WARPS * 32, MDG_BUILD_MINB) k_build(Dev d)
     RB_FOR_PARTICLE_SUBS(build_unit, BUILD_SUBS)

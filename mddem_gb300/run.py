@@ -86,8 +86,45 @@ def _insert(doc, cfg, seed):
     return out
 
 
+def _device_spec(doc, cfg, seed):
+    """[gpu] generate = "device": the device generator call that makes the
+    system (mdg_generate_fcc / mdg_generate_gas) instead of a host state; a
+    granular config needs one random insertion block in the whole domain
+    without directional velocity."""
+    if cfg.kind == "lj":
+        lat = doc.get("lattice")
+        if not lat or lat.get("style", "fcc") != "fcc":
+            raise RunError("an LJ config needs [lattice] style = \"fcc\"")
+        rho = float(lat.get("density", 0.85))
+        n = 4
+        for d in range(3):
+            n *= int(math.floor(cfg.box[d] / (4.0 / rho) ** (1.0 / 3.0)))
+        return {"generate": "fcc", "n": n, "density": rho, "temperature": float(lat.get("temperature", 0.85)),
+                "mass": float(lat.get("mass", 1.0)), "skin": float(lat.get("skin", 1.25)), "seed": seed,
+                "type_fractions": lat.get("type_fractions"), "type_masses": lat.get("type_masses")}
+    blocks = doc.get("particles", {}).get("insert", [])
+    if len(blocks) != 1:
+        raise RunError('generate = "device": one [[particles.insert]] block')
+    b = blocks[0]
+    if b.get("source", "random") != "random" or "rate" in b or "region" in b:
+        raise RunError('generate = "device": random insertion in the whole domain only')
+    if any(float(b.get(k, 0.0)) != 0.0 for k in ("velocity_x", "velocity_y", "velocity_z")):
+        raise RunError('generate = "device": directional velocities are not supported')
+    rad = b["radius"]
+    rmin, rmax = (float(rad["min"]), float(rad["max"])) if isinstance(rad, dict) else (float(rad), float(rad))
+    names = [m.name for m in cfg.materials]
+    mat = b.get("material", names[0])
+    if mat not in names:
+        raise RunError(f"material {mat!r} is not in [[dem.materials]]")
+    return {"generate": "gas", "n": int(b["count"]), "radius": (rmin, rmax), "density": float(b.get("density", 2500.0)),
+            "sep_factor": 1.1, "velocity": "gaussian", "speed": float(b.get("velocity", 0.0)),
+            "material": names.index(mat), "seed": seed}
+
+
 def setup(text, seed=0, precision=None):
-    """(config, initial state, run settings) from a reference TOML text."""
+    """(config, initial state, run settings) from a reference TOML text; with
+    [gpu] generate = "device" the state is the device generator's spec (a dict
+    with "generate")."""
     doc = tomllib.loads(text)
     cfg = config.from_toml(text)
     if precision:
@@ -95,7 +132,15 @@ def setup(text, seed=0, precision=None):
     run = doc.get("run", {})
     if isinstance(run, list):
         run = run[0] if run else {}
-    if cfg.kind == "lj":
+    gen = doc.get("gpu", {}).get("generate", "host")
+    if gen not in ("host", "device"):
+        raise RunError(f"generate = {gen!r}: host or device")
+    if gen == "device":
+        st = _device_spec(doc, cfg, seed)
+        if cfg.kind == "dem" and cfg.dt == 0.0:
+            m = cfg.materials[0]
+            cfg = cfg.replace(dt=config.rayleigh_dt(st["radius"][0], st["density"], m.youngs_mod, m.poisson_ratio))
+    elif cfg.kind == "lj":
         lat = doc.get("lattice")
         if not lat or lat.get("style", "fcc") != "fcc":
             raise RunError("an LJ config needs [lattice] style = \"fcc\"")
@@ -167,9 +212,18 @@ def run(text, seed=0, precision=None, steps=None, out=sys.stdout):
     if src:
         st, hist, base, _ = restart.read_restart(src)
         print(f"# Restart: reading from {src}", file=out)
-    n = len(st["tag"])
-    ctx = capi.Context(cfg, n)
-    ctx.upload(st)
+    if "generate" in st:  # made on the device
+        spec = dict(st)
+        kind, n = spec.pop("generate"), spec.pop("n")
+        ctx = capi.Context(cfg, n)
+        if kind == "fcc":
+            ctx.generate_fcc(**spec)
+        else:
+            ctx.generate_gas(n, **spec)
+    else:
+        n = len(st["tag"])
+        ctx = capi.Context(cfg, n)
+        ctx.upload(st)
     if src and hist is not None and len(hist[0]):
         ctx.set_history(*hist)
     meas = s["measure"]

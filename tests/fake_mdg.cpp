@@ -185,4 +185,8 @@ int mdg_rsa_spheres(size_t n, const double lo[3], const double hi[3], double rmi
     return MDG_OK;
 }
 
+// The device generators are not faked: a config that asks for them needs a GPU.
+int mdg_generate_fcc(mdg_ctx*, int, const mdg_fcc_spec*, size_t*) { return MDG_ERR_NODEVICE; }
+int mdg_generate_gas(mdg_ctx*, int, const mdg_gas_spec*, size_t*) { return MDG_ERR_NODEVICE; }
+
 }  // extern "C"

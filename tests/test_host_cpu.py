@@ -568,3 +568,73 @@ def test_resume_with_a_damaged_history_count_is_an_error(fake_runner, tmp_path, 
     p.write_text(text + "read = true\n")
     r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
     assert r.returncode == 1 and "contact-history" in r.stderr, (r.returncode, r.stderr)
+
+
+GAS_DEVICE = """
+[domain]
+x_high = 0.025
+y_high = 0.025
+z_high = 0.025
+
+[neighbor]
+skin_fraction = 1.1
+bin_size = 0.005
+
+[run]
+steps = 200
+
+[[dem.materials]]
+name = "glass"
+youngs_mod = 8.7e9
+poisson_ratio = 0.3
+restitution = 0.95
+friction = 0.4
+
+[[particles.insert]]
+material = "glass"
+count = 500
+radius = { distribution = "uniform", min = 0.0008, max = 0.0012 }
+density = 2500.0
+velocity = 0.3
+
+[gpu]
+generate = "device"
+"""
+
+
+@pytest.mark.parametrize("text,n", [(GAS_DEVICE, 500), (LJ.replace("[gpu]", '[gpu]\ngenerate = "device"'), None)],
+                         ids=["gas", "lj"])
+def test_device_generation_resolves_alike(runner, tmp_path, text, n):
+    """[gpu] generate = "device": both hosts register the device generator
+    (mdg_generate_gas / mdg_generate_fcc) instead of a host state, with the same
+    particle count and the same dt (granular: from the smallest radius the
+    block allows)."""
+    from mddem_gb300 import run
+
+    if "[gpu]" not in text:
+        text += '\n[gpu]\ngenerate = "device"\n'
+    r = _run(runner, tmp_path, text, "--check")
+    assert r.returncode == 0, r.stderr
+    got = json.loads(r.stdout)
+    cfg, st, _ = run.setup(text, seed=0)
+    assert st["generate"] in ("gas", "fcc")
+    assert got["generate"] == "device" and got["n"] == st["n"]
+    if n:
+        assert st["n"] == n
+    assert got["dt"] == cfg.dt
+
+
+@pytest.mark.parametrize("edit,msg", [
+    (('generate = "device"', 'generate = "gpu"'), "host or device"),
+    (("velocity = 0.3", "velocity = 0.3\nvelocity_x = 0.1"), "velocity_x"),
+    (("density = 2500.0", 'density = 2500.0\nregion = { type = "block", min = [0, 0, 0], max = [0.01, 0.01, 0.01] }'),
+     "whole domain"),
+])
+def test_device_generation_refusals(runner, tmp_path, edit, msg):
+    from mddem_gb300 import run
+
+    text = GAS_DEVICE.replace(*edit)
+    r = _run(runner, tmp_path, text, "--check")
+    assert r.returncode == 1 and msg in r.stderr, r.stderr
+    with pytest.raises(run.RunError):
+        run.setup(text, seed=0)

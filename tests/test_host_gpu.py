@@ -8,7 +8,7 @@ import subprocess
 
 import pytest
 
-from test_host_cpu import LJ, REBOUND
+from test_host_cpu import GAS_DEVICE, LJ, REBOUND
 
 pytestmark = pytest.mark.gpu
 
@@ -49,3 +49,28 @@ def test_mdg_run_wall_rebound(gpu_lib, tmp_path):
     assert step == 6000 and len(st["tag"]) == 1 and hist is not None
     assert st["vel"][0, 2] == pytest.approx(0.9, rel=0.04)
     assert (tmp_path / "output" / "restart" / "restart_3000_rank0.bin").exists()
+
+
+def test_device_generated_configs_run_alike(gpu_lib, tmp_path, monkeypatch):
+    """[gpu] generate = "device": both hosts make the same system on the
+    device (same generator, same seed), so the C++ host's thermo lines equal
+    the Python runner's, and a restart file written by the C++ host holds the
+    generated particles."""
+    import io
+
+    from mddem_gb300 import restart, run
+
+    monkeypatch.chdir(tmp_path)  # the Python runner writes its output directory here too
+    gas = GAS_DEVICE.replace("[run]\nsteps = 200\n", "[run]\nsteps = 200\nthermo = 100\n\n[restart]\ninterval = 200\n")
+    lj = LJ.replace("[gpu]", '[gpu]\ngenerate = "device"') + "\n[run]\nsteps = 100\nthermo = 50\n"
+    for text in (gas, lj):
+        r = _run(tmp_path, text)
+        assert r.returncode == 0, r.stderr
+        assert "generated on the device" in r.stdout
+        cpp = [l for l in r.stdout.splitlines() if not l.startswith("#")]
+        buf = io.StringIO()
+        run.run(text, out=buf)
+        py = [l for l in buf.getvalue().splitlines() if not l.startswith("#")]
+        assert cpp == py
+    st, _, step, _ = restart.read_restart(tmp_path / "output" / "restart" / "restart_200_rank0.bin")
+    assert step == 200 and len(st["tag"]) == 500
