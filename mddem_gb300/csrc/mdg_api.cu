@@ -354,15 +354,20 @@ int cuda_err(cudaError_t e) {
 // neighbor_setup + compute_bin_grid (crates/mddem_core/src/neighbor.rs:480-541,
 // 290-371) for one rank, from the uploaded cutoff radii.
 // List build mode (all give the same rows): under about 6 particles per bin
-// a thread per particle; a warp per bin from 512 bins on (and no more bins
-// than particles, as bins take particle slots); else a warp per particle.
-// Measured on GB300 (LJ melts, rho 0.85): a warp per particle is faster up
-// to about 7000 atoms (343 bins: 59 against 75 us), a warp per bin from
-// about 1300 bins on (27436 atoms: 99 against 203 us).
-int auto_build_mode(const SysParams& p, size_t n) {
+// a thread per particle; a warp per bin from 512 bins on in a single-system
+// context, from 64 in a batch (and no more bins than particles, as bins take
+// particle slots); else a warp per particle.  Measured on GB300 (LJ melts,
+// rho 0.85), one system alone: a warp per particle is faster up to about
+// 7000 atoms (343 bins: 59 against 75 us: a few hundred warps leave the GPU
+// idle), a warp per bin from about 1300 bins on (27436 atoms: 99 against
+// 203 us).  In a batch several systems rebuild in the same launch and fill
+// the GPU together, and a warp per bin does about half the work per atom:
+// the served stream runs 3.06 G particle-steps/s with the threshold at 512
+// bins, 3.15 G at 216, 3.16 G at 64.
+int auto_build_mode(const SysParams& p, size_t n, bool batch) {
     const double nbins = (double)p.nc[0] * (double)p.nc[1] * (double)p.nc[2];
     if ((double)n < 6.0 * nbins) return 2;
-    if (nbins >= 512.0 && (size_t)p.ncell <= n) return 0;
+    if (nbins >= (batch ? 64.0 : 512.0) && (size_t)p.ncell <= n) return 0;
     return 1;
 }
 
@@ -396,7 +401,7 @@ int setup_grid(const mdg_config& c, double min_skin, double max_skin, size_t n, 
     }
     if (ncell > (1LL << 30)) return MDG_ERR_CONFIG;
     p.ncell = (int)ncell;
-    p.build_mode = auto_build_mode(p, n);
+    p.build_mode = auto_build_mode(p, n, false);
     p.max_cutoff = max_cutoff;
     p.stencil_cut_sq = max_cutoff * max_cutoff;
     // stencil membership of every offset (compute_bin_grid's distance test,
@@ -1093,6 +1098,7 @@ static int prepare_system(mdg_ctx* c, int sys, size_t n, double min_cut, double 
     SysParams& p = c->sp[sys];
     int r = setup_grid(k, min_cut, max_cut, n, p);
     if (r) return r;
+    if (c->nsys > 1) p.build_mode = auto_build_mode(p, n, true);
     if (c->build_mode >= 0) p.build_mode = c->build_mode;
     p.n = (int)n;
     p.nb = (int)((n + BLK - 1) / BLK);
@@ -1556,7 +1562,7 @@ int mdg_set_build_mode(mdg_ctx* c, int mode) {
     for (int s = 0; s < c->nsys; s++) {
         if (!c->uploaded[s]) continue;
         SysParams& p = c->sp[s];
-        p.build_mode = mode >= 0 ? mode : auto_build_mode(p, (size_t)p.n);
+        p.build_mode = mode >= 0 ? mode : auto_build_mode(p, (size_t)p.n, c->nsys > 1);
         e = cudaMemcpy(c->d_sp + s, &p, sizeof(SysParams), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return cuda_err(e);
     }
