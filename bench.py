@@ -342,7 +342,7 @@ SERVE_BUDGET_GB = 96        # admission budget of resident jobs' device bytes (G
 SERVE_SLOT_MULT = 2         # times the slot counts of workloads.SERVE_*_SLOTS
 SERVE_WINDOW = 80           # timed pumps by default: the steady state while jobs keep arriving
 SERVE_WARMUP = 10           # pumps of the stream before the timed window
-SERVE_GROUPS = "kind"       # slots per batch context (workloads.serve_groups)
+SERVE_GROUPS = "split"      # slots per batch context (workloads.serve_groups): DEM, LJ <= 16384, LJ 100000
 PLAIN_SAMPLE_STEPS = 200
 # (jobs, backlog, arrivals per pump, budget GB, slot multiplier) of --sweep;
 # each setting's arrivals last about as long as the timed window
@@ -756,7 +756,7 @@ def serve_phases(a, trace, made, at_tick, pumps=2):
     srv = serve_server(a)
     order = sorted(range(len(trace)), key=lambda k: trace[k].arrival)
     nxt, tick, sid = 0, 0, {}
-    rows, mix, samples, rebuilt = [], None, [], {}
+    rows, mix, samples, rebuilt, ctx_rows = [], None, [], {}, []
     while tick < at_tick + pumps:
         while nxt < len(order) and trace[order[nxt]].arrival <= tick:
             k = order[nxt]
@@ -779,6 +779,12 @@ def serve_phases(a, trace, made, at_tick, pumps=2):
                 for q in live:
                     kind = c.configs[q].kind
                     rebuilt[kind] = rebuilt.get(kind, 0) + c.n[q] * (c.thermo(q)["nbuilds"] - nb0[q])
+                t_c = per[-1][0]
+                kinds = {c.configs[q].kind for q in live}
+                ctx_rows.append({"kind": "+".join(sorted(kinds)), "particles": int(sum(c.n[q] for q in live)),
+                                 "step_ms": float(t_c[:, 0].mean()),
+                                 "phases_ms": {ph: float(t_c[:, 1 + i].mean())
+                                               for i, ph in enumerate(("initial", "rebuild", "force", "final"))}})
             rows.append((sum(q[0] for q in per), sum(q[1] for q in per), np.max([q[2] for q in per], axis=0)))
             active, pending = srv.pump(0)
         for info in srv.poll():
@@ -796,7 +802,8 @@ def serve_phases(a, trace, made, at_tick, pumps=2):
     ph = {q: float(t[:, 1 + i].mean()) for i, q in enumerate(names)}
     return {"at_pump": at_tick, "timesteps": int(len(t)), "step_ms": float(t[:, 0].mean()), "phases_ms": ph,
             "rebuild_steps_frac": float(rb.mean()), "kernels_per_step": float(kern.mean()),
-            "rebuilt_particles_per_step": {k: v / len(t) for k, v in rebuilt.items()}}, mix, samples
+            "rebuilt_particles_per_step": {k: v / len(t) for k, v in rebuilt.items()},
+            "per_context": ctx_rows}, mix, samples
 
 
 def serve_roofline(a, phases, mix, served_rate):
@@ -1140,7 +1147,7 @@ def main():
     ap.add_argument("--backlog", type=int, default=SERVE_BACKLOG, help="served stream: jobs queued at the start")
     ap.add_argument("--budget-gb", type=float, default=SERVE_BUDGET_GB, help="served stream: admission HBM budget")
     ap.add_argument("--slot-mult", type=int, default=SERVE_SLOT_MULT, help="served stream: slot count multiplier")
-    ap.add_argument("--groups", default=SERVE_GROUPS, choices=("kind", "size", "class"),
+    ap.add_argument("--groups", default=SERVE_GROUPS, choices=("kind", "split", "size", "class"),
                     help="served stream: slots per batch context (one context and stream per group)")
     ap.add_argument("--no-error", action="store_true", help="skip the precision-form error block")
     ap.add_argument("--sweep", action="store_true",

@@ -935,10 +935,12 @@ int mdg_batch_create(const mdg_config* cfgs, const size_t* capacity, int nsys, m
             p.hcap = 0;
         }
         if (k.virial) c->any_virial = true;
-        // threads per particle of the LJ force kernel: explicit, or 4 for the
-        // mixed path (the measured best on GB300 for ~78-entry rows) and 1 for fp64
+        // threads per particle of the LJ force kernel: explicit, or 2 for the
+        // mixed path and 1 for fp64 (measured on GB300 with ~76-entry rows:
+        // the served stream 3.47 G particle-steps/s at 2 against 3.40 G at 4
+        // and 3.03 G at 8; LJ 256k alone 0.068 against 0.074 ms per force)
         if (k.threads_per_particle > 0) c->tpp_lj = k.threads_per_particle;
-        else if (k.kind == MDG_KIND_LJ && k.precision == MDG_MIXED) c->tpp_lj = 4;
+        else if (k.kind == MDG_KIND_LJ && k.precision == MDG_MIXED) c->tpp_lj = 2;
         // the physics of the slot (replaceable by mdg_configure_system)
         std::vector<double> tabs;
         apply_physics(c, s, k, tabs);

@@ -156,15 +156,23 @@ SERVE_DEM_SLOTS = [(128, 32), (1024, 24), (8192, 16), (65536, 12), (200000, 8)]
 SERVE_LJ_SLOTS = [(2048, 8), (16384, 8), (100000, 6)]
 
 
-def serve_groups(cfgs, caps, policy="kind", small=1024):
+SERVE_SPLIT = {"lj": 16384, "dem": None}  # "split": the larger slots of a kind get their own context
+
+
+def serve_groups(cfgs, caps, policy="kind", small=1024, split=None):
     """Per-slot group ids for capi.Server(groups=...): "kind" one batch
-    context per particle kind; "size" the slots of capacity <= `small` apart
-    from the larger ones of their kind; "class" one context per (kind,
-    capacity)."""
+    context per particle kind; "split" as "kind", with the slots of a kind
+    above its `split` capacity (default SERVE_SPLIT) in a context of their
+    own; "size" the slots of capacity <= `small` apart from the larger ones
+    of their kind; "class" one context per (kind, capacity)."""
+    split = SERVE_SPLIT if split is None else split
     keys = []
     for c, cap in zip(cfgs, caps):
         if policy == "kind":
             keys.append(c.kind)
+        elif policy == "split":
+            lim = split.get(c.kind)
+            keys.append((c.kind, lim is not None and cap > lim))
         elif policy == "size":
             keys.append((c.kind, cap <= small))
         elif policy == "class":
