@@ -67,3 +67,21 @@ def test_oracle_rsa_places_the_library_spheres():
         a = capi.rsa_spheres(n, (0.0,) * 3, (box,) * 3, rmin, rmax, sep, inset, seed)
         b = oracle.rsa_spheres(n, (0.0,) * 3, (box,) * 3, rmin, rmax, sep, inset, seed)
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_serve_groups_place_slots_by_kind_and_size():
+    """The bench's "split" grouping: one context for the gases, one for the LJ
+    slots up to 16384 atoms, one for the larger LJ slots; "kind" two; a
+    group never mixes kinds."""
+    from mddem_gb300 import workloads as w
+
+    cfgs, caps = w.serve_slots("mixed", "displacement", mult=2)
+    for policy, want in (("kind", 2), ("split", 3), ("class", 8)):
+        g = w.serve_groups(cfgs, caps, policy)
+        assert len(set(g)) == want, policy
+        for k in set(g):
+            assert len({c.kind for c, gg in zip(cfgs, g) if gg == k}) == 1
+    g = w.serve_groups(cfgs, caps, "split")
+    small = {gg for c, cap, gg in zip(cfgs, caps, g) if c.kind == "lj" and cap <= 16384}
+    large = {gg for c, cap, gg in zip(cfgs, caps, g) if c.kind == "lj" and cap > 16384}
+    assert len(small) == 1 and len(large) == 1 and small != large
