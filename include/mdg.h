@@ -320,6 +320,12 @@ int  mdg_msd(mdg_ctx* ctx, int sys, double* msd);
  * is ordered on it, so a caller may record events on it or make its own
  * streams wait for it. */
 int  mdg_get_stream(mdg_ctx* ctx, void** stream);
+/* Run the context's work on a new stream of CUDA priority `priority`
+ * (lower numbers run first; clamped to the device's range; 0 = the default).
+ * No counterpart in the reference: contexts launched side by side (several
+ * batches, the server's slot groups) can put a latency-bound chain ahead of a
+ * bandwidth-bound one.  Not while a launch is in flight (MDG_ERR_STATE). */
+int  mdg_set_stream_priority(mdg_ctx* ctx, int priority);
 /* Every system's step budget, status word and step counter in one device
  * read (arrays of mdg_num_systems entries; any may be NULL). */
 int  mdg_get_progress(mdg_ctx* ctx, int64_t* remaining, int32_t* status, int64_t* steps);

@@ -33,7 +33,7 @@ EXPORTS = [
     "mdg_get_remaining", "mdg_get_status", "mdg_configure_system", "mdg_server_create", "mdg_server_create_grouped", "mdg_server_destroy",
     "mdg_server_submit", "mdg_server_pump", "mdg_server_poll", "mdg_server_fetch", "mdg_server_context",
     "mdg_server_slot_context",
-    "mdg_rsa_spheres", "mdg_counter_draw", "mdg_generate_fcc", "mdg_generate_gas", "mdg_get_progress", "mdg_get_stream", "mdg_server_stats",
+    "mdg_rsa_spheres", "mdg_counter_draw", "mdg_set_stream_priority", "mdg_generate_fcc", "mdg_generate_gas", "mdg_get_progress", "mdg_get_stream", "mdg_server_stats",
     "mdg_server_resident", "mdg_get_config", "mdg_set_threads_per_particle", "mdg_get_threads_per_particle",
     "mdg_set_build_mode", "mdg_autotune", "mdg_rdf", "mdg_msd_reset", "mdg_msd",
 ]
@@ -214,6 +214,7 @@ def load(path: str = LIB_PATH):
     lib.mdg_rsa_spheres.argtypes = [C.c_size_t, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double,
                                     C.c_double, C.c_double, C.c_int, C.c_uint64, C.c_uint64,
                                     C.POINTER(C.c_double), C.POINTER(C.c_double), C.POINTER(C.c_size_t)]
+    lib.mdg_set_stream_priority.argtypes = [C.c_void_p, C.c_int]
     lib.mdg_counter_draw.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64]
     lib.mdg_counter_draw.restype = C.c_uint64
     lib.mdg_generate_fcc.argtypes = [C.c_void_p, C.c_int, C.POINTER(FccSpec), C.POINTER(C.c_size_t)]
@@ -695,6 +696,11 @@ class Context:
         v = C.c_double()
         _check(self.lib.mdg_msd(self.h, sys, C.byref(v)), "mdg_msd")
         return v.value
+
+    def stream_priority(self, priority):
+        """mdg_set_stream_priority: run on a new stream of CUDA priority
+        `priority` (lower first, clamped to the device's range)."""
+        _check(self.lib.mdg_set_stream_priority(self.h, int(priority)), "mdg_set_stream_priority")
 
     def threads_per_particle(self, tpp=None):
         if tpp is not None:

@@ -1652,6 +1652,23 @@ int mdg_get_stream(mdg_ctx* c, void** stream) {
     return MDG_OK;
 }
 
+int mdg_set_stream_priority(mdg_ctx* c, int priority) {
+    if (!c) return MDG_ERR_ARG;
+    if (c->pending_steps) return MDG_ERR_STATE;  // a launch is in flight on the old stream
+    int least = 0, greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e != cudaSuccess) return cuda_err(e);
+    const int p = std::min(least, std::max(greatest, priority));
+    e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(e);
+    cudaStream_t s = nullptr;
+    e = cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, p);
+    if (e != cudaSuccess) return cuda_err(e);
+    cudaStreamDestroy(c->stream);
+    c->stream = s;
+    return MDG_OK;
+}
+
 int mdg_get_progress(mdg_ctx* c, int64_t* remaining, int32_t* status, int64_t* steps) {
     if (!c) return MDG_ERR_ARG;
     cudaError_t e = cudaStreamSynchronize(c->stream);

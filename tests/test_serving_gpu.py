@@ -178,3 +178,24 @@ def test_server_walled_and_typed_jobs(gpu_lib, precision):
         got, ref = srv.fetch(jid), _alone(cfg, st, steps)
         assert _same(got, ref, ("pos", "vel", "omega") if cfg.kind == "dem" else ("pos", "vel")), k
     srv.close()
+
+
+def test_stream_priority_keeps_results(gpu_lib):
+    """mdg_set_stream_priority moves a context to a new stream of another
+    priority: the same steps give the same bits, and it is refused while a
+    launch is in flight."""
+    from mddem_gb300 import capi, config, inputs
+
+    cfg = config.lj_fluid_config(precision="mixed")
+    st = inputs.lj_fcc(6, 10.06, 0.85, 0.85, seed=61)
+    ref = _alone(cfg, st, 60)
+    with capi.Context(cfg, len(st["tag"])) as c:
+        c.stream_priority(-5)
+        c.upload(st)
+        c.step(30)
+        c.stream_priority(0)
+        c.step(30)
+        assert _same(c.download(), ref)
+        assert c.lib.mdg_step_async(c.h, 10) == 0
+        assert c.lib.mdg_set_stream_priority(c.h, -1) == 10  # MDG_ERR_STATE
+        assert c.lib.mdg_step_wait(c.h) == 0
