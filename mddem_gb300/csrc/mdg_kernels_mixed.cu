@@ -41,6 +41,59 @@ struct Kahan {
 // the common path keeps its registers.  MT: systems with a multi-type pair
 // table gather the partner's type and look up lj1, lj2 and the squared cutoff
 // (pair_table.get(ti, tj), fp32 copies); also its own instantiation.
+// The LJ pair force is cut off without a shift, so it jumps by f(rc) at the
+// cutoff (about 1e-3 of a particle's pair-force sum).  The fp32 separation
+// can fall on the other side of rc than the fp64 one for a pair within
+// rounding of it; such pairs (fp32 r^2 within LJ_CUT_BAND of rc^2, about 10x
+// the fp32 separation's error) are decided with the fp64 path's own
+// arithmetic (k_lj_fp64: the owner frame, image shift, fma sum), so both
+// paths count the same pairs: k_lj_mixed leaves them out of its main loop and
+// decides them in a second pass over the row, run only by a lane that met
+// one.  At LJ 256k about two pairs lie that close to the cutoff in any step.
+constexpr float LJ_CUT_BAND = 2e-6f;
+
+__device__ __noinline__ bool lj_within_fp64(const Dev& d, const SysParams& sp, long long i, uint32_t e, double cut2) {
+    const long long j = sp.p0 + (e & IDX_MASK);
+    const uint32_t code = e >> IDX_BITS;
+    const bool own = code >= 27u;
+    const int sc = (int)(own ? code - 27u : code);
+    const int s3[3] = {sc / 9 - 1, (sc / 3) % 3 - 1, sc % 3 - 1};
+    const double4 xi = d.pos[i], xj = d.pos[j];
+    const double a[3] = {own ? xj.x : xi.x, own ? xj.y : xi.y, own ? xj.z : xi.z};
+    const double b[3] = {own ? xi.x : xj.x, own ? xi.y : xj.y, own ? xi.z : xj.z};
+    double dd[3];
+    for (int q = 0; q < 3; q++) {
+        const int sq = own ? s3[q] : -s3[q];
+        const double img = sq > 0 ? __dadd_rn(a[q], sp.L[q]) : (sq < 0 ? __dadd_rn(a[q], -sp.L[q]) : a[q]);
+        dd[q] = __dsub_rn(img, b[q]);
+    }
+    const double r2 = fma(dd[0], dd[0], fma(dd[1], dd[1], __dmul_rn(dd[2], dd[2])));
+    return r2 < cut2;
+}
+
+// One LJ pair's force on the particle (fp32, compensated sums) and, on owner
+// entries of systems with `virial`, its virial terms.
+template <bool VIR>
+__device__ __forceinline__ void lj_pair_add(float dx, float dy, float dz, float r2, float lj1, float lj2, bool owner_vir,
+                                            Kahan& kx, Kahan& ky, Kahan& kz, float& w0, float& w1, float& w2,
+                                            float& w3, float& w4, float& w5) {
+    const float r2inv = __frcp_rn(r2);
+    const float r6inv = r2inv * r2inv * r2inv;
+    const float fpair = r2inv * r6inv * (lj1 * r6inv - lj2);
+    kx.add(-fpair * dx);
+    ky.add(-fpair * dy);
+    kz.add(-fpair * dz);
+    if (VIR && owner_vir) {  // owner entry: the reference's half-list pair
+        const float px = -fpair * dx, py = -fpair * dy, pz = -fpair * dz;
+        w0 += dx * px;
+        w1 += dy * py;
+        w2 += dz * pz;
+        w3 += dx * py;
+        w4 += dx * pz;
+        w5 += dy * pz;
+    }
+}
+
 template <int TPP, bool VIR, bool MT>
 __global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
     const int pb = d.blk_run[blockIdx.x / TPP];
@@ -65,6 +118,8 @@ __global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
         const long long tq = (long long)sp.nmat * sp.nmat;
         const long long trow = mt ? sp.mat0 + (long long)d.type[i] * sp.nmat : 0;
         const float s0 = sp.uscale[0], s1 = sp.uscale[1], s2 = sp.uscale[2];
+        bool near = false;  // a pair within fp32 rounding of the cutoff
+        const float in2_ = cut2_ * (1.f - LJ_CUT_BAND), out2_ = cut2_ * (1.f + LJ_CUT_BAND);
         // U entries in flight per lane: list loads first, then the gathers, then
         // the arithmetic, so each lane keeps U independent load chains open
         constexpr int U = 4;
@@ -99,22 +154,42 @@ __global__ void __launch_bounds__(BLK, MDG_LJ_MINB) k_lj_mixed(Dev d) {
                     lj2 = __ldg(d.matf + o + TL_LJ2 * tq);
                     cut2 = __ldg(d.matf + o + TL_CUT2 * tq);
                 }
-                if (r2 >= cut2) continue;
-                const float r2inv = __frcp_rn(r2);
-                const float r6inv = r2inv * r2inv * r2inv;
-                const float fpair = r2inv * r6inv * (lj1 * r6inv - lj2);
-                kx.add(-fpair * dx);
-                ky.add(-fpair * dy);
-                kz.add(-fpair * dz);
-                if (VIR && vir && (e[u] >> IDX_BITS) >= 27u) {  // owner entry: the reference's half-list pair
-                    const float px = -fpair * dx, py = -fpair * dy, pz = -fpair * dz;
-                    w0 += dx * px;
-                    w1 += dy * py;
-                    w2 += dz * pz;
-                    w3 += dx * py;
-                    w4 += dx * pz;
-                    w5 += dy * pz;
+                // one compare for the pairs well inside the cutoff; those within
+                // the band around it are decided after the loop
+                const float in2 = (MT && mt) ? cut2 * (1.f - LJ_CUT_BAND) : in2_;
+                if (r2 >= in2) {
+                    near |= r2 <= ((MT && mt) ? cut2 * (1.f + LJ_CUT_BAND) : out2_);
+                    continue;
                 }
+                lj_pair_add<VIR>(dx, dy, dz, r2, lj1, lj2, vir && (e[u] >> IDX_BITS) >= 27u, kx, ky, kz, w0, w1, w2,
+                                 w3, w4, w5);
+            }
+        }
+        if (near) {
+            // rare: this lane's pairs within fp32 rounding of the cutoff, counted
+            // when the fp64 arithmetic of k_lj_fp64 counts them
+            for (int k = lane; k < nn; k += TPP) {
+                const uint32_t e = __ldg(d.nlist + base + (long long)k * sp.npad);
+                const long long j = sp.p0 + (e & IDX_MASK);
+                const uint4 uj = __ldg(d.posu + j);
+                const float dx = (float)(int)(uj.x - ui.x) * s0;
+                const float dy = (float)(int)(uj.y - ui.y) * s1;
+                const float dz = (float)(int)(uj.z - ui.z) * s2;
+                const float r2 = dx * dx + dy * dy + dz * dz;
+                float lj1 = lj1_, lj2 = lj2_, cut2 = cut2_;
+                double c64 = sp.lj_cut2;
+                if (MT && mt) {
+                    const long long o = trow + __ldg(d.type + j);
+                    lj1 = __ldg(d.matf + o + TL_LJ1 * tq);
+                    lj2 = __ldg(d.matf + o + TL_LJ2 * tq);
+                    cut2 = __ldg(d.matf + o + TL_CUT2 * tq);
+                    c64 = __ldg(d.mat + o + TL_CUT2 * tq);
+                }
+                if (!(r2 >= cut2 * (1.f - LJ_CUT_BAND) && r2 <= cut2 * (1.f + LJ_CUT_BAND)) ||
+                    !lj_within_fp64(d, sp, i, e, c64))
+                    continue;
+                lj_pair_add<VIR>(dx, dy, dz, r2, lj1, lj2, vir && (e >> IDX_BITS) >= 27u, kx, ky, kz, w0, w1, w2, w3,
+                                 w4, w5);
             }
         }
     }
@@ -1101,6 +1176,7 @@ int launch_initial_mixed(const Dev& d, cudaStream_t st, int nh_only, const long 
     k_initial_mixed<<<d.nrun, BLK, 0, st>>>(d, nh_only, loop);
     return 1;
 }
+
 
 template <bool VIR, bool MT>
 void launch_lj_mixed(const Dev& dall, int tpp, cudaStream_t st) {

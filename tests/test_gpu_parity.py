@@ -432,3 +432,39 @@ def test_mixed_dem_grazing_contacts_in_a_large_box(gpu_lib):
     mag = np.linalg.norm(f64, axis=1)
     assert np.all(mag > 0)
     assert rel_err(fmx, f64, mag) <= 1e-5
+
+
+@pytest.mark.parametrize("dr", [-1e-9, 1e-9, -3e-7, 3e-7])
+def test_mixed_lj_pairs_at_the_cutoff_count_like_fp64(gpu_lib, dr):
+    """The LJ force is cut off without a shift (a jump of f(rc) at rc): a pair
+    within fp32 rounding of the cutoff must be counted by the mixed path
+    exactly when the FP64 path counts it, or its particles' force error is
+    ~1e-3.  Two atoms at rc + dr, along x and along a diagonal through a
+    periodic face."""
+    import numpy as np
+
+    from mddem_gb300 import capi, config
+
+    cfg = config.lj_fluid_config(nose_hoover=False)
+    rc = cfg.lj_cutoff * cfg.lj_sigma
+    L = cfg.box[0]
+    for a, u in (((5.0, 5.0, 5.0), (1.0, 0.0, 0.0)), ((L - 0.7, 3.1, 2.2), (0.6, 0.64, 0.48))):
+        u = np.asarray(u) / np.linalg.norm(u)
+        pa = np.asarray(a)
+        pb = (pa + (rc + dr) * u) % L
+        st = {"tag": np.arange(2, dtype=np.uint32), "type": np.zeros(2, np.uint32),
+              "pos": np.array([pa, pb]), "vel": np.zeros((2, 3)), "mass": np.ones(2),
+              "cutoff_radius": np.full(2, 1.25)}
+        f = {}
+        for prec in ("fp64", "mixed"):
+            c = capi.Context(cfg.replace(precision=prec), 2)
+            c.upload(st)
+            c.force_only()
+            f[prec] = c.download()["force"]
+            c.close()
+        inside = bool(np.any(f["fp64"] != 0.0))
+        assert inside == (dr < 0.0)
+        if inside:
+            assert np.max(np.abs(f["mixed"] - f["fp64"])) <= 1e-5 * np.max(np.abs(f["fp64"])), (a, dr)
+        else:
+            assert not np.any(f["mixed"] != 0.0), (a, dr)

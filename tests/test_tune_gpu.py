@@ -48,8 +48,12 @@ def test_autotune_keeps_state_and_picks_candidates(gpu_lib):
     ctx.step(50)
     ref.step(50)
     # positions compared under the minimum image: a different skin wraps
-    # particles into the box at different rebuild steps
-    for k, box, tol in ((0, 10.06, 1e-6), (1, 0.02, 1e-9 * 0.02)):
+    # particles into the box at different rebuild steps.  The LJ force is cut
+    # off without a shift: the two runs' rounding-level position differences
+    # can put a pair that sits at rc on different sides of it in one step, a
+    # kick of f(rc) dt (about 2e-4 in velocity, ~1e-5 sigma after 25 steps),
+    # so the LJ bound is 1e-4 sigma; the granular forces are continuous
+    for k, box, tol in ((0, 10.06, 1e-4), (1, 0.02, 1e-9 * 0.02)):
         (pa,) = by_tag(ctx.download(k), "pos")
         (pb,) = by_tag(ref.download(k), "pos")
         d = pa - pb
