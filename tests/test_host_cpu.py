@@ -638,3 +638,15 @@ def test_device_generation_refusals(runner, tmp_path, edit, msg):
     assert r.returncode == 1 and msg in r.stderr, r.stderr
     with pytest.raises(run.RunError):
         run.setup(text, seed=0)
+
+
+def test_device_generation_failure_exits_1(fake_runner, tmp_path):
+    """[gpu] generate = "device" with a library whose generator fails (the CPU
+    stand-in has no device): the context is created for the generator's count,
+    the failure is reported as a configuration error and the run exits 1."""
+    p = tmp_path / "config.toml"
+    p.write_text(GAS_DEVICE)
+    r = subprocess.run([fake_runner, str(p)], capture_output=True, text=True, timeout=60, cwd=tmp_path)
+    assert r.returncode == 1
+    assert "fake: create kind=0 capacity=500" in r.stderr
+    assert "device generator" in r.stderr
